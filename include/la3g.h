@@ -1,0 +1,220 @@
+/*
+ * la3g.h — C ABI of the GB300-native LA3 vertex-program engine.
+ *
+ * One GPU, one process.  The library owns all device memory; callers own the
+ * host buffers they pass in.  Every call returns an la3g_status; no C++
+ * exception crosses this boundary.  la3g_last_error_string() describes the
+ * last failure of the calling thread.
+ *
+ * Vertex ids are the ids of the input file.  A graph loaded with n vertices
+ * has nslots = n + 1 slots (ids 0..n; the reference sizes its single tile
+ * n + 1 wide, matrix/matrix2d.hpp:6-9); every per-vertex output array has
+ * nslots entries indexed by vertex id.  For a bipartite graph
+ * n = ndocs + nterms and term t (1-based in the file) is vertex ndocs + t.
+ *
+ * Threading: a graph handle is not re-entrant; calls on one handle must not
+ * overlap.  Different handles may be used from different threads.  The
+ * server API (la3g_server_*) is thread-safe for submit/poll.
+ *
+ * Every entry point below names the reference interface it stands in for.
+ * The reference has no C ABI of its own: it is a C++ template library whose
+ * plugin API is the VertexProgram<W, M, A, S> class
+ * (src/vprogram/vertex_program.h:21-383) driven by six app run() functions.
+ */
+#ifndef LA3G_H
+#define LA3G_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum la3g_status
+{
+  LA3G_OK = 0,
+  LA3G_EINVAL = 1,    /* bad argument (null handle, id out of range, wrong graph kind) */
+  LA3G_EIO = 2,       /* file cannot be opened or read                                 */
+  LA3G_EFORMAT = 3,   /* file is not a whole number of records, or bad header          */
+  LA3G_ENOMEM = 4,    /* host or device allocation failed                              */
+  LA3G_EBUDGET = 5,   /* server admission: request does not fit the HBM budget         */
+  LA3G_ETIMEOUT = 6,  /* a bounded device-side wait ran out                             */
+  LA3G_ECUDA = 7,     /* a CUDA runtime call failed                                     */
+  LA3G_EBUSY = 8,     /* server queue full / no result ready yet                        */
+} la3g_status;
+
+/* Load flags (Graph::load_directed / load_undirected / load_bipartite,
+ * src/matrix/graph.h:38-47).  No DIRECTED bit = undirected (each record is
+ * stored in both directions, graph.hpp:187-191). */
+enum la3g_load_flags
+{
+  LA3G_DIRECTED = 1u << 0,   /* transpose: messages flow along out-edges (graph.hpp:171-172)   */
+  LA3G_REVERSE = 1u << 1,    /* reverse_edges: no transpose                                     */
+  LA3G_ACYCLIC = 1u << 2,    /* remove_cycles: orient every edge by original id (:174-179)     */
+  LA3G_BIPARTITE = 1u << 3,  /* left = docs 1..n, right = terms shifted by n (:162-163)        */
+  LA3G_WEIGHTED = 1u << 4,   /* records are {u32 src, u32 dst, u32 weight} triples              */
+};
+
+typedef struct la3g_graph la3g_graph;
+
+typedef struct la3g_graph_info
+{
+  uint32_t nslots;      /* n + 1                                                  */
+  uint32_t nvertices;   /* n                                                      */
+  uint32_t nleft;       /* bipartite: ndocs                                       */
+  uint32_t flags;
+  uint64_t nrecords;    /* records read                                           */
+  uint64_t nentries;    /* stored entries after self-loop removal and dedup       */
+  uint32_t nregular, nsink, nsource, nisolated;  /* processed_matrix2d.hpp:203-228 */
+  uint64_t device_bytes; /* HBM held by the graph                                  */
+} la3g_graph_info;
+
+typedef struct la3g_stats
+{
+  double device_ms;      /* device time of the call's compute (CUDA events)              */
+  double host_ms;        /* wall time of the whole call, copies included                 */
+  uint32_t iterations;   /* BSP iterations run                                            */
+  uint32_t pull_iterations; /* of which ran bottom-up / pull                             */
+  uint64_t teps_edges;   /* numerator of the app's GTEPS definition                       */
+  uint64_t edges_examined; /* edges the kernels read (algorithmic-byte accounting)        */
+  uint64_t algo_bytes;   /* algorithmic bytes of the call's kernels                       */
+  uint32_t kernel_launches; /* kernels launched by the call                               */
+  uint32_t reserved;
+} la3g_stats;
+
+/* Edge lists produced by the generators (host memory, owned by the library
+ * until la3g_edges_free). */
+typedef struct la3g_edges
+{
+  uint32_t* src;
+  uint32_t* dst;
+  uint32_t* w;        /* NULL when unweighted */
+  uint64_t m;
+  uint32_t n;         /* vertices (bipartite: ndocs) */
+  uint32_t nright;    /* bipartite: nterms, else 0   */
+  int weighted;
+  int reserved;
+} la3g_edges;
+
+/* ---- errors ------------------------------------------------------------ */
+
+const char* la3g_last_error_string(void);
+const char* la3g_status_string(int status);
+
+/* ---- graphs: replaces Graph<W>::load_binary and its wrappers
+ *      (src/matrix/graph.hpp:37-214, 224-258) -------------------------- */
+
+/* Loads an LA3 binary edge list and builds the device matrix.  n = number of
+ * vertices as on the app command line (0: read the 16-byte header);
+ * nright = nterms for LA3G_BIPARTITE, else ignored. */
+int la3g_graph_load(const char* path, uint32_t n, uint32_t nright, uint32_t flags, la3g_graph** out);
+
+/* Same, from LA3 records already in host memory (8-byte pairs or 12-byte
+ * triples, as on disk, no header). */
+int la3g_graph_from_records(const void* records, uint64_t nrecords, uint32_t n, uint32_t nright,
+                            uint32_t flags, la3g_graph** out);
+
+/* Same, from a generator's edge list (n = 0: use e->n / e->nright). */
+int la3g_graph_from_edges(const la3g_edges* e, uint32_t n, uint32_t nright, uint32_t flags,
+                          la3g_graph** out);
+
+void la3g_graph_free(la3g_graph* g);
+int la3g_graph_info_get(const la3g_graph* g, la3g_graph_info* out);
+
+/* Reverse-engine view: vertex id -> internal position (Locator order
+ * regular, sink, source, isolated; src/utils/locator.h:84-120).  Either
+ * array may be NULL. */
+int la3g_graph_positions(const la3g_graph* g, uint32_t* pos_of_id, uint32_t* id_of_pos);
+
+/* ---- apps (replace the six app run() functions) ------------------------ */
+
+/* PageRank, FP64, un-normalised, alpha = 0.15: the reference pr app
+ * (src/apps/graph_analytics/pr.cpp:11-55, pr.h:12-46) on a graph loaded with
+ * LA3G_DIRECTED.  iters = 0 runs until no rank moves by more than 1e-5.
+ * Sums follow the reference's order, so ranks are bit-identical to it. */
+int la3g_pr(la3g_graph* g, uint32_t iters, double* rank_out, uint32_t* degree_out, la3g_stats* st);
+
+/* PageRank with FP32 SpMV and FP32 accumulation (precision study); the
+ * residual (L1 of the rank change) and the dangling mass stay FP64.  Stops
+ * after iters iterations or when the L1 residual drops below tol (tol <= 0:
+ * fixed iterations).  residual_out: last L1 residual. */
+int la3g_pr_f32(la3g_graph* g, uint32_t iters, double tol, double* rank_out, double* residual_out,
+                la3g_stats* st);
+
+/* BFS (src/apps/graph_analytics/bfs.cpp:11-37, bfs.h:11-49) on an undirected
+ * graph: hops (uint8, 255 = unreached) and parent (the hashed id of the
+ * frontier neighbour that the reference writes last, i.e. the largest).
+ * Either output may be NULL (results stay on the device). */
+int la3g_bfs(la3g_graph* g, uint32_t root, uint8_t* hops_out, uint32_t* parent_out, la3g_stats* st);
+
+/* SSSP (src/apps/graph_analytics/sssp.cpp:11-37, sssp.h:11-46) on a graph
+ * loaded with LA3G_DIRECTED | LA3G_WEIGHTED: uint32 distances,
+ * 2147483647 = unreached. */
+int la3g_sssp(la3g_graph* g, uint32_t root, uint32_t* dist_out, la3g_stats* st);
+
+/* Connected components (src/apps/graph_analytics/cc.cpp:11-31, cc.h:11-38)
+ * on an undirected graph: labels as the reference computes them (the least
+ * vertex id of each component when vertex 0 has no edges). */
+int la3g_cc(la3g_graph* g, uint32_t* label_out, la3g_stats* st);
+
+/* Triangle counting (src/apps/graph_analytics/tc.cpp:11-52, tc.h:47-99) on
+ * a graph loaded with LA3G_DIRECTED | LA3G_ACYCLIC: total and, per vertex,
+ * the triangles in which it is the middle vertex by id (uint32, wrapping as
+ * the reference's accumulator does).  per_vertex_out may be NULL. */
+int la3g_tc(la3g_graph* g, uint64_t* total_out, uint32_t* per_vertex_out, la3g_stats* st);
+
+/* BM25 (src/apps/information_retrieval/bm25.cpp:8-114, bm25.h:11-92) on a
+ * graph loaded with LA3G_BIPARTITE (undirected).  prepare runs the IDF and
+ * the two doc-length passes; length_out (nslots, nullable) receives the
+ * state each vertex holds afterwards (idf for terms, K(d) for docs). */
+int la3g_bm25_prepare(la3g_graph* g, uint64_t* collection_ntokens_out, float* avg_doc_length_out,
+                      float* length_out);
+
+/* One query: term_vids are term VERTEX ids (ndocs + term index) in query
+ * order, as prepare_queries produces them (helpers.hpp:76-123); the
+ * reference's pairing of values with terms for non-ascending lists is kept.
+ * Writes the first min(k, touched) docs in the order score desc, id asc.
+ * all_scores_out (nslots floats) and active_out (nslots bytes) are optional
+ * full dumps of the scored docs. */
+int la3g_bm25_query(la3g_graph* g, const uint32_t* term_vids, uint32_t nterms, uint32_t k,
+                    uint32_t* ids_out, float* scores_out, uint32_t* nout, float* all_scores_out,
+                    uint8_t* active_out, la3g_stats* st);
+
+/* ---- batched multi-source forms (no reference counterpart; the reference
+ *      runs one root per VertexProgram, bfs.cpp:11-37 / sssp.cpp:11-37) ---- */
+
+/* hops_out: nroots x nslots bytes, row r = la3g_bfs(roots[r]) hops. */
+int la3g_bfs_batch(la3g_graph* g, const uint32_t* roots, uint32_t nroots, uint8_t* hops_out,
+                   la3g_stats* st);
+/* dist_out: nroots x nslots uint32, row r = la3g_sssp(roots[r]) distances. */
+int la3g_sssp_batch(la3g_graph* g, const uint32_t* roots, uint32_t nroots, uint32_t* dist_out,
+                    la3g_stats* st);
+
+/* ---- synthetic inputs -------------------------------------------------- */
+
+int la3g_gen_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c, uint64_t seed,
+                  int weighted, uint64_t wseed, la3g_edges* out);
+int la3g_gen_er(uint32_t n, uint64_t m, uint64_t seed, int weighted, uint64_t wseed, la3g_edges* out);
+int la3g_gen_bipartite(uint32_t ndocs, uint32_t nterms, uint32_t terms_per_doc, double zipf_s,
+                       double df_cap, uint64_t seed, la3g_edges* out);
+/* Writes LA3 binary records (the layout tools/mtx2bin.cpp:77-111 writes),
+ * with the 16-byte header when header != 0. */
+int la3g_edges_write(const la3g_edges* e, const char* path, int header);
+void la3g_edges_free(la3g_edges* e);
+
+/* ---- measurement ------------------------------------------------------- */
+
+/* When on, every kernel launch of the library is bracketed by CUDA events on
+ * its stream and its time is accumulated per kernel name. */
+void la3g_profile_enable(int on);
+void la3g_profile_reset(void);
+/* JSON object {"kernel": {"launches": L, "ms": T, "bytes": B}, ...}; returns
+ * the length needed (excluding the terminating NUL). */
+size_t la3g_profile_report(char* buf, size_t cap);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,314 @@
+"""la3_gb300 — GB300-native LA3 vertex-program engine (host-side mirror).
+
+The reference's user-facing surface is the `Graph<W>::load_*` calls
+(src/matrix/graph.h:38-47) and the six apps' `run()` functions
+(src/apps/graph_analytics/*.cpp, src/apps/information_retrieval/bm25.cpp).
+This module exposes the same loads and apps over the native C ABI
+(include/la3g.h); every result is a numpy array indexed by vertex id with
+n + 1 slots, as the reference's per-vertex states are.
+
+Nothing here computes on the CPU: every call goes to libla3g, which runs
+on the GPU, and a missing library raises at first use.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _native as N
+from ._native import LA3GError, Stats
+
+DIRECTED = 1
+REVERSE = 2
+ACYCLIC = 4
+BIPARTITE = 8
+WEIGHTED = 16
+
+SSSP_INF = 0x7FFFFFFF
+BFS_INF = 255
+
+
+def _ptr(a: Optional[np.ndarray], ctype):
+    if a is None:
+        return None
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+@dataclass
+class Info:
+    nslots: int
+    nvertices: int
+    nleft: int
+    flags: int
+    nrecords: int
+    nentries: int
+    nregular: int
+    nsink: int
+    nsource: int
+    nisolated: int
+    device_bytes: int
+
+
+class Graph:
+    """A device-resident graph (Graph<W> + its CSCMatrix2D in the reference)."""
+
+    def __init__(self, handle: C.c_void_p, flags: int):
+        self._h = handle
+        self.flags = flags
+        self.info = self._info()
+
+    # -- loads (graph.hpp:224-258) ------------------------------------------
+    @classmethod
+    def load(cls, path: str, n: int, flags: int, nright: int = 0) -> "Graph":
+        h = C.c_void_p()
+        N.check(N.lib().la3g_graph_load(str(path).encode(), n, nright, flags, C.byref(h)))
+        return cls(h, flags)
+
+    @classmethod
+    def load_directed(cls, path: str, n: int, reverse_edges: bool = False, remove_cycles: bool = False,
+                      weighted: bool = False) -> "Graph":
+        f = DIRECTED | (REVERSE if reverse_edges else 0) | (ACYCLIC if remove_cycles else 0)
+        return cls.load(path, n, f | (WEIGHTED if weighted else 0))
+
+    @classmethod
+    def load_undirected(cls, path: str, n: int, weighted: bool = False) -> "Graph":
+        return cls.load(path, n, WEIGHTED if weighted else 0)
+
+    @classmethod
+    def load_bipartite(cls, path: str, ndocs: int, nterms: int, directed: bool = False,
+                       weighted: bool = True) -> "Graph":
+        f = BIPARTITE | (DIRECTED if directed else 0) | (WEIGHTED if weighted else 0)
+        return cls.load(path, ndocs, f, nright=nterms)
+
+    @classmethod
+    def from_records(cls, records: np.ndarray, n: int, flags: int, nright: int = 0) -> "Graph":
+        rec = np.ascontiguousarray(records, dtype=np.uint32)
+        wpr = 3 if flags & WEIGHTED else 2
+        if rec.size % wpr:
+            raise ValueError("records must hold whole records")
+        h = C.c_void_p()
+        N.check(N.lib().la3g_graph_from_records(rec.ctypes.data_as(C.c_void_p), rec.size // wpr, n, nright, flags,
+                                                C.byref(h)))
+        return cls(h, flags)
+
+    @classmethod
+    def from_edges(cls, edges: "EdgeList", flags: int, n: int = 0, nright: int = 0) -> "Graph":
+        h = C.c_void_p()
+        N.check(N.lib().la3g_graph_from_edges(C.byref(edges._e), n, nright, flags, C.byref(h)))
+        return cls(h, flags)
+
+    def _info(self) -> Info:
+        gi = N.GraphInfo()
+        N.check(N.lib().la3g_graph_info_get(self._h, C.byref(gi)))
+        return Info(**{k: getattr(gi, k) for k, _ in gi._fields_})
+
+    @property
+    def nslots(self) -> int:
+        return self.info.nslots
+
+    def positions(self) -> tuple[np.ndarray, np.ndarray]:
+        pos = np.empty(self.nslots, np.uint32)
+        ids = np.empty(self.nslots, np.uint32)
+        N.check(N.lib().la3g_graph_positions(self._h, _ptr(pos, C.c_uint32), _ptr(ids, C.c_uint32)))
+        return pos, ids
+
+    def free(self) -> None:
+        if self._h:
+            N.lib().la3g_graph_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.free()
+
+
+# -- apps ------------------------------------------------------------------
+
+def pagerank(G: Graph, iters: int, want_rank: bool = True, want_degree: bool = True):
+    """pr.cpp:11-55: FP64 ranks (bit-identical to the reference) + out-degrees."""
+    st = Stats()
+    rank = np.empty(G.nslots, np.float64) if want_rank else None
+    deg = np.empty(G.nslots, np.uint32) if want_degree else None
+    N.check(N.lib().la3g_pr(G._h, iters, _ptr(rank, C.c_double), _ptr(deg, C.c_uint32), C.byref(st)))
+    return rank, deg, st
+
+
+def pagerank_f32(G: Graph, iters: int, tol: float = 0.0):
+    """FP32 SpMV / FP32 accumulation variant; returns (rank as f64, L1 residual, stats)."""
+    st = Stats()
+    rank = np.empty(G.nslots, np.float64)
+    res = C.c_double(0.0)
+    N.check(N.lib().la3g_pr_f32(G._h, iters, tol, _ptr(rank, C.c_double), C.byref(res), C.byref(st)))
+    return rank, res.value, st
+
+
+def bfs(G: Graph, root: int, want_hops: bool = True, want_parent: bool = True):
+    """bfs.cpp:11-37: (hops uint8 with 255 = unreached, parent hashed id, stats)."""
+    st = Stats()
+    hops = np.empty(G.nslots, np.uint8) if want_hops else None
+    parent = np.empty(G.nslots, np.uint32) if want_parent else None
+    N.check(N.lib().la3g_bfs(G._h, root, _ptr(hops, C.c_uint8), _ptr(parent, C.c_uint32), C.byref(st)))
+    return hops, parent, st
+
+
+def sssp(G: Graph, root: int, want_dist: bool = True):
+    """sssp.cpp:11-37: uint32 distances, 2147483647 = unreached."""
+    st = Stats()
+    dist = np.empty(G.nslots, np.uint32) if want_dist else None
+    N.check(N.lib().la3g_sssp(G._h, root, _ptr(dist, C.c_uint32), C.byref(st)))
+    return dist, st
+
+
+def cc(G: Graph, want_labels: bool = True):
+    """cc.cpp:11-31: component labels."""
+    st = Stats()
+    lab = np.empty(G.nslots, np.uint32) if want_labels else None
+    N.check(N.lib().la3g_cc(G._h, _ptr(lab, C.c_uint32), C.byref(st)))
+    return lab, st
+
+
+def tc(G: Graph, want_per_vertex: bool = True):
+    """tc.cpp:11-52: (total, per-vertex middle-vertex counts, stats)."""
+    st = Stats()
+    total = C.c_uint64(0)
+    per = np.empty(G.nslots, np.uint32) if want_per_vertex else None
+    N.check(N.lib().la3g_tc(G._h, C.byref(total), _ptr(per, C.c_uint32), C.byref(st)))
+    return total.value, per, st
+
+
+class BM25:
+    """bm25.cpp:8-114 over a bipartite graph: prepare once, then query."""
+
+    def __init__(self, G: Graph, want_length: bool = False):
+        self.G = G
+        ntok = C.c_uint64(0)
+        avg = C.c_float(0)
+        self.length = np.empty(G.nslots, np.float32) if want_length else None
+        N.check(N.lib().la3g_bm25_prepare(G._h, C.byref(ntok), C.byref(avg), _ptr(self.length, C.c_float)))
+        self.collection_ntokens = ntok.value
+        self.avg_doc_length = avg.value
+
+    def query(self, term_vids: Sequence[int], k: int = 10, full: bool = False):
+        q = np.ascontiguousarray(np.asarray(term_vids, dtype=np.uint32))
+        ids = np.empty(max(k, 1), np.uint32)
+        scores = np.empty(max(k, 1), np.float32)
+        nout = C.c_uint32(0)
+        st = Stats()
+        alls = np.empty(self.G.nslots, np.float32) if full else None
+        act = np.empty(self.G.nslots, np.uint8) if full else None
+        N.check(N.lib().la3g_bm25_query(self.G._h, _ptr(q, C.c_uint32), q.size, k, _ptr(ids, C.c_uint32),
+                                        _ptr(scores, C.c_float), C.byref(nout), _ptr(alls, C.c_float),
+                                        _ptr(act, C.c_uint8), C.byref(st)))
+        n = nout.value
+        return ids[:n].copy(), scores[:n].copy(), (alls, act), st
+
+
+def bfs_batch(G: Graph, roots: Sequence[int], want_hops: bool = True):
+    r = np.ascontiguousarray(np.asarray(roots, dtype=np.uint32))
+    st = Stats()
+    hops = np.empty((r.size, G.nslots), np.uint8) if want_hops else None
+    N.check(N.lib().la3g_bfs_batch(G._h, _ptr(r, C.c_uint32), r.size, _ptr(hops, C.c_uint8), C.byref(st)))
+    return hops, st
+
+
+def sssp_batch(G: Graph, roots: Sequence[int], want_dist: bool = True):
+    r = np.ascontiguousarray(np.asarray(roots, dtype=np.uint32))
+    st = Stats()
+    dist = np.empty((r.size, G.nslots), np.uint32) if want_dist else None
+    N.check(N.lib().la3g_sssp_batch(G._h, _ptr(r, C.c_uint32), r.size, _ptr(dist, C.c_uint32), C.byref(st)))
+    return dist, st
+
+
+# -- synthetic inputs ---------------------------------------------------------
+
+class EdgeList:
+    """A generator's edge list (host memory owned by libla3g)."""
+
+    def __init__(self):
+        self._e = N.Edges()
+
+    @classmethod
+    def rmat(cls, scale: int, edge_factor: int = 16, a: float = 0.57, b: float = 0.19, c: float = 0.19,
+             seed: int = 1, weighted: bool = False, wseed: int = 2) -> "EdgeList":
+        e = cls()
+        N.check(N.lib().la3g_gen_rmat(scale, edge_factor, a, b, c, seed, int(weighted), wseed, C.byref(e._e)))
+        return e
+
+    @classmethod
+    def er(cls, n: int, m: int, seed: int = 1, weighted: bool = False, wseed: int = 2) -> "EdgeList":
+        e = cls()
+        N.check(N.lib().la3g_gen_er(n, m, seed, int(weighted), wseed, C.byref(e._e)))
+        return e
+
+    @classmethod
+    def bipartite(cls, ndocs: int, nterms: int, terms_per_doc: int = 50, zipf_s: float = 1.1, df_cap: float = 0.9,
+                  seed: int = 1) -> "EdgeList":
+        e = cls()
+        N.check(N.lib().la3g_gen_bipartite(ndocs, nterms, terms_per_doc, zipf_s, df_cap, seed, C.byref(e._e)))
+        return e
+
+    @property
+    def m(self) -> int:
+        return self._e.m
+
+    @property
+    def n(self) -> int:
+        return self._e.n
+
+    @property
+    def nright(self) -> int:
+        return self._e.nright
+
+    def arrays(self) -> tuple[np.ndarray, np.ndarray, Optional[np.ndarray]]:
+        m = self._e.m
+        src = np.ctypeslib.as_array(self._e.src, shape=(m,)).copy() if m else np.empty(0, np.uint32)
+        dst = np.ctypeslib.as_array(self._e.dst, shape=(m,)).copy() if m else np.empty(0, np.uint32)
+        w = None
+        if self._e.weighted and m:
+            w = np.ctypeslib.as_array(self._e.w, shape=(m,)).copy()
+        return src, dst, w
+
+    def write(self, path: str, header: bool = False) -> None:
+        N.check(N.lib().la3g_edges_write(C.byref(self._e), str(path).encode(), int(header)))
+
+    def free(self) -> None:
+        N.lib().la3g_edges_free(C.byref(self._e))
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def profile(on: bool = True) -> None:
+    N.lib().la3g_profile_enable(int(on))
+
+
+def profile_reset() -> None:
+    N.lib().la3g_profile_reset()
+
+
+def profile_report() -> dict:
+    import json
+    L = N.lib()
+    n = L.la3g_profile_report(None, 0)
+    buf = C.create_string_buffer(n + 1)
+    L.la3g_profile_report(buf, n + 1)
+    return json.loads(buf.value.decode())
+
+
+__all__ = ["Graph", "EdgeList", "BM25", "LA3GError", "Stats", "pagerank", "pagerank_f32", "bfs", "sssp", "cc", "tc",
+           "bfs_batch", "sssp_batch", "profile", "profile_reset", "profile_report", "DIRECTED", "REVERSE", "ACYCLIC",
+           "BIPARTITE", "WEIGHTED", "SSSP_INF", "BFS_INF"]

@@ -1,0 +1,396 @@
+// BFS: the reference bfs app (src/apps/graph_analytics/bfs.cpp:11-37,
+// bfs.h:11-49) on the device, direction-optimising.
+//
+// Reference semantics kept exactly (np = 1):
+//   * hops are uint8 with 255 = unvisited; apply at iteration i sets
+//     hops = (uint8)(i + 1) on a touched vertex whose hops are 255
+//     (bfs.h:41-48); the loop stops after the first iteration that activates
+//     nothing (execute_non_opt, vertex_program_execute.hpp:166-248);
+//   * parent: gather returns edge.src (the hashed id of the column) and
+//     combine keeps the last value written (bfs.h:39-40).  The SpMV walks the
+//     active columns in ascending position = ascending hashed id, so the
+//     last writer of a row is its frontier neighbour with the LARGEST hashed
+//     id.  Top-down keeps it with atomicMax; bottom-up scans a vertex's
+//     neighbours from the highest position down and stops at the first one
+//     in the frontier, which is that same neighbour.
+//
+// Direction switching follows Beamer et al. (alpha = 14, beta = 24): go
+// bottom-up when the frontier's edges exceed the unvisited edges / alpha,
+// back top-down when the frontier holds fewer than n / beta vertices.
+#include <algorithm>
+#include <cstring>
+
+#include "la3g_internal.h"
+
+namespace la3g {
+
+struct BfsCounters
+{
+  unsigned long long next_count;   // vertices activated this iteration
+  unsigned long long next_degsum;  // their degrees
+};
+
+struct BfsScratch
+{
+  uint8_t* hops = nullptr;
+  uint32_t* parent = nullptr;
+  uint32_t* cand = nullptr;        // top-down parent candidate + 1 (0 = none)
+  uint32_t* list[2] = {nullptr, nullptr};
+  uint32_t* bits[2] = {nullptr, nullptr};
+  BfsCounters* ctr = nullptr;      // device
+  BfsCounters* hctr = nullptr;     // pinned host mirror
+  unsigned long long* red = nullptr;  // reduction scratch
+  uint32_t words = 0;
+};
+
+static void bfs_scratch_free(void* p)
+{
+  BfsScratch* s = (BfsScratch*) p;
+  if (s->hctr) cudaFreeHost(s->hctr);
+  delete s;
+}
+
+__global__ void k_bfs_init(uint32_t N, uint8_t* hops, uint32_t* parent, uint32_t* cand)
+{
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x)
+  {
+    hops[p] = 255;
+    parent[p] = 0;
+    cand[p] = 0;
+  }
+}
+
+// Top-down: one warp per frontier vertex, lanes over its neighbours.
+__global__ void __launch_bounds__(256)
+k_bfs_td(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ hash_of_pos,
+         const uint32_t* __restrict__ front, uint32_t nfront, const uint8_t* __restrict__ hops, uint32_t* cand,
+         uint32_t* next, BfsCounters* ctr)
+{
+  const int lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t f = warp; f < nfront; f += nwarps)
+  {
+    const uint32_t u = front[f];
+    const uint32_t hu = hash_of_pos[u] + 1;
+    const uint32_t b = ptr[u], e = ptr[u + 1];
+    for (uint32_t i0 = b; i0 < e; i0 += 32)
+    {
+      const uint32_t i = i0 + lane;
+      bool add = false;
+      uint32_t v = 0;
+      if (i < e)
+      {
+        v = col[i];
+        if (hops[v] == 255)
+        {
+          uint32_t old = atomicMax(&cand[v], hu);
+          add = old == 0;
+        }
+      }
+      const unsigned mask = __ballot_sync(0xffffffffu, add);
+      if (mask)
+      {
+        uint32_t base = 0;
+        if (lane == 0) base = (uint32_t) atomicAdd(&ctr->next_count, (unsigned long long) __popc(mask));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (add) next[base + __popc(mask & ((1u << lane) - 1))] = v;
+      }
+    }
+  }
+}
+
+// Top-down apply: the newly touched vertices take hops and parent.
+__global__ void k_bfs_td_apply(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ next, uint32_t n,
+                               uint8_t hop, uint8_t* hops, uint32_t* parent, uint32_t* cand, BfsCounters* ctr)
+{
+  unsigned long long deg = 0;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+  {
+    uint32_t v = next[i];
+    hops[v] = hop;
+    parent[v] = cand[v] - 1;
+    cand[v] = 0;
+    deg += ptr[v + 1] - ptr[v];
+  }
+  for (int o = 16; o > 0; o >>= 1) deg += __shfl_xor_sync(0xffffffffu, deg, o);
+  if ((threadIdx.x & 31) == 0 && deg) atomicAdd(&ctr->next_degsum, deg);
+}
+
+// Bottom-up: one thread per unvisited vertex, neighbours from the highest
+// position down; the first frontier neighbour is the parent.
+__global__ void __launch_bounds__(256)
+k_bfs_bu(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ hash_of_pos,
+         uint32_t nrows, const uint32_t* __restrict__ fbits, uint32_t* nbits, uint8_t hop, uint8_t* hops,
+         uint32_t* parent, BfsCounters* ctr)
+{
+  unsigned long long cnt = 0, deg = 0;
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nrows; v += gridDim.x * blockDim.x)
+  {
+    if (hops[v] != 255) continue;
+    const uint32_t b = ptr[v], e = ptr[v + 1];
+    for (uint32_t i = e; i > b; i--)
+    {
+      const uint32_t u = col[i - 1];
+      if (fbits[u >> 5] & (1u << (u & 31)))
+      {
+        hops[v] = hop;
+        parent[v] = hash_of_pos[u];
+        atomicOr(&nbits[v >> 5], 1u << (v & 31));
+        cnt++;
+        deg += e - b;
+        break;
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1)
+  {
+    cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    deg += __shfl_xor_sync(0xffffffffu, deg, o);
+  }
+  if ((threadIdx.x & 31) == 0 && cnt)
+  {
+    atomicAdd(&ctr->next_count, cnt);
+    atomicAdd(&ctr->next_degsum, deg);
+  }
+}
+
+__global__ void k_list_to_bits(const uint32_t* __restrict__ list, uint32_t n, uint32_t* bits)
+{
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+  {
+    uint32_t v = list[i];
+    atomicOr(&bits[v >> 5], 1u << (v & 31));
+  }
+}
+
+__global__ void k_bits_to_list(const uint32_t* __restrict__ bits, uint32_t words, uint32_t* list, unsigned long long* count)
+{
+  const int lane = threadIdx.x & 31;
+  for (uint32_t w0 = blockIdx.x * blockDim.x; w0 < words; w0 += gridDim.x * blockDim.x)
+  {
+    uint32_t w = w0 + threadIdx.x;
+    uint32_t x = w < words ? bits[w] : 0;
+    uint32_t c = __popc(x);
+    uint32_t incl = c;
+    for (int o = 1; o < 32; o <<= 1)
+    {
+      uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    uint32_t base = 0;
+    if (lane == 31 && total) base = (uint32_t) atomicAdd(count, (unsigned long long) total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    uint32_t o = base + incl - c;
+    while (x)
+    {
+      int bpos = __ffs(x) - 1;
+      x &= x - 1;
+      list[o++] = w * 32 + bpos;
+    }
+  }
+}
+
+__global__ void k_reached_degsum(const uint32_t* __restrict__ ptr, const uint8_t* __restrict__ hops, uint32_t nrows,
+                                 unsigned long long* out)
+{
+  unsigned long long s = 0;
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nrows; v += gridDim.x * blockDim.x)
+    if (hops[v] != 255) s += ptr[v + 1] - ptr[v];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0 && s) atomicAdd(out, s);
+}
+
+template <class T>
+__global__ void k_by_id(uint32_t N, const uint32_t* __restrict__ id_of_pos, const T* __restrict__ val, T* __restrict__ out)
+{
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) out[id_of_pos[p]] = val[p];
+}
+
+__global__ void k_bfs_root(uint32_t rp, uint8_t* hops, uint32_t* list) { hops[rp] = 0; list[0] = rp; }
+
+static int bfs_scratch(la3g_graph* G, BfsScratch** out)
+{
+  BfsScratch* bs = (BfsScratch*) G->slot[kSlotBfs];
+  if (bs) { *out = bs; return LA3G_OK; }
+  bs = new (std::nothrow) BfsScratch();
+  if (!bs) return set_error(LA3G_ENOMEM, "out of host memory");
+  G->slot[kSlotBfs] = bs;
+  G->slot_free[kSlotBfs] = bfs_scratch_free;
+  const uint32_t N = G->g.nslots;
+  bs->words = (N + 31) / 32 + 1;
+  LA3G_TRY(galloc(G, &bs->hops, N));
+  LA3G_TRY(galloc(G, &bs->parent, N));
+  LA3G_TRY(galloc(G, &bs->cand, N));
+  LA3G_TRY(galloc(G, &bs->list[0], N));
+  LA3G_TRY(galloc(G, &bs->list[1], N));
+  LA3G_TRY(galloc(G, &bs->bits[0], bs->words));
+  LA3G_TRY(galloc(G, &bs->bits[1], bs->words));
+  LA3G_TRY(galloc(G, &bs->ctr, 1));
+  LA3G_TRY(galloc(G, &bs->red, 1));
+  LA3G_CUDA(cudaHostAlloc(&bs->hctr, sizeof(BfsCounters), cudaHostAllocDefault));
+  *out = bs;
+  return LA3G_OK;
+}
+
+// Runs BFS from `root` with results left on the device (positions).
+static int bfs_run(la3g_graph* G, BfsScratch* bs, uint32_t root, la3g_stats* st)
+{
+  DevGraph& g = G->g;
+  cudaStream_t s = G->stream;
+  const uint32_t N = g.nslots, nrows = g.nrows();
+  k_bfs_init<<<grid_for(N, 256), 256, 0, s>>>(N, bs->hops, bs->parent, bs->cand);
+  LA3G_LAUNCHED();
+  tls_launches++;
+  uint32_t iter = 0, pull_iters = 0;
+  if (root >= N)
+  {
+    if (st) st->iterations = 1;
+    return LA3G_OK;  // no vertex matches the root: every hop stays 255
+  }
+  uint32_t rp = 0;
+  LA3G_CUDA(cudaMemcpyAsync(&rp, g.pos_of_id + root, 4, cudaMemcpyDeviceToHost, s));
+  LA3G_CUDA(cudaStreamSynchronize(s));
+  k_bfs_root<<<1, 1, 0, s>>>(rp, bs->hops, bs->list[0]);
+  LA3G_LAUNCHED();
+  tls_launches++;
+  // An isolated root has no edges: iteration 0 activates nothing.
+  uint64_t nfront = rp < nrows ? 1 : 0;
+  uint32_t h_ptr[2];
+  LA3G_CUDA(cudaMemcpyAsync(h_ptr, g.in_ptr + rp, 8, cudaMemcpyDeviceToHost, s));
+  LA3G_CUDA(cudaStreamSynchronize(s));
+  uint64_t front_deg = nfront ? h_ptr[1] - h_ptr[0] : 0;
+  uint64_t unvisited_deg = g.nent - front_deg;
+  bool bottom_up = false, front_is_list = true;
+  int cur = 0;
+  const double alpha = 14.0, beta = 24.0;
+  uint64_t edges_examined = 0;
+  for (;;)
+  {
+    if (iter > 100000) return set_error(LA3G_ETIMEOUT, "bfs did not converge");
+    // choose direction
+    if (!bottom_up && (double) front_deg > (double) unvisited_deg / alpha) bottom_up = true;
+    else if (bottom_up && (double) nfront < (double) N / beta) bottom_up = false;
+    LA3G_CUDA(cudaMemsetAsync(bs->ctr, 0, sizeof(BfsCounters), s));
+    const uint8_t hop = (uint8_t) (iter + 1);
+    if (nfront == 0)
+    {
+      iter++;
+      break;  // nothing active: this iteration activates nothing
+    }
+    if (bottom_up)
+    {
+      if (front_is_list)
+      {
+        LA3G_CUDA(cudaMemsetAsync(bs->bits[cur], 0, (size_t) bs->words * 4, s));
+        k_list_to_bits<<<grid_for(nfront, 256), 256, 0, s>>>(bs->list[cur], (uint32_t) nfront, bs->bits[cur]);
+        LA3G_LAUNCHED();
+        tls_launches++;
+      }
+      LA3G_CUDA(cudaMemsetAsync(bs->bits[cur ^ 1], 0, (size_t) bs->words * 4, s));
+      {
+        ProfileScope p("bfs_bottom_up", s, 4.0 * unvisited_deg + 8.0 * nrows + N / 8.0);
+        k_bfs_bu<<<grid_for(nrows, 256, kSMs * 16), 256, 0, s>>>(g.in_ptr, g.in_col, g.hash_of_pos, nrows, bs->bits[cur],
+                                                                bs->bits[cur ^ 1], hop, bs->hops, bs->parent, bs->ctr);
+        LA3G_LAUNCHED();
+      }
+      edges_examined += unvisited_deg;
+      front_is_list = false;
+      pull_iters++;
+    }
+    else
+    {
+      if (!front_is_list)
+      {
+        LA3G_CUDA(cudaMemsetAsync(bs->red, 0, 8, s));
+        k_bits_to_list<<<grid_for(bs->words, 256), 256, 0, s>>>(bs->bits[cur], bs->words, bs->list[cur], bs->red);
+        LA3G_LAUNCHED();
+        tls_launches++;
+      }
+      {
+        ProfileScope p("bfs_top_down", s, 4.0 * front_deg + 8.0 * nfront + 1.0 * front_deg);
+        k_bfs_td<<<grid_for(nfront * 32, 256), 256, 0, s>>>(g.in_ptr, g.in_col, g.hash_of_pos, bs->list[cur], (uint32_t) nfront,
+                                                            bs->hops, bs->cand, bs->list[cur ^ 1], bs->ctr);
+        LA3G_LAUNCHED();
+      }
+      edges_examined += front_deg;
+      LA3G_CUDA(cudaMemcpyAsync(bs->hctr, bs->ctr, sizeof(BfsCounters), cudaMemcpyDeviceToHost, s));
+      LA3G_CUDA(cudaStreamSynchronize(s));
+      uint32_t nn = (uint32_t) bs->hctr->next_count;
+      if (nn)
+      {
+        k_bfs_td_apply<<<grid_for(nn, 256), 256, 0, s>>>(g.in_ptr, bs->list[cur ^ 1], nn, hop, bs->hops, bs->parent,
+                                                         bs->cand, bs->ctr);
+        LA3G_LAUNCHED();
+        tls_launches++;
+      }
+      front_is_list = true;
+    }
+    LA3G_CUDA(cudaMemcpyAsync(bs->hctr, bs->ctr, sizeof(BfsCounters), cudaMemcpyDeviceToHost, s));
+    LA3G_CUDA(cudaStreamSynchronize(s));
+    nfront = bs->hctr->next_count;
+    front_deg = bs->hctr->next_degsum;
+    unvisited_deg -= std::min<uint64_t>(unvisited_deg, front_deg);
+    cur ^= 1;
+    iter++;
+    if (nfront == 0) break;
+  }
+  if (st)
+  {
+    st->iterations = iter;
+    st->pull_iterations = pull_iters;
+    st->edges_examined = edges_examined;
+  }
+  return LA3G_OK;
+}
+
+}  // namespace la3g
+
+using namespace la3g;
+
+extern "C" int la3g_bfs(la3g_graph* G, uint32_t root, uint8_t* hops_out, uint32_t* parent_out, la3g_stats* st)
+{
+  if (!G) return set_error(LA3G_EINVAL, "null graph");
+  DevGraph& g = G->g;
+  if (g.directed()) return set_error(LA3G_EINVAL, "bfs needs an undirected graph (load without LA3G_DIRECTED)");
+  CallTimer T(G, st);
+  BfsScratch* bs = nullptr;
+  LA3G_TRY(bfs_scratch(G, &bs));
+  cudaStream_t s = G->stream;
+  const uint32_t N = g.nslots;
+  T.device_begin();
+  LA3G_TRY(bfs_run(G, bs, root, st));
+  T.device_end();
+  if (st)
+  {
+    LA3G_CUDA(cudaMemsetAsync(bs->red, 0, 8, s));
+    k_reached_degsum<<<grid_for(g.nrows(), 256), 256, 0, s>>>(g.in_ptr, bs->hops, g.nrows(), bs->red);
+    LA3G_LAUNCHED();
+    unsigned long long sum = 0;
+    LA3G_CUDA(cudaMemcpyAsync(&sum, bs->red, 8, cudaMemcpyDeviceToHost, s));
+    LA3G_CUDA(cudaStreamSynchronize(s));
+    st->teps_edges = sum / 2;
+    st->algo_bytes = st->edges_examined * 4 + (uint64_t) N * 6;
+  }
+  if (hops_out || parent_out)
+  {
+    DevBuf tmp;
+    LA3G_TRY(tmp.alloc((size_t) N * 4));
+    if (hops_out)
+    {
+      k_by_id<uint8_t><<<grid_for(N, 256), 256, 0, s>>>(N, g.id_of_pos, bs->hops, tmp.as<uint8_t>());
+      LA3G_LAUNCHED();
+      LA3G_CUDA(cudaMemcpyAsync(hops_out, tmp.p, N, cudaMemcpyDeviceToHost, s));
+      LA3G_CUDA(cudaStreamSynchronize(s));
+    }
+    if (parent_out)
+    {
+      k_by_id<uint32_t><<<grid_for(N, 256), 256, 0, s>>>(N, g.id_of_pos, bs->parent, tmp.as<uint32_t>());
+      LA3G_LAUNCHED();
+      LA3G_CUDA(cudaMemcpyAsync(parent_out, tmp.p, (size_t) N * 4, cudaMemcpyDeviceToHost, s));
+      LA3G_CUDA(cudaStreamSynchronize(s));
+    }
+  }
+  return T.finish();
+}

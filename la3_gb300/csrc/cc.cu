@@ -1,0 +1,249 @@
+// Connected components: the reference cc app (src/apps/graph_analytics/
+// cc.cpp:11-31, cc.h:11-38) on the device.
+//
+// The reference propagates labels (initially the vertex's own id) with
+// combine y2 = (y2 == 0) ? y1 : min(y1, y2) until nothing changes.  When
+// vertex 0 has no edges no label is ever 0, combine is a plain min, and
+// the fixed point is: every vertex with edges carries the least id of its
+// component, every isolated vertex its own id.  That fixed point is computed
+// here with a lock-free union-find whose roots are always the least id of
+// their set (a root is only ever hooked under a root with a smaller id),
+// followed by full path compression.
+//
+// When vertex 0 does have edges, label 0 behaves as "no value yet" and the
+// outcome depends on the order messages arrive in, so that case runs the
+// reference's BSP iterations literally: each row folds the messages of its
+// active in-neighbours in ascending column order with the reference's
+// combine.
+#include <algorithm>
+#include <cstring>
+
+#include "la3g_internal.h"
+
+namespace la3g {
+
+struct CcScratch
+{
+  uint32_t* label = nullptr;   // by original id (union-find parents)
+  uint32_t* lab_pos = nullptr; // BSP path: labels by position
+  uint32_t* msg = nullptr;
+  uint8_t* active[2] = {nullptr, nullptr};
+  int* flag = nullptr;
+};
+
+static void cc_scratch_free(void* p) { delete (CcScratch*) p; }
+
+__global__ void k_cc_init(uint32_t N, uint32_t* parent)
+{
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < N; v += gridDim.x * blockDim.x) parent[v] = v;
+}
+
+__device__ __forceinline__ uint32_t cc_find(uint32_t* parent, uint32_t v)
+{
+  // path halving; concurrent halving writes only ever point further up
+  uint32_t p = parent[v];
+  while (p != v)
+  {
+    uint32_t gp = parent[p];
+    if (gp != p) parent[v] = gp;
+    v = p;
+    p = gp;
+  }
+  return v;
+}
+
+// One warp per row (position u), lanes over its neighbours v > u; every
+// undirected edge is united once.  Vertices are handled by original id.
+__global__ void __launch_bounds__(256)
+k_cc_hook(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ id_of_pos,
+          uint32_t nrows, uint32_t* parent)
+{
+  const int lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t u = warp; u < nrows; u += nwarps)
+  {
+    const uint32_t b = ptr[u], e = ptr[u + 1];
+    const uint32_t iu = id_of_pos[u];
+    for (uint32_t i = b + lane; i < e; i += 32)
+    {
+      const uint32_t v = col[i];
+      if (v <= u) continue;
+      uint32_t ru = cc_find(parent, iu), rv = cc_find(parent, id_of_pos[v]);
+      while (ru != rv)
+      {
+        if (ru > rv) { uint32_t t = ru; ru = rv; rv = t; }
+        // hook the larger root under the smaller one
+        uint32_t old = atomicCAS(&parent[rv], rv, ru);
+        if (old == rv) break;
+        rv = cc_find(parent, old);
+        ru = cc_find(parent, ru);
+      }
+    }
+  }
+}
+
+__global__ void k_cc_flatten(uint32_t N, uint32_t* parent)
+{
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < N; v += gridDim.x * blockDim.x)
+  {
+    uint32_t r = v;
+    while (parent[r] != r) r = parent[r];
+    parent[v] = r;
+  }
+}
+
+// ---- literal BSP path (vertex 0 has edges) ---------------------------------
+
+__global__ void k_ccb_init(uint32_t N, uint32_t nrows, const uint32_t* __restrict__ id_of_pos, uint32_t* lab,
+                           uint32_t* msg, uint8_t* act)
+{
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x)
+  {
+    lab[p] = id_of_pos[p];  // init: label = vid, returns true (cc.h:28)
+    msg[p] = id_of_pos[p];
+    act[p] = p < nrows;     // regular vertices scatter
+  }
+}
+
+// One thread per row: fold active in-neighbours in column order.
+__global__ void k_ccb_step(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, uint32_t nrows,
+                           const uint8_t* __restrict__ act, uint8_t* next_act, const uint32_t* __restrict__ msg,
+                           uint32_t* lab, uint32_t* next_msg, int* flag)
+{
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += gridDim.x * blockDim.x)
+  {
+    uint32_t y = 0;
+    bool touched = false;
+    for (uint32_t i = ptr[r]; i < ptr[r + 1]; i++)
+    {
+      uint32_t c = col[i];
+      if (!act[c]) continue;
+      uint32_t m = msg[c];
+      y = (y == 0) ? m : min(m, y);
+      touched = true;
+    }
+    bool activated = false;
+    if (touched)
+    {
+      uint32_t f = 0;
+      f = (f == 0) ? y : min(y, f);  // combine(partial, A())
+      uint32_t old = lab[r];
+      uint32_t nl = min(old, f);
+      lab[r] = nl;
+      activated = nl != old;
+    }
+    next_act[r] = activated;
+    if (activated) { next_msg[r] = lab[r]; *flag = 1; }
+  }
+}
+
+__global__ void k_ccb_copy_msg(uint32_t nrows, const uint8_t* __restrict__ act, const uint32_t* __restrict__ src,
+                               uint32_t* dst)
+{
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += gridDim.x * blockDim.x)
+    if (act[r]) dst[r] = src[r];
+}
+
+__global__ void k_ccb_by_id(uint32_t N, const uint32_t* __restrict__ id_of_pos, const uint32_t* __restrict__ lab,
+                            uint32_t* out)
+{
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) out[id_of_pos[p]] = lab[p];
+}
+
+static int cc_scratch(la3g_graph* G, CcScratch** out)
+{
+  CcScratch* cs = (CcScratch*) G->slot[kSlotCc];
+  if (cs) { *out = cs; return LA3G_OK; }
+  cs = new (std::nothrow) CcScratch();
+  if (!cs) return set_error(LA3G_ENOMEM, "out of host memory");
+  G->slot[kSlotCc] = cs;
+  G->slot_free[kSlotCc] = cc_scratch_free;
+  LA3G_TRY(galloc(G, &cs->label, G->g.nslots));
+  LA3G_TRY(galloc(G, &cs->flag, 1));
+  *out = cs;
+  return LA3G_OK;
+}
+
+}  // namespace la3g
+
+using namespace la3g;
+
+extern "C" int la3g_cc(la3g_graph* G, uint32_t* label_out, la3g_stats* st)
+{
+  if (!G) return set_error(LA3G_EINVAL, "null graph");
+  DevGraph& g = G->g;
+  if (g.directed()) return set_error(LA3G_EINVAL, "cc needs an undirected graph (load without LA3G_DIRECTED)");
+  CallTimer T(G, st);
+  CcScratch* cs = nullptr;
+  LA3G_TRY(cc_scratch(G, &cs));
+  cudaStream_t s = G->stream;
+  const uint32_t N = g.nslots, nrows = g.nrows();
+  uint32_t p0 = 0;
+  LA3G_CUDA(cudaMemcpyAsync(&p0, g.pos_of_id, 4, cudaMemcpyDeviceToHost, s));
+  LA3G_CUDA(cudaStreamSynchronize(s));
+  const bool zero_has_edges = p0 < nrows;
+  uint32_t iters = 0;
+  T.device_begin();
+  if (!zero_has_edges)
+  {
+    k_cc_init<<<grid_for(N, 256), 256, 0, s>>>(N, cs->label);
+    LA3G_LAUNCHED();
+    tls_launches++;
+    {
+      ProfileScope p("cc_hook", s, 4.0 * g.nent + 4.0 * (nrows + 1) + 8.0 * N);
+      k_cc_hook<<<grid_for((uint64_t) nrows * 32, 256, kSMs * 32), 256, 0, s>>>(g.in_ptr, g.in_col, g.id_of_pos, nrows,
+                                                                               cs->label);
+      LA3G_LAUNCHED();
+    }
+    {
+      ProfileScope p("cc_flatten", s, 8.0 * N);
+      k_cc_flatten<<<grid_for(N, 256), 256, 0, s>>>(N, cs->label);
+      LA3G_LAUNCHED();
+    }
+    iters = 1;
+  }
+  else
+  {
+    if (!cs->lab_pos)
+    {
+      LA3G_TRY(galloc(G, &cs->lab_pos, N));
+      LA3G_TRY(galloc(G, &cs->msg, 2 * (size_t) N));
+      LA3G_TRY(galloc(G, &cs->active[0], N));
+      LA3G_TRY(galloc(G, &cs->active[1], N));
+    }
+    uint32_t* msg[2] = {cs->msg, cs->msg + N};
+    k_ccb_init<<<grid_for(N, 256), 256, 0, s>>>(N, nrows, g.id_of_pos, cs->lab_pos, msg[0], cs->active[0]);
+    LA3G_LAUNCHED();
+    int cur = 0;
+    for (;;)
+    {
+      if (iters > 10000000) return set_error(LA3G_ETIMEOUT, "cc did not converge");
+      LA3G_CUDA(cudaMemsetAsync(cs->flag, 0, 4, s));
+      {
+        ProfileScope p("cc_bsp_step", s, 4.0 * g.nent);
+        k_ccb_step<<<grid_for(nrows, 256), 256, 0, s>>>(g.in_ptr, g.in_col, nrows, cs->active[cur], cs->active[cur ^ 1],
+                                                        msg[cur], cs->lab_pos, msg[cur ^ 1], cs->flag);
+        LA3G_LAUNCHED();
+      }
+      iters++;
+      int f = 0;
+      LA3G_CUDA(cudaMemcpyAsync(&f, cs->flag, 4, cudaMemcpyDeviceToHost, s));
+      LA3G_CUDA(cudaStreamSynchronize(s));
+      cur ^= 1;
+      if (!f) break;
+    }
+    k_ccb_by_id<<<grid_for(N, 256), 256, 0, s>>>(N, g.id_of_pos, cs->lab_pos, cs->label);
+    LA3G_LAUNCHED();
+  }
+  T.device_end();
+  if (st)
+  {
+    st->iterations = iters;
+    st->teps_edges = g.nent;
+    st->edges_examined = g.nent;
+    st->algo_bytes = (uint64_t) (4.0 * g.nent + 12.0 * N);
+  }
+  if (label_out) LA3G_CUDA(cudaMemcpyAsync(label_out, cs->label, (size_t) N * 4, cudaMemcpyDeviceToHost, s));
+  return T.finish();
+}

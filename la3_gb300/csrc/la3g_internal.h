@@ -1,0 +1,206 @@
+// Internal declarations shared by the library's translation units.
+#ifndef LA3G_INTERNAL_H
+#define LA3G_INTERNAL_H
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "la3g.h"
+
+#ifdef __CUDACC__
+#include <cuda_runtime.h>
+#endif
+
+namespace la3g {
+
+// Records `code` and a printf-style message as the thread's last error and
+// returns `code`.
+int set_error(int code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
+unsigned host_threads();
+
+// Hashing of vertex ids: SimpleBucketHasher at one rank
+// (src/matrix/hashers.h:39-68) or the identity (NullHasher) for bipartite
+// graphs.
+struct Hasher
+{
+  uint64_t height = 0, max_range = 0;
+  bool null_hash = false;
+#ifdef __CUDACC__
+  __host__ __device__
+#endif
+  inline uint32_t hash(uint64_t v) const
+  {
+    if (null_hash || v >= max_range) return (uint32_t) v;
+    return (uint32_t) (v / 128u + ((uint32_t) v % 128u) * height);
+  }
+#ifdef __CUDACC__
+  __host__ __device__
+#endif
+  inline uint32_t unhash(uint64_t v) const
+  {
+    if (null_hash || v >= max_range) return (uint32_t) v;
+    return (uint32_t) (v / height + (v % height) * 128u);
+  }
+};
+
+}  // namespace la3g
+
+#ifdef __CUDACC__
+
+namespace la3g {
+
+#define LA3G_CUDA(call)                                                                         \
+  do {                                                                                          \
+    cudaError_t err_ = (call);                                                                  \
+    if (err_ != cudaSuccess)                                                                    \
+      return ::la3g::set_error(LA3G_ECUDA, "%s:%d %s: %s", __FILE__, __LINE__, #call,           \
+                               cudaGetErrorString(err_));                                       \
+  } while (0)
+
+#define LA3G_TRY(expr)                \
+  do {                                \
+    int rc_ = (expr);                 \
+    if (rc_ != LA3G_OK) return rc_;   \
+  } while (0)
+
+// Checks the launch that was just made (configuration errors only; the
+// kernel itself is checked at the next synchronisation).
+#define LA3G_LAUNCHED() LA3G_CUDA(cudaGetLastError())
+
+constexpr int kSMs = 152;  // GB300: 2 dies x 76 SMs
+
+inline unsigned grid_for(uint64_t n, unsigned block, unsigned max_blocks = kSMs * 16)
+{
+  uint64_t g = (n + block - 1) / block;
+  if (g < 1) g = 1;
+  if (g > max_blocks) g = max_blocks;
+  return (unsigned) g;
+}
+
+// Kernel-level profiling: when on, a launch is bracketed by events on its
+// stream and its time accumulated under `name` with `bytes` algorithmic
+// bytes.  Always counts the launch.
+struct ProfileScope
+{
+  const char* name;
+  cudaStream_t stream;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  double bytes;
+  ProfileScope(const char* name, cudaStream_t s, double bytes);
+  ~ProfileScope();
+};
+
+extern thread_local uint32_t tls_launches;
+
+// Scoped device buffer for temporaries.
+struct DevBuf
+{
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { if (p) cudaFree(p); }
+  int alloc(size_t n)
+  {
+    if (n <= bytes && p) return LA3G_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, n ? n : 16);
+    if (e != cudaSuccess)
+    {
+      cudaGetLastError();
+      p = nullptr;
+      return set_error(LA3G_ENOMEM, "device allocation of %zu bytes failed: %s", n, cudaGetErrorString(e));
+    }
+    bytes = n;
+    return LA3G_OK;
+  }
+  template <class T>
+  T* as() const { return (T*) p; }
+};
+
+// The device image of a graph in internal order.
+struct DevGraph
+{
+  uint32_t flags = 0;
+  uint32_t nvertices = 0, nslots = 0, nleft = 0;
+  uint64_t nrecords = 0, nent = 0;
+  uint32_t nreg = 0, nsink = 0, nsrc = 0;
+  Hasher hasher;
+  bool directed() const { return flags & LA3G_DIRECTED; }
+  bool weighted() const { return flags & LA3G_WEIGHTED; }
+  uint32_t src_base() const { return nreg + nsink; }
+  uint32_t iso_base() const { return nreg + nsink + nsrc; }
+  uint32_t nrows() const { return nreg + nsink; }
+
+  uint32_t* id_of_pos = nullptr;    // [nslots] original id of each position
+  uint32_t* pos_of_id = nullptr;    // [nslots]
+  uint32_t* hash_of_pos = nullptr;  // [nslots] hashed id (Edge::src / Edge::dst)
+
+  // Pull CSR over rows = positions [0, nreg + nsink): in-neighbours (column
+  // positions) in the reference's order: source columns first, then regular
+  // columns, each ascending.  For undirected graphs this is the only CSR.
+  uint32_t* in_ptr = nullptr;  // [nslots + 1]
+  uint32_t* in_col = nullptr;  // [nent]
+  uint32_t* in_w = nullptr;    // [nent] when weighted
+
+  // Push CSR over columns = positions: out-neighbours (row positions),
+  // ascending, so regular rows come before sink rows.  Built on demand for
+  // directed graphs; the same arrays as the pull CSR for undirected graphs.
+  uint32_t* out_ptr = nullptr;  // [nslots + 1]
+  uint32_t* out_row = nullptr;
+  uint32_t* out_w = nullptr;
+};
+
+// Per-app device scratch cached on a graph handle (allocated on first use).
+enum AppSlot { kSlotPr = 0, kSlotBfs, kSlotSssp, kSlotCc, kSlotTc, kSlotBm25, kSlotBatch, kSlotVp, kSlotCount };
+
+}  // namespace la3g
+
+struct la3g_graph
+{
+  la3g::DevGraph g;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::vector<void*> allocations;
+  uint64_t device_bytes = 0;
+  void* slot[la3g::kSlotCount] = {};
+  void (*slot_free[la3g::kSlotCount])(void*) = {};
+};
+
+namespace la3g {
+
+// Graph-owned device allocation (freed by la3g_graph_free).
+int galloc_bytes(la3g_graph* G, void** p, size_t bytes);
+template <class T>
+int galloc(la3g_graph* G, T** p, size_t count)
+{
+  return galloc_bytes(G, (void**) p, count * sizeof(T));
+}
+
+int build_push_csr(la3g_graph* G);
+
+// Bracket an app call: events on the graph's stream and the host clock.
+struct CallTimer
+{
+  la3g_graph* G;
+  la3g_stats* st;
+  double t0;
+  uint32_t launches0;
+  CallTimer(la3g_graph* G, la3g_stats* st);
+  void device_begin();
+  void device_end();
+  int finish();  // synchronises and fills st
+};
+
+double now_ms();
+
+}  // namespace la3g
+
+#endif  // __CUDACC__
+
+#endif

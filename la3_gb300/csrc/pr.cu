@@ -1,0 +1,495 @@
+// PageRank: the reference pr app (src/apps/graph_analytics/pr.cpp:11-55,
+// pr.h:12-46) on the device.
+//
+// Reference semantics kept exactly:
+//   * degree = number of distinct out-neighbours (DegVertex on the reversed
+//     graph, pr.cpp:14-21, degree.h:24-35);
+//   * rank starts at alpha = 0.15; x = rank / degree (pr.h:37);
+//   * every iteration (the app is stationary) each regular row sums the
+//     messages of its in-neighbours, source columns first, then regular
+//     columns, each ascending (vertex_program_execute.hpp:479-482,
+//     564-603), in FP64, one addition at a time in that order; then
+//     rank = alpha + (1 - alpha) * y (pr.h:40-45);
+//   * sinks are computed once after the iterations from the final regular
+//     ranks (vertex_program_execute.hpp:131-148); sources and isolated
+//     vertices keep alpha.
+// Every floating-point operation is an explicit round-to-nearest intrinsic,
+// so nothing is contracted into an FMA and the result is bit-identical to
+// the reference built without contraction.
+//
+// Kernel layout (pr_pull): one warp owns 32 consecutive rows; it streams the
+// rows' in-edges in chunks of 32 x 8 entries through shared memory (coalesced
+// index loads, gathered x values) and each lane adds its own row's values in
+// order.  Rows longer than kLongRow are skipped there and summed by a single
+// lane that walks the row sequentially with its warp prefetching the values;
+// those warps are the first blocks of the same launch, so the long chains
+// start first.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include <cub/device/device_radix_sort.cuh>
+
+#include "la3g_internal.h"
+
+namespace la3g {
+
+static constexpr double kAlpha = 0.15;
+static constexpr double kTol = 1e-5;
+static constexpr uint32_t kLongRow = 1024;
+static constexpr int kChunk = 256;  // edges staged per warp per step
+static constexpr int kWarpsPerBlock = 8;
+
+struct PrScratch
+{
+  uint32_t* deg = nullptr;      // [nslots] out-degree
+  double* rank = nullptr;       // [nslots]
+  double* x[2] = {nullptr, nullptr};  // [nslots] messages (scatter values)
+  uint32_t* long_rows = nullptr;      // rows with degree > kLongRow, descending
+  uint32_t nlong = 0;
+  int* flag = nullptr;          // any-activated flag
+  float* xf[2] = {nullptr, nullptr};  // FP32 study
+  float* rankf = nullptr;
+  double* resid = nullptr;
+  bool ready = false;
+};
+
+static void pr_scratch_free(void* p) { delete (PrScratch*) p; }
+
+__global__ void k_outdeg(const uint32_t* __restrict__ col, uint64_t m, uint32_t* __restrict__ deg)
+{
+  for (uint64_t e = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; e < m; e += (uint64_t) gridDim.x * blockDim.x)
+    atomicAdd(&deg[col[e]], 1u);
+}
+
+__global__ void k_pr_init(uint32_t N, uint32_t nreg, uint32_t src_base, uint32_t iso_base,
+                          const uint32_t* __restrict__ deg, double* rank, double* x0, double* x1)
+{
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x)
+  {
+    rank[p] = kAlpha;
+    // init(vid, other, s) returns true for everyone, so regular and source
+    // vertices scatter rank / degree (pr.h:34-37); sinks and isolated
+    // vertices have no out-edges and are never read as columns.
+    double xv = 0.0;
+    if (p < nreg || (p >= src_base && p < iso_base)) xv = __ddiv_rn(kAlpha, (double) deg[p]);
+    x0[p] = xv;
+    x1[p] = xv;
+  }
+}
+
+__global__ void k_mark_long(const uint32_t* __restrict__ ptr, uint32_t nrows, uint32_t* keys, uint32_t* vals,
+                            uint32_t* count)
+{
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += gridDim.x * blockDim.x)
+  {
+    uint32_t d = ptr[r + 1] - ptr[r];
+    if (d > kLongRow)
+    {
+      uint32_t i = atomicAdd(count, 1u);
+      keys[i] = ~d;  // ascending sort of ~d = descending degree
+      vals[i] = r;
+    }
+  }
+}
+
+// rank = alpha + (1 - alpha) * y with y = 0.0 + partial (combine into A()).
+__device__ __forceinline__ double pr_apply(double partial)
+{
+  double y = __dadd_rn(0.0, partial);
+  return __dadd_rn(kAlpha, __dmul_rn(1.0 - kAlpha, y));
+}
+
+__device__ __forceinline__ void pr_finish_row(uint32_t r, double acc, const uint32_t* __restrict__ deg, double* rank,
+                                              double* xnext, int* flag, bool write_x)
+{
+  double old = rank[r];
+  double nr = pr_apply(acc);
+  rank[r] = nr;
+  if (write_x) xnext[r] = __ddiv_rn(nr, (double) deg[r]);
+  if (flag && fabs(__dsub_rn(nr, old)) > kTol) *flag = 1;
+}
+
+// Rows [row_lo, row_hi).  Blocks [0, long_blocks) take the long rows (one
+// warp per row, descending length); the rest take 32-row tiles.
+__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+k_pr_pull(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const double* __restrict__ x,
+          double* __restrict__ xnext, double* __restrict__ rank, const uint32_t* __restrict__ deg,
+          const uint32_t* __restrict__ long_rows, uint32_t nlong, uint32_t long_blocks, uint32_t row_lo,
+          uint32_t row_hi, int* flag, int write_x)
+{
+  __shared__ double sx[kWarpsPerBlock][kChunk];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  if (blockIdx.x < long_blocks)
+  {
+    for (uint32_t li = blockIdx.x * kWarpsPerBlock + wib; li < nlong; li += long_blocks * kWarpsPerBlock)
+    {
+      uint32_t r = long_rows[li];
+      if (r < row_lo || r >= row_hi) continue;
+      uint32_t b = ptr[r], e = ptr[r + 1];
+      double acc = 0.0;
+      // prefetch one chunk ahead; lane 0 adds sequentially
+      double v[kChunk / 32];
+#pragma unroll
+      for (int k = 0; k < kChunk / 32; k++)
+      {
+        uint32_t i = b + k * 32 + lane;
+        v[k] = i < e ? x[col[i]] : 0.0;
+      }
+      for (uint32_t base = b; base < e; base += kChunk)
+      {
+#pragma unroll
+        for (int k = 0; k < kChunk / 32; k++) sx[wib][k * 32 + lane] = v[k];
+        __syncwarp();
+        uint32_t nb = base + kChunk;
+#pragma unroll
+        for (int k = 0; k < kChunk / 32; k++)
+        {
+          uint32_t i = nb + k * 32 + lane;
+          v[k] = i < e ? x[col[i]] : 0.0;
+        }
+        if (lane == 0)
+        {
+          uint32_t n = min((uint32_t) kChunk, e - base);
+          if (n == kChunk)
+          {
+#pragma unroll 32
+            for (uint32_t j = 0; j < kChunk; j++) acc = __dadd_rn(acc, sx[wib][j]);
+          }
+          else
+          {
+            for (uint32_t j = 0; j < n; j++) acc = __dadd_rn(acc, sx[wib][j]);
+          }
+        }
+        __syncwarp();
+      }
+      if (lane == 0) pr_finish_row(r, acc, deg, rank, xnext, flag, write_x);
+    }
+    return;
+  }
+  const uint32_t ntiles = (row_hi - row_lo + 31) / 32;
+  const uint32_t nwarps = (gridDim.x - long_blocks) * kWarpsPerBlock;
+  for (uint32_t t = (blockIdx.x - long_blocks) * kWarpsPerBlock + wib; t < ntiles; t += nwarps)
+  {
+    const uint32_t r0 = row_lo + t * 32;
+    const uint32_t r = r0 + lane;
+    const bool valid = r < row_hi;
+    uint32_t rb = valid ? ptr[r] : 0, re = valid ? ptr[r + 1] : 0;
+    const bool mine = valid && (re - rb) <= kLongRow;
+    if (!mine) { rb = 0; re = 0; }
+    // Walk the short rows' edges in chunks; each chunk starts at the lowest
+    // edge any lane still needs, which skips over the long rows' edges.
+    const uint32_t te = ptr[min(r0 + 32, row_hi)];
+    double acc = 0.0;
+    uint32_t cur = rb;  // next edge of my row to add
+    for (;;)
+    {
+      const uint32_t base = __reduce_min_sync(0xffffffffu, cur < re ? cur : 0xffffffffu);
+      if (base == 0xffffffffu) break;
+      const uint32_t lim = min(base + kChunk, te);
+#pragma unroll
+      for (int k = 0; k < kChunk / 32; k++)
+      {
+        uint32_t i = base + k * 32 + lane;
+        if (i < lim) sx[wib][k * 32 + lane] = x[col[i]];
+      }
+      __syncwarp();
+      const uint32_t stop = min(re, lim);
+      for (; cur < stop; cur++) acc = __dadd_rn(acc, sx[wib][cur - base]);
+      __syncwarp();
+    }
+    if (mine) pr_finish_row(r, acc, deg, rank, xnext, flag, write_x);
+  }
+}
+
+__global__ void k_scatter_pos(uint32_t N, const uint32_t* __restrict__ id_of_pos, const double* __restrict__ val,
+                              double* __restrict__ out)
+{
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) out[id_of_pos[p]] = val[p];
+}
+
+__global__ void k_scatter_pos_u32(uint32_t N, const uint32_t* __restrict__ id_of_pos, const uint32_t* __restrict__ val,
+                                  uint32_t* __restrict__ out)
+{
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) out[id_of_pos[p]] = val[p];
+}
+
+static int pr_prepare(la3g_graph* G, PrScratch** out)
+{
+  DevGraph& g = G->g;
+  cudaStream_t s = G->stream;
+  PrScratch* ps = (PrScratch*) G->slot[kSlotPr];
+  if (ps && ps->ready) { *out = ps; return LA3G_OK; }
+  if (!ps)
+  {
+    ps = new (std::nothrow) PrScratch();
+    if (!ps) return set_error(LA3G_ENOMEM, "out of host memory");
+    G->slot[kSlotPr] = ps;
+    G->slot_free[kSlotPr] = pr_scratch_free;
+  }
+  const uint32_t N = g.nslots;
+  LA3G_TRY(galloc(G, &ps->deg, N));
+  LA3G_TRY(galloc(G, &ps->rank, N));
+  LA3G_TRY(galloc(G, &ps->x[0], N));
+  LA3G_TRY(galloc(G, &ps->x[1], N));
+  LA3G_TRY(galloc(G, &ps->flag, 4));
+  LA3G_CUDA(cudaMemsetAsync(ps->deg, 0, (size_t) N * 4, s));
+  if (g.nent)
+  {
+    ProfileScope ps_("pr_outdeg", s, (double) g.nent * 4);
+    k_outdeg<<<grid_for(g.nent, 256), 256, 0, s>>>(g.in_col, g.nent, ps->deg);
+    LA3G_LAUNCHED();
+  }
+  // long rows, sorted by descending degree
+  DevBuf keys, vals, keys2, vals2, cnt;
+  LA3G_TRY(keys.alloc((size_t) g.nrows() * 4 + 4));
+  LA3G_TRY(vals.alloc((size_t) g.nrows() * 4 + 4));
+  LA3G_TRY(cnt.alloc(4));
+  LA3G_CUDA(cudaMemsetAsync(cnt.p, 0, 4, s));
+  if (g.nrows())
+  {
+    k_mark_long<<<grid_for(g.nrows(), 256), 256, 0, s>>>(g.in_ptr, g.nrows(), keys.as<uint32_t>(), vals.as<uint32_t>(),
+                                                         cnt.as<uint32_t>());
+    LA3G_LAUNCHED();
+  }
+  uint32_t nlong = 0;
+  LA3G_CUDA(cudaMemcpyAsync(&nlong, cnt.p, 4, cudaMemcpyDeviceToHost, s));
+  LA3G_CUDA(cudaStreamSynchronize(s));
+  ps->nlong = nlong;
+  LA3G_TRY(galloc(G, &ps->long_rows, nlong + 1));
+  if (nlong)
+  {
+    LA3G_TRY(keys2.alloc((size_t) nlong * 4 + 4));
+    size_t tb = 0;
+    LA3G_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tb, keys.as<uint32_t>(), keys2.as<uint32_t>(), vals.as<uint32_t>(),
+                                              ps->long_rows, nlong, 0, 32, s));
+    DevBuf tmp;
+    LA3G_TRY(tmp.alloc(tb));
+    LA3G_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tb, keys.as<uint32_t>(), keys2.as<uint32_t>(), vals.as<uint32_t>(),
+                                              ps->long_rows, nlong, 0, 32, s));
+  }
+  LA3G_CUDA(cudaStreamSynchronize(s));
+  ps->ready = true;
+  *out = ps;
+  return LA3G_OK;
+}
+
+static int pr_launch(la3g_graph* G, PrScratch* ps, const double* x, double* xnext, uint32_t row_lo, uint32_t row_hi,
+                     int* flag, bool write_x)
+{
+  DevGraph& g = G->g;
+  if (row_hi <= row_lo) return LA3G_OK;
+  const uint32_t long_blocks = ps->nlong ? std::min<uint32_t>((ps->nlong + kWarpsPerBlock - 1) / kWarpsPerBlock, kSMs) : 0;
+  const uint32_t ntiles = (row_hi - row_lo + 31) / 32;
+  const uint32_t tile_blocks = std::min<uint32_t>((ntiles + kWarpsPerBlock - 1) / kWarpsPerBlock, kSMs * 8);
+  uint64_t edges = 0;  // algorithmic bytes: 4 B index per edge + per-row ptr, x, rank, xnext
+  (void) edges;
+  double bytes = 4.0 * (double) g.nent + 4.0 * (row_hi - row_lo + 1) + 8.0 * (double) g.nslots +
+                 (write_x ? 16.0 : 8.0) * (row_hi - row_lo) + 4.0 * (row_hi - row_lo);
+  ProfileScope p("pr_pull_f64", G->stream, bytes);
+  k_pr_pull<<<long_blocks + std::max<uint32_t>(tile_blocks, 1), kWarpsPerBlock * 32, 0, G->stream>>>(
+      g.in_ptr, g.in_col, x, xnext, ps->rank, ps->deg, ps->long_rows, ps->nlong, long_blocks, row_lo, row_hi, flag,
+      write_x ? 1 : 0);
+  LA3G_LAUNCHED();
+  return LA3G_OK;
+}
+
+// ------------------------------------------------------------------ FP32 study
+
+__global__ void k_prf_init(uint32_t N, uint32_t nrows_reg, uint32_t src_base, uint32_t iso_base,
+                           const uint32_t* __restrict__ deg, float* rankf, double* rank, float* x0, float* x1)
+{
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x)
+  {
+    rankf[p] = (float) kAlpha;
+    rank[p] = kAlpha;
+    float xv = 0.0f;
+    bool scat = (p < nrows_reg) || (p >= src_base && p < iso_base);
+    if (scat && deg[p]) xv = (float) kAlpha / (float) deg[p];
+    x0[p] = xv;
+    x1[p] = xv;
+  }
+}
+
+// FP32 SpMV with FP32 accumulation: warp per 32-row tile, each lane its row
+// (any order inside a row is allowed here); the L1 residual is reduced in
+// FP64.
+__global__ void __launch_bounds__(256)
+k_prf_pull(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const float* __restrict__ x,
+           float* __restrict__ xnext, float* __restrict__ rankf, double* __restrict__ rank,
+           const uint32_t* __restrict__ deg, uint32_t row_lo, uint32_t row_hi, double* resid, int write_x)
+{
+  const int lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  double local = 0.0;
+  for (uint32_t r = row_lo + warp; r < row_hi; r += nwarps)
+  {
+    uint32_t b = ptr[r], e = ptr[r + 1];
+    float acc = 0.0f;
+    for (uint32_t i = b + lane; i < e; i += 32) acc += x[col[i]];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0)
+    {
+      float nr = (float) kAlpha + (float) (1.0 - kAlpha) * acc;
+      double d = fabs((double) nr - (double) rankf[r]);
+      local += d;
+      rankf[r] = nr;
+      rank[r] = (double) nr;
+      if (write_x) xnext[r] = nr / (float) deg[r];
+    }
+  }
+  if (lane == 0 && local != 0.0) atomicAdd(resid, local);
+}
+
+}  // namespace la3g
+
+using namespace la3g;
+
+extern "C" int la3g_pr(la3g_graph* G, uint32_t iters, double* rank_out, uint32_t* degree_out, la3g_stats* st)
+{
+  if (!G) return set_error(LA3G_EINVAL, "null graph");
+  DevGraph& g = G->g;
+  if (!g.directed() || (g.flags & (LA3G_REVERSE | LA3G_ACYCLIC | LA3G_BIPARTITE)))
+    return set_error(LA3G_EINVAL, "pagerank needs a graph loaded with LA3G_DIRECTED only");
+  CallTimer T(G, st);
+  PrScratch* ps = nullptr;
+  LA3G_TRY(pr_prepare(G, &ps));
+  cudaStream_t s = G->stream;
+  const uint32_t N = g.nslots;
+  T.device_begin();
+  k_pr_init<<<grid_for(N, 256), 256, 0, s>>>(N, g.nreg, g.src_base(), g.iso_base(), ps->deg, ps->rank, ps->x[0], ps->x[1]);
+  LA3G_LAUNCHED();
+  tls_launches++;
+  // k_pr_init gives regular and source vertices a message; sinks and
+  // isolated vertices never scatter (their x stays 0 and is never read).
+  uint32_t it = 0;
+  int cur = 0;
+  const bool until = iters == 0;
+  for (;;)
+  {
+    if (!until && it >= iters) break;
+    if (until) LA3G_CUDA(cudaMemsetAsync(ps->flag, 0, 4, s));
+    LA3G_TRY(pr_launch(G, ps, ps->x[cur], ps->x[cur ^ 1], 0, g.nreg, until ? ps->flag : nullptr, true));
+    cur ^= 1;
+    it++;
+    if (until)
+    {
+      int f = 0;
+      LA3G_CUDA(cudaMemcpyAsync(&f, ps->flag, 4, cudaMemcpyDeviceToHost, s));
+      LA3G_CUDA(cudaStreamSynchronize(s));
+      if (!f) break;
+    }
+  }
+  // sink pass from the final messages (vertex_program_execute.hpp:131-148)
+  LA3G_TRY(pr_launch(G, ps, ps->x[cur], ps->x[cur ^ 1], g.nreg, g.nreg + g.nsink, nullptr, false));
+  T.device_end();
+  if (st)
+  {
+    st->iterations = it;
+    st->teps_edges = (uint64_t) it * g.nent;
+    st->edges_examined = (uint64_t) it * g.nent + g.nent;
+    st->algo_bytes = (uint64_t) ((4.0 * g.nent + 28.0 * N) * it);
+  }
+  if (rank_out || degree_out)
+  {
+    DevBuf tmp;
+    LA3G_TRY(tmp.alloc((size_t) N * 8));
+    if (rank_out)
+    {
+      k_scatter_pos<<<grid_for(N, 256), 256, 0, s>>>(N, g.id_of_pos, ps->rank, tmp.as<double>());
+      LA3G_LAUNCHED();
+      LA3G_CUDA(cudaMemcpyAsync(rank_out, tmp.p, (size_t) N * 8, cudaMemcpyDeviceToHost, s));
+      LA3G_CUDA(cudaStreamSynchronize(s));
+    }
+    if (degree_out)
+    {
+      k_scatter_pos_u32<<<grid_for(N, 256), 256, 0, s>>>(N, g.id_of_pos, ps->deg, tmp.as<uint32_t>());
+      LA3G_LAUNCHED();
+      LA3G_CUDA(cudaMemcpyAsync(degree_out, tmp.p, (size_t) N * 4, cudaMemcpyDeviceToHost, s));
+      LA3G_CUDA(cudaStreamSynchronize(s));
+    }
+  }
+  return T.finish();
+}
+
+extern "C" int la3g_pr_f32(la3g_graph* G, uint32_t iters, double tol, double* rank_out, double* residual_out,
+                           la3g_stats* st)
+{
+  if (!G) return set_error(LA3G_EINVAL, "null graph");
+  DevGraph& g = G->g;
+  if (!g.directed() || (g.flags & (LA3G_REVERSE | LA3G_ACYCLIC | LA3G_BIPARTITE)))
+    return set_error(LA3G_EINVAL, "pagerank needs a graph loaded with LA3G_DIRECTED only");
+  if (iters == 0) return set_error(LA3G_EINVAL, "iters must be > 0");
+  CallTimer T(G, st);
+  PrScratch* ps = nullptr;
+  LA3G_TRY(pr_prepare(G, &ps));
+  cudaStream_t s = G->stream;
+  const uint32_t N = g.nslots;
+  if (!ps->rankf)
+  {
+    LA3G_TRY(galloc(G, &ps->rankf, N));
+    LA3G_TRY(galloc(G, &ps->xf[0], N));
+    LA3G_TRY(galloc(G, &ps->xf[1], N));
+    LA3G_TRY(galloc(G, &ps->resid, 1));
+  }
+  T.device_begin();
+  k_prf_init<<<grid_for(N, 256), 256, 0, s>>>(N, g.nreg, g.src_base(), g.iso_base(), ps->deg, ps->rankf, ps->rank,
+                                              ps->xf[0], ps->xf[1]);
+  LA3G_LAUNCHED();
+  tls_launches++;
+  int cur = 0;
+  uint32_t it = 0;
+  double res = 0.0;
+  const unsigned blocks = grid_for((uint64_t) g.nreg * 32, 256, kSMs * 8);
+  for (; it < iters;)
+  {
+    LA3G_CUDA(cudaMemsetAsync(ps->resid, 0, 8, s));
+    {
+      ProfileScope p("pr_pull_f32", s, 4.0 * g.nent + 4.0 * (g.nreg + 1) + 4.0 * N + 12.0 * g.nreg + 4.0 * g.nreg);
+      k_prf_pull<<<blocks, 256, 0, s>>>(g.in_ptr, g.in_col, ps->xf[cur], ps->xf[cur ^ 1], ps->rankf, ps->rank, ps->deg, 0,
+                                        g.nreg, ps->resid, 1);
+      LA3G_LAUNCHED();
+    }
+    cur ^= 1;
+    it++;
+    if (tol > 0)
+    {
+      LA3G_CUDA(cudaMemcpyAsync(&res, ps->resid, 8, cudaMemcpyDeviceToHost, s));
+      LA3G_CUDA(cudaStreamSynchronize(s));
+      if (res < tol) break;
+    }
+  }
+  if (g.nsink)
+  {
+    const unsigned sb = grid_for((uint64_t) g.nsink * 32, 256, kSMs * 8);
+    ProfileScope p("pr_pull_f32", s, 4.0 * g.nent);
+    k_prf_pull<<<sb, 256, 0, s>>>(g.in_ptr, g.in_col, ps->xf[cur], ps->xf[cur ^ 1], ps->rankf, ps->rank, ps->deg, g.nreg,
+                                  g.nreg + g.nsink, ps->resid, 0);
+    LA3G_LAUNCHED();
+  }
+  T.device_end();
+  if (tol <= 0)
+  {
+    LA3G_CUDA(cudaMemcpyAsync(&res, ps->resid, 8, cudaMemcpyDeviceToHost, s));
+  }
+  if (st)
+  {
+    st->iterations = it;
+    st->teps_edges = (uint64_t) it * g.nent;
+    st->edges_examined = (uint64_t) it * g.nent;
+    st->algo_bytes = (uint64_t) ((4.0 * g.nent + 20.0 * N) * it);
+  }
+  if (rank_out)
+  {
+    DevBuf tmp;
+    LA3G_TRY(tmp.alloc((size_t) N * 8));
+    k_scatter_pos<<<grid_for(N, 256), 256, 0, s>>>(N, g.id_of_pos, ps->rank, tmp.as<double>());
+    LA3G_LAUNCHED();
+    LA3G_CUDA(cudaMemcpyAsync(rank_out, tmp.p, (size_t) N * 8, cudaMemcpyDeviceToHost, s));
+  }
+  LA3G_TRY(T.finish());
+  if (residual_out) *residual_out = res;
+  return LA3G_OK;
+}

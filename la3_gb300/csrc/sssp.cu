@@ -1,0 +1,295 @@
+// SSSP: the reference sssp app (src/apps/graph_analytics/sssp.cpp:11-37,
+// sssp.h:11-46) on the device.
+//
+// Reference semantics kept exactly (np = 1, the optimizable path
+// execute_, vertex_program_execute.hpp:55-163):
+//   * dist is uint32 with INF = 2^31 - 1; gather = msg + weight in uint32
+//     arithmetic; combine = min; apply = min and activates on change;
+//   * iteration i relaxes the out-edges of the vertices activated in
+//     iteration i - 1 (the root in iteration 0, if it has out-edges), with
+//     the message each of them scattered when it was activated, into the
+//     REGULAR rows only;
+//   * after convergence the sink rows are computed once from every regular
+//     vertex's final distance (activated or not, INF included) and from the
+//     root's message if the root is a source (:131-148).
+// Push relaxation uses atomicMin on dist: the value a row holds after the
+// iteration is min(old, min over messages) exactly as apply computes it,
+// and a row is activated iff some relaxation lowered it.
+#include <algorithm>
+#include <cstring>
+
+#include "la3g_internal.h"
+
+namespace la3g {
+
+static constexpr uint32_t kInf = 0x7FFFFFFFu;
+
+struct SsspScratch
+{
+  uint32_t* dist = nullptr;
+  uint32_t* msg = nullptr;
+  uint32_t* stamp = nullptr;
+  uint32_t* list[2] = {nullptr, nullptr};
+  unsigned long long* ctr = nullptr;  // [0] next count, [1] next out-degree sum, [2] scratch
+  unsigned long long* hctr = nullptr;
+};
+
+static void sssp_scratch_free(void* p)
+{
+  SsspScratch* s = (SsspScratch*) p;
+  if (s->hctr) cudaFreeHost(s->hctr);
+  delete s;
+}
+
+__global__ void k_sssp_init(uint32_t N, uint32_t* dist, uint32_t* stamp)
+{
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x)
+  {
+    dist[p] = kInf;
+    stamp[p] = 0;
+  }
+}
+
+__global__ void k_sssp_root(uint32_t rp, int push, uint32_t* dist, uint32_t* msg, uint32_t* list)
+{
+  dist[rp] = 0;
+  msg[rp] = 0;
+  if (push) list[0] = rp;
+}
+
+// One warp per frontier vertex; lanes over its out-edges into regular rows.
+__global__ void __launch_bounds__(256)
+k_sssp_push(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ row, const uint32_t* __restrict__ w,
+            const uint32_t* __restrict__ front, uint32_t nfront, const uint32_t* __restrict__ msg, uint32_t nreg,
+            uint32_t* dist, uint32_t* stamp, uint32_t tag, uint32_t* next, unsigned long long* ctr)
+{
+  const int lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t f = warp; f < nfront; f += nwarps)
+  {
+    const uint32_t u = front[f];
+    const uint32_t mu = msg[u];
+    const uint32_t b = ptr[u], e = ptr[u + 1];
+    for (uint32_t i0 = b; i0 < e; i0 += 32)
+    {
+      const uint32_t i = i0 + lane;
+      bool add = false;
+      uint32_t v = 0;
+      bool more = true;
+      if (i < e)
+      {
+        v = row[i];
+        if (v < nreg)
+        {
+          const uint32_t cand = mu + w[i];
+          if (cand < dist[v])
+          {
+            const uint32_t old = atomicMin(&dist[v], cand);
+            if (cand < old) add = atomicExch(&stamp[v], tag) != tag;
+          }
+        }
+        else more = false;  // rows ascend: the rest are sinks
+      }
+      const unsigned mask = __ballot_sync(0xffffffffu, add);
+      if (mask)
+      {
+        uint32_t base = 0;
+        if (lane == 0) base = (uint32_t) atomicAdd(&ctr[0], (unsigned long long) __popc(mask));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (add) next[base + __popc(mask & ((1u << lane) - 1))] = v;
+      }
+      if (!__any_sync(0xffffffffu, more)) break;
+    }
+  }
+}
+
+// Activated vertices scatter their new distance.
+__global__ void k_sssp_apply(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ next, uint32_t n,
+                             const uint32_t* __restrict__ dist, uint32_t* msg, unsigned long long* ctr)
+{
+  unsigned long long deg = 0;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+  {
+    uint32_t v = next[i];
+    msg[v] = dist[v];
+    deg += ptr[v + 1] - ptr[v];
+  }
+  for (int o = 16; o > 0; o >>= 1) deg += __shfl_xor_sync(0xffffffffu, deg, o);
+  if ((threadIdx.x & 31) == 0 && deg) atomicAdd(&ctr[1], deg);
+}
+
+// Sink pass: y = min over in-neighbours (regular: final dist; the root if it
+// is a source: its message 0) of msg + w; dist = min(dist, y).
+__global__ void k_sssp_sinks(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col,
+                             const uint32_t* __restrict__ w, uint32_t nreg, uint32_t nsink, uint32_t src_root,
+                             uint32_t* dist)
+{
+  for (uint32_t v = nreg + blockIdx.x * blockDim.x + threadIdx.x; v < nreg + nsink; v += gridDim.x * blockDim.x)
+  {
+    uint32_t y = kInf;
+    for (uint32_t i = ptr[v]; i < ptr[v + 1]; i++)
+    {
+      const uint32_t c = col[i];
+      uint32_t cand;
+      if (c < nreg) cand = dist[c] + w[i];
+      else if (c == src_root) cand = 0u + w[i];
+      else continue;
+      y = min(y, cand);
+    }
+    dist[v] = min(dist[v], y);
+  }
+}
+
+__global__ void k_reached_outdeg(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ dist, uint32_t N,
+                                 unsigned long long* out)
+{
+  unsigned long long s = 0;
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < N; v += gridDim.x * blockDim.x)
+    if (dist[v] != kInf) s += ptr[v + 1] - ptr[v];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0 && s) atomicAdd(out, s);
+}
+
+__global__ void k_u32_by_id(uint32_t N, const uint32_t* __restrict__ id_of_pos, const uint32_t* __restrict__ val,
+                            uint32_t* __restrict__ out)
+{
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) out[id_of_pos[p]] = val[p];
+}
+
+static int sssp_scratch(la3g_graph* G, SsspScratch** out)
+{
+  SsspScratch* ss = (SsspScratch*) G->slot[kSlotSssp];
+  if (ss) { *out = ss; return LA3G_OK; }
+  ss = new (std::nothrow) SsspScratch();
+  if (!ss) return set_error(LA3G_ENOMEM, "out of host memory");
+  G->slot[kSlotSssp] = ss;
+  G->slot_free[kSlotSssp] = sssp_scratch_free;
+  const uint32_t N = G->g.nslots;
+  LA3G_TRY(galloc(G, &ss->dist, N));
+  LA3G_TRY(galloc(G, &ss->msg, N));
+  LA3G_TRY(galloc(G, &ss->stamp, N));
+  LA3G_TRY(galloc(G, &ss->list[0], N));
+  LA3G_TRY(galloc(G, &ss->list[1], N));
+  LA3G_TRY(galloc(G, &ss->ctr, 4));
+  LA3G_CUDA(cudaHostAlloc(&ss->hctr, 4 * sizeof(unsigned long long), cudaHostAllocDefault));
+  *out = ss;
+  return LA3G_OK;
+}
+
+static int sssp_run(la3g_graph* G, SsspScratch* ss, uint32_t root, la3g_stats* st)
+{
+  DevGraph& g = G->g;
+  cudaStream_t s = G->stream;
+  const uint32_t N = g.nslots;
+  k_sssp_init<<<grid_for(N, 256), 256, 0, s>>>(N, ss->dist, ss->stamp);
+  LA3G_LAUNCHED();
+  tls_launches++;
+  uint32_t rp = 0xFFFFFFFFu, src_root = 0xFFFFFFFFu;
+  uint64_t nfront = 0, front_deg = 0;
+  if (root < N)
+  {
+    LA3G_CUDA(cudaMemcpyAsync(&rp, g.pos_of_id + root, 4, cudaMemcpyDeviceToHost, s));
+    LA3G_CUDA(cudaStreamSynchronize(s));
+    // init returns true for the root; regular and source vertices scatter.
+    const bool scat = rp < g.nreg || (rp >= g.src_base() && rp < g.iso_base());
+    if (rp >= g.src_base() && rp < g.iso_base()) src_root = rp;
+    k_sssp_root<<<1, 1, 0, s>>>(rp, scat ? 1 : 0, ss->dist, ss->msg, ss->list[0]);
+    LA3G_LAUNCHED();
+    tls_launches++;
+    nfront = scat ? 1 : 0;
+    if (scat)
+    {
+      uint32_t hp[2];
+      LA3G_CUDA(cudaMemcpyAsync(hp, g.out_ptr + rp, 8, cudaMemcpyDeviceToHost, s));
+      LA3G_CUDA(cudaStreamSynchronize(s));
+      front_deg = hp[1] - hp[0];
+    }
+  }
+  uint32_t iter = 0;
+  int cur = 0;
+  uint64_t examined = 0;
+  for (;;)
+  {
+    if (iter > 1000000) return set_error(LA3G_ETIMEOUT, "sssp did not converge");
+    iter++;
+    if (nfront == 0) break;
+    LA3G_CUDA(cudaMemsetAsync(ss->ctr, 0, 2 * sizeof(unsigned long long), s));
+    {
+      ProfileScope p("sssp_push", s, 8.0 * front_deg + 12.0 * nfront);
+      k_sssp_push<<<grid_for(nfront * 32, 256), 256, 0, s>>>(g.out_ptr, g.out_row, g.out_w, ss->list[cur],
+                                                            (uint32_t) nfront, ss->msg, g.nreg, ss->dist, ss->stamp,
+                                                            iter, ss->list[cur ^ 1], ss->ctr);
+      LA3G_LAUNCHED();
+    }
+    examined += front_deg;
+    LA3G_CUDA(cudaMemcpyAsync(ss->hctr, ss->ctr, 8, cudaMemcpyDeviceToHost, s));
+    LA3G_CUDA(cudaStreamSynchronize(s));
+    uint64_t nn = ss->hctr[0];
+    if (nn)
+    {
+      k_sssp_apply<<<grid_for(nn, 256), 256, 0, s>>>(g.out_ptr, ss->list[cur ^ 1], (uint32_t) nn, ss->dist, ss->msg,
+                                                     ss->ctr);
+      LA3G_LAUNCHED();
+      tls_launches++;
+      LA3G_CUDA(cudaMemcpyAsync(ss->hctr, ss->ctr, 16, cudaMemcpyDeviceToHost, s));
+      LA3G_CUDA(cudaStreamSynchronize(s));
+    }
+    nfront = nn;
+    front_deg = nn ? ss->hctr[1] : 0;
+    cur ^= 1;
+  }
+  if (g.nsink)
+  {
+    ProfileScope p("sssp_sinks", s, 8.0 * g.nent);
+    k_sssp_sinks<<<grid_for(g.nsink, 256), 256, 0, s>>>(g.in_ptr, g.in_col, g.in_w, g.nreg, g.nsink, src_root, ss->dist);
+    LA3G_LAUNCHED();
+  }
+  if (st)
+  {
+    st->iterations = iter;
+    st->edges_examined = examined;
+  }
+  return LA3G_OK;
+}
+
+}  // namespace la3g
+
+using namespace la3g;
+
+extern "C" int la3g_sssp(la3g_graph* G, uint32_t root, uint32_t* dist_out, la3g_stats* st)
+{
+  if (!G) return set_error(LA3G_EINVAL, "null graph");
+  DevGraph& g = G->g;
+  if (!g.directed() || !g.weighted() || (g.flags & (LA3G_REVERSE | LA3G_ACYCLIC | LA3G_BIPARTITE)))
+    return set_error(LA3G_EINVAL, "sssp needs a graph loaded with LA3G_DIRECTED | LA3G_WEIGHTED");
+  CallTimer T(G, st);
+  LA3G_TRY(build_push_csr(G));
+  SsspScratch* ss = nullptr;
+  LA3G_TRY(sssp_scratch(G, &ss));
+  cudaStream_t s = G->stream;
+  const uint32_t N = g.nslots;
+  T.device_begin();
+  LA3G_TRY(sssp_run(G, ss, root, st));
+  T.device_end();
+  if (st)
+  {
+    LA3G_CUDA(cudaMemsetAsync(ss->ctr + 2, 0, 8, s));
+    k_reached_outdeg<<<grid_for(N, 256), 256, 0, s>>>(g.out_ptr, ss->dist, N, ss->ctr + 2);
+    LA3G_LAUNCHED();
+    LA3G_CUDA(cudaMemcpyAsync(ss->hctr + 2, ss->ctr + 2, 8, cudaMemcpyDeviceToHost, s));
+    LA3G_CUDA(cudaStreamSynchronize(s));
+    st->teps_edges = ss->hctr[2];
+    st->algo_bytes = st->edges_examined * 8 + (uint64_t) N * 8;
+  }
+  if (dist_out)
+  {
+    DevBuf tmp;
+    LA3G_TRY(tmp.alloc((size_t) N * 4));
+    k_u32_by_id<<<grid_for(N, 256), 256, 0, s>>>(N, g.id_of_pos, ss->dist, tmp.as<uint32_t>());
+    LA3G_LAUNCHED();
+    LA3G_CUDA(cudaMemcpyAsync(dist_out, tmp.p, (size_t) N * 4, cudaMemcpyDeviceToHost, s));
+    LA3G_CUDA(cudaStreamSynchronize(s));
+  }
+  return T.finish();
+}

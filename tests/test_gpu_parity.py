@@ -1,0 +1,159 @@
+"""GPU path vs the reference: every golden case (reference outputs) and
+larger seeded graphs checked against the C oracle.  Calls go through the C
+ABI (la3_gb300 is a ctypes binding of libla3g)."""
+import numpy as np
+import pytest
+
+from conftest import GOLD
+
+DATA = GOLD / "data"
+pytestmark = pytest.mark.gpu
+
+
+def _cases(golden, app):
+    return sorted(k for k, v in golden.items() if v["app"] == app)
+
+
+def test_pagerank_golden(gpu, golden):
+    L = gpu
+    for name in _cases(golden, "pr"):
+        c = golden[name]
+        ref = np.load(GOLD / f"{name}.npz")
+        g = L.Graph.load_directed(DATA / c["file"], c["n"])
+        rank, deg, st = L.pagerank(g, c["iters"])
+        assert np.array_equal(deg, ref["degree"]), name
+        assert np.array_equal(rank.view(np.uint64), ref["rank"].view(np.uint64)), (
+            name, float(np.abs(rank - ref["rank"]).max()))
+
+
+def test_bfs_golden(gpu, golden):
+    L = gpu
+    for name in _cases(golden, "bfs"):
+        c = golden[name]
+        ref = np.load(GOLD / f"{name}.npz")
+        g = L.Graph.load_undirected(DATA / c["file"], c["n"])
+        hops, parent, st = L.bfs(g, c["root"])
+        assert np.array_equal(hops, ref["hops"]), name
+        assert np.array_equal(parent, ref["parent"]), name
+
+
+def test_sssp_golden(gpu, golden):
+    L = gpu
+    for name in _cases(golden, "sssp"):
+        c = golden[name]
+        ref = np.load(GOLD / f"{name}.npz")
+        g = L.Graph.load_directed(DATA / c["file"], c["n"], weighted=True)
+        dist, st = L.sssp(g, c["root"])
+        assert np.array_equal(dist, ref["dist"]), name
+
+
+def test_cc_golden(gpu, golden):
+    L = gpu
+    for name in _cases(golden, "cc"):
+        c = golden[name]
+        ref = np.load(GOLD / f"{name}.npz")
+        g = L.Graph.load_undirected(DATA / c["file"], c["n"])
+        lab, st = L.cc(g)
+        assert np.array_equal(lab, ref["label"]), name
+
+
+def test_tc_golden(gpu, golden):
+    L = gpu
+    for name in _cases(golden, "tc"):
+        c = golden[name]
+        ref = np.load(GOLD / f"{name}.npz")
+        g = L.Graph.load_directed(DATA / c["file"], c["n"], remove_cycles=True)
+        total, per, st = L.tc(g)
+        assert np.array_equal(per, ref["ntri"]), name
+        assert total == c["triangles"], name
+
+
+@pytest.fixture(scope="module")
+def rmat16(gpu, tmp_path_factory):
+    d = tmp_path_factory.mktemp("rmat16")
+    e = gpu.EdgeList.rmat(16, 16, seed=2026)
+    ew = gpu.EdgeList.rmat(16, 16, seed=2026, weighted=True, wseed=7)
+    p, pw = d / "g.bin", d / "g.w.bin"
+    e.write(p)
+    ew.write(pw)
+    return p, pw, 1 << 16
+
+
+def _roots(n, k, seed):
+    return [int(x) for x in np.random.default_rng(seed).integers(1, n + 1, k)]
+
+
+def test_pagerank_rmat16_vs_oracle(gpu, oracle, rmat16):
+    p, _, n = rmat16
+    rank, deg, st = gpu.pagerank(gpu.Graph.load_directed(p, n), 20)
+    orank, odeg = oracle.OracleGraph(p, n, oracle.DIRECTED).pagerank(20)
+    assert np.array_equal(deg, odeg)
+    assert np.array_equal(rank.view(np.uint64), orank.view(np.uint64)), float(np.abs(rank - orank).max())
+    assert st.iterations == 20
+
+
+def test_bfs_sssp_cc_tc_rmat16_vs_oracle(gpu, oracle, rmat16):
+    p, pw, n = rmat16
+    gu = gpu.Graph.load_undirected(p, n)
+    ou = oracle.OracleGraph(p, n, 0)
+    for r in _roots(n, 4, 1):
+        h, par, st = gpu.bfs(gu, r)
+        oh, op, oit = ou.bfs(r)
+        assert np.array_equal(h, oh) and np.array_equal(par, op), r
+        assert st.iterations == oit
+    lab, _ = gpu.cc(gu)
+    olab, _ = ou.cc()
+    assert np.array_equal(lab, olab)
+    gw = gpu.Graph.load_directed(pw, n, weighted=True)
+    ow = oracle.OracleGraph(pw, n, oracle.DIRECTED | oracle.WEIGHTED)
+    for r in _roots(n, 4, 2):
+        d, st = gpu.sssp(gw, r)
+        od, oit = ow.sssp(r)
+        assert np.array_equal(d, od), r
+        assert st.iterations == oit
+    total, per, _ = gpu.tc(gpu.Graph.load_directed(p, n, remove_cycles=True))
+    ototal, oper = oracle.OracleGraph(p, n, oracle.DIRECTED | oracle.ACYCLIC).tc()
+    assert total == ototal and np.array_equal(per, oper)
+
+
+def test_graph_structure_vs_oracle(gpu, oracle, rmat16):
+    p, pw, n = rmat16
+    for flags in (0, gpu.DIRECTED, gpu.DIRECTED | gpu.ACYCLIC, gpu.DIRECTED | gpu.REVERSE):
+        g = gpu.Graph.load(p, n, flags)
+        og = oracle.OracleGraph(p, n, flags)
+        assert (g.info.nregular, g.info.nsink, g.info.nsource) == og.classes(), flags
+        assert g.info.nentries == og.nedges
+        pos, ids = g.positions()
+        opos, oids = og.positions()
+        assert np.array_equal(pos, opos) and np.array_equal(ids, oids)
+
+
+def test_repeated_calls_are_identical(gpu, rmat16):
+    p, pw, n = rmat16
+    g = gpu.Graph.load_undirected(p, n)
+    a = gpu.bfs(g, 11)[:2]
+    b = gpu.bfs(g, 11)[:2]
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    gd = gpu.Graph.load_directed(p, n)
+    r1 = gpu.pagerank(gd, 5)[0]
+    r2 = gpu.pagerank(gd, 5)[0]
+    assert np.array_equal(r1.view(np.uint64), r2.view(np.uint64))
+
+
+def test_wrong_graph_kind_is_rejected(gpu, rmat16):
+    p, pw, n = rmat16
+    g = gpu.Graph.load_undirected(p, n)
+    with pytest.raises(gpu.LA3GError):
+        gpu.pagerank(g, 3)
+    with pytest.raises(gpu.LA3GError):
+        gpu.sssp(g, 1)
+    with pytest.raises(gpu.LA3GError):
+        gpu.tc(g)
+
+
+def test_out_of_range_ids_rejected(gpu, tmp_path):
+    p = tmp_path / "bad.bin"
+    np.array([[1, 2], [3, 99]], np.uint32).tofile(p)
+    with pytest.raises(gpu.LA3GError) as ei:
+        gpu.Graph.load_undirected(p, 8)
+    assert ei.value.status == 1
