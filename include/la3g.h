@@ -122,6 +122,12 @@ int la3g_graph_from_edges(const la3g_edges* e, uint32_t n, uint32_t nright, uint
 void la3g_graph_free(la3g_graph* g);
 int la3g_graph_info_get(const la3g_graph* g, la3g_graph_info* out);
 
+/* Runs the graph's subsequent calls on the caller's CUDA stream (a
+ * cudaStream_t passed as void*; NULL = back to the graph's own stream).
+ * The reference has no streams; this exists so that a caller can bracket
+ * calls with its own CUDA events. */
+int la3g_graph_set_stream(la3g_graph* g, void* cuda_stream);
+
 /* Reverse-engine view: vertex id -> internal position (Locator order
  * regular, sink, source, isolated; src/utils/locator.h:84-120).  Either
  * array may be NULL. */

@@ -109,6 +109,11 @@ class Graph:
     def nslots(self) -> int:
         return self.info.nslots
 
+    def set_stream(self, cuda_stream: int | None) -> None:
+        """Run subsequent calls on the given cudaStream_t (an int handle, e.g.
+        torch.cuda.current_stream().cuda_stream); None = the graph's own."""
+        N.check(N.lib().la3g_graph_set_stream(self._h, C.c_void_p(cuda_stream) if cuda_stream else None))
+
     def positions(self) -> tuple[np.ndarray, np.ndarray]:
         pos = np.empty(self.nslots, np.uint32)
         ids = np.empty(self.nslots, np.uint32)

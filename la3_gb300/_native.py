@@ -81,6 +81,7 @@ SIGNATURES = {
     "la3g_graph_from_edges": (C.c_int, [C.POINTER(Edges), C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(_P)]),
     "la3g_graph_free": (None, [_P]),
     "la3g_graph_info_get": (C.c_int, [_P, C.POINTER(GraphInfo)]),
+    "la3g_graph_set_stream": (C.c_int, [_P, _P]),
     "la3g_graph_positions": (C.c_int, [_P, _u32p, _u32p]),
     "la3g_pr": (C.c_int, [_P, C.c_uint32, _f64p, _u32p, _statp]),
     "la3g_pr_f32": (C.c_int, [_P, C.c_uint32, C.c_double, _f64p, _f64p, _statp]),

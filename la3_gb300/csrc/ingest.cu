@@ -363,13 +363,14 @@ static int new_graph(uint32_t n, uint32_t nright, uint32_t flags, la3g_graph** o
   *out = nullptr;
   la3g_graph* g = new (std::nothrow) la3g_graph();
   if (!g) return set_error(LA3G_ENOMEM, "out of host memory");
-  if (cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking) != cudaSuccess ||
+  if (cudaStreamCreateWithFlags(&g->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&g->ev0) != cudaSuccess || cudaEventCreate(&g->ev1) != cudaSuccess)
   {
     cudaError_t e = cudaGetLastError();
     la3g_graph_free(g);
     return set_error(LA3G_ECUDA, "cannot create a CUDA stream: %s", cudaGetErrorString(e));
   }
+  g->stream = g->own_stream;
   DevGraph& d = g->g;
   const bool bip = flags & LA3G_BIPARTITE;
   d.flags = flags;
@@ -402,13 +403,22 @@ extern "C" void la3g_graph_free(la3g_graph* g)
 {
   if (!g) return;
   if (g->stream) cudaStreamSynchronize(g->stream);
+  if (g->own_stream && g->own_stream != g->stream) cudaStreamSynchronize(g->own_stream);
   for (int i = 0; i < kSlotCount; i++)
     if (g->slot[i] && g->slot_free[i]) g->slot_free[i](g->slot[i]);
   for (void* p : g->allocations) cudaFree(p);
   if (g->ev0) cudaEventDestroy(g->ev0);
   if (g->ev1) cudaEventDestroy(g->ev1);
-  if (g->stream) cudaStreamDestroy(g->stream);
+  if (g->own_stream) cudaStreamDestroy(g->own_stream);
   delete g;
+}
+
+extern "C" int la3g_graph_set_stream(la3g_graph* g, void* cuda_stream)
+{
+  if (!g) return set_error(LA3G_EINVAL, "null graph");
+  LA3G_CUDA(cudaStreamSynchronize(g->stream));
+  g->stream = cuda_stream ? (cudaStream_t) cuda_stream : g->own_stream;
+  return LA3G_OK;
 }
 
 extern "C" int la3g_graph_from_records(const void* records, uint64_t nrec, uint32_t n, uint32_t nright,

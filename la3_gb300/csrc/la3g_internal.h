@@ -164,7 +164,8 @@ enum AppSlot { kSlotPr = 0, kSlotBfs, kSlotSssp, kSlotCc, kSlotTc, kSlotBm25, kS
 struct la3g_graph
 {
   la3g::DevGraph g;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;       // stream the calls run on
+  cudaStream_t own_stream = nullptr;   // the graph's own stream
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::vector<void*> allocations;
   uint64_t device_bytes = 0;

@@ -238,6 +238,7 @@ static int sssp_run(la3g_graph* G, SsspScratch* ss, uint32_t root, la3g_stats* s
     nfront = nn;
     front_deg = nn ? ss->hctr[1] : 0;
     cur ^= 1;
+    if (nn == 0) break;  // this iteration activated nothing
   }
   if (g.nsink)
   {

@@ -25,6 +25,7 @@ namespace la3g {
 struct TcScratch
 {
   uint32_t* ntri = nullptr;
+  uint32_t* esrc = nullptr;  // lower endpoint of each oriented edge
   unsigned long long* total = nullptr;
 };
 
@@ -36,40 +37,41 @@ __device__ __forceinline__ uint32_t ckey(uint32_t c, uint32_t src_base, uint32_t
   return c >= src_base ? c - src_base : c + nsrc;
 }
 
+// Lower endpoint of every push-CSR entry.
+__global__ void k_tc_expand(const uint32_t* __restrict__ optr, uint32_t ncols, uint32_t* __restrict__ src)
+{
+  for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < ncols; u += gridDim.x * blockDim.x)
+    for (uint32_t e = optr[u]; e < optr[u + 1]; e++) src[e] = u;
+}
+
+// One warp per oriented edge (u, v): lanes take the elements of the shorter
+// of N<(u), N<(v) and binary-search them in the longer one.
 __global__ void __launch_bounds__(256)
-k_tc(const uint32_t* __restrict__ optr, const uint32_t* __restrict__ orow, const uint32_t* __restrict__ iptr,
-     const uint32_t* __restrict__ icol, uint32_t ncols, uint32_t src_base, uint32_t nsrc, uint32_t* ntri)
+k_tc(const uint32_t* __restrict__ esrc, const uint32_t* __restrict__ orow, uint64_t m, const uint32_t* __restrict__ iptr,
+     const uint32_t* __restrict__ icol, uint32_t src_base, uint32_t nsrc, uint32_t* ntri)
 {
   const int lane = threadIdx.x & 31;
-  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-  // warps walk columns u; inside, each oriented edge (u, v) in turn
-  for (uint32_t u = warp; u < ncols; u += nwarps)
+  const uint64_t warp = ((uint64_t) blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t) gridDim.x * blockDim.x) >> 5;
+  for (uint64_t e = warp; e < m; e += nwarps)
   {
-    const uint32_t eb = optr[u], ee = optr[u + 1];
-    if (eb == ee) continue;
-    const uint32_t ub = iptr[u], ue = iptr[u + 1];
+    const uint32_t u = esrc[e], v = orow[e];
+    const uint32_t ub = iptr[u], ue = iptr[u + 1], vb = iptr[v], ve = iptr[v + 1];
+    uint32_t ab = ub, ae = ue, bb = vb, be = ve;
+    if (ae - ab > be - bb) { ab = vb; ae = ve; bb = ub; be = ue; }
+    if (ab == ae) continue;
     uint32_t acc = 0;
-    for (uint32_t e = eb; e < ee; e++)
+    for (uint32_t i = ab + lane; i < ae; i += 32)
     {
-      const uint32_t v = orow[e];
-      const uint32_t vb = iptr[v], ve = iptr[v + 1];
-      // shorter list A, longer list B
-      uint32_t ab = ub, ae = ue, bb = vb, be = ve;
-      if (ae - ab > be - bb) { ab = vb; ae = ve; bb = ub; be = ue; }
-      if (ab == ae) continue;
-      for (uint32_t i = ab + lane; i < ae; i += 32)
+      const uint32_t key = ckey(icol[i], src_base, nsrc);
+      uint32_t lo = bb, hi = be;
+      while (lo < hi)
       {
-        const uint32_t key = ckey(icol[i], src_base, nsrc);
-        uint32_t lo = bb, hi = be;
-        while (lo < hi)
-        {
-          uint32_t mid = (lo + hi) >> 1;
-          if (ckey(icol[mid], src_base, nsrc) < key) lo = mid + 1;
-          else hi = mid;
-        }
-        if (lo < be && ckey(icol[lo], src_base, nsrc) == key) acc++;
+        uint32_t mid = (lo + hi) >> 1;
+        if (ckey(icol[mid], src_base, nsrc) < key) lo = mid + 1;
+        else hi = mid;
       }
+      if (lo < be && ckey(icol[lo], src_base, nsrc) == key) acc++;
     }
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane == 0 && acc) atomicAdd(&ntri[u], acc);
@@ -111,6 +113,9 @@ extern "C" int la3g_tc(la3g_graph* G, uint64_t* total_out, uint32_t* per_vertex_
     G->slot_free[kSlotTc] = tc_scratch_free;
     LA3G_TRY(galloc(G, &ts->ntri, g.nslots));
     LA3G_TRY(galloc(G, &ts->total, 1));
+    LA3G_TRY(galloc(G, &ts->esrc, g.nent + 1));
+    k_tc_expand<<<grid_for(g.nslots, 256), 256, 0, G->stream>>>(g.out_ptr, g.nslots, ts->esrc);
+    LA3G_LAUNCHED();
   }
   cudaStream_t s = G->stream;
   const uint32_t N = g.nslots;
@@ -119,8 +124,8 @@ extern "C" int la3g_tc(la3g_graph* G, uint64_t* total_out, uint32_t* per_vertex_
   LA3G_CUDA(cudaMemsetAsync(ts->total, 0, 8, s));
   {
     ProfileScope p("tc_intersect", s, 8.0 * g.nent);
-    k_tc<<<grid_for((uint64_t) N * 32, 256, kSMs * 32), 256, 0, s>>>(g.out_ptr, g.out_row, g.in_ptr, g.in_col, N,
-                                                                     g.src_base(), g.nsrc, ts->ntri);
+    k_tc<<<grid_for((uint64_t) g.nent * 32, 256, kSMs * 32), 256, 0, s>>>(ts->esrc, g.out_row, g.nent, g.in_ptr,
+                                                                          g.in_col, g.src_base(), g.nsrc, ts->ntri);
     LA3G_LAUNCHED();
   }
   k_tc_sum<<<grid_for(N, 256), 256, 0, s>>>(N, ts->ntri, ts->total);
