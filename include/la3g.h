@@ -197,6 +197,29 @@ int la3g_bfs_batch(la3g_graph* g, const uint32_t* roots, uint32_t nroots, uint8_
 int la3g_sssp_batch(la3g_graph* g, const uint32_t* roots, uint32_t nroots, uint32_t* dist_out,
                     la3g_stats* st);
 
+/* ---- caller-allocated form -------------------------------------------- */
+
+/* BFS that allocates nothing.  It has no counterpart in the reference: it is
+ * for callers that cannot allocate device memory at call time — code running
+ * under a memory manager that owns every device byte, a serving loop that
+ * must not take cudaMalloc/cudaFree's implicit device synchronisation on its
+ * latency path, or a host that pre-reserves all memory at start-up.  The
+ * caller passes an undirected graph already in device memory as a CSR over
+ * vertices 0..nvertices-1 (row_ptr: nvertices + 1 offsets; col: neighbour
+ * ids, each row sorted by ascending key; key: one uint32 per vertex) and the
+ * device output arrays hops and parent (nvertices each).  Results follow
+ * la3g_bfs: hops 255 = unreached; parent = the key of the frontier neighbour
+ * with the largest key (with key = the hashed id of the reference's bucket
+ * hasher, hops and parent equal la3g_bfs's).  The library's temporaries sit in
+ * one fixed device array of about 12.8 MB, so nvertices is limited to
+ * 1048576 (2^20); larger graphs are rejected with LA3G_EINVAL.  The first
+ * call on a device looks the array up and caches its address: make that call
+ * before capturing a stream.  Calls share the array, so calls that overlap on
+ * the GPU race; run them one at a time.  cuda_stream: a cudaStream_t as void*
+ * (NULL = the default stream).  st may be NULL. */
+int la3g_bfs_noalloc(const uint32_t* row_ptr, const uint32_t* col, const uint32_t* key, uint32_t nvertices,
+                     uint32_t root, uint8_t* hops, uint32_t* parent, void* cuda_stream, la3g_stats* st);
+
 /* ---- synthetic inputs -------------------------------------------------- */
 
 int la3g_gen_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c, uint64_t seed,

@@ -93,6 +93,7 @@ SIGNATURES = {
     "la3g_bm25_query": (C.c_int, [_P, _u32p, C.c_uint32, C.c_uint32, _u32p, _f32p, _u32p, _f32p, _u8p, _statp]),
     "la3g_bfs_batch": (C.c_int, [_P, _u32p, C.c_uint32, _u8p, _statp]),
     "la3g_sssp_batch": (C.c_int, [_P, _u32p, C.c_uint32, _u32p, _statp]),
+    "la3g_bfs_noalloc": (C.c_int, [_P, _P, _P, C.c_uint32, C.c_uint32, _P, _P, _P, _statp]),
     "la3g_gen_rmat": (C.c_int, [C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double, C.c_uint64, C.c_int,
                                 C.c_uint64, C.POINTER(Edges)]),
     "la3g_gen_er": (C.c_int, [C.c_uint32, C.c_uint64, C.c_uint64, C.c_int, C.c_uint64, C.POINTER(Edges)]),

@@ -19,6 +19,7 @@
 // back top-down when the frontier holds fewer than n / beta vertices.
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 
 #include "la3g_internal.h"
 
@@ -393,4 +394,180 @@ extern "C" int la3g_bfs(la3g_graph* G, uint32_t root, uint8_t* hops_out, uint32_
     }
   }
   return T.finish();
+}
+
+// ---------------------------------------------------------------------------
+// la3g_bfs_noalloc: the same BFS kernels over a CSR the caller already holds
+// in device memory, with every temporary in one fixed device array, so the
+// call itself never allocates.
+//
+// The scratch lives in `g_bfs_noalloc_scratch`, a file-scope __device__
+// array: each GPU that loads this library holds it (kNoAllocScratchBytes,
+// about 12.8 MB) until the process exits.  Host code must not hand the
+// array's name to a kernel (on the host it only names a stand-in object);
+// its device address is looked up once per device with
+// cudaGetSymbolAddress, on the first call made while that device is
+// current, and cached.  That first call therefore does the set-up and should
+// come before any stream capture that includes this entry point.
+//
+// All calls share the one array and it keeps whatever the last call left in
+// it; the call clears what has to start at zero.  Two calls whose work
+// overlaps on the GPU (different streams, or different host threads on one
+// device) race on the array: serialise them.
+// ---------------------------------------------------------------------------
+
+namespace la3g {
+
+static constexpr uint32_t kNoAllocMaxVertices = 1u << 20;
+static constexpr size_t kNaAlign = 256;
+static constexpr size_t na_round(size_t b) { return (b + kNaAlign - 1) / kNaAlign * kNaAlign; }
+static constexpr uint32_t kNaWords = kNoAllocMaxVertices / 32 + 1;
+static constexpr size_t kNaCandOff = 0;
+static constexpr size_t kNaList0Off = kNaCandOff + na_round(sizeof(uint32_t) * kNoAllocMaxVertices);
+static constexpr size_t kNaList1Off = kNaList0Off + na_round(sizeof(uint32_t) * kNoAllocMaxVertices);
+static constexpr size_t kNaBits0Off = kNaList1Off + na_round(sizeof(uint32_t) * kNoAllocMaxVertices);
+static constexpr size_t kNaBits1Off = kNaBits0Off + na_round(sizeof(uint32_t) * kNaWords);
+static constexpr size_t kNaCtrOff = kNaBits1Off + na_round(sizeof(uint32_t) * kNaWords);
+static constexpr size_t kNaRedOff = kNaCtrOff + na_round(sizeof(BfsCounters));
+static constexpr size_t kNoAllocScratchBytes = kNaRedOff + na_round(sizeof(unsigned long long));
+
+static __device__ __align__(256) unsigned char g_bfs_noalloc_scratch[kNoAllocScratchBytes];
+
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_addr[256];
+
+// Device address of the scratch array for the current device (looked up
+// once per device).
+static int noalloc_scratch(unsigned char** out)
+{
+  int dev = 0;
+  LA3G_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 256) return set_error(LA3G_EINVAL, "device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[dev])
+  {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_bfs_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+    {
+      cudaGetLastError();
+      return set_error(LA3G_ECUDA, "cudaGetSymbolAddress(scratch) failed on device %d: %s", dev,
+                       cudaGetErrorString(e));
+    }
+    g_noalloc_addr[dev] = p;
+  }
+  *out = (unsigned char*) g_noalloc_addr[dev];
+  return LA3G_OK;
+}
+
+}  // namespace la3g
+
+extern "C" int la3g_bfs_noalloc(const uint32_t* row_ptr, const uint32_t* col, const uint32_t* key,
+                                uint32_t nvertices, uint32_t root, uint8_t* hops, uint32_t* parent,
+                                void* cuda_stream, la3g_stats* st)
+{
+  using namespace la3g;
+  if (st) std::memset(st, 0, sizeof *st);
+  if (nvertices == 0 || nvertices > kNoAllocMaxVertices)
+    return set_error(LA3G_EINVAL,
+                     "la3g_bfs_noalloc: nvertices = %u; it must be between 1 and %u (the size of its fixed scratch)",
+                     nvertices, kNoAllocMaxVertices);
+  if (!row_ptr || !col || !key || !hops || !parent)
+    return set_error(LA3G_EINVAL, "la3g_bfs_noalloc: row_ptr, col, key, hops and parent must be device pointers");
+  unsigned char* base = nullptr;
+  LA3G_TRY(noalloc_scratch(&base));
+  cudaStream_t s = (cudaStream_t) cuda_stream;
+  uint32_t* cand = (uint32_t*) (base + kNaCandOff);
+  uint32_t* list[2] = {(uint32_t*) (base + kNaList0Off), (uint32_t*) (base + kNaList1Off)};
+  uint32_t* bits[2] = {(uint32_t*) (base + kNaBits0Off), (uint32_t*) (base + kNaBits1Off)};
+  BfsCounters* ctr = (BfsCounters*) (base + kNaCtrOff);
+  unsigned long long* red = (unsigned long long*) (base + kNaRedOff);
+  const uint32_t N = nvertices;
+  const uint32_t words = (N + 31) / 32 + 1;
+  double t0 = now_ms();
+
+  // hops = 255, parent = 0 and the candidates cleared (they must start at 0)
+  k_bfs_init<<<grid_for(N, 256), 256, 0, s>>>(N, hops, parent, cand);
+  LA3G_LAUNCHED();
+  uint32_t iter = 0, pull_iters = 0;
+  if (root < N)
+  {
+    uint32_t m = 0, rp[2] = {0, 0};
+    LA3G_CUDA(cudaMemcpyAsync(&m, row_ptr + N, 4, cudaMemcpyDeviceToHost, s));
+    LA3G_CUDA(cudaMemcpyAsync(rp, row_ptr + root, 8, cudaMemcpyDeviceToHost, s));
+    LA3G_CUDA(cudaStreamSynchronize(s));
+    k_bfs_root<<<1, 1, 0, s>>>(root, hops, list[0]);
+    LA3G_LAUNCHED();
+    uint64_t nfront = rp[1] > rp[0] ? 1 : 0;
+    uint64_t front_deg = rp[1] - rp[0];
+    uint64_t unvisited_deg = m - front_deg;
+    bool bottom_up = false, front_is_list = true;
+    int cur = 0;
+    BfsCounters h;
+    for (;;)
+    {
+      if (iter > 100000) return set_error(LA3G_ETIMEOUT, "la3g_bfs_noalloc did not converge");
+      if (!bottom_up && (double) front_deg > (double) unvisited_deg / 14.0) bottom_up = true;
+      else if (bottom_up && (double) nfront < (double) N / 24.0) bottom_up = false;
+      const uint8_t hop = (uint8_t) (iter + 1);
+      if (nfront == 0) { iter++; break; }
+      LA3G_CUDA(cudaMemsetAsync(ctr, 0, sizeof(BfsCounters), s));
+      if (bottom_up)
+      {
+        if (front_is_list)
+        {
+          LA3G_CUDA(cudaMemsetAsync(bits[cur], 0, (size_t) words * 4, s));
+          k_list_to_bits<<<grid_for(nfront, 256), 256, 0, s>>>(list[cur], (uint32_t) nfront, bits[cur]);
+          LA3G_LAUNCHED();
+        }
+        LA3G_CUDA(cudaMemsetAsync(bits[cur ^ 1], 0, (size_t) words * 4, s));
+        k_bfs_bu<<<grid_for(N, 256, kSMs * 16), 256, 0, s>>>(row_ptr, col, key, N, bits[cur], bits[cur ^ 1], hop, hops,
+                                                            parent, ctr);
+        LA3G_LAUNCHED();
+        front_is_list = false;
+        pull_iters++;
+      }
+      else
+      {
+        if (!front_is_list)
+        {
+          LA3G_CUDA(cudaMemsetAsync(red, 0, 8, s));
+          k_bits_to_list<<<grid_for(words, 256), 256, 0, s>>>(bits[cur], words, list[cur], red);
+          LA3G_LAUNCHED();
+        }
+        k_bfs_td<<<grid_for(nfront * 32, 256), 256, 0, s>>>(row_ptr, col, key, list[cur], (uint32_t) nfront, hops, cand,
+                                                            list[cur ^ 1], ctr);
+        LA3G_LAUNCHED();
+        LA3G_CUDA(cudaMemcpyAsync(&h, ctr, sizeof h, cudaMemcpyDeviceToHost, s));
+        LA3G_CUDA(cudaStreamSynchronize(s));
+        if (h.next_count)
+        {
+          k_bfs_td_apply<<<grid_for(h.next_count, 256), 256, 0, s>>>(row_ptr, list[cur ^ 1], (uint32_t) h.next_count,
+                                                                     hop, hops, parent, cand, ctr);
+          LA3G_LAUNCHED();
+        }
+        front_is_list = true;
+      }
+      LA3G_CUDA(cudaMemcpyAsync(&h, ctr, sizeof h, cudaMemcpyDeviceToHost, s));
+      LA3G_CUDA(cudaStreamSynchronize(s));
+      nfront = h.next_count;
+      front_deg = h.next_degsum;
+      unvisited_deg -= std::min<uint64_t>(unvisited_deg, front_deg);
+      cur ^= 1;
+      iter++;
+      if (nfront == 0) break;
+    }
+  }
+  else
+  {
+    iter = 1;
+  }
+  LA3G_CUDA(cudaStreamSynchronize(s));
+  if (st)
+  {
+    st->iterations = iter;
+    st->pull_iterations = pull_iters;
+    st->host_ms = now_ms() - t0;
+  }
+  return LA3G_OK;
 }
