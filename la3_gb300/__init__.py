@@ -219,6 +219,28 @@ class BM25:
         return ids[:n].copy(), scores[:n].copy(), (alls, act), st
 
 
+def read_queries(labels_path: str, queries_path: str, ndocs: int) -> list[list[int]]:
+    """prepare_queries (helpers.hpp:76-123): the label on line i of the term
+    labels file is term vertex ndocs + i + 1; each query line is a list of
+    labels; a label that is not in the file maps to vertex 0."""
+    ids = {}
+    with open(labels_path) as f:
+        i = 0
+        for line in f:
+            parts = line.split()
+            if not parts:
+                continue
+            ids[parts[0]] = i + 1 + ndocs
+            i += 1
+    out = []
+    with open(queries_path) as f:
+        for line in f:
+            toks = line.split()
+            if toks:
+                out.append([ids.get(t, 0) for t in toks])
+    return out
+
+
 def bfs_batch(G: Graph, roots: Sequence[int], want_hops: bool = True):
     r = np.ascontiguousarray(np.asarray(roots, dtype=np.uint32))
     st = Stats()
@@ -315,5 +337,5 @@ def profile_report() -> dict:
 
 
 __all__ = ["Graph", "EdgeList", "BM25", "LA3GError", "Stats", "pagerank", "pagerank_f32", "bfs", "sssp", "cc", "tc",
-           "bfs_batch", "sssp_batch", "profile", "profile_reset", "profile_report", "DIRECTED", "REVERSE", "ACYCLIC",
+           "bfs_batch", "sssp_batch", "read_queries", "profile", "profile_reset", "profile_report", "DIRECTED", "REVERSE", "ACYCLIC",
            "BIPARTITE", "WEIGHTED", "SSSP_INF", "BFS_INF"]

@@ -4,17 +4,6 @@
 
 using namespace la3g;
 
-extern "C" int la3g_bm25_prepare(la3g_graph*, uint64_t*, float*, float*)
-{
-  return set_error(LA3G_EINVAL, "la3g_bm25_prepare is not available in this build");
-}
-
-extern "C" int la3g_bm25_query(la3g_graph*, const uint32_t*, uint32_t, uint32_t, uint32_t*, float*, uint32_t*, float*,
-                               uint8_t*, la3g_stats*)
-{
-  return set_error(LA3G_EINVAL, "la3g_bm25_query is not available in this build");
-}
-
 extern "C" int la3g_bfs_batch(la3g_graph*, const uint32_t*, uint32_t, uint8_t*, la3g_stats*)
 {
   return set_error(LA3G_EINVAL, "la3g_bfs_batch is not available in this build");

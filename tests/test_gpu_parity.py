@@ -157,3 +157,49 @@ def test_out_of_range_ids_rejected(gpu, tmp_path):
     with pytest.raises(gpu.LA3GError) as ei:
         gpu.Graph.load_undirected(p, 8)
     assert ei.value.status == 1
+
+
+def test_bm25_golden(gpu, golden):
+    L = gpu
+    for name in _cases(golden, "bm25"):
+        c = golden[name]
+        ref = np.load(GOLD / f"{name}.npz")
+        g = L.Graph.load_bipartite(DATA / c["file"], c["ndocs"], c["nterms"])
+        b = L.BM25(g, want_length=True)
+        assert b.collection_ntokens == c["collection_ntokens"], name
+        assert np.array_equal(b.length.view(np.uint32), ref["length"].view(np.uint32)), name
+        queries = L.read_queries(DATA / c["labels"], DATA / c["queries"], c["ndocs"])
+        for qi, q in enumerate(queries):
+            ids, sc, (alls, act), st = b.query(q, c["k"], full=True)
+            rid, rsc = ref[f"q{qi}_ids"], ref[f"q{qi}_scores"]
+            assert np.array_equal(np.flatnonzero(act), np.sort(rid)), (name, qi)
+            order = np.argsort(rid)
+            assert np.array_equal(alls[rid[order]].view(np.uint32), rsc[order].view(np.uint32)), (name, qi)
+            # canonical top-k: score desc, id asc over the reference's scores
+            want = sorted(zip(rid.tolist(), rsc.tolist()), key=lambda t: (-t[1], t[0]))[: c["k"]]
+            assert ids.tolist() == [w[0] for w in want], (name, qi)
+            assert np.array_equal(sc, np.array([w[1] for w in want], np.float32)), (name, qi)
+
+
+def test_bm25_corpus_vs_oracle(gpu, oracle, tmp_path):
+    L = gpu
+    D, T = 20000, 3000
+    e = L.EdgeList.bipartite(D, T, 30, seed=77)
+    p = tmp_path / "c.w.bp.bin"
+    e.write(p)
+    g = L.Graph.load_bipartite(p, D, T)
+    b = L.BM25(g, want_length=True)
+    og = oracle.OracleGraph(p, D, oracle.BIPARTITE | oracle.WEIGHTED, nright=T)
+    ob = oracle.OracleBM25(og)
+    assert b.collection_ntokens == ob.collection_ntokens
+    assert np.array_equal(b.length.view(np.uint32), ob.length.view(np.uint32))
+    rng = np.random.default_rng(3)
+    for qi in range(30):
+        q = sorted(set(int(x) for x in rng.integers(D + 1, D + T + 1, int(rng.integers(2, 9)))))
+        if qi % 5 == 4:
+            q = q[::-1] + [q[0]]  # not ascending, with a repeat: the reference's pairing
+        ids, sc, (alls, act), _ = b.query(q, 10, full=True)
+        oids, osc, oscores, oact = ob.query(q, 10)
+        assert np.array_equal(act, oact), qi
+        assert np.array_equal(alls.view(np.uint32), oscores.view(np.uint32)), qi
+        assert ids.tolist() == oids.tolist() and np.array_equal(sc, osc), qi
