@@ -286,6 +286,8 @@ def gpu_line(args, rank: int, world: int, local: int) -> dict | None:
     # L2: every step's inputs (s22 CSR ~ 0.5 GB) are larger than the 129 MB L2;
     # additionally the L2 is flushed before each step by writing 256 MB.
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    flush.fill_(1)  # first touch maps the pages (hundreds of ms): keep it out of the timed region
+    torch.cuda.synchronize()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
     app_ev = [[torch.cuda.Event(enable_timing=True) for _ in range(5)] for _ in range(K)]
     edges = 0.0

@@ -21,6 +21,7 @@
 #include <cstring>
 #include <mutex>
 
+#include "frontier.cuh"
 #include "la3g_internal.h"
 
 namespace la3g {
@@ -31,15 +32,29 @@ struct BfsCounters
   unsigned long long next_degsum;  // their degrees
 };
 
+// Frontier counters of la3g_bfs: a frontier is kept as two lists, vertices
+// of degree <= kBigDeg ("small", one warp each) and hubs ("big", whose edges
+// the whole grid shares), so that no warp serialises on a hub.
+struct FrontierCounters
+{
+  unsigned long long raw;      // vertices touched by the expansion
+  unsigned long long degsum;   // degrees of the next frontier
+  unsigned long long nsmall;   // next frontier: small list length
+  unsigned long long packed;   // next frontier: hub slots and hub tasks (frontier.cuh)
+};
+
 struct BfsScratch
 {
   uint8_t* hops = nullptr;
   uint32_t* parent = nullptr;
   uint32_t* cand = nullptr;        // top-down parent candidate + 1 (0 = none)
-  uint32_t* list[2] = {nullptr, nullptr};
+  uint32_t* raw = nullptr;         // touched vertices of a top-down step
+  uint32_t* small[2] = {nullptr, nullptr};
+  uint32_t* big[2] = {nullptr, nullptr};
+  uint32_t* big_task0[2] = {nullptr, nullptr};
   uint32_t* bits[2] = {nullptr, nullptr};
-  BfsCounters* ctr = nullptr;      // device
-  BfsCounters* hctr = nullptr;     // pinned host mirror
+  FrontierCounters* ctr = nullptr;      // device
+  FrontierCounters* hctr = nullptr;     // pinned host mirror
   unsigned long long* red = nullptr;  // reduction scratch
   uint32_t words = 0;
 };
@@ -193,6 +208,143 @@ __global__ void k_bits_to_list(const uint32_t* __restrict__ bits, uint32_t words
   }
 }
 
+// Top-down over a split frontier.  Hubs first: every warp of the grid
+// takes a slice of each hub's edges; then one warp per small vertex.  A
+// touched unvisited vertex keeps the largest key + 1 in cand; the thread that
+// moves cand away from 0 records the vertex in `raw`.
+__device__ __forceinline__ void td_visit(uint32_t v, bool valid, uint32_t hu, const uint8_t* __restrict__ hops,
+                                         uint32_t* cand, uint32_t* raw, FrontierCounters* ctr, int lane)
+{
+  bool add = false;
+  if (valid && hops[v] == 255) add = atomicMax(&cand[v], hu) == 0;
+  const unsigned mask = __ballot_sync(0xffffffffu, add);
+  if (mask)
+  {
+    uint32_t base = 0;
+    if (lane == 0) base = (uint32_t) atomicAdd(&ctr->raw, (unsigned long long) __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (add) raw[base + __popc(mask & ((1u << lane) - 1))] = v;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+k_bfs_td_split(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ key,
+               const uint32_t* __restrict__ small, uint32_t nsmall, const uint32_t* __restrict__ big,
+               const uint32_t* __restrict__ big_task0, uint32_t nbig, uint32_t ntasks,
+               const uint8_t* __restrict__ hops, uint32_t* cand, uint32_t* raw, FrontierCounters* ctr)
+{
+  const int lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t t = warp; t < ntasks; t += nwarps)
+  {
+    const uint32_t slot = hub_of_task(big_task0, nbig, t);
+    const uint32_t u = big[slot];
+    const uint32_t hu = key[u] + 1;
+    const uint32_t b = ptr[u] + (t - big_task0[slot]) * kHubTask;
+    const uint32_t e = min(b + kHubTask, ptr[u + 1]);
+    for (uint32_t i0 = b; i0 < e; i0 += 32)
+    {
+      const uint32_t i = i0 + lane;
+      td_visit(i < e ? col[i] : 0, i < e, hu, hops, cand, raw, ctr, lane);
+    }
+  }
+  for (uint32_t f = warp; f < nsmall; f += nwarps)
+  {
+    const uint32_t u = small[f];
+    const uint32_t hu = key[u] + 1;
+    const uint32_t b = ptr[u], e = ptr[u + 1];
+    for (uint32_t i0 = b; i0 < e; i0 += 32)
+    {
+      const uint32_t i = i0 + lane;
+      td_visit(i < e ? col[i] : 0, i < e, hu, hops, cand, raw, ctr, lane);
+    }
+  }
+}
+
+__device__ __forceinline__ void push_split(uint32_t v, uint32_t deg, uint32_t* small, uint32_t* big,
+                                           uint32_t* big_task0, FrontierCounters* ctr)
+{
+  if (deg > kBigDeg) hub_append(v, deg, big, big_task0, &ctr->packed);
+  else small[atomicAdd(&ctr->nsmall, 1ull)] = v;
+}
+
+// Top-down apply: touched vertices take hops and parent and form the next
+// frontier, split by degree.
+__global__ void k_bfs_td_apply_split(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ raw, uint8_t hop,
+                                     uint8_t* hops, uint32_t* parent, uint32_t* cand, uint32_t* small, uint32_t* big,
+                                     uint32_t* big_task0, FrontierCounters* ctr)
+{
+  unsigned long long deg = 0;
+  const uint32_t n = (uint32_t) ctr->raw;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+  {
+    uint32_t v = raw[i];
+    hops[v] = hop;
+    parent[v] = cand[v] - 1;
+    cand[v] = 0;
+    uint32_t d = ptr[v + 1] - ptr[v];
+    deg += d;
+    push_split(v, d, small, big, big_task0, ctr);
+  }
+  for (int o = 16; o > 0; o >>= 1) deg += __shfl_xor_sync(0xffffffffu, deg, o);
+  if ((threadIdx.x & 31) == 0 && deg) atomicAdd(&ctr->degsum, deg);
+}
+
+// Bottom-up with the split counters (same scan as k_bfs_bu).
+__global__ void __launch_bounds__(256)
+k_bfs_bu_split(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ key,
+               uint32_t nrows, const uint32_t* __restrict__ fbits, uint32_t* nbits, uint8_t hop, uint8_t* hops,
+               uint32_t* parent, FrontierCounters* ctr)
+{
+  unsigned long long cnt = 0, deg = 0;
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nrows; v += gridDim.x * blockDim.x)
+  {
+    if (hops[v] != 255) continue;
+    const uint32_t b = ptr[v], e = ptr[v + 1];
+    for (uint32_t i = e; i > b; i--)
+    {
+      const uint32_t u = col[i - 1];
+      if (fbits[u >> 5] & (1u << (u & 31)))
+      {
+        hops[v] = hop;
+        parent[v] = key[u];
+        atomicOr(&nbits[v >> 5], 1u << (v & 31));
+        cnt++;
+        deg += e - b;
+        break;
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1)
+  {
+    cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    deg += __shfl_xor_sync(0xffffffffu, deg, o);
+  }
+  if ((threadIdx.x & 31) == 0 && cnt)
+  {
+    atomicAdd(&ctr->raw, cnt);
+    atomicAdd(&ctr->degsum, deg);
+  }
+}
+
+// Bitmap frontier -> split lists.
+__global__ void k_bits_to_split(const uint32_t* __restrict__ bits, uint32_t words, const uint32_t* __restrict__ ptr,
+                                uint32_t* small, uint32_t* big, uint32_t* big_task0, FrontierCounters* ctr)
+{
+  for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < words; w += gridDim.x * blockDim.x)
+  {
+    uint32_t x = bits[w];
+    while (x)
+    {
+      int b = __ffs(x) - 1;
+      x &= x - 1;
+      uint32_t v = w * 32 + b;
+      push_split(v, ptr[v + 1] - ptr[v], small, big, big_task0, ctr);
+    }
+  }
+}
+
 __global__ void k_reached_degsum(const uint32_t* __restrict__ ptr, const uint8_t* __restrict__ hops, uint32_t nrows,
                                  unsigned long long* out)
 {
@@ -211,6 +363,13 @@ __global__ void k_by_id(uint32_t N, const uint32_t* __restrict__ id_of_pos, cons
 
 __global__ void k_bfs_root(uint32_t rp, uint8_t* hops, uint32_t* list) { hops[rp] = 0; list[0] = rp; }
 
+__global__ void k_bfs_root_split(uint32_t rp, uint8_t* hops, uint32_t* list, uint32_t* task0)
+{
+  hops[rp] = 0;
+  list[0] = rp;
+  task0[0] = 0;
+}
+
 static int bfs_scratch(la3g_graph* G, BfsScratch** out)
 {
   BfsScratch* bs = (BfsScratch*) G->slot[kSlotBfs];
@@ -224,13 +383,18 @@ static int bfs_scratch(la3g_graph* G, BfsScratch** out)
   LA3G_TRY(galloc(G, &bs->hops, N));
   LA3G_TRY(galloc(G, &bs->parent, N));
   LA3G_TRY(galloc(G, &bs->cand, N));
-  LA3G_TRY(galloc(G, &bs->list[0], N));
-  LA3G_TRY(galloc(G, &bs->list[1], N));
+  LA3G_TRY(galloc(G, &bs->raw, N));
+  LA3G_TRY(galloc(G, &bs->small[0], N));
+  LA3G_TRY(galloc(G, &bs->small[1], N));
+  LA3G_TRY(galloc(G, &bs->big[0], N));
+  LA3G_TRY(galloc(G, &bs->big[1], N));
+  LA3G_TRY(galloc(G, &bs->big_task0[0], N));
+  LA3G_TRY(galloc(G, &bs->big_task0[1], N));
   LA3G_TRY(galloc(G, &bs->bits[0], bs->words));
   LA3G_TRY(galloc(G, &bs->bits[1], bs->words));
   LA3G_TRY(galloc(G, &bs->ctr, 1));
   LA3G_TRY(galloc(G, &bs->red, 1));
-  LA3G_CUDA(cudaHostAlloc(&bs->hctr, sizeof(BfsCounters), cudaHostAllocDefault));
+  LA3G_CUDA(cudaHostAlloc(&bs->hctr, sizeof(FrontierCounters), cudaHostAllocDefault));
   *out = bs;
   return LA3G_OK;
 }
@@ -253,89 +417,126 @@ static int bfs_run(la3g_graph* G, BfsScratch* bs, uint32_t root, la3g_stats* st)
   uint32_t rp = 0;
   LA3G_CUDA(cudaMemcpyAsync(&rp, g.pos_of_id + root, 4, cudaMemcpyDeviceToHost, s));
   LA3G_CUDA(cudaStreamSynchronize(s));
-  k_bfs_root<<<1, 1, 0, s>>>(rp, bs->hops, bs->list[0]);
+  uint32_t h_ptr[2] = {0, 0};
+  if (rp < nrows)
+  {
+    LA3G_CUDA(cudaMemcpyAsync(h_ptr, g.in_ptr + rp, 8, cudaMemcpyDeviceToHost, s));
+    LA3G_CUDA(cudaStreamSynchronize(s));
+  }
+  uint64_t front_deg = h_ptr[1] - h_ptr[0];
+  // An isolated root has no edges: iteration 0 activates nothing.
+  uint64_t nsmall = 0, nbig = 0, ntasks = 0;
+  if (rp < nrows) (front_deg > kBigDeg ? nbig : nsmall) = 1;
+  if (nbig) ntasks = (front_deg + kHubTask - 1) / kHubTask;
+  k_bfs_root_split<<<1, 1, 0, s>>>(rp, bs->hops, nbig ? bs->big[0] : bs->small[0], bs->big_task0[0]);
   LA3G_LAUNCHED();
   tls_launches++;
-  // An isolated root has no edges: iteration 0 activates nothing.
-  uint64_t nfront = rp < nrows ? 1 : 0;
-  uint32_t h_ptr[2];
-  LA3G_CUDA(cudaMemcpyAsync(h_ptr, g.in_ptr + rp, 8, cudaMemcpyDeviceToHost, s));
-  LA3G_CUDA(cudaStreamSynchronize(s));
-  uint64_t front_deg = nfront ? h_ptr[1] - h_ptr[0] : 0;
   uint64_t unvisited_deg = g.nent - front_deg;
   bool bottom_up = false, front_is_list = true;
   int cur = 0;
   const double alpha = 14.0, beta = 24.0;
   uint64_t edges_examined = 0;
+  const unsigned td_blocks = kSMs * 8;
   for (;;)
   {
     if (iter > 100000) return set_error(LA3G_ETIMEOUT, "bfs did not converge");
-    // choose direction
+    const uint64_t nfront = nsmall + nbig;
     if (!bottom_up && (double) front_deg > (double) unvisited_deg / alpha) bottom_up = true;
     else if (bottom_up && (double) nfront < (double) N / beta) bottom_up = false;
-    LA3G_CUDA(cudaMemsetAsync(bs->ctr, 0, sizeof(BfsCounters), s));
     const uint8_t hop = (uint8_t) (iter + 1);
     if (nfront == 0)
     {
       iter++;
       break;  // nothing active: this iteration activates nothing
     }
+    LA3G_CUDA(cudaMemsetAsync(bs->ctr, 0, sizeof(FrontierCounters), s));
     if (bottom_up)
     {
       if (front_is_list)
       {
         LA3G_CUDA(cudaMemsetAsync(bs->bits[cur], 0, (size_t) bs->words * 4, s));
-        k_list_to_bits<<<grid_for(nfront, 256), 256, 0, s>>>(bs->list[cur], (uint32_t) nfront, bs->bits[cur]);
-        LA3G_LAUNCHED();
-        tls_launches++;
+        if (nsmall)
+        {
+          k_list_to_bits<<<grid_for(nsmall, 256), 256, 0, s>>>(bs->small[cur], (uint32_t) nsmall, bs->bits[cur]);
+          LA3G_LAUNCHED();
+          tls_launches++;
+        }
+        if (nbig)
+        {
+          k_list_to_bits<<<grid_for(nbig, 256), 256, 0, s>>>(bs->big[cur], (uint32_t) nbig, bs->bits[cur]);
+          LA3G_LAUNCHED();
+          tls_launches++;
+        }
       }
       LA3G_CUDA(cudaMemsetAsync(bs->bits[cur ^ 1], 0, (size_t) bs->words * 4, s));
       {
         ProfileScope p("bfs_bottom_up", s, 4.0 * unvisited_deg + 8.0 * nrows + N / 8.0);
-        k_bfs_bu<<<grid_for(nrows, 256, kSMs * 16), 256, 0, s>>>(g.in_ptr, g.in_col, g.hash_of_pos, nrows, bs->bits[cur],
-                                                                bs->bits[cur ^ 1], hop, bs->hops, bs->parent, bs->ctr);
+        k_bfs_bu_split<<<grid_for(nrows, 256, kSMs * 16), 256, 0, s>>>(g.in_ptr, g.in_col, g.hash_of_pos, nrows,
+                                                                      bs->bits[cur], bs->bits[cur ^ 1], hop, bs->hops,
+                                                                      bs->parent, bs->ctr);
         LA3G_LAUNCHED();
       }
       edges_examined += unvisited_deg;
       front_is_list = false;
       pull_iters++;
+      LA3G_CUDA(cudaMemcpyAsync(bs->hctr, bs->ctr, sizeof(FrontierCounters), cudaMemcpyDeviceToHost, s));
+      LA3G_CUDA(cudaStreamSynchronize(s));
+      const uint64_t nn = bs->hctr->raw;
+      front_deg = bs->hctr->degsum;
+      bool next_bottom_up = !((double) nn < (double) N / beta);
+      if (nn && !next_bottom_up)
+      {
+        // leaving bottom-up: the next frontier becomes split lists
+        LA3G_CUDA(cudaMemsetAsync(&bs->ctr->nsmall, 0, 16, s));
+        k_bits_to_split<<<grid_for(bs->words, 256), 256, 0, s>>>(bs->bits[cur ^ 1], bs->words, g.in_ptr,
+                                                                  bs->small[cur ^ 1], bs->big[cur ^ 1],
+                                                                  bs->big_task0[cur ^ 1], bs->ctr);
+        LA3G_LAUNCHED();
+        tls_launches++;
+        LA3G_CUDA(cudaMemcpyAsync(bs->hctr, bs->ctr, sizeof(FrontierCounters), cudaMemcpyDeviceToHost, s));
+        LA3G_CUDA(cudaStreamSynchronize(s));
+        nsmall = bs->hctr->nsmall;
+        nbig = bs->hctr->packed >> kHubSlotShift;
+        ntasks = bs->hctr->packed & ((1ull << kHubSlotShift) - 1);
+        front_is_list = true;
+      }
+      else
+      {
+        nsmall = nn;  // count only; the frontier stays a bitmap
+        nbig = 0;
+        ntasks = 0;
+      }
     }
     else
     {
-      if (!front_is_list)
-      {
-        LA3G_CUDA(cudaMemsetAsync(bs->red, 0, 8, s));
-        k_bits_to_list<<<grid_for(bs->words, 256), 256, 0, s>>>(bs->bits[cur], bs->words, bs->list[cur], bs->red);
-        LA3G_LAUNCHED();
-        tls_launches++;
-      }
       {
         ProfileScope p("bfs_top_down", s, 4.0 * front_deg + 8.0 * nfront + 1.0 * front_deg);
-        k_bfs_td<<<grid_for(nfront * 32, 256), 256, 0, s>>>(g.in_ptr, g.in_col, g.hash_of_pos, bs->list[cur], (uint32_t) nfront,
-                                                            bs->hops, bs->cand, bs->list[cur ^ 1], bs->ctr);
+        k_bfs_td_split<<<td_blocks, 256, 0, s>>>(g.in_ptr, g.in_col, g.hash_of_pos, bs->small[cur], (uint32_t) nsmall,
+                                                 bs->big[cur], bs->big_task0[cur], (uint32_t) nbig, (uint32_t) ntasks,
+                                                 bs->hops, bs->cand, bs->raw, bs->ctr);
         LA3G_LAUNCHED();
       }
       edges_examined += front_deg;
-      LA3G_CUDA(cudaMemcpyAsync(bs->hctr, bs->ctr, sizeof(BfsCounters), cudaMemcpyDeviceToHost, s));
+      // the apply kernel reads the touched count on the device: one host
+      // synchronisation per iteration
+      k_bfs_td_apply_split<<<kSMs * 4, 256, 0, s>>>(g.in_ptr, bs->raw, hop, bs->hops, bs->parent, bs->cand,
+                                                   bs->small[cur ^ 1], bs->big[cur ^ 1], bs->big_task0[cur ^ 1],
+                                                   bs->ctr);
+      LA3G_LAUNCHED();
+      tls_launches++;
+      LA3G_CUDA(cudaMemcpyAsync(bs->hctr, bs->ctr, sizeof(FrontierCounters), cudaMemcpyDeviceToHost, s));
       LA3G_CUDA(cudaStreamSynchronize(s));
-      uint32_t nn = (uint32_t) bs->hctr->next_count;
-      if (nn)
-      {
-        k_bfs_td_apply<<<grid_for(nn, 256), 256, 0, s>>>(g.in_ptr, bs->list[cur ^ 1], nn, hop, bs->hops, bs->parent,
-                                                         bs->cand, bs->ctr);
-        LA3G_LAUNCHED();
-        tls_launches++;
-      }
+      const uint64_t nn = bs->hctr->raw;
+      nsmall = nn ? bs->hctr->nsmall : 0;
+      nbig = nn ? bs->hctr->packed >> kHubSlotShift : 0;
+      ntasks = nn ? bs->hctr->packed & ((1ull << kHubSlotShift) - 1) : 0;
+      front_deg = nn ? bs->hctr->degsum : 0;
       front_is_list = true;
     }
-    LA3G_CUDA(cudaMemcpyAsync(bs->hctr, bs->ctr, sizeof(BfsCounters), cudaMemcpyDeviceToHost, s));
-    LA3G_CUDA(cudaStreamSynchronize(s));
-    nfront = bs->hctr->next_count;
-    front_deg = bs->hctr->next_degsum;
     unvisited_deg -= std::min<uint64_t>(unvisited_deg, front_deg);
     cur ^= 1;
     iter++;
-    if (nfront == 0) break;
+    if (nsmall + nbig == 0) break;
   }
   if (st)
   {

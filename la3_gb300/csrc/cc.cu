@@ -8,7 +8,10 @@
 // component, every isolated vertex its own id.  That fixed point is computed
 // here with a lock-free union-find whose roots are always the least id of
 // their set (a root is only ever hooked under a root with a smaller id),
-// followed by full path compression.
+// followed by full path compression.  Edges are processed Afforest-style
+// (Sutton et al.): each vertex first unites with two neighbours, the giant
+// component is found by sampling, and only vertices outside it then walk
+// their remaining edges.
 //
 // When vertex 0 does have edges, label 0 behaves as "no value yet" and the
 // outcome depends on the order messages arrive in, so that case runs the
@@ -17,6 +20,7 @@
 // combine.
 #include <algorithm>
 #include <cstring>
+#include <vector>
 
 #include "la3g_internal.h"
 
@@ -25,6 +29,7 @@ namespace la3g {
 struct CcScratch
 {
   uint32_t* label = nullptr;   // by original id (union-find parents)
+  uint32_t* probe = nullptr;   // roots of sampled vertices
   uint32_t* lab_pos = nullptr; // BSP path: labels by position
   uint32_t* msg = nullptr;
   uint8_t* active[2] = {nullptr, nullptr};
@@ -52,34 +57,62 @@ __device__ __forceinline__ uint32_t cc_find(uint32_t* parent, uint32_t v)
   return v;
 }
 
-// One warp per row (position u), lanes over its neighbours v > u; every
-// undirected edge is united once.  Vertices are handled by original id.
+__device__ __forceinline__ void cc_union(uint32_t* parent, uint32_t a, uint32_t b)
+{
+  uint32_t ru = cc_find(parent, a), rv = cc_find(parent, b);
+  while (ru != rv)
+  {
+    if (ru > rv) { uint32_t t = ru; ru = rv; rv = t; }
+    // hook the larger root under the smaller one
+    uint32_t old = atomicCAS(&parent[rv], rv, ru);
+    if (old == rv) break;
+    rv = cc_find(parent, old);
+    ru = cc_find(parent, ru);
+  }
+}
+
+// Afforest-style sampling: every row unites with its first `k` neighbours.
+__global__ void k_cc_sample(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col,
+                            const uint32_t* __restrict__ id_of_pos, uint32_t nrows, uint32_t k, uint32_t* parent)
+{
+  for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < nrows; u += gridDim.x * blockDim.x)
+  {
+    const uint32_t b = ptr[u], e = min(ptr[u + 1], ptr[u] + k);
+    const uint32_t iu = id_of_pos[u];
+    for (uint32_t i = b; i < e; i++) cc_union(parent, iu, id_of_pos[col[i]]);
+  }
+}
+
+// Remaining edges (from the k-th neighbour on) of the rows whose root is not
+// the sampled giant root; the graph is symmetric, so every edge that leaves
+// the giant component is seen from its other endpoint.  One warp per row.
 __global__ void __launch_bounds__(256)
-k_cc_hook(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ id_of_pos,
-          uint32_t nrows, uint32_t* parent)
+k_cc_rest(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ id_of_pos,
+          uint32_t nrows, uint32_t k, uint32_t giant, uint32_t* parent)
 {
   const int lane = threadIdx.x & 31;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t u = warp; u < nrows; u += nwarps)
   {
-    const uint32_t b = ptr[u], e = ptr[u + 1];
+    const uint32_t b = ptr[u] + k, e = ptr[u + 1];
+    if (b >= e) continue;
     const uint32_t iu = id_of_pos[u];
-    for (uint32_t i = b + lane; i < e; i += 32)
-    {
-      const uint32_t v = col[i];
-      if (v <= u) continue;
-      uint32_t ru = cc_find(parent, iu), rv = cc_find(parent, id_of_pos[v]);
-      while (ru != rv)
-      {
-        if (ru > rv) { uint32_t t = ru; ru = rv; rv = t; }
-        // hook the larger root under the smaller one
-        uint32_t old = atomicCAS(&parent[rv], rv, ru);
-        if (old == rv) break;
-        rv = cc_find(parent, old);
-        ru = cc_find(parent, ru);
-      }
-    }
+    if (cc_find(parent, iu) == giant) continue;
+    for (uint32_t i = b + lane; i < e; i += 32) cc_union(parent, iu, id_of_pos[col[i]]);
+  }
+}
+
+__global__ void k_cc_probe(const uint32_t* __restrict__ id_of_pos, uint32_t nrows, uint32_t nsamples, uint64_t seed,
+                           uint32_t* parent, uint32_t* out)
+{
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nsamples; i += gridDim.x * blockDim.x)
+  {
+    uint64_t x = seed + 0x9E3779B97F4A7C15ull * (i + 1);
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    x ^= x >> 31;
+    out[i] = cc_find(parent, id_of_pos[(uint32_t) (x % nrows)]);
   }
 }
 
@@ -138,13 +171,6 @@ __global__ void k_ccb_step(const uint32_t* __restrict__ ptr, const uint32_t* __r
   }
 }
 
-__global__ void k_ccb_copy_msg(uint32_t nrows, const uint8_t* __restrict__ act, const uint32_t* __restrict__ src,
-                               uint32_t* dst)
-{
-  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += gridDim.x * blockDim.x)
-    if (act[r]) dst[r] = src[r];
-}
-
 __global__ void k_ccb_by_id(uint32_t N, const uint32_t* __restrict__ id_of_pos, const uint32_t* __restrict__ lab,
                             uint32_t* out)
 {
@@ -185,15 +211,15 @@ extern "C" int la3g_cc(la3g_graph* G, uint32_t* label_out, la3g_stats* st)
   const bool zero_has_edges = p0 < nrows;
   uint32_t iters = 0;
   T.device_begin();
-  if (!zero_has_edges)
+  if (!zero_has_edges && nrows)
   {
+    const uint32_t k = 2, nsamples = 1024;
     k_cc_init<<<grid_for(N, 256), 256, 0, s>>>(N, cs->label);
     LA3G_LAUNCHED();
     tls_launches++;
     {
-      ProfileScope p("cc_hook", s, 4.0 * g.nent + 4.0 * (nrows + 1) + 8.0 * N);
-      k_cc_hook<<<grid_for((uint64_t) nrows * 32, 256, kSMs * 32), 256, 0, s>>>(g.in_ptr, g.in_col, g.id_of_pos, nrows,
-                                                                               cs->label);
+      ProfileScope p("cc_sample", s, 8.0 * nrows + 12.0 * nrows);
+      k_cc_sample<<<grid_for(nrows, 256), 256, 0, s>>>(g.in_ptr, g.in_col, g.id_of_pos, nrows, k, cs->label);
       LA3G_LAUNCHED();
     }
     {
@@ -201,6 +227,38 @@ extern "C" int la3g_cc(la3g_graph* G, uint32_t* label_out, la3g_stats* st)
       k_cc_flatten<<<grid_for(N, 256), 256, 0, s>>>(N, cs->label);
       LA3G_LAUNCHED();
     }
+    if (!cs->probe) LA3G_TRY(galloc(G, &cs->probe, nsamples));
+    k_cc_probe<<<4, 256, 0, s>>>(g.id_of_pos, nrows, nsamples, 0x5A3Dull, cs->label, cs->probe);
+    LA3G_LAUNCHED();
+    tls_launches++;
+    std::vector<uint32_t> h(nsamples);
+    LA3G_CUDA(cudaMemcpyAsync(h.data(), cs->probe, nsamples * 4, cudaMemcpyDeviceToHost, s));
+    LA3G_CUDA(cudaStreamSynchronize(s));
+    std::sort(h.begin(), h.end());
+    uint32_t giant = h[0], best = 0;
+    for (uint32_t i = 0, j; i < nsamples; i = j)
+    {
+      for (j = i; j < nsamples && h[j] == h[i]; j++) {}
+      if (j - i > best) { best = j - i; giant = h[i]; }
+    }
+    {
+      ProfileScope p("cc_rest", s, 4.0 * g.nent + 4.0 * (nrows + 1) + 8.0 * N);
+      k_cc_rest<<<grid_for((uint64_t) nrows * 32, 256, kSMs * 32), 256, 0, s>>>(g.in_ptr, g.in_col, g.id_of_pos, nrows,
+                                                                               k, giant, cs->label);
+      LA3G_LAUNCHED();
+    }
+    {
+      ProfileScope p("cc_flatten", s, 8.0 * N);
+      k_cc_flatten<<<grid_for(N, 256), 256, 0, s>>>(N, cs->label);
+      LA3G_LAUNCHED();
+    }
+    iters = 1;
+  }
+  else if (!zero_has_edges)
+  {
+    k_cc_init<<<grid_for(N, 256), 256, 0, s>>>(N, cs->label);
+    LA3G_LAUNCHED();
+    tls_launches++;
     iters = 1;
   }
   else

@@ -1,0 +1,61 @@
+// Split frontiers shared by the top-down BFS and the SSSP relaxation.
+//
+// A frontier is kept as two lists: "small" vertices (at most kBigDeg edges,
+// one warp each) and hubs.  A hub's edges are cut into tasks of kHubTask
+// edges; the tasks of all hubs are numbered consecutively and warps take
+// tasks, so a hub with a million edges is spread over a thousand warps while
+// a warp never loops over hubs it has no work in.
+//
+// Appending a hub reserves its list slot and its first task number with one
+// 64-bit atomicAdd on a packed counter (slot in the high 24 bits, task count
+// in the low 40), so task numbers ascend with list slots and a warp finds
+// the hub of task t by a binary search over the slots' first tasks.
+#ifndef LA3G_FRONTIER_CUH
+#define LA3G_FRONTIER_CUH
+
+#include <cstdint>
+
+namespace la3g {
+
+static constexpr uint32_t kBigDeg = 512;
+static constexpr uint32_t kHubTask = 1024;
+static constexpr int kHubSlotShift = 40;
+
+__device__ __forceinline__ unsigned long long hub_pack_inc(uint32_t ntasks)
+{
+  return (1ull << kHubSlotShift) | (unsigned long long) ntasks;
+}
+
+// Appends hub v with `deg` edges; `packed` counts slots and tasks.
+__device__ __forceinline__ void hub_append(uint32_t v, uint32_t deg, uint32_t* big, uint32_t* big_task0,
+                                           unsigned long long* packed)
+{
+  const uint32_t ntasks = (deg + kHubTask - 1) / kHubTask;
+  const unsigned long long old = atomicAdd(packed, hub_pack_inc(ntasks));
+  const uint32_t slot = (uint32_t) (old >> kHubSlotShift);
+  big[slot] = v;
+  big_task0[slot] = (uint32_t) (old & ((1ull << kHubSlotShift) - 1));
+}
+
+__device__ __forceinline__ uint32_t hub_count(unsigned long long packed) { return (uint32_t) (packed >> kHubSlotShift); }
+__device__ __forceinline__ uint32_t hub_tasks(unsigned long long packed)
+{
+  return (uint32_t) (packed & ((1ull << kHubSlotShift) - 1));
+}
+
+// Slot whose task range holds task t (task0 ascends with the slot).
+__device__ __forceinline__ uint32_t hub_of_task(const uint32_t* __restrict__ task0, uint32_t nbig, uint32_t t)
+{
+  uint32_t lo = 0, hi = nbig;
+  while (hi - lo > 1)
+  {
+    uint32_t mid = (lo + hi) >> 1;
+    if (task0[mid] <= t) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+}  // namespace la3g
+
+#endif

@@ -18,19 +18,28 @@
 #include <algorithm>
 #include <cstring>
 
+#include "frontier.cuh"
 #include "la3g_internal.h"
 
 namespace la3g {
 
 static constexpr uint32_t kInf = 0x7FFFFFFFu;
 
+// The frontier is two lists: vertices with at most kBigDeg out-edges into
+// regular rows (one warp each) and hubs (their edges shared by the grid).
 struct SsspScratch
 {
   uint32_t* dist = nullptr;
   uint32_t* msg = nullptr;
   uint32_t* stamp = nullptr;
-  uint32_t* list[2] = {nullptr, nullptr};
-  unsigned long long* ctr = nullptr;  // [0] next count, [1] next out-degree sum, [2] scratch
+  uint32_t* reg_end = nullptr;   // [nslots] end of each vertex's out-edges into regular rows
+  uint32_t* raw = nullptr;       // vertices lowered in the current iteration
+  uint32_t* small[2] = {nullptr, nullptr};
+  uint32_t* big[2] = {nullptr, nullptr};
+  uint32_t* big_task0[2] = {nullptr, nullptr};
+  // [0] raw count, [1] next degree sum, [2] next small count, [3] hub slots and tasks (frontier.cuh),
+  // [4] scratch
+  unsigned long long* ctr = nullptr;
   unsigned long long* hctr = nullptr;
 };
 
@@ -50,70 +59,107 @@ __global__ void k_sssp_init(uint32_t N, uint32_t* dist, uint32_t* stamp)
   }
 }
 
-__global__ void k_sssp_root(uint32_t rp, int push, uint32_t* dist, uint32_t* msg, uint32_t* list)
+__global__ void k_sssp_root(uint32_t rp, int push, uint32_t* dist, uint32_t* msg, uint32_t* list, uint32_t* task0)
 {
   dist[rp] = 0;
   msg[rp] = 0;
-  if (push) list[0] = rp;
+  if (push) { list[0] = rp; task0[0] = 0; }
 }
 
-// One warp per frontier vertex; lanes over its out-edges into regular rows.
+// End of the regular-row part of every out-edge list (rows ascend, so the
+// sinks come last).
+__global__ void k_sssp_reg_end(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ row, uint32_t N,
+                               uint32_t nreg, uint32_t* reg_end)
+{
+  for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < N; u += gridDim.x * blockDim.x)
+  {
+    uint32_t lo = ptr[u], hi = ptr[u + 1];
+    while (lo < hi)
+    {
+      uint32_t mid = (lo + hi) >> 1;
+      if (row[mid] < nreg) lo = mid + 1;
+      else hi = mid;
+    }
+    reg_end[u] = lo;
+  }
+}
+
+__device__ __forceinline__ void relax(uint32_t v, uint32_t cand, bool valid, uint32_t* dist, uint32_t* stamp,
+                                      uint32_t tag, uint32_t* raw, unsigned long long* ctr, int lane)
+{
+  bool add = false;
+  if (valid && cand < dist[v])
+  {
+    const uint32_t old = atomicMin(&dist[v], cand);
+    if (cand < old) add = atomicExch(&stamp[v], tag) != tag;
+  }
+  const unsigned mask = __ballot_sync(0xffffffffu, add);
+  if (mask)
+  {
+    uint32_t base = 0;
+    if (lane == 0) base = (uint32_t) atomicAdd(&ctr[0], (unsigned long long) __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (add) raw[base + __popc(mask & ((1u << lane) - 1))] = v;
+  }
+}
+
+// Relaxation over a split frontier: hubs first (all warps share each hub's
+// edges), then one warp per small vertex.  Messages are the distances the
+// frontier vertices held when they were activated (msg), as the reference's
+// scatter values are.
 __global__ void __launch_bounds__(256)
-k_sssp_push(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ row, const uint32_t* __restrict__ w,
-            const uint32_t* __restrict__ front, uint32_t nfront, const uint32_t* __restrict__ msg, uint32_t nreg,
-            uint32_t* dist, uint32_t* stamp, uint32_t tag, uint32_t* next, unsigned long long* ctr)
+k_sssp_push(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ reg_end, const uint32_t* __restrict__ row,
+            const uint32_t* __restrict__ w, const uint32_t* __restrict__ small, uint32_t nsmall,
+            const uint32_t* __restrict__ big, const uint32_t* __restrict__ big_task0, uint32_t nbig, uint32_t ntasks,
+            const uint32_t* __restrict__ msg, uint32_t* dist, uint32_t* stamp, uint32_t tag, uint32_t* raw,
+            unsigned long long* ctr)
 {
   const int lane = threadIdx.x & 31;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t f = warp; f < nfront; f += nwarps)
+  for (uint32_t t = warp; t < ntasks; t += nwarps)
   {
-    const uint32_t u = front[f];
+    const uint32_t slot = hub_of_task(big_task0, nbig, t);
+    const uint32_t u = big[slot];
     const uint32_t mu = msg[u];
-    const uint32_t b = ptr[u], e = ptr[u + 1];
+    const uint32_t b = ptr[u] + (t - big_task0[slot]) * kHubTask;
+    const uint32_t e = min(b + kHubTask, reg_end[u]);
     for (uint32_t i0 = b; i0 < e; i0 += 32)
     {
       const uint32_t i = i0 + lane;
-      bool add = false;
-      uint32_t v = 0;
-      bool more = true;
-      if (i < e)
-      {
-        v = row[i];
-        if (v < nreg)
-        {
-          const uint32_t cand = mu + w[i];
-          if (cand < dist[v])
-          {
-            const uint32_t old = atomicMin(&dist[v], cand);
-            if (cand < old) add = atomicExch(&stamp[v], tag) != tag;
-          }
-        }
-        else more = false;  // rows ascend: the rest are sinks
-      }
-      const unsigned mask = __ballot_sync(0xffffffffu, add);
-      if (mask)
-      {
-        uint32_t base = 0;
-        if (lane == 0) base = (uint32_t) atomicAdd(&ctr[0], (unsigned long long) __popc(mask));
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (add) next[base + __popc(mask & ((1u << lane) - 1))] = v;
-      }
-      if (!__any_sync(0xffffffffu, more)) break;
+      const bool ok = i < e;
+      relax(ok ? row[i] : 0, ok ? mu + w[i] : 0, ok, dist, stamp, tag, raw, ctr, lane);
+    }
+  }
+  for (uint32_t f = warp; f < nsmall; f += nwarps)
+  {
+    const uint32_t u = small[f];
+    const uint32_t mu = msg[u];
+    const uint32_t b = ptr[u], e = reg_end[u];
+    for (uint32_t i0 = b; i0 < e; i0 += 32)
+    {
+      const uint32_t i = i0 + lane;
+      const bool ok = i < e;
+      relax(ok ? row[i] : 0, ok ? mu + w[i] : 0, ok, dist, stamp, tag, raw, ctr, lane);
     }
   }
 }
 
-// Activated vertices scatter their new distance.
-__global__ void k_sssp_apply(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ next, uint32_t n,
-                             const uint32_t* __restrict__ dist, uint32_t* msg, unsigned long long* ctr)
+// Activated vertices scatter their new distance and form the next frontier.
+__global__ void k_sssp_apply(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ reg_end,
+                             const uint32_t* __restrict__ raw, const uint32_t* __restrict__ dist, uint32_t* msg,
+                             uint32_t* small, uint32_t* big, uint32_t* big_task0, unsigned long long* ctr)
 {
   unsigned long long deg = 0;
+  const uint32_t n = (uint32_t) ctr[0];
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
   {
-    uint32_t v = next[i];
+    uint32_t v = raw[i];
     msg[v] = dist[v];
-    deg += ptr[v + 1] - ptr[v];
+    uint32_t d = reg_end[v] - ptr[v];
+    deg += d;
+    if (d > kBigDeg) hub_append(v, d, big, big_task0, &ctr[3]);
+    else if (d) small[atomicAdd(&ctr[2], 1ull)] = v;
   }
   for (int o = 16; o > 0; o >>= 1) deg += __shfl_xor_sync(0xffffffffu, deg, o);
   if ((threadIdx.x & 31) == 0 && deg) atomicAdd(&ctr[1], deg);
@@ -169,10 +215,18 @@ static int sssp_scratch(la3g_graph* G, SsspScratch** out)
   LA3G_TRY(galloc(G, &ss->dist, N));
   LA3G_TRY(galloc(G, &ss->msg, N));
   LA3G_TRY(galloc(G, &ss->stamp, N));
-  LA3G_TRY(galloc(G, &ss->list[0], N));
-  LA3G_TRY(galloc(G, &ss->list[1], N));
-  LA3G_TRY(galloc(G, &ss->ctr, 4));
-  LA3G_CUDA(cudaHostAlloc(&ss->hctr, 4 * sizeof(unsigned long long), cudaHostAllocDefault));
+  LA3G_TRY(galloc(G, &ss->reg_end, N));
+  LA3G_TRY(galloc(G, &ss->raw, N));
+  LA3G_TRY(galloc(G, &ss->small[0], N));
+  LA3G_TRY(galloc(G, &ss->small[1], N));
+  LA3G_TRY(galloc(G, &ss->big[0], N));
+  LA3G_TRY(galloc(G, &ss->big[1], N));
+  LA3G_TRY(galloc(G, &ss->big_task0[0], N));
+  LA3G_TRY(galloc(G, &ss->big_task0[1], N));
+  LA3G_TRY(galloc(G, &ss->ctr, 8));
+  LA3G_CUDA(cudaHostAlloc(&ss->hctr, 8 * sizeof(unsigned long long), cudaHostAllocDefault));
+  k_sssp_reg_end<<<grid_for(N, 256), 256, 0, G->stream>>>(G->g.out_ptr, G->g.out_row, N, G->g.nreg, ss->reg_end);
+  LA3G_LAUNCHED();
   *out = ss;
   return LA3G_OK;
 }
@@ -186,7 +240,7 @@ static int sssp_run(la3g_graph* G, SsspScratch* ss, uint32_t root, la3g_stats* s
   LA3G_LAUNCHED();
   tls_launches++;
   uint32_t rp = 0xFFFFFFFFu, src_root = 0xFFFFFFFFu;
-  uint64_t nfront = 0, front_deg = 0;
+  uint64_t nsmall = 0, nbig = 0, ntasks = 0, front_deg = 0;
   if (root < N)
   {
     LA3G_CUDA(cudaMemcpyAsync(&rp, g.pos_of_id + root, 4, cudaMemcpyDeviceToHost, s));
@@ -194,51 +248,61 @@ static int sssp_run(la3g_graph* G, SsspScratch* ss, uint32_t root, la3g_stats* s
     // init returns true for the root; regular and source vertices scatter.
     const bool scat = rp < g.nreg || (rp >= g.src_base() && rp < g.iso_base());
     if (rp >= g.src_base() && rp < g.iso_base()) src_root = rp;
-    k_sssp_root<<<1, 1, 0, s>>>(rp, scat ? 1 : 0, ss->dist, ss->msg, ss->list[0]);
-    LA3G_LAUNCHED();
-    tls_launches++;
-    nfront = scat ? 1 : 0;
+    uint32_t re = 0, hp[2] = {0, 0};
     if (scat)
     {
-      uint32_t hp[2];
       LA3G_CUDA(cudaMemcpyAsync(hp, g.out_ptr + rp, 8, cudaMemcpyDeviceToHost, s));
+      LA3G_CUDA(cudaMemcpyAsync(&re, ss->reg_end + rp, 4, cudaMemcpyDeviceToHost, s));
       LA3G_CUDA(cudaStreamSynchronize(s));
-      front_deg = hp[1] - hp[0];
+      front_deg = re - hp[0];
     }
+    const bool hub = front_deg > kBigDeg;
+    k_sssp_root<<<1, 1, 0, s>>>(rp, scat ? 1 : 0, ss->dist, ss->msg, hub ? ss->big[0] : ss->small[0],
+                                ss->big_task0[0]);
+    LA3G_LAUNCHED();
+    tls_launches++;
+    if (scat) (hub ? nbig : nsmall) = 1;
+    if (scat && hub) ntasks = (front_deg + kHubTask - 1) / kHubTask;
   }
   uint32_t iter = 0;
   int cur = 0;
   uint64_t examined = 0;
+  const unsigned blocks = kSMs * 8;
   for (;;)
   {
     if (iter > 1000000) return set_error(LA3G_ETIMEOUT, "sssp did not converge");
     iter++;
-    if (nfront == 0) break;
-    LA3G_CUDA(cudaMemsetAsync(ss->ctr, 0, 2 * sizeof(unsigned long long), s));
+    if (nsmall + nbig == 0) break;
+    LA3G_CUDA(cudaMemsetAsync(ss->ctr, 0, 4 * sizeof(unsigned long long), s));
     {
-      ProfileScope p("sssp_push", s, 8.0 * front_deg + 12.0 * nfront);
-      k_sssp_push<<<grid_for(nfront * 32, 256), 256, 0, s>>>(g.out_ptr, g.out_row, g.out_w, ss->list[cur],
-                                                            (uint32_t) nfront, ss->msg, g.nreg, ss->dist, ss->stamp,
-                                                            iter, ss->list[cur ^ 1], ss->ctr);
+      ProfileScope p("sssp_push", s, 8.0 * front_deg + 12.0 * (nsmall + nbig));
+      k_sssp_push<<<blocks, 256, 0, s>>>(g.out_ptr, ss->reg_end, g.out_row, g.out_w, ss->small[cur], (uint32_t) nsmall,
+                                         ss->big[cur], ss->big_task0[cur], (uint32_t) nbig, (uint32_t) ntasks, ss->msg,
+                                         ss->dist, ss->stamp, iter, ss->raw, ss->ctr);
       LA3G_LAUNCHED();
     }
     examined += front_deg;
-    LA3G_CUDA(cudaMemcpyAsync(ss->hctr, ss->ctr, 8, cudaMemcpyDeviceToHost, s));
+    k_sssp_apply<<<kSMs * 4, 256, 0, s>>>(g.out_ptr, ss->reg_end, ss->raw, ss->dist, ss->msg, ss->small[cur ^ 1],
+                                         ss->big[cur ^ 1], ss->big_task0[cur ^ 1], ss->ctr);
+    LA3G_LAUNCHED();
+    tls_launches++;
+    LA3G_CUDA(cudaMemcpyAsync(ss->hctr, ss->ctr, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
     LA3G_CUDA(cudaStreamSynchronize(s));
-    uint64_t nn = ss->hctr[0];
-    if (nn)
-    {
-      k_sssp_apply<<<grid_for(nn, 256), 256, 0, s>>>(g.out_ptr, ss->list[cur ^ 1], (uint32_t) nn, ss->dist, ss->msg,
-                                                     ss->ctr);
-      LA3G_LAUNCHED();
-      tls_launches++;
-      LA3G_CUDA(cudaMemcpyAsync(ss->hctr, ss->ctr, 16, cudaMemcpyDeviceToHost, s));
-      LA3G_CUDA(cudaStreamSynchronize(s));
-    }
-    nfront = nn;
-    front_deg = nn ? ss->hctr[1] : 0;
+    const uint64_t nn = ss->hctr[0];
+    nsmall = ss->hctr[2];
+    nbig = ss->hctr[3] >> kHubSlotShift;
+    ntasks = ss->hctr[3] & ((1ull << kHubSlotShift) - 1);
+    front_deg = ss->hctr[1];
     cur ^= 1;
-    if (nn == 0) break;  // this iteration activated nothing
+    // A vertex lowered only into sink-free regular rows with no regular
+    // out-edges is activated but has nothing to relax; the loop still runs
+    // the next iteration only if something was activated.
+    if (nn == 0) break;
+    if (nsmall + nbig == 0)
+    {
+      iter++;  // the next iteration runs with messages that reach no regular row
+      break;
+    }
   }
   if (g.nsink)
   {

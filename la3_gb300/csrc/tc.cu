@@ -3,78 +3,386 @@
 //
 // The reference orients every edge from the lower to the higher original id
 // (remove_cycles, graph.hpp:174-179), collects for each vertex v the list
-// N<(v) of its lower neighbours (GnVertex), and then, for every oriented
-// edge (u, v) with u < v, adds |N<(u) ∩ N<(v)| to u (CtVertex gathers at
-// the lower endpoint, accumulating in uint32).  Each triangle w < u < v is
-// counted once, at its middle vertex u.
+// N<(v) of its lower neighbours (GnVertex), and for every oriented edge
+// (u, v), u < v, adds |N<(u) ∩ N<(v)| to u, accumulating in uint32 (CtVertex).
+// Each triangle a < b < c is therefore counted once, at its middle vertex b.
 //
-// On the device the lists are the rows of the pull CSR of the graph loaded
-// with LA3G_DIRECTED | LA3G_ACYCLIC (rows = higher endpoint, entries = lower
-// endpoints, all sorted by one column key), and the oriented edges are the
-// rows of the push CSR (column u -> its higher neighbours v).  One warp
-// handles one edge: lanes take the elements of the shorter list and binary-
-// search them in the longer one; the warp's count goes to u with one
-// atomicAdd (uint32, wrapping as the reference's accumulator does).
+// Here the triangles are found once each by the usual degree ordering
+// instead: rank(x) = (degree, id), N+(x) = neighbours of higher rank (sorted
+// by id), and every triangle x < y < w in rank order is found while scanning
+// the edge (x, y) as w ∈ N+(x) ∩ N+(y).  The middle vertex BY ID is then the
+// median of the three ids; since y and w both lie in N+(x), the warp that
+// owns x keeps one shared-memory counter per element of N+(x) (plus one for
+// x) and adds every found triangle to the counter of its middle vertex,
+// flushing them to the global uint32 counts once per x.  The per-vertex
+// counts are those of the reference (sums are order-free); the lists stay
+// short (max |N+| is about sqrt(2m)), which is what makes this fast on
+// skewed graphs.
 #include <algorithm>
 #include <cstring>
+#include <cub/device/device_radix_sort.cuh>
 
 #include "la3g_internal.h"
 
 namespace la3g {
 
+static constexpr uint32_t kTcCap = 1024;     // N+(x) held in shared memory up to this length
+static constexpr uint32_t kTcSmall = 192;    // lists up to this length use the high-occupancy variant
+
 struct TcScratch
 {
-  uint32_t* ntri = nullptr;
-  uint32_t* esrc = nullptr;  // lower endpoint of each oriented edge
+  uint32_t* plus_ptr = nullptr;  // [nslots + 1] by original id
+  uint32_t* plus_col = nullptr;  // [nent] ids, each row ascending
+  uint32_t* order = nullptr;     // ids with 0 < |N+| <= kTcSmall, heaviest first
+  uint32_t* order_mid = nullptr; // ids with kTcSmall < |N+| <= kTcCap, heaviest first
+  uint32_t* big = nullptr;       // ids with |N+| > kTcCap
+  uint32_t norder = 0, nmid = 0, nbig = 0;
+  uint32_t* ntri = nullptr;      // [nslots] by id
+  unsigned int* next = nullptr;  // dynamic work counter
   unsigned long long* total = nullptr;
+  double work = 0;               // sum over x of |N+(x)| + sum_y |N+(y)| (list elements read)
 };
 
 static void tc_scratch_free(void* p) { delete (TcScratch*) p; }
 
-// column key: sources first, then regular columns (the in-CSR sort order)
-__device__ __forceinline__ uint32_t ckey(uint32_t c, uint32_t src_base, uint32_t nsrc)
+// Undirected degree by id: lower + higher neighbours.
+__global__ void k_tc_deg(const uint32_t* __restrict__ iptr, const uint32_t* __restrict__ optr,
+                         const uint32_t* __restrict__ id_of_pos, uint32_t N, uint32_t* deg)
 {
-  return c >= src_base ? c - src_base : c + nsrc;
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x)
+    deg[id_of_pos[p]] = (iptr[p + 1] - iptr[p]) + (optr[p + 1] - optr[p]);
 }
 
-// Lower endpoint of every push-CSR entry.
-__global__ void k_tc_expand(const uint32_t* __restrict__ optr, uint32_t ncols, uint32_t* __restrict__ src)
+// Every undirected edge once (push CSR of the id-oriented graph), emitted as
+// (lower rank, higher rank) = id(x) << 32 | id(y).
+__global__ void k_tc_rank_edges(const uint32_t* __restrict__ optr, const uint32_t* __restrict__ orow, uint32_t N,
+                                const uint32_t* __restrict__ id_of_pos, const uint32_t* __restrict__ deg,
+                                uint64_t* keys)
 {
-  for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < ncols; u += gridDim.x * blockDim.x)
-    for (uint32_t e = optr[u]; e < optr[u + 1]; e++) src[e] = u;
-}
-
-// One warp per oriented edge (u, v): lanes take the elements of the shorter
-// of N<(u), N<(v) and binary-search them in the longer one.
-__global__ void __launch_bounds__(256)
-k_tc(const uint32_t* __restrict__ esrc, const uint32_t* __restrict__ orow, uint64_t m, const uint32_t* __restrict__ iptr,
-     const uint32_t* __restrict__ icol, uint32_t src_base, uint32_t nsrc, uint32_t* ntri)
-{
-  const int lane = threadIdx.x & 31;
-  const uint64_t warp = ((uint64_t) blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const uint64_t nwarps = ((uint64_t) gridDim.x * blockDim.x) >> 5;
-  for (uint64_t e = warp; e < m; e += nwarps)
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x)
   {
-    const uint32_t u = esrc[e], v = orow[e];
-    const uint32_t ub = iptr[u], ue = iptr[u + 1], vb = iptr[v], ve = iptr[v + 1];
-    uint32_t ab = ub, ae = ue, bb = vb, be = ve;
-    if (ae - ab > be - bb) { ab = vb; ae = ve; bb = ub; be = ue; }
-    if (ab == ae) continue;
-    uint32_t acc = 0;
-    for (uint32_t i = ab + lane; i < ae; i += 32)
+    const uint32_t a = id_of_pos[p];
+    const uint32_t da = deg[a];
+    for (uint32_t e = optr[p]; e < optr[p + 1]; e++)
     {
-      const uint32_t key = ckey(icol[i], src_base, nsrc);
-      uint32_t lo = bb, hi = be;
-      while (lo < hi)
+      const uint32_t b = id_of_pos[orow[e]];
+      const uint32_t db = deg[b];
+      const bool a_low = da < db || (da == db && a < b);
+      keys[e] = a_low ? ((uint64_t) a << 32 | b) : ((uint64_t) b << 32 | a);
+    }
+  }
+}
+
+__global__ void k_tc_split_keys(const uint64_t* __restrict__ keys, uint64_t m, uint32_t* col)
+{
+  for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (uint64_t) gridDim.x * blockDim.x)
+    col[i] = (uint32_t) keys[i];
+}
+
+__global__ void k_tc_rows(const uint64_t* __restrict__ k, uint64_t m, uint32_t N, uint32_t* ptr)
+{
+  for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i <= m; i += (uint64_t) gridDim.x * blockDim.x)
+  {
+    int64_t r = i < m ? (int64_t) (k[i] >> 32) : (int64_t) N;
+    int64_t rp = i == 0 ? -1 : (int64_t) (k[i - 1] >> 32);
+    for (int64_t q = rp + 1; q <= r; q++) ptr[q] = (uint32_t) i;
+  }
+}
+
+// Work estimate per vertex and the lists of vertices to process.
+__global__ void k_tc_work(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, uint32_t N,
+                          uint32_t* wkey, uint32_t* wid, uint32_t* big, unsigned long long* counts)
+{
+  for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < N; x += gridDim.x * blockDim.x)
+  {
+    const uint32_t b = ptr[x], e = ptr[x + 1];
+    if (b == e) continue;
+    uint64_t w = e - b;
+    for (uint32_t i = b; i < e; i++) w += ptr[col[i] + 1] - ptr[col[i]];
+    if (e - b > kTcCap)
+    {
+      big[atomicAdd(&counts[1], 1ull)] = x;
+    }
+    else
+    {
+      // keys: class bit on top (small lists first), then ~work (heaviest first)
+      const uint32_t cls = (e - b) > kTcSmall ? 1u : 0u;
+      const unsigned long long slot = atomicAdd(&counts[0], 1ull);
+      const uint32_t wq = (uint32_t) (w < 0x7FFFFFFFull ? w : 0x7FFFFFFFull);
+      wkey[slot] = (cls << 31) | (0x7FFFFFFFu - wq);
+      wid[slot] = x;
+      if (cls) atomicAdd(&counts[3], 1ull);
+    }
+    atomicAdd(&counts[2], (unsigned long long) w);
+  }
+}
+
+__device__ __forceinline__ uint32_t lower_bound_s(const uint32_t* s, uint32_t n, uint32_t key)
+{
+  uint32_t lo = 0, hi = n;
+  while (lo < hi)
+  {
+    uint32_t mid = (lo + hi) >> 1;
+    if (s[mid] < key) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// One warp per vertex x (fetched dynamically, heaviest first).  Shared
+// memory holds N+(x), the prefix offsets of the per-y work, and one counter
+// per element of N+(x).  For each y in N+(x) the shorter of N+(y) and N+(x)
+// is walked and its elements looked up in the other (a shared-memory binary
+// search into N+(x), or a global one into N+(y)); lanes share the
+// concatenated work of all y.  A hit w closes the triangle {x, y, w}, which
+// is counted at its middle id.
+template <uint32_t CAP, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
+k_tc_rank(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ order,
+          uint32_t norder, unsigned int* next, uint32_t* ntri)
+{
+  __shared__ uint32_t s_list[WARPS][CAP];
+  __shared__ uint32_t s_off[WARPS][CAP + 1];
+  __shared__ uint32_t s_cnt[WARPS][CAP];
+  __shared__ uint32_t s_x[WARPS];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  uint32_t* L = s_list[wib];
+  uint32_t* O = s_off[wib];
+  uint32_t* Cn = s_cnt[wib];
+  for (;;)
+  {
+    uint32_t k = 0;
+    if (lane == 0) k = atomicAdd(next, 1u);
+    k = __shfl_sync(0xffffffffu, k, 0);
+    if (k >= norder) break;
+    const uint32_t x = order[k];
+    const uint32_t xb = ptr[x], d = ptr[x + 1] - xb;
+    // stage N+(x), the work offsets (min(|N+(y)|, d) per y) and zeroed counters
+    uint32_t base = 0;
+    for (uint32_t j0 = 0; j0 < d; j0 += 32)
+    {
+      const uint32_t j = j0 + lane;
+      uint32_t len = 0;
+      if (j < d)
+      {
+        const uint32_t y = col[xb + j];
+        len = min(ptr[y + 1] - ptr[y], d);
+        L[j] = y;
+        Cn[j] = 0;
+      }
+      uint32_t incl = len;
+      for (int o = 1; o < 32; o <<= 1)
+      {
+        uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+      }
+      if (j < d) O[j] = base + incl - len;
+      base += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    if (lane == 0)
+    {
+      O[d] = base;
+      s_x[wib] = 0;
+    }
+    __syncwarp();
+    const uint32_t total = base;
+    for (uint32_t t0 = 0; t0 < total; t0 += 32)
+    {
+      const uint32_t t = t0 + lane;
+      if (t < total)
+      {
+        // y-index: the last j with O[j] <= t
+        uint32_t lo = 0, hi = d;
+        while (hi - lo > 1)
+        {
+          uint32_t mid = (lo + hi) >> 1;
+          if (O[mid] <= t) lo = mid;
+          else hi = mid;
+        }
+        const uint32_t jy = lo;
+        const uint32_t y = L[jy];
+        const uint32_t yb = ptr[y], ylen = ptr[y + 1] - yb;
+        const uint32_t r = t - O[jy];
+        uint32_t w, pw;
+        bool hit;
+        if (ylen <= d)
+        {
+          w = col[yb + r];
+          pw = lower_bound_s(L, d, w);
+          hit = pw < d && L[pw] == w;
+        }
+        else
+        {
+          pw = r;
+          w = L[r];
+          uint32_t a = yb, c = yb + ylen;
+          while (a < c)
+          {
+            uint32_t mid = (a + c) >> 1;
+            if (col[mid] < w) a = mid + 1;
+            else c = mid;
+          }
+          hit = a < yb + ylen && col[a] == w;
+        }
+        if (hit)
+        {
+          const uint32_t mn = min(x, y), mx = max(x, y);
+          if (w < mn) { if (mn == x) atomicAdd(&s_x[wib], 1u); else atomicAdd(&Cn[jy], 1u); }
+          else if (w > mx) { if (mx == x) atomicAdd(&s_x[wib], 1u); else atomicAdd(&Cn[jy], 1u); }
+          else atomicAdd(&Cn[pw], 1u);
+        }
+      }
+    }
+    __syncwarp();
+    for (uint32_t j = lane; j < d; j += 32)
+      if (Cn[j]) atomicAdd(&ntri[L[j]], Cn[j]);
+    if (lane == 0 && s_x[wib]) atomicAdd(&ntri[x], s_x[wib]);
+    __syncwarp();
+  }
+}
+
+// Heavy vertices (kTcSmall < |N+(x)| <= kTcCap): the same walk with a whole
+// block per x.
+template <uint32_t CAP, int THREADS>
+__global__ void __launch_bounds__(THREADS)
+k_tc_rank_block(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ order,
+                uint32_t norder, unsigned int* next, uint32_t* ntri)
+{
+  constexpr int PER = (CAP + THREADS - 1) / THREADS;
+  __shared__ uint32_t L[CAP];
+  __shared__ uint32_t O[CAP + 1];
+  __shared__ uint32_t Cn[CAP];
+  __shared__ uint32_t s_warp[THREADS / 32];
+  __shared__ uint32_t s_k, s_x;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  for (;;)
+  {
+    if (threadIdx.x == 0) s_k = atomicAdd(next, 1u);
+    __syncthreads();
+    const uint32_t k = s_k;
+    if (k >= norder) break;
+    const uint32_t x = order[k];
+    const uint32_t xb = ptr[x], d = ptr[x + 1] - xb;
+    // stage: thread i owns elements [i * PER, i * PER + PER)
+    uint32_t len[PER];
+    uint32_t mine = 0;
+#pragma unroll
+    for (int q = 0; q < PER; q++)
+    {
+      const uint32_t j = threadIdx.x * PER + q;
+      len[q] = 0;
+      if (j < d)
+      {
+        const uint32_t y = col[xb + j];
+        len[q] = min(ptr[y + 1] - ptr[y], d);
+        L[j] = y;
+        Cn[j] = 0;
+      }
+      mine += len[q];
+    }
+    uint32_t incl = mine;
+    for (int o = 1; o < 32; o <<= 1)
+    {
+      uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    if (lane == 31) s_warp[wib] = incl;
+    if (threadIdx.x == 0) s_x = 0;
+    __syncthreads();
+    uint32_t wbase = 0;
+    for (int w = 0; w < wib; w++) wbase += s_warp[w];
+    uint32_t run = wbase + incl - mine;
+#pragma unroll
+    for (int q = 0; q < PER; q++)
+    {
+      const uint32_t j = threadIdx.x * PER + q;
+      if (j < d) O[j] = run;
+      run += len[q];
+    }
+    uint32_t total = 0;
+    for (int w = 0; w < THREADS / 32; w++) total += s_warp[w];
+    if (threadIdx.x == 0) O[d] = total;
+    __syncthreads();
+    for (uint32_t t = threadIdx.x; t < total; t += THREADS)
+    {
+      uint32_t lo = 0, hi = d;
+      while (hi - lo > 1)
       {
         uint32_t mid = (lo + hi) >> 1;
-        if (ckey(icol[mid], src_base, nsrc) < key) lo = mid + 1;
+        if (O[mid] <= t) lo = mid;
         else hi = mid;
       }
-      if (lo < be && ckey(icol[lo], src_base, nsrc) == key) acc++;
+      const uint32_t jy = lo;
+      const uint32_t y = L[jy];
+      const uint32_t yb = ptr[y], ylen = ptr[y + 1] - yb;
+      const uint32_t r = t - O[jy];
+      uint32_t w, pw;
+      bool hit;
+      if (ylen <= d)
+      {
+        w = col[yb + r];
+        pw = lower_bound_s(L, d, w);
+        hit = pw < d && L[pw] == w;
+      }
+      else
+      {
+        pw = r;
+        w = L[r];
+        uint32_t a = yb, c = yb + ylen;
+        while (a < c)
+        {
+          uint32_t mid = (a + c) >> 1;
+          if (col[mid] < w) a = mid + 1;
+          else c = mid;
+        }
+        hit = a < yb + ylen && col[a] == w;
+      }
+      if (hit)
+      {
+        const uint32_t mn = min(x, y), mx = max(x, y);
+        if (w < mn) { if (mn == x) atomicAdd(&s_x, 1u); else atomicAdd(&Cn[jy], 1u); }
+        else if (w > mx) { if (mx == x) atomicAdd(&s_x, 1u); else atomicAdd(&Cn[jy], 1u); }
+        else atomicAdd(&Cn[pw], 1u);
+      }
     }
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0 && acc) atomicAdd(&ntri[u], acc);
+    __syncthreads();
+    for (uint32_t j = threadIdx.x; j < d; j += THREADS)
+      if (Cn[j]) atomicAdd(&ntri[L[j]], Cn[j]);
+    if (threadIdx.x == 0 && s_x) atomicAdd(&ntri[x], s_x);
+    __syncthreads();
+  }
+}
+
+// Vertices whose N+ exceeds kTcCap: one warp each, lists read from global
+// memory, every hit added with a global atomic.
+__global__ void __launch_bounds__(256)
+k_tc_rank_big(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ big,
+              uint32_t nbig, uint32_t* ntri)
+{
+  const int lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t k = warp; k < nbig; k += nwarps)
+  {
+    const uint32_t x = big[k];
+    const uint32_t xb = ptr[x], xe = ptr[x + 1];
+    for (uint32_t j = xb; j < xe; j++)
+    {
+      const uint32_t y = col[j];
+      const uint32_t mn = min(x, y), mx = max(x, y);
+      for (uint32_t i = ptr[y] + lane; i < ptr[y + 1]; i += 32)
+      {
+        const uint32_t w = col[i];
+        uint32_t lo = xb, hi = xe;
+        while (lo < hi)
+        {
+          uint32_t mid = (lo + hi) >> 1;
+          if (col[mid] < w) lo = mid + 1;
+          else hi = mid;
+        }
+        if (lo < xe && col[lo] == w) atomicAdd(&ntri[w < mn ? mn : (w > mx ? mx : w)], 1u);
+      }
+    }
   }
 }
 
@@ -86,10 +394,70 @@ __global__ void k_tc_sum(uint32_t N, const uint32_t* __restrict__ ntri, unsigned
   if ((threadIdx.x & 31) == 0 && s) atomicAdd(total, s);
 }
 
-__global__ void k_tc_by_id(uint32_t N, const uint32_t* __restrict__ id_of_pos, const uint32_t* __restrict__ v,
-                           uint32_t* out)
+static int tc_prepare(la3g_graph* G, TcScratch* ts)
 {
-  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) out[id_of_pos[p]] = v[p];
+  DevGraph& g = G->g;
+  cudaStream_t s = G->stream;
+  const uint32_t N = g.nslots;
+  const uint64_t m = g.nent;
+  LA3G_TRY(galloc(G, &ts->plus_ptr, N + 1));
+  LA3G_TRY(galloc(G, &ts->plus_col, m + 1));
+  LA3G_TRY(galloc(G, &ts->ntri, N));
+  LA3G_TRY(galloc(G, &ts->total, 1));
+  LA3G_TRY(galloc(G, &ts->next, 2));
+  DevBuf deg, k1, k2, tmp, wkey, wid, wkey2, cnt;
+  LA3G_TRY(deg.alloc((size_t) N * 4));
+  LA3G_TRY(k1.alloc(m * 8 + 8));
+  LA3G_TRY(k2.alloc(m * 8 + 8));
+  k_tc_deg<<<grid_for(N, 256), 256, 0, s>>>(g.in_ptr, g.out_ptr, g.id_of_pos, N, deg.as<uint32_t>());
+  LA3G_LAUNCHED();
+  if (m)
+  {
+    k_tc_rank_edges<<<grid_for(N, 256), 256, 0, s>>>(g.out_ptr, g.out_row, N, g.id_of_pos, deg.as<uint32_t>(),
+                                                     k1.as<uint64_t>());
+    LA3G_LAUNCHED();
+    size_t tb = 0;
+    int end_bit = 33;
+    while (end_bit < 64 && ((uint64_t) N >> (end_bit - 32)) != 0) end_bit++;
+    LA3G_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, tb, k1.as<uint64_t>(), k2.as<uint64_t>(), m, 0, end_bit, s));
+    LA3G_TRY(tmp.alloc(tb));
+    LA3G_CUDA(cub::DeviceRadixSort::SortKeys(tmp.p, tb, k1.as<uint64_t>(), k2.as<uint64_t>(), m, 0, end_bit, s));
+    k_tc_split_keys<<<grid_for(m, 256), 256, 0, s>>>(k2.as<uint64_t>(), m, ts->plus_col);
+    LA3G_LAUNCHED();
+  }
+  k_tc_rows<<<grid_for(m + 1, 256), 256, 0, s>>>(k2.as<uint64_t>(), m, N, ts->plus_ptr);
+  LA3G_LAUNCHED();
+  LA3G_TRY(wkey.alloc((size_t) N * 4));
+  LA3G_TRY(wid.alloc((size_t) N * 4));
+  LA3G_TRY(wkey2.alloc((size_t) N * 4));
+  LA3G_TRY(cnt.alloc(4 * 8));
+  LA3G_TRY(galloc(G, &ts->order, N));
+  LA3G_TRY(galloc(G, &ts->big, N));
+  LA3G_CUDA(cudaMemsetAsync(cnt.p, 0, 32, s));
+  k_tc_work<<<grid_for(N, 256), 256, 0, s>>>(ts->plus_ptr, ts->plus_col, N, wkey.as<uint32_t>(), wid.as<uint32_t>(),
+                                             ts->big, cnt.as<unsigned long long>());
+  LA3G_LAUNCHED();
+  unsigned long long hc[4];
+  LA3G_CUDA(cudaMemcpyAsync(hc, cnt.p, 32, cudaMemcpyDeviceToHost, s));
+  LA3G_CUDA(cudaStreamSynchronize(s));
+  ts->nmid = (uint32_t) hc[3];
+  ts->norder = (uint32_t) hc[0];  // small + mid, sorted: small first
+  ts->nbig = (uint32_t) hc[1];
+  ts->work = (double) hc[2];
+  if (ts->norder)
+  {
+    size_t tb = 0;
+    LA3G_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tb, wkey.as<uint32_t>(), wkey2.as<uint32_t>(), wid.as<uint32_t>(),
+                                              ts->order, ts->norder, 0, 32, s));
+    DevBuf t2;
+    LA3G_TRY(t2.alloc(tb));
+    LA3G_CUDA(cub::DeviceRadixSort::SortPairs(t2.p, tb, wkey.as<uint32_t>(), wkey2.as<uint32_t>(), wid.as<uint32_t>(),
+                                              ts->order, ts->norder, 0, 32, s));
+  }
+  LA3G_CUDA(cudaStreamSynchronize(s));
+  ts->order_mid = ts->order + (ts->norder - ts->nmid);
+  ts->norder -= ts->nmid;
+  return LA3G_OK;
 }
 
 }  // namespace la3g
@@ -111,22 +479,34 @@ extern "C" int la3g_tc(la3g_graph* G, uint64_t* total_out, uint32_t* per_vertex_
     if (!ts) return set_error(LA3G_ENOMEM, "out of host memory");
     G->slot[kSlotTc] = ts;
     G->slot_free[kSlotTc] = tc_scratch_free;
-    LA3G_TRY(galloc(G, &ts->ntri, g.nslots));
-    LA3G_TRY(galloc(G, &ts->total, 1));
-    LA3G_TRY(galloc(G, &ts->esrc, g.nent + 1));
-    k_tc_expand<<<grid_for(g.nslots, 256), 256, 0, G->stream>>>(g.out_ptr, g.nslots, ts->esrc);
-    LA3G_LAUNCHED();
+    LA3G_TRY(tc_prepare(G, ts));
   }
   cudaStream_t s = G->stream;
   const uint32_t N = g.nslots;
   T.device_begin();
   LA3G_CUDA(cudaMemsetAsync(ts->ntri, 0, (size_t) N * 4, s));
   LA3G_CUDA(cudaMemsetAsync(ts->total, 0, 8, s));
+  LA3G_CUDA(cudaMemsetAsync(ts->next, 0, 8, s));
+  if (ts->nmid)
   {
-    ProfileScope p("tc_intersect", s, 8.0 * g.nent);
-    k_tc<<<grid_for((uint64_t) g.nent * 32, 256, kSMs * 32), 256, 0, s>>>(ts->esrc, g.out_row, g.nent, g.in_ptr,
-                                                                          g.in_col, g.src_base(), g.nsrc, ts->ntri);
+    ProfileScope p("tc_rank_mid", s, 0.0);
+    k_tc_rank_block<kTcCap, 256><<<kSMs * 8, 256, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->order_mid, ts->nmid,
+                                                          ts->next + 1, ts->ntri);
     LA3G_LAUNCHED();
+  }
+  if (ts->norder)
+  {
+    ProfileScope p("tc_rank", s, 4.0 * ts->work + 8.0 * N);
+    k_tc_rank<kTcSmall, 8><<<kSMs * 8, 8 * 32, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->order, ts->norder, ts->next,
+                                                       ts->ntri);
+    LA3G_LAUNCHED();
+  }
+  if (ts->nbig)
+  {
+    k_tc_rank_big<<<grid_for((uint64_t) ts->nbig * 32, 256), 256, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->big, ts->nbig,
+                                                                           ts->ntri);
+    LA3G_LAUNCHED();
+    tls_launches++;
   }
   k_tc_sum<<<grid_for(N, 256), 256, 0, s>>>(N, ts->ntri, ts->total);
   LA3G_LAUNCHED();
@@ -134,23 +514,15 @@ extern "C" int la3g_tc(la3g_graph* G, uint64_t* total_out, uint32_t* per_vertex_
   T.device_end();
   unsigned long long total = 0;
   LA3G_CUDA(cudaMemcpyAsync(&total, ts->total, 8, cudaMemcpyDeviceToHost, s));
-  if (per_vertex_out)
-  {
-    DevBuf tmp;
-    LA3G_TRY(tmp.alloc((size_t) N * 4));
-    k_tc_by_id<<<grid_for(N, 256), 256, 0, s>>>(N, g.id_of_pos, ts->ntri, tmp.as<uint32_t>());
-    LA3G_LAUNCHED();
-    LA3G_CUDA(cudaMemcpyAsync(per_vertex_out, tmp.p, (size_t) N * 4, cudaMemcpyDeviceToHost, s));
-    LA3G_CUDA(cudaStreamSynchronize(s));
-  }
+  if (per_vertex_out) LA3G_CUDA(cudaMemcpyAsync(per_vertex_out, ts->ntri, (size_t) N * 4, cudaMemcpyDeviceToHost, s));
   LA3G_TRY(T.finish());
   if (total_out) *total_out = total;
   if (st)
   {
     st->iterations = 2;
     st->teps_edges = g.nent;
-    st->edges_examined = g.nent;
-    st->algo_bytes = (uint64_t) (8.0 * g.nent + 8.0 * N);
+    st->edges_examined = (uint64_t) ts->work;
+    st->algo_bytes = (uint64_t) (4.0 * ts->work + 8.0 * N);
   }
   return LA3G_OK;
 }
