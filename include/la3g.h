@@ -197,6 +197,16 @@ int la3g_bfs_batch(la3g_graph* g, const uint32_t* roots, uint32_t nroots, uint8_
 int la3g_sssp_batch(la3g_graph* g, const uint32_t* roots, uint32_t nroots, uint32_t* dist_out,
                     la3g_stats* st);
 
+/* Tunes the batched BFS for this graph (level mode: per-level CUDA graph or
+ * persistent kernel; block size; push/pull threshold) by timing each
+ * combination on the given roots; the best is kept on the graph handle.
+ * report (nullable) receives a JSON list of the timings. */
+int la3g_batch_autotune(la3g_graph* g, const uint32_t* roots, uint32_t nroots, char* report, size_t cap);
+
+/* Sets the batched-BFS configuration by hand: mode 0 = per-level CUDA graph,
+ * 1 = persistent kernel; block 128 / 256 / 512; push_frac in [0, 1]. */
+int la3g_batch_config(la3g_graph* g, int mode, int block, double push_frac);
+
 /* ---- caller-allocated form -------------------------------------------- */
 
 /* BFS that allocates nothing.  It has no counterpart in the reference: it is

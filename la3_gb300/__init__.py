@@ -249,6 +249,20 @@ def bfs_batch(G: Graph, roots: Sequence[int], want_hops: bool = True):
     return hops, st
 
 
+def batch_autotune(G: Graph, roots: Sequence[int]) -> list:
+    """Times the batched-BFS configurations on `roots`; keeps the best on G."""
+    import json
+    r = np.ascontiguousarray(np.asarray(roots, dtype=np.uint32))
+    buf = C.create_string_buffer(1 << 14)
+    N.check(N.lib().la3g_batch_autotune(G._h, _ptr(r, C.c_uint32), r.size, buf, len(buf)))
+    return json.loads(buf.value.decode())
+
+
+def batch_config(G: Graph, mode: int, block: int = 256, push_frac: float = 0.05) -> None:
+    """mode 0: per-level CUDA graph; 1: persistent kernel."""
+    N.check(N.lib().la3g_batch_config(G._h, mode, block, push_frac))
+
+
 def sssp_batch(G: Graph, roots: Sequence[int], want_dist: bool = True):
     r = np.ascontiguousarray(np.asarray(roots, dtype=np.uint32))
     st = Stats()
@@ -337,5 +351,5 @@ def profile_report() -> dict:
 
 
 __all__ = ["Graph", "EdgeList", "BM25", "LA3GError", "Stats", "pagerank", "pagerank_f32", "bfs", "sssp", "cc", "tc",
-           "bfs_batch", "sssp_batch", "read_queries", "profile", "profile_reset", "profile_report", "DIRECTED", "REVERSE", "ACYCLIC",
+           "bfs_batch", "sssp_batch", "batch_autotune", "batch_config", "read_queries", "profile", "profile_reset", "profile_report", "DIRECTED", "REVERSE", "ACYCLIC",
            "BIPARTITE", "WEIGHTED", "SSSP_INF", "BFS_INF"]
