@@ -186,7 +186,8 @@ def run_reference_sample(steps: int, scale: int, tc_scale: int, nroots: int = 4,
         ew.write(d / "g.w.bin")
         L.EdgeList.rmat(tc_scale, 16, seed=TC_SEED).write(d / "t.bin")
         src, dst, _ = e.arrays()
-        cand = np.unique(np.concatenate([src, dst]))
+        # roots with out-edges, so that the directed SSSP from them does work too
+        cand = np.unique(src[src != dst])
         roots = rank_roots(cand, nroots, 0, seed)
         env = dict(os.environ, OMP_NUM_THREADS="2")
         t0 = time.time()
@@ -249,38 +250,40 @@ def gpu_line(args, rank: int, world: int, local: int) -> dict | None:
     GT = L.Graph.from_edges(et, L.DIRECTED | L.ACYCLIC)
     pos, ids = GU.positions()
     nonisolated = ids[: GU.info.nregular + GU.info.nsink]
+    # SSSP roots: vertices with out-edges in the directed graph (regular and
+    # source positions); a sink root reaches nothing
+    _, wids = GW.positions()
+    iw = GW.info
+    with_out = np.concatenate([wids[: iw.nregular], wids[iw.nregular + iw.nsink: iw.nregular + iw.nsink + iw.nsource]])
     del e, ew, et
     K, W = args.steps, args.warmup
     roots = rank_roots(np.sort(nonisolated), K + W, rank)
+    sroots = rank_roots(np.sort(with_out), K + W, rank, seed=98)
     for g in (GU, GW, GT):
         g.set_stream(stream.cuda_stream)
     setup_s = time.time() - t_setup
 
     # TEPS numerators per root (computed once, outside every timed region)
-    teps = {}
+    teps_b, teps_s = {}, {}
     for r in set(roots):
         _, _, sb = L.bfs(GU, r, False, False)
+        teps_b[r] = sb.teps_edges
+    for r in set(sroots):
         _, ss = L.sssp(GW, r, False)
-        teps[r] = (sb.teps_edges, ss.teps_edges)
+        teps_s[r] = ss.teps_edges
     _, sc = L.cc(GU, False)
     _, _, stc = L.tc(GT, False)
     cc_e, tc_e = sc.teps_edges, stc.teps_edges
 
-    def step(r, outs=None):
-        if outs is None:
-            L.N.lib().la3g_bfs(GU._h, r, None, None, None)
-            L.N.lib().la3g_sssp(GW._h, r, None, None)
-            L.N.lib().la3g_cc(GU._h, None, None)
-            L.N.lib().la3g_tc(GT._h, None, None, None)
-        else:
-            L.bfs(GU, r)
-            L.sssp(GW, r)
-            L.cc(GU)
-            L.tc(GT)
+    def step(k):
+        L.N.check(L.N.lib().la3g_bfs(GU._h, roots[k], None, None, None))
+        L.N.check(L.N.lib().la3g_sssp(GW._h, sroots[k], None, None))
+        L.N.check(L.N.lib().la3g_cc(GU._h, None, None))
+        L.N.check(L.N.lib().la3g_tc(GT._h, None, None, None))
 
     # warm-up
     for k in range(W):
-        step(roots[k])
+        step(k)
     torch.cuda.synchronize()
 
     # L2: every step's inputs (s22 CSR ~ 0.5 GB) are larger than the 129 MB L2;
@@ -294,7 +297,7 @@ def gpu_line(args, rank: int, world: int, local: int) -> dict | None:
     app_edges = {"bfs": 0, "sssp": 0, "cc": 0, "tc": 0}
     lib = L.N.lib()
     with ClockSampler(local) as clocks:
-        step(roots[0])  # one more untimed step with the sampler running
+        step(0)  # one more untimed step with the sampler running
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
@@ -302,21 +305,20 @@ def gpu_line(args, rank: int, world: int, local: int) -> dict | None:
         with torch.cuda.stream(stream):
             ev[0].record(stream)
             for k in range(K):
-                r = roots[W + k]
+                r, rs = roots[W + k], sroots[W + k]
                 flush.fill_(k & 0xFF)
                 a = app_ev[k]
                 a[0].record(stream)
                 L.N.check(lib.la3g_bfs(GU._h, r, None, None, None))
                 a[1].record(stream)
-                L.N.check(lib.la3g_sssp(GW._h, r, None, None))
+                L.N.check(lib.la3g_sssp(GW._h, rs, None, None))
                 a[2].record(stream)
                 L.N.check(lib.la3g_cc(GU._h, None, None))
                 a[3].record(stream)
                 L.N.check(lib.la3g_tc(GT._h, None, None, None))
                 a[4].record(stream)
-                be, se = teps[r]
-                app_edges["bfs"] += be
-                app_edges["sssp"] += se
+                app_edges["bfs"] += teps_b[r]
+                app_edges["sssp"] += teps_s[rs]
                 app_edges["cc"] += cc_e
                 app_edges["tc"] += tc_e
             ev[1].record(stream)
@@ -338,23 +340,24 @@ def gpu_line(args, rank: int, world: int, local: int) -> dict | None:
     hops, par, dist, lab, ntri = (pin(N, torch.uint8), pin(N, torch.int32).view(np.uint32),
                                   pin(N, torch.int32).view(np.uint32), pin(N, torch.int32).view(np.uint32),
                                   pin(NT, torch.int32).view(np.uint32))
-    roots_h = pin(K, torch.int32).view(np.uint32)
-    roots_h[:] = roots[W:W + K]
+    roots_h = pin(2 * K, torch.int32).view(np.uint32)
+    roots_h[:K] = roots[W:W + K]
+    roots_h[K:] = sroots[W:W + K]
     import ctypes as C
     u8p, u32p = C.POINTER(C.c_uint8), C.POINTER(C.c_uint32)
     tot = C.c_uint64()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for k in range(K):
-        r = int(roots_h[k])
+        r, rs = int(roots_h[k]), int(roots_h[K + k])
         L.N.check(lib.la3g_bfs(GU._h, r, hops.ctypes.data_as(u8p), par.ctypes.data_as(u32p), None))
-        L.N.check(lib.la3g_sssp(GW._h, r, dist.ctypes.data_as(u32p), None))
+        L.N.check(lib.la3g_sssp(GW._h, rs, dist.ctypes.data_as(u32p), None))
         L.N.check(lib.la3g_cc(GU._h, lab.ctypes.data_as(u32p), None))
         L.N.check(lib.la3g_tc(GT._h, C.byref(tot), ntri.ctypes.data_as(u32p), None))
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     e2e_edges, e2e_s = reduce_results(edges, e2e_s, device=dev)
-    e2e = {"value": e2e_edges / e2e_s / 1e9, "unit": "GTEPS", "h2d_bytes_per_step": 8,
+    e2e = {"value": e2e_edges / e2e_s / 1e9, "unit": "GTEPS", "h2d_bytes_per_step": 16,
            "d2h_bytes_per_step": N * (1 + 4 + 4 + 4) + NT * 4 + 8}
 
     # roofline of the dominant kernel: per-launch CUDA events inside the library
@@ -362,7 +365,7 @@ def gpu_line(args, rank: int, world: int, local: int) -> dict | None:
     L.profile(True)
     with torch.cuda.stream(stream):
         for k in range(min(K, 2)):
-            step(roots[W + k])
+            step(W + k)
     torch.cuda.synchronize()
     L.profile(False)
     prof = L.profile_report()
@@ -399,9 +402,8 @@ def gpu_line(args, rank: int, world: int, local: int) -> dict | None:
     }
     # kernels of this library per step (counted by the library)
     st = [L.Stats() for _ in range(4)]
-    r = roots[W]
-    lib.la3g_bfs(GU._h, r, None, None, C.byref(st[0]))
-    lib.la3g_sssp(GW._h, r, None, C.byref(st[1]))
+    lib.la3g_bfs(GU._h, roots[W], None, None, C.byref(st[0]))
+    lib.la3g_sssp(GW._h, sroots[W], None, C.byref(st[1]))
     lib.la3g_cc(GU._h, None, C.byref(st[2]))
     lib.la3g_tc(GT._h, None, None, C.byref(st[3]))
     launches_per_step = sum(s.kernel_launches for s in st)

@@ -207,6 +207,72 @@ int la3g_batch_autotune(la3g_graph* g, const uint32_t* roots, uint32_t nroots, c
  * 1 = persistent kernel; block 128 / 256 / 512; push_frac in [0, 1]. */
 int la3g_batch_config(la3g_graph* g, int mode, int block, double push_frac);
 
+/* ---- serving loop (no reference counterpart; the reference answers one
+ *      query per VertexProgram run, bfs.cpp:11-37, sssp.cpp:11-37,
+ *      bm25.cpp:8-114) ------------------------------------------------------ */
+
+typedef struct la3g_server la3g_server;
+
+enum
+{
+  LA3G_QUERY_BFS = 1,   /* hops from root (la3g_bfs) */
+  LA3G_QUERY_SSSP = 2,  /* distances from root (la3g_sssp) */
+  LA3G_QUERY_BM25 = 3   /* top-k documents (la3g_bm25_query) */
+};
+
+typedef struct la3g_query
+{
+  uint32_t kind;          /* LA3G_QUERY_* */
+  uint32_t graph;         /* id returned by la3g_server_add_graph */
+  uint32_t root;          /* BFS / SSSP root vertex id */
+  uint32_t k;             /* BM25: documents wanted */
+  const uint32_t* terms;  /* BM25: term vertex ids (copied at submit) */
+  uint32_t nterms;
+  void* out;              /* BFS: uint8 hops[nslots]; SSSP: uint32 dist[nslots]; BM25: uint32 ids[k]; may be NULL */
+  float* scores_out;      /* BM25: scores[k]; may be NULL */
+} la3g_query;
+
+typedef struct la3g_query_result
+{
+  int status;             /* LA3G_OK or the query's error */
+  uint32_t kind;
+  double queue_ms;        /* submit -> admitted into a lane / started */
+  double latency_ms;      /* submit -> result written */
+  uint32_t in_flight;     /* queries on the graph's engine when it was admitted */
+  uint32_t nout;          /* BM25: documents written */
+} la3g_query_result;
+
+typedef struct la3g_server_stats
+{
+  uint64_t budget_bytes, used_bytes;
+  uint64_t completed, queued, pending;
+  uint32_t ngraphs, reserved;
+} la3g_server_stats;
+
+/* A server with an HBM budget (bytes).  bfs_lanes / sssp_lanes: queries one
+ * BFS / SSSP engine holds at once (multiples of 64; 0 = 128 / 64). */
+int la3g_server_create(uint64_t budget_bytes, uint32_t bfs_lanes, uint32_t sssp_lanes, la3g_server** out);
+/* Makes a loaded graph resident in the server: undirected graphs serve BFS,
+ * DIRECTED|WEIGHTED graphs SSSP, BIPARTITE graphs BM25 (prepared here if
+ * needed).  The graph's device bytes plus its engine's lane state must fit
+ * in the budget left (the lane count is halved down to 64 first), else
+ * LA3G_EBUDGET.  The caller keeps ownership but must not use the graph while
+ * it is served; la3g_server_free releases it. */
+int la3g_server_add_graph(la3g_server* s, la3g_graph* g, uint32_t* graph_id);
+/* Queues a query and returns its ticket at once; thread-safe.  The query's
+ * output buffers must stay valid until the ticket is polled done. */
+int la3g_server_submit(la3g_server* s, const la3g_query* q, uint64_t* ticket);
+/* Waits up to timeout_ms (0 = do not wait, < 0 = forever) for the ticket:
+ * LA3G_OK with res filled (the ticket is then released), or LA3G_EBUSY while
+ * it is still pending.  Thread-safe. */
+int la3g_server_poll(la3g_server* s, uint64_t ticket, int timeout_ms, la3g_query_result* res);
+int la3g_server_info(la3g_server* s, la3g_server_stats* out);
+/* Lanes the engine of graph_id was given (after budget halving). */
+int la3g_server_lanes(la3g_server* s, uint32_t graph_id, uint32_t* lanes);
+/* Stops the workers (queries still queued are dropped) and frees the
+ * server's device state; the graphs stay with the caller. */
+void la3g_server_free(la3g_server* s);
+
 /* ---- caller-allocated form -------------------------------------------- */
 
 /* BFS that allocates nothing.  It has no counterpart in the reference: it is

@@ -13,6 +13,7 @@ on the GPU, and a missing library raises at first use.
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 from dataclasses import dataclass
 from typing import Optional, Sequence
 
@@ -35,6 +36,10 @@ def _ptr(a: Optional[np.ndarray], ctype):
     if a is None:
         return None
     return a.ctypes.data_as(C.POINTER(ctype))
+
+
+def _addr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data
 
 
 @dataclass
@@ -121,6 +126,11 @@ class Graph:
         return pos, ids
 
     def free(self) -> None:
+        # servers that hold this graph go first (they must not outlive it)
+        for ref in getattr(self, "_servers", ()):
+            srv = ref()
+            if srv is not None:
+                srv.free()
         if self._h:
             N.lib().la3g_graph_free(self._h)
             self._h = None
@@ -239,6 +249,96 @@ def read_queries(labels_path: str, queries_path: str, ndocs: int) -> list[list[i
             if toks:
                 out.append([ids.get(t, 0) for t in toks])
     return out
+
+
+QUERY_BFS, QUERY_SSSP, QUERY_BM25 = 1, 2, 3
+
+
+class Server:
+    """Serving loop over resident graphs (la3g_server_*): queries are queued
+    with submit_* and collected with poll; BFS / SSSP queries of one graph
+    share its engine's lanes (continuous batching), each graph runs on its
+    own worker and stream."""
+
+    def __init__(self, budget_bytes: int, bfs_lanes: int = 0, sssp_lanes: int = 0):
+        h = C.c_void_p()
+        N.check(N.lib().la3g_server_create(budget_bytes, bfs_lanes, sssp_lanes, C.byref(h)))
+        self._h = h
+        self._graphs = {}
+        self._live = {}  # ticket -> output buffers (kept alive until polled)
+
+    def add_graph(self, G: Graph) -> int:
+        gid = C.c_uint32()
+        N.check(N.lib().la3g_server_add_graph(self._h, G._h, C.byref(gid)))
+        self._graphs[gid.value] = G
+        if not hasattr(G, "_servers"):
+            G._servers = []
+        G._servers.append(weakref.ref(self))
+        return gid.value
+
+    def lanes(self, gid: int) -> int:
+        n = C.c_uint32()
+        N.check(N.lib().la3g_server_lanes(self._h, gid, C.byref(n)))
+        return n.value
+
+    def _submit(self, q, bufs) -> int:
+        t = C.c_uint64()
+        N.check(N.lib().la3g_server_submit(self._h, C.byref(q), C.byref(t)))
+        self._live[t.value] = bufs
+        return t.value
+
+    def _graph(self, gid: int) -> Graph:
+        G = self._graphs.get(gid)
+        if G is None:
+            raise LA3GError(1, f"no such graph id {gid}")
+        return G
+
+    def submit_bfs(self, gid: int, root: int, want: bool = True) -> int:
+        out = np.empty(self._graph(gid).nslots, np.uint8) if want else None
+        q = N.Query(kind=QUERY_BFS, graph=gid, root=root, out=_addr(out))
+        return self._submit(q, (out,))
+
+    def submit_sssp(self, gid: int, root: int, want: bool = True) -> int:
+        out = np.empty(self._graph(gid).nslots, np.uint32) if want else None
+        q = N.Query(kind=QUERY_SSSP, graph=gid, root=root, out=_addr(out))
+        return self._submit(q, (out,))
+
+    def submit_bm25(self, gid: int, term_vids: Sequence[int], k: int = 10) -> int:
+        terms = np.ascontiguousarray(term_vids, dtype=np.uint32)
+        ids = np.zeros(k, np.uint32)
+        sc = np.zeros(k, np.float32)
+        q = N.Query(kind=QUERY_BM25, graph=gid, k=k, terms=_ptr(terms, C.c_uint32), nterms=terms.size,
+                    out=_addr(ids), scores_out=_ptr(sc, C.c_float))
+        return self._submit(q, (ids, sc))
+
+    def poll(self, ticket: int, timeout_ms: int = -1):
+        """(result struct, outputs) when done, None while pending."""
+        r = N.QueryResult()
+        st = N.lib().la3g_server_poll(self._h, ticket, timeout_ms, C.byref(r))
+        if st == 8:  # LA3G_EBUSY
+            return None
+        N.check(st)
+        bufs = self._live.pop(ticket)
+        if r.kind == QUERY_BM25:
+            bufs = (bufs[0][: r.nout], bufs[1][: r.nout])
+        return r, bufs
+
+    def info(self) -> dict:
+        s = N.ServerStats()
+        N.check(N.lib().la3g_server_info(self._h, C.byref(s)))
+        return {f: getattr(s, f) for f, _ in N.ServerStats._fields_ if f != "reserved"}
+
+    def free(self) -> None:
+        if self._h:
+            N.lib().la3g_server_free(self._h)
+            self._h = None
+            self._live.clear()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
 
 
 def bfs_batch(G: Graph, roots: Sequence[int], want_hops: bool = True):

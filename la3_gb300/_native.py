@@ -64,6 +64,42 @@ class Edges(C.Structure):
     ]
 
 
+class Query(C.Structure):
+    _fields_ = [
+        ("kind", C.c_uint32),
+        ("graph", C.c_uint32),
+        ("root", C.c_uint32),
+        ("k", C.c_uint32),
+        ("terms", C.POINTER(C.c_uint32)),
+        ("nterms", C.c_uint32),
+        ("out", C.c_void_p),
+        ("scores_out", C.POINTER(C.c_float)),
+    ]
+
+
+class QueryResult(C.Structure):
+    _fields_ = [
+        ("status", C.c_int),
+        ("kind", C.c_uint32),
+        ("queue_ms", C.c_double),
+        ("latency_ms", C.c_double),
+        ("in_flight", C.c_uint32),
+        ("nout", C.c_uint32),
+    ]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [
+        ("budget_bytes", C.c_uint64),
+        ("used_bytes", C.c_uint64),
+        ("completed", C.c_uint64),
+        ("queued", C.c_uint64),
+        ("pending", C.c_uint64),
+        ("ngraphs", C.c_uint32),
+        ("reserved", C.c_uint32),
+    ]
+
+
 _P = C.c_void_p
 _u32p = C.POINTER(C.c_uint32)
 _u8p = C.POINTER(C.c_uint8)
@@ -103,6 +139,13 @@ SIGNATURES = {
                                      C.POINTER(Edges)]),
     "la3g_edges_write": (C.c_int, [C.POINTER(Edges), C.c_char_p, C.c_int]),
     "la3g_edges_free": (None, [C.POINTER(Edges)]),
+    "la3g_server_create": (C.c_int, [C.c_uint64, C.c_uint32, C.c_uint32, C.POINTER(_P)]),
+    "la3g_server_add_graph": (C.c_int, [_P, _P, _u32p]),
+    "la3g_server_submit": (C.c_int, [_P, C.POINTER(Query), _u64p]),
+    "la3g_server_poll": (C.c_int, [_P, C.c_uint64, C.c_int, C.POINTER(QueryResult)]),
+    "la3g_server_info": (C.c_int, [_P, C.POINTER(ServerStats)]),
+    "la3g_server_lanes": (C.c_int, [_P, C.c_uint32, _u32p]),
+    "la3g_server_free": (None, [_P]),
     "la3g_profile_enable": (None, [C.c_int]),
     "la3g_profile_reset": (None, []),
     "la3g_profile_report": (C.c_size_t, [C.c_char_p, C.c_size_t]),

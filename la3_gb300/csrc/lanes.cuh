@@ -1,0 +1,170 @@
+// Kernels shared by the batched SSSP (la3g_sssp_batch) and the serving
+// loop's SSSP lanes: distances are kept [vertex][root] (uint32, INF =
+// 2^31 - 1) with one frontier bit per (vertex, root) packed 64 roots to a
+// word; an iteration relaxes the out-edges of every active (vertex, word)
+// pair.  Everything here has internal linkage so that each translation unit
+// that includes it gets its own copy.
+#ifndef LA3G_LANES_CUH
+#define LA3G_LANES_CUH
+
+#include <cstdint>
+
+#include "frontier.cuh"
+
+namespace la3g {
+
+static constexpr uint32_t kInfD = 0x7FFFFFFFu;
+
+// Active (vertex, word) pairs of the batched SSSP are kept as a split
+// frontier: pairs whose vertex has at most kBigDeg regular out-edges are
+// listed for one warp each; the edges of bigger ones are cut into tasks of
+// kHubTask edges that warps take one at a time.
+struct PairList
+{
+  uint32_t* small;
+  uint32_t* hub;
+  uint32_t* hub_t0;
+  unsigned long long* nsmall;
+  unsigned long long* packed;
+};
+
+static __device__ __forceinline__ void bs_list_pair(uint32_t i, uint32_t deg, const PairList& L)
+{
+  if (deg <= kBigDeg) L.small[atomicAdd(L.nsmall, 1ull)] = i;
+  else hub_append(i, deg, L.hub, L.hub_t0, L.packed);
+}
+
+// Relaxes edges [k0, k1) of the vertex of pair i: lane l handles roots
+// 64w + l and 64w + l + 32, so the distances of one edge's target are read
+// contiguously; the roots an edge improved are ORed into the target's
+// next-frontier word at once.
+static __device__ __forceinline__ void bs_relax_range(uint32_t i, uint32_t k0, uint32_t k1, int lane, uint32_t R, uint32_t W,
+                                               const uint32_t* __restrict__ row, const uint32_t* __restrict__ wgt,
+                                               const uint64_t* __restrict__ front, uint64_t* next,
+                                               const uint32_t* __restrict__ msg, uint32_t* dist)
+{
+  const uint32_t u = i / W, w = i % W;
+  const uint64_t f = front[i];
+  const uint32_t r0 = w * 64 + lane, r1 = r0 + 32;
+  const bool h0 = (f >> lane) & 1ull, h1 = (f >> (lane + 32)) & 1ull;
+  const uint32_t m0 = h0 ? msg[(uint64_t) u * R + r0] : 0, m1 = h1 ? msg[(uint64_t) u * R + r1] : 0;
+  for (uint32_t k = k0; k < k1; k++)
+  {
+    const uint32_t v = row[k], wt = wgt[k];
+    bool i0 = false, i1 = false;
+    if (h0)
+    {
+      const uint32_t cand = m0 + wt;
+      uint32_t* p = &dist[(uint64_t) v * R + r0];
+      i0 = cand < *p && cand < atomicMin(p, cand);
+    }
+    if (h1)
+    {
+      const uint32_t cand = m1 + wt;
+      uint32_t* p = &dist[(uint64_t) v * R + r1];
+      i1 = cand < *p && cand < atomicMin(p, cand);
+    }
+    const uint64_t mask = (uint64_t) __ballot_sync(0xffffffffu, i0) | ((uint64_t) __ballot_sync(0xffffffffu, i1) << 32);
+    if (lane == 0 && mask) atomicOr((unsigned long long*) &next[(uint64_t) v * W + w], (unsigned long long) mask);
+  }
+}
+
+static __global__ void __launch_bounds__(256)
+k_bs_relax(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ reg_end, const uint32_t* __restrict__ row,
+           const uint32_t* __restrict__ wgt, uint32_t R, uint32_t W, const uint64_t* __restrict__ front, PairList L,
+           uint64_t* next, const uint32_t* __restrict__ msg, uint32_t* dist)
+{
+  const int lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t ns = (uint32_t) *L.nsmall;
+  const unsigned long long pk = *L.packed;
+  const uint32_t nbig = hub_count(pk), ntasks = hub_tasks(pk);
+  for (uint32_t a = warp; a < ntasks + ns; a += nwarps)
+  {
+    if (a < ntasks)
+    {
+      const uint32_t slot = hub_of_task(L.hub_t0, nbig, a);
+      const uint32_t i = L.hub[slot], u = i / W;
+      const uint32_t k0 = ptr[u] + (a - L.hub_t0[slot]) * kHubTask;
+      bs_relax_range(i, k0, min(k0 + kHubTask, reg_end[u]), lane, R, W, row, wgt, front, next, msg, dist);
+    }
+    else
+    {
+      const uint32_t i = L.small[a - ntasks], u = i / W;
+      bs_relax_range(i, ptr[u], reg_end[u], lane, R, W, row, wgt, front, next, msg, dist);
+    }
+  }
+}
+
+// After a relaxation: the old frontier words are cleared (they become the
+// next "next" buffer); messages = current distances of the newly lowered
+// roots; the words holding them form the next active list.  alive (W words,
+// optional) collects the roots that still have a frontier.
+static __global__ void k_bs_apply(uint32_t N, uint32_t R, uint32_t W, const uint32_t* __restrict__ ptr,
+                                  const uint32_t* __restrict__ reg_end, const uint64_t* __restrict__ next,
+                                  const uint32_t* __restrict__ dist, uint32_t* msg, PairList out, uint64_t* front_old,
+                                  PairList old, uint64_t* alive = nullptr)
+{
+  const uint64_t tid = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x, nth = (uint64_t) gridDim.x * blockDim.x;
+  const uint64_t ns = *old.nsmall, nb = hub_count(*old.packed);
+  for (uint64_t k = tid; k < ns; k += nth) front_old[old.small[k]] = 0;
+  for (uint64_t k = tid; k < nb; k += nth) front_old[old.hub[k]] = 0;
+  const uint64_t NW = (uint64_t) N * W;
+  for (uint64_t i = tid; i < NW; i += nth)
+  {
+    uint64_t f = next[i];
+    if (!f) continue;
+    const uint32_t v = (uint32_t) (i / W), w = (uint32_t) (i % W);
+    bs_list_pair((uint32_t) i, reg_end[v] - ptr[v], out);
+    if (alive && (alive[w] & f) != f) atomicOr((unsigned long long*) &alive[w], (unsigned long long) f);
+    while (f)
+    {
+      const int bpos = __ffsll((long long) f) - 1;
+      f &= f - 1;
+      const uint64_t j = (uint64_t) v * R + w * 64 + bpos;
+      msg[j] = dist[j];
+    }
+  }
+}
+
+// Initial active list: the nonzero words of the root frontier.
+static __global__ void k_bs_list(uint64_t NW, uint32_t W, const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ reg_end,
+                          const uint64_t* __restrict__ front, PairList out)
+{
+  for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < NW; i += (uint64_t) gridDim.x * blockDim.x)
+    if (front[i])
+    {
+      const uint32_t v = (uint32_t) (i / W);
+      bs_list_pair((uint32_t) i, reg_end[v] - ptr[v], out);
+    }
+}
+
+static __global__ void k_max_u32(const uint32_t* __restrict__ a, uint64_t n, unsigned int* out)
+{
+  unsigned int m = 0;
+  for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t) gridDim.x * blockDim.x)
+    m = max(m, a[i]);
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+static __global__ void k_reg_end(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ row, uint32_t N, uint32_t nreg,
+                          uint32_t* reg_end)
+{
+  for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < N; u += gridDim.x * blockDim.x)
+  {
+    uint32_t lo = ptr[u], hi = ptr[u + 1];
+    while (lo < hi)
+    {
+      uint32_t mid = (lo + hi) >> 1;
+      if (row[mid] < nreg) lo = mid + 1;
+      else hi = mid;
+    }
+    reg_end[u] = lo;
+  }
+}
+
+}  // namespace la3g
+
+#endif

@@ -311,35 +311,80 @@ __global__ void k_prf_init(uint32_t N, uint32_t nrows_reg, uint32_t src_base, ui
   }
 }
 
-// FP32 SpMV with FP32 accumulation: warp per 32-row tile, each lane its row
-// (any order inside a row is allowed here); the L1 residual is reduced in
-// FP64.
+__device__ __forceinline__ double prf_finish(uint32_t r, float acc, float* __restrict__ xnext, float* __restrict__ rankf,
+                                             double* __restrict__ rank, const uint32_t* __restrict__ deg, int write_x)
+{
+  const float nr = (float) kAlpha + (float) (1.0 - kAlpha) * acc;
+  const double d = fabs((double) nr - (double) rankf[r]);
+  rankf[r] = nr;
+  rank[r] = (double) nr;
+  if (write_x) xnext[r] = nr / (float) deg[r];
+  return d;
+}
+
+// FP32 SpMV with FP32 accumulation (any order inside a row is allowed
+// here).  The first `long_blocks` blocks take the rows longer than
+// kLongRow, one block per row with a shared-memory reduction; the others
+// give each row of at most kLongRow edges a group of 8 lanes (four rows per
+// warp), so average-degree rows keep the lanes busy.  The L1 residual is
+// reduced in FP64.
 __global__ void __launch_bounds__(256)
 k_prf_pull(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const float* __restrict__ x,
            float* __restrict__ xnext, float* __restrict__ rankf, double* __restrict__ rank,
-           const uint32_t* __restrict__ deg, uint32_t row_lo, uint32_t row_hi, double* resid, int write_x)
+           const uint32_t* __restrict__ deg, const uint32_t* __restrict__ long_rows, uint32_t nlong,
+           uint32_t long_blocks, uint32_t row_lo, uint32_t row_hi, double* resid, int write_x)
 {
   const int lane = threadIdx.x & 31;
-  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   double local = 0.0;
-  for (uint32_t r = row_lo + warp; r < row_hi; r += nwarps)
+  if (blockIdx.x < long_blocks)
   {
-    uint32_t b = ptr[r], e = ptr[r + 1];
-    float acc = 0.0f;
-    for (uint32_t i = b + lane; i < e; i += 32) acc += x[col[i]];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0)
+    __shared__ float part[8];
+    for (uint32_t k = blockIdx.x; k < nlong; k += long_blocks)
     {
-      float nr = (float) kAlpha + (float) (1.0 - kAlpha) * acc;
-      double d = fabs((double) nr - (double) rankf[r]);
-      local += d;
-      rankf[r] = nr;
-      rank[r] = (double) nr;
-      if (write_x) xnext[r] = nr / (float) deg[r];
+      const uint32_t r = long_rows[k];
+      if (r < row_lo || r >= row_hi) continue;  // uniform per block
+      float acc = 0.0f;
+      for (uint32_t i = ptr[r] + threadIdx.x; i < ptr[r + 1]; i += blockDim.x) acc += x[col[i]];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (lane == 0) part[threadIdx.x >> 5] = acc;
+      __syncthreads();
+      if (threadIdx.x == 0)
+      {
+        float t = 0.0f;
+        for (int w = 0; w < (int) (blockDim.x >> 5); w++) t += part[w];
+        local += prf_finish(r, t, xnext, rankf, rank, deg, write_x);
+      }
+      __syncthreads();
     }
+    if (threadIdx.x == 0 && local != 0.0) atomicAdd(resid, local);
+    return;
   }
+  const uint32_t sub = lane & 7;
+  const uint32_t group = ((blockIdx.x - long_blocks) * blockDim.x + threadIdx.x) >> 3;
+  const uint32_t ngroups = ((gridDim.x - long_blocks) * blockDim.x) >> 3;
+  const uint32_t nrows = row_hi - row_lo;
+  // all 8-lane groups of a warp run the same number of rounds
+  const uint32_t rounds = (nrows + ngroups - 1) / ngroups;
+  for (uint32_t k = 0; k < rounds; k++)
+  {
+    const uint32_t r = row_lo + group + k * ngroups;
+    float acc = 0.0f;
+    bool mine = false;
+    if (r < row_hi)
+    {
+      const uint32_t b = ptr[r], e = ptr[r + 1];
+      mine = (e - b) <= kLongRow;
+      if (mine)
+        for (uint32_t i = b + sub; i < e; i += 8) acc += x[col[i]];
+    }
+    acc += __shfl_xor_sync(0xffffffffu, acc, 4);
+    acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+    acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+    if (mine && sub == 0) local += prf_finish(r, acc, xnext, rankf, rank, deg, write_x);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
   if (lane == 0 && local != 0.0) atomicAdd(resid, local);
 }
 
@@ -442,14 +487,18 @@ extern "C" int la3g_pr_f32(la3g_graph* G, uint32_t iters, double tol, double* ra
   int cur = 0;
   uint32_t it = 0;
   double res = 0.0;
-  const unsigned blocks = grid_for((uint64_t) g.nreg * 32, 256, kSMs * 8);
+  const uint32_t long_blocks = ps->nlong ? std::min<uint32_t>(ps->nlong, kSMs * 2) : 0;
+  const unsigned blocks = long_blocks + std::max<uint32_t>(grid_for((uint64_t) g.nreg * 8, 256, kSMs * 8), 1);
+  // algorithmic bytes per iteration (FP32 form of the FP64 count): column
+  // index per edge, row offsets, x read, rank read + write, next x write
+  const double it_bytes = 4.0 * g.nent + 4.0 * (g.nreg + 1) + 4.0 * N + 8.0 * g.nreg + 8.0 * g.nreg + 4.0 * g.nreg;
   for (; it < iters;)
   {
     LA3G_CUDA(cudaMemsetAsync(ps->resid, 0, 8, s));
     {
-      ProfileScope p("pr_pull_f32", s, 4.0 * g.nent + 4.0 * (g.nreg + 1) + 4.0 * N + 12.0 * g.nreg + 4.0 * g.nreg);
-      k_prf_pull<<<blocks, 256, 0, s>>>(g.in_ptr, g.in_col, ps->xf[cur], ps->xf[cur ^ 1], ps->rankf, ps->rank, ps->deg, 0,
-                                        g.nreg, ps->resid, 1);
+      ProfileScope p("pr_pull_f32", s, it_bytes);
+      k_prf_pull<<<blocks, 256, 0, s>>>(g.in_ptr, g.in_col, ps->xf[cur], ps->xf[cur ^ 1], ps->rankf, ps->rank, ps->deg,
+                                        ps->long_rows, ps->nlong, long_blocks, 0, g.nreg, ps->resid, 1);
       LA3G_LAUNCHED();
     }
     cur ^= 1;
@@ -461,19 +510,17 @@ extern "C" int la3g_pr_f32(la3g_graph* G, uint32_t iters, double tol, double* ra
       if (res < tol) break;
     }
   }
+  // the residual of the last iteration (the sink pass below reuses the counter)
+  if (tol <= 0) LA3G_CUDA(cudaMemcpyAsync(&res, ps->resid, 8, cudaMemcpyDeviceToHost, s));
   if (g.nsink)
   {
-    const unsigned sb = grid_for((uint64_t) g.nsink * 32, 256, kSMs * 8);
-    ProfileScope p("pr_pull_f32", s, 4.0 * g.nent);
-    k_prf_pull<<<sb, 256, 0, s>>>(g.in_ptr, g.in_col, ps->xf[cur], ps->xf[cur ^ 1], ps->rankf, ps->rank, ps->deg, g.nreg,
-                                  g.nreg + g.nsink, ps->resid, 0);
+    const unsigned sb = long_blocks + std::max<uint32_t>(grid_for((uint64_t) g.nsink * 8, 256, kSMs * 8), 1);
+    LA3G_CUDA(cudaMemsetAsync(ps->resid, 0, 8, s));
+    k_prf_pull<<<sb, 256, 0, s>>>(g.in_ptr, g.in_col, ps->xf[cur], ps->xf[cur ^ 1], ps->rankf, ps->rank, ps->deg,
+                                  ps->long_rows, ps->nlong, long_blocks, g.nreg, g.nreg + g.nsink, ps->resid, 0);
     LA3G_LAUNCHED();
   }
   T.device_end();
-  if (tol <= 0)
-  {
-    LA3G_CUDA(cudaMemcpyAsync(&res, ps->resid, 8, cudaMemcpyDeviceToHost, s));
-  }
   if (st)
   {
     st->iterations = it;

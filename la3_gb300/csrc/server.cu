@@ -1,0 +1,1017 @@
+// Serving loop: BFS / SSSP / BM25 queries against several device-resident
+// graphs, admitted as they arrive.
+//
+// The reference answers one query per VertexProgram run (bfs.cpp:11-37,
+// sssp.cpp:11-37, bm25.cpp:8-114); here every resident graph gets an engine
+// with its own worker thread and CUDA stream, so work on different graphs
+// overlaps on the device:
+//
+//  * BFS and SSSP engines run "lanes": a query occupies one bit of a 64-bit
+//    frontier word per vertex (the batched layout), and one engine iteration
+//    advances every occupied lane by one BSP step.  Between iterations the
+//    worker retires lanes whose frontier emptied (their results are copied
+//    out and the lane's state reset) and admits queued queries into free
+//    lanes.  Continuous batching: a query never waits for a batch to drain.
+//    Each lane's arithmetic is that of the single-root call, and lanes never
+//    read one another's bits, so a result does not depend on the mix.
+//  * BM25 engines run their queries one after another on their corpus.
+//
+// Admission by HBM budget: a graph joins only if its device bytes plus the
+// engine's lane state fit in what is left of the budget (the lane count is
+// halved down to 64 before LA3G_EBUDGET is returned); queries then wait for a
+// free lane of their graph's engine.
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "la3g_internal.h"
+#include "lanes.cuh"
+
+namespace la3g {
+namespace {
+
+constexpr uint32_t kOutChunk = 16;  // lanes retired per output pass (staging size)
+
+double wall_ms()
+{
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct Ticket
+{
+  la3g_query q{};
+  std::vector<uint32_t> terms;
+  int status = -1;  // -1 pending
+  double submit_ms = 0, start_ms = 0, done_ms = 0;
+  uint32_t in_flight = 0;
+  uint32_t nout = 0;
+};
+
+// ------------------------------------------------------------------ BFS lanes
+
+__global__ void k_lb_admit(const uint32_t* __restrict__ adm, uint32_t n, uint32_t N, uint32_t W,
+                           const uint32_t* __restrict__ ptr, uint32_t level, uint64_t* vis, uint64_t* front,
+                           uint8_t* hops, uint32_t* lane_base, uint64_t* alive, unsigned long long* front_deg)
+{
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+  {
+    const uint32_t l = adm[2 * j], p = adm[2 * j + 1];
+    const uint32_t w = l / 64;
+    const unsigned long long bit = 1ull << (l % 64);
+    atomicOr((unsigned long long*) &vis[(uint64_t) p * W + w], bit);
+    atomicOr((unsigned long long*) &front[(uint64_t) p * W + w], bit);
+    atomicOr((unsigned long long*) &alive[w], bit);
+    hops[(uint64_t) l * N + p] = 0;
+    lane_base[l] = level;
+    atomicAdd(front_deg, (unsigned long long) (ptr[p + 1] - ptr[p]));
+  }
+}
+
+__device__ __forceinline__ void lb_record(uint64_t nb, uint32_t v, uint32_t w, uint32_t N, uint32_t level,
+                                          const uint32_t* __restrict__ lane_base, uint8_t* hops)
+{
+  while (nb)
+  {
+    const int b = __ffsll((long long) nb) - 1;
+    nb &= nb - 1;
+    const uint32_t l = w * 64 + b;
+    hops[(uint64_t) l * N + v] = (uint8_t) (level - lane_base[l] + 1);
+  }
+}
+
+// Bottom-up step over (vertex, word) pairs for the lanes in alive_cur.
+__global__ void k_lb_pull(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, uint32_t nrows,
+                          uint32_t N, uint32_t W, uint64_t* vis, const uint64_t* __restrict__ front, uint64_t* next,
+                          const uint64_t* __restrict__ alive_cur, uint64_t* alive_next, uint8_t* hops,
+                          const uint32_t* __restrict__ lane_base, uint32_t level, unsigned long long* front_deg)
+{
+  unsigned long long deg = 0;
+  const uint64_t NW = (uint64_t) nrows * W;
+  for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < NW; i += (uint64_t) gridDim.x * blockDim.x)
+  {
+    const uint32_t v = (uint32_t) (i / W), w = (uint32_t) (i % W);
+    const uint64_t seen = vis[i];
+    const uint64_t want = ~seen & alive_cur[w];
+    uint64_t nb = 0;
+    if (want)
+    {
+      uint64_t acc = 0;
+      for (uint32_t e = ptr[v]; e < ptr[v + 1]; e++)
+      {
+        acc |= front[(uint64_t) col[e] * W + w];
+        if ((acc & want) == want) break;
+      }
+      nb = acc & want;
+    }
+    next[i] = nb;
+    if (nb)
+    {
+      vis[i] = seen | nb;
+      deg += ptr[v + 1] - ptr[v];
+      atomicOr((unsigned long long*) &alive_next[w], (unsigned long long) nb);
+      lb_record(nb, v, w, N, level, lane_base, hops);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) deg += __shfl_xor_sync(0xffffffffu, deg, o);
+  if ((threadIdx.x & 31) == 0 && deg) atomicAdd(front_deg, deg);
+}
+
+__global__ void k_lb_clear(uint64_t n, uint64_t* buf)
+{
+  for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t) gridDim.x * blockDim.x)
+    buf[i] = 0;
+}
+
+__global__ void k_lb_list(uint64_t NW, const uint64_t* __restrict__ front, uint32_t* active, unsigned long long* n)
+{
+  for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < NW; i += (uint64_t) gridDim.x * blockDim.x)
+    if (front[i]) active[atomicAdd(n, 1ull)] = (uint32_t) i;
+}
+
+// Top-down step: one warp per listed frontier word, ORing it into the
+// neighbours' next words (masked by visited).
+__global__ void k_lb_push(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, uint32_t W,
+                          const uint64_t* __restrict__ front, const uint64_t* __restrict__ vis, uint64_t* next,
+                          const uint32_t* __restrict__ active, const unsigned long long* __restrict__ nactive)
+{
+  const uint32_t n = (uint32_t) *nactive;
+  const int lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t a = warp; a < n; a += nwarps)
+  {
+    const uint32_t i = active[a];
+    const uint32_t u = i / W, w = i % W;
+    const uint64_t f = front[i];
+    for (uint32_t e = ptr[u] + lane; e < ptr[u + 1]; e += 32)
+    {
+      const uint64_t j = (uint64_t) col[e] * W + w;
+      const uint64_t nb = f & ~vis[j];
+      if (nb && (next[j] & nb) != nb) atomicOr((unsigned long long*) &next[j], (unsigned long long) nb);
+    }
+  }
+}
+
+// After a push: new bits = next & ~visited; the old frontier words are
+// cleared so that the buffer can serve as the next "next".
+__global__ void k_lb_apply(const uint32_t* __restrict__ ptr, uint32_t nrows, uint32_t N, uint32_t W, uint64_t* vis,
+                           uint64_t* front, uint64_t* next, uint64_t* alive_next, uint8_t* hops,
+                           const uint32_t* __restrict__ lane_base, uint32_t level, unsigned long long* front_deg)
+{
+  unsigned long long deg = 0;
+  const uint64_t NW = (uint64_t) nrows * W;
+  for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < NW; i += (uint64_t) gridDim.x * blockDim.x)
+  {
+    front[i] = 0;
+    const uint64_t x = next[i];
+    if (!x) continue;
+    const uint64_t nb = x & ~vis[i];
+    next[i] = nb;
+    if (nb)
+    {
+      const uint32_t v = (uint32_t) (i / W), w = (uint32_t) (i % W);
+      vis[i] |= nb;
+      deg += ptr[v + 1] - ptr[v];
+      atomicOr((unsigned long long*) &alive_next[w], (unsigned long long) nb);
+      lb_record(nb, v, w, N, level, lane_base, hops);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) deg += __shfl_xor_sync(0xffffffffu, deg, o);
+  if ((threadIdx.x & 31) == 0 && deg) atomicAdd(front_deg, deg);
+}
+
+// Retiring lanes: hops by id into the staging rows, hops reset to 255.
+__global__ void k_lb_out(const uint32_t* __restrict__ lanes, uint32_t nl, uint32_t N,
+                         const uint32_t* __restrict__ id_of_pos, uint8_t* hops, uint8_t* staging)
+{
+  const uint64_t n = (uint64_t) nl * N;
+  for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t) gridDim.x * blockDim.x)
+  {
+    const uint32_t j = (uint32_t) (i / N), p = (uint32_t) (i % N);
+    uint8_t* h = &hops[(uint64_t) lanes[j] * N + p];
+    staging[(uint64_t) j * N + id_of_pos[p]] = *h;
+    *h = 255;
+  }
+}
+
+// Clears the retired lanes' bits (mask: W words) from the bitmaps.
+__global__ void k_lb_unset(uint64_t NW, uint32_t W, const uint64_t* __restrict__ mask, uint64_t* a, uint64_t* b)
+{
+  for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < NW; i += (uint64_t) gridDim.x * blockDim.x)
+  {
+    const uint64_t m = mask[i % W];
+    if (a[i] & m) a[i] &= ~m;
+    if (b && (b[i] & m)) b[i] &= ~m;
+  }
+}
+
+__global__ void k_lb_fill_u8(uint64_t n, uint8_t* p, uint8_t v)
+{
+  for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t) gridDim.x * blockDim.x)
+    p[i] = v;
+}
+
+// ------------------------------------------------------------------ SSSP lanes
+
+__global__ void k_ls_fill_u32(uint64_t n, uint32_t* p, uint32_t v)
+{
+  for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t) gridDim.x * blockDim.x)
+    p[i] = v;
+}
+
+__global__ void k_ls_admit(const uint32_t* __restrict__ adm, uint32_t n, uint32_t L, uint32_t W,
+                           const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ reg_end, uint32_t nreg,
+                           uint32_t src_base, uint32_t iso_base, uint32_t* dist, uint32_t* msg, uint64_t* front,
+                           uint32_t* rpos, PairList list)
+{
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+  {
+    const uint32_t l = adm[2 * j], p = adm[2 * j + 1];
+    dist[(uint64_t) p * L + l] = 0;
+    msg[(uint64_t) p * L + l] = 0;
+    rpos[l] = p;
+    if (p < nreg || (p >= src_base && p < iso_base))
+    {
+      const uint64_t i = (uint64_t) p * W + l / 64;
+      const unsigned long long old = atomicOr((unsigned long long*) &front[i], 1ull << (l % 64));
+      if (!old) bs_list_pair((uint32_t) i, reg_end[p] - ptr[p], list);
+    }
+  }
+}
+
+// Sink rows of the retiring lanes, once, from their final regular
+// distances (vertex_program_execute.hpp:131-148), then distances by id into
+// the staging rows and the lanes' columns reset to INF.
+__global__ void k_ls_sinks(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col,
+                           const uint32_t* __restrict__ wgt, uint32_t nreg, uint32_t nsink, uint32_t L,
+                           const uint32_t* __restrict__ lanes, uint32_t nl, const uint32_t* __restrict__ rpos,
+                           uint32_t src_base, uint32_t iso_base, uint32_t* dist)
+{
+  const uint64_t n = (uint64_t) nsink * nl;
+  for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t) gridDim.x * blockDim.x)
+  {
+    const uint32_t v = nreg + (uint32_t) (i / nl), l = lanes[i % nl];
+    const uint32_t rp = rpos[l];
+    uint32_t y = kInfD;
+    for (uint32_t e = ptr[v]; e < ptr[v + 1]; e++)
+    {
+      const uint32_t c = col[e];
+      uint32_t cand;
+      if (c < nreg) cand = dist[(uint64_t) c * L + l] + wgt[e];
+      else if (c == rp && rp >= src_base && rp < iso_base) cand = wgt[e];
+      else continue;
+      y = min(y, cand);
+    }
+    uint32_t* d = &dist[(uint64_t) v * L + l];
+    *d = min(*d, y);
+  }
+}
+
+__global__ void k_ls_out(const uint32_t* __restrict__ lanes, uint32_t nl, uint32_t N, uint32_t L,
+                         const uint32_t* __restrict__ id_of_pos, uint32_t* dist, uint32_t* staging)
+{
+  const uint64_t n = (uint64_t) nl * N;
+  for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t) gridDim.x * blockDim.x)
+  {
+    const uint32_t j = (uint32_t) (i % nl), p = (uint32_t) (i / nl);
+    uint32_t* d = &dist[(uint64_t) p * L + lanes[j]];
+    staging[(uint64_t) j * N + id_of_pos[p]] = *d;
+    *d = kInfD;
+  }
+}
+
+}  // namespace
+}  // namespace la3g
+
+using namespace la3g;
+
+// ------------------------------------------------------------------ engines
+
+struct la3g_server;
+
+namespace {
+
+enum EngineKind
+{
+  kEngBfs = 1,
+  kEngSssp = 2,
+  kEngBm25 = 3
+};
+
+struct Engine
+{
+  la3g_server* S = nullptr;
+  la3g_graph* G = nullptr;
+  int kind = 0;
+  uint32_t id = 0;
+  std::deque<Ticket*> queue;  // guarded by the server mutex
+  std::condition_variable cv;
+  std::thread th;
+  bool stop = false;
+  uint64_t bytes = 0;         // engine state bytes (the graph's own are counted apart)
+  int error = LA3G_OK;        // sticky CUDA error of the worker
+  std::string error_msg;
+  // lanes
+  uint32_t L = 0, W = 0, N = 0;
+  std::vector<Ticket*> lane;
+  std::vector<uint32_t> base_h;     // BFS: level at which the lane was admitted
+  std::vector<uint32_t> pos_of_id;  // host copy
+  bool exact_lanes = true;          // SSSP: max weight * N < INF
+  DevBuf vis, buf[2], hops, lane_base, alive[2], active, ctr, adm, ret, mask, staging;
+  // SSSP
+  DevBuf dist, msg, sfront[2], small[2], hub[2], hub_t0[2], reg_end, rpos;
+  unsigned long long* hctr = nullptr;  // pinned: counters + alive words
+};
+
+}  // namespace
+
+struct la3g_server
+{
+  uint64_t budget = 0, used = 0;
+  uint32_t bfs_lanes = 128, sssp_lanes = 64;
+  std::mutex mu;
+  std::condition_variable done_cv;
+  std::unordered_map<uint64_t, Ticket*> tickets;
+  uint64_t next_ticket = 1;
+  std::vector<Engine*> engines;
+  std::atomic<uint64_t> completed{0};
+};
+
+namespace {
+
+uint64_t bfs_lane_bytes(uint32_t N, uint32_t L)
+{
+  const uint64_t W = L / 64;
+  return (uint64_t) N * W * 8 * 3 + (uint64_t) N * L + (uint64_t) N * W * 4 + (uint64_t) kOutChunk * N + 4096 + L * 16;
+}
+
+uint64_t sssp_lane_bytes(uint32_t N, uint32_t L)
+{
+  const uint64_t W = L / 64;
+  return (uint64_t) N * L * 4 * 2 + (uint64_t) N * W * 8 * 2 + (uint64_t) N * W * 4 * 6 + (uint64_t) N * 4 +
+         (uint64_t) kOutChunk * N * 4 + 4096 + L * 16;
+}
+
+void finish_ticket(la3g_server* S, Ticket* t, int status)
+{
+  std::lock_guard<std::mutex> lk(S->mu);
+  t->status = status;
+  t->done_ms = wall_ms();
+  S->completed++;
+  S->done_cv.notify_all();
+}
+
+void engine_fail(Engine* E, int st)
+{
+  // a CUDA error leaves the engine unusable: fail everything it holds
+  E->error = st;
+  E->error_msg = la3g_last_error_string();
+  std::vector<Ticket*> all;
+  {
+    std::lock_guard<std::mutex> lk(E->S->mu);
+    for (Ticket* t : E->queue) all.push_back(t);
+    E->queue.clear();
+  }
+  for (Ticket*& t : E->lane)
+    if (t)
+    {
+      all.push_back(t);
+      t = nullptr;
+    }
+  for (Ticket* t : all) finish_ticket(E->S, t, st);
+}
+
+// Pops up to `free_lanes` queued tickets (waits while there is no work).
+// Returns false when the engine stops.
+bool take_work(Engine* E, uint32_t busy, uint32_t free_lanes, std::vector<Ticket*>& got)
+{
+  std::unique_lock<std::mutex> lk(E->S->mu);
+  while (!E->stop && busy == 0 && E->queue.empty()) E->cv.wait(lk);
+  if (E->stop) return false;
+  while (free_lanes && !E->queue.empty())
+  {
+    got.push_back(E->queue.front());
+    E->queue.pop_front();
+    free_lanes--;
+  }
+  return true;
+}
+
+int bfs_engine_init(Engine* E)
+{
+  DevGraph& g = E->G->g;
+  cudaStream_t s = E->G->stream;
+  const uint32_t N = E->N, W = E->W, L = E->L;
+  const uint64_t NW = (uint64_t) N * W;
+  LA3G_TRY(E->vis.alloc(NW * 8));
+  LA3G_TRY(E->buf[0].alloc(NW * 8));
+  LA3G_TRY(E->buf[1].alloc(NW * 8));
+  LA3G_TRY(E->hops.alloc((uint64_t) L * N));
+  LA3G_TRY(E->lane_base.alloc((uint64_t) L * 4));
+  LA3G_TRY(E->alive[0].alloc(W * 8));
+  LA3G_TRY(E->alive[1].alloc(W * 8));
+  LA3G_TRY(E->active.alloc(NW * 4));
+  LA3G_TRY(E->ctr.alloc(8 * 8));
+  LA3G_TRY(E->adm.alloc((uint64_t) L * 8));
+  LA3G_TRY(E->ret.alloc((uint64_t) L * 4));
+  LA3G_TRY(E->mask.alloc(W * 8));
+  LA3G_TRY(E->staging.alloc((uint64_t) kOutChunk * N));
+  LA3G_CUDA(cudaMemsetAsync(E->vis.p, 0, NW * 8, s));
+  LA3G_CUDA(cudaMemsetAsync(E->buf[0].p, 0, NW * 8, s));
+  LA3G_CUDA(cudaMemsetAsync(E->buf[1].p, 0, NW * 8, s));
+  LA3G_CUDA(cudaMemsetAsync(E->alive[0].p, 0, W * 8, s));
+  LA3G_CUDA(cudaMemsetAsync(E->alive[1].p, 0, W * 8, s));
+  k_lb_fill_u8<<<kSMs * 8, 256, 0, s>>>((uint64_t) L * N, E->hops.as<uint8_t>(), 255);
+  LA3G_LAUNCHED();
+  (void) g;
+  return LA3G_OK;
+}
+
+int sssp_engine_init(Engine* E)
+{
+  DevGraph& g = E->G->g;
+  cudaStream_t s = E->G->stream;
+  const uint32_t N = E->N, W = E->W, L = E->L;
+  const uint64_t NW = (uint64_t) N * W;
+  LA3G_TRY(E->dist.alloc((uint64_t) N * L * 4));
+  LA3G_TRY(E->msg.alloc((uint64_t) N * L * 4));
+  for (int c = 0; c < 2; c++)
+  {
+    LA3G_TRY(E->sfront[c].alloc(NW * 8));
+    LA3G_TRY(E->small[c].alloc(NW * 4));
+    LA3G_TRY(E->hub[c].alloc(NW * 4));
+    LA3G_TRY(E->hub_t0[c].alloc(NW * 4));
+    LA3G_CUDA(cudaMemsetAsync(E->sfront[c].p, 0, NW * 8, s));
+  }
+  LA3G_TRY(E->reg_end.alloc((uint64_t) N * 4));
+  LA3G_TRY(E->rpos.alloc((uint64_t) L * 4));
+  LA3G_TRY(E->alive[0].alloc(W * 8));
+  LA3G_TRY(E->ctr.alloc(8 * 8));
+  LA3G_TRY(E->adm.alloc((uint64_t) L * 8));
+  LA3G_TRY(E->ret.alloc((uint64_t) L * 4));
+  LA3G_TRY(E->staging.alloc((uint64_t) kOutChunk * N * 4));
+  LA3G_CUDA(cudaMemsetAsync(E->ctr.p, 0, 64, s));
+  k_ls_fill_u32<<<kSMs * 8, 256, 0, s>>>((uint64_t) N * L, E->dist.as<uint32_t>(), kInfD);
+  LA3G_LAUNCHED();
+  k_reg_end<<<grid_for(N, 256), 256, 0, s>>>(g.out_ptr, g.out_row, N, g.nreg, E->reg_end.as<uint32_t>());
+  LA3G_LAUNCHED();
+  // lanes are exact regardless of relaxation order only if no distance can
+  // reach INF; otherwise every query runs the single-root path
+  DevBuf m;
+  LA3G_TRY(m.alloc(4));
+  LA3G_CUDA(cudaMemsetAsync(m.p, 0, 4, s));
+  if (g.nent)
+  {
+    k_max_u32<<<grid_for(g.nent, 256), 256, 0, s>>>(g.out_w, g.nent, m.as<unsigned int>());
+    LA3G_LAUNCHED();
+  }
+  unsigned int maxw = 0;
+  LA3G_CUDA(cudaMemcpyAsync(&maxw, m.p, 4, cudaMemcpyDeviceToHost, s));
+  LA3G_CUDA(cudaStreamSynchronize(s));
+  E->exact_lanes = (uint64_t) maxw * (uint64_t) N < (uint64_t) kInfD;
+  return LA3G_OK;
+}
+
+// Copies each retiring lane's result into its ticket's output (when
+// `deliver`) and frees the lane: its bits leave the visited bitmap and, for
+// lanes leaving early, the current frontier and alive mask as well.
+int bfs_retire(Engine* E, const std::vector<uint32_t>& lanes, bool deliver, uint64_t* front, uint64_t* alive)
+{
+  DevGraph& g = E->G->g;
+  cudaStream_t s = E->G->stream;
+  const uint32_t N = E->N, W = E->W;
+  for (size_t j0 = 0; j0 < lanes.size(); j0 += kOutChunk)
+  {
+    const uint32_t nl = (uint32_t) std::min<size_t>(kOutChunk, lanes.size() - j0);
+    LA3G_CUDA(cudaMemcpyAsync(E->ret.p, lanes.data() + j0, nl * 4, cudaMemcpyHostToDevice, s));
+    k_lb_out<<<kSMs * 8, 256, 0, s>>>(E->ret.as<uint32_t>(), nl, N, g.id_of_pos, E->hops.as<uint8_t>(),
+                                      E->staging.as<uint8_t>());
+    LA3G_LAUNCHED();
+    tls_launches++;
+    for (uint32_t j = 0; deliver && j < nl; j++)
+    {
+      Ticket* t = E->lane[lanes[j0 + j]];
+      if (t->q.out)
+        LA3G_CUDA(cudaMemcpyAsync(t->q.out, E->staging.as<uint8_t>() + (size_t) j * N, N, cudaMemcpyDeviceToHost, s));
+    }
+    LA3G_CUDA(cudaStreamSynchronize(s));
+  }
+  std::vector<uint64_t> m(W, 0);
+  for (uint32_t l : lanes) m[l / 64] |= 1ull << (l % 64);
+  LA3G_CUDA(cudaMemcpyAsync(E->mask.p, m.data(), W * 8, cudaMemcpyHostToDevice, s));
+  k_lb_unset<<<kSMs * 8, 256, 0, s>>>((uint64_t) N * W, W, E->mask.as<uint64_t>(), E->vis.as<uint64_t>(), front);
+  LA3G_LAUNCHED();
+  tls_launches++;
+  if (alive)
+  {
+    k_lb_unset<<<1, 64, 0, s>>>(W, W, E->mask.as<uint64_t>(), alive, nullptr);
+    LA3G_LAUNCHED();
+  }
+  LA3G_CUDA(cudaStreamSynchronize(s));
+  return LA3G_OK;
+}
+
+// Runs one query alone through the single-root entry point (used for BFS
+// lanes that would pass 254 levels and for SSSP graphs whose weights could
+// reach INF).
+int run_single(Engine* E, Ticket* t)
+{
+  if (E->kind == kEngBfs) return la3g_bfs(E->G, t->q.root, (uint8_t*) t->q.out, nullptr, nullptr);
+  return la3g_sssp(E->G, t->q.root, (uint32_t*) t->q.out, nullptr);
+}
+
+// Admits queued tickets into free lanes; tickets that need no lane (root
+// out of range) or must run alone are completed here.  Returns the
+// (lane, position) pairs to initialise on the device.
+int admit(Engine* E, std::vector<Ticket*>& got, uint32_t& busy, std::vector<uint32_t>& adm, uint32_t level)
+{
+  adm.clear();
+  const double now = wall_ms();
+  for (Ticket* t : got)
+  {
+    t->start_ms = now;
+    const uint32_t root = t->q.root;
+    if (root >= E->N)
+    {
+      // no such vertex: nothing is reached (la3g_bfs / la3g_sssp give the same)
+      if (t->q.out)
+      {
+        if (E->kind == kEngBfs) std::memset(t->q.out, 255, E->N);
+        else
+          for (uint32_t i = 0; i < E->N; i++) ((uint32_t*) t->q.out)[i] = kInfD;
+      }
+      finish_ticket(E->S, t, LA3G_OK);
+      continue;
+    }
+    if (E->kind == kEngSssp && !E->exact_lanes)
+    {
+      finish_ticket(E->S, t, run_single(E, t));
+      continue;
+    }
+    uint32_t l = 0;
+    while (E->lane[l]) l++;
+    E->lane[l] = t;
+    E->base_h[l] = level;
+    busy++;
+    t->in_flight = busy;
+    adm.push_back(l);
+    adm.push_back(E->pos_of_id[root]);
+  }
+  return LA3G_OK;
+}
+
+int bfs_loop(Engine* E)
+{
+  DevGraph& g = E->G->g;
+  cudaStream_t s = E->G->stream;
+  const uint32_t N = E->N, W = E->W, L = E->L, nrows = g.nrows();
+  const uint64_t NW = (uint64_t) nrows * W;
+  unsigned long long* ctr = E->ctr.as<unsigned long long>();
+  uint32_t level = 0, busy = 0;
+  int cur = 0;
+  std::vector<Ticket*> got;
+  std::vector<uint32_t> adm, fin;
+  LA3G_CUDA(cudaMemsetAsync(ctr, 0, 64, s));
+  for (;;)
+  {
+    got.clear();
+    if (!take_work(E, busy, L - busy, got)) return LA3G_OK;
+    LA3G_TRY(admit(E, got, busy, adm, level));
+    if (!adm.empty())
+    {
+      const uint32_t n = (uint32_t) adm.size() / 2;
+      LA3G_CUDA(cudaMemcpyAsync(E->adm.p, adm.data(), adm.size() * 4, cudaMemcpyHostToDevice, s));
+      k_lb_admit<<<grid_for(n, 128), 128, 0, s>>>(E->adm.as<uint32_t>(), n, N, W, g.in_ptr, level,
+                                                 E->vis.as<uint64_t>(), E->buf[cur].as<uint64_t>(),
+                                                 E->hops.as<uint8_t>(), E->lane_base.as<uint32_t>(),
+                                                 E->alive[cur].as<uint64_t>(), ctr + 1);
+      LA3G_LAUNCHED();
+      tls_launches++;
+    }
+    if (busy == 0) continue;
+    uint64_t* front = E->buf[cur].as<uint64_t>();
+    uint64_t* next = E->buf[cur ^ 1].as<uint64_t>();
+    // lanes that would need hop 255 leave for the single-root path, which
+    // follows the reference's uint8 wrap exactly
+    fin.clear();
+    for (uint32_t l = 0; l < L; l++)
+      if (E->lane[l] && level - E->base_h[l] + 1 >= 255) fin.push_back(l);
+    if (!fin.empty())
+    {
+      LA3G_TRY(bfs_retire(E, fin, false, front, E->alive[cur].as<uint64_t>()));
+      for (uint32_t l : fin)
+      {
+        Ticket* t = E->lane[l];
+        E->lane[l] = nullptr;
+        busy--;
+        finish_ticket(E->S, t, run_single(E, t));
+      }
+      if (busy == 0) continue;
+    }
+    // one level for every occupied lane: push while the frontier's edges
+    // are few, pull otherwise
+    unsigned long long front_deg = 0;
+    LA3G_CUDA(cudaMemcpyAsync(&front_deg, ctr + 1, 8, cudaMemcpyDeviceToHost, s));
+    LA3G_CUDA(cudaStreamSynchronize(s));
+    LA3G_CUDA(cudaMemsetAsync(ctr, 0, 3 * 8, s));
+    LA3G_CUDA(cudaMemsetAsync(E->alive[cur ^ 1].p, 0, W * 8, s));
+    const bool push = (double) front_deg * 20.0 < (double) g.nent;
+    if (!push)
+    {
+      k_lb_pull<<<kSMs * 8, 256, 0, s>>>(g.in_ptr, g.in_col, nrows, N, W, E->vis.as<uint64_t>(), front, next,
+                                         E->alive[cur].as<uint64_t>(), E->alive[cur ^ 1].as<uint64_t>(),
+                                         E->hops.as<uint8_t>(), E->lane_base.as<uint32_t>(), level, ctr + 1);
+      LA3G_LAUNCHED();
+      k_lb_clear<<<kSMs * 8, 256, 0, s>>>(NW, front);
+      LA3G_LAUNCHED();
+      tls_launches += 2;
+    }
+    else
+    {
+      k_lb_list<<<kSMs * 8, 256, 0, s>>>(NW, front, E->active.as<uint32_t>(), ctr + 2);
+      LA3G_LAUNCHED();
+      k_lb_push<<<kSMs * 8, 256, 0, s>>>(g.in_ptr, g.in_col, W, front, E->vis.as<uint64_t>(), next,
+                                         E->active.as<uint32_t>(), ctr + 2);
+      LA3G_LAUNCHED();
+      k_lb_apply<<<kSMs * 8, 256, 0, s>>>(g.in_ptr, nrows, N, W, E->vis.as<uint64_t>(), front, next,
+                                          E->alive[cur ^ 1].as<uint64_t>(), E->hops.as<uint8_t>(),
+                                          E->lane_base.as<uint32_t>(), level, ctr + 1);
+      LA3G_LAUNCHED();
+      tls_launches += 3;
+    }
+    LA3G_CUDA(cudaMemcpyAsync(E->hctr, E->alive[cur ^ 1].p, W * 8, cudaMemcpyDeviceToHost, s));
+    LA3G_CUDA(cudaStreamSynchronize(s));
+    cur ^= 1;
+    level++;
+    // a lane that found no new vertex is finished
+    fin.clear();
+    for (uint32_t l = 0; l < L; l++)
+      if (E->lane[l] && !((E->hctr[l / 64] >> (l % 64)) & 1ull)) fin.push_back(l);
+    if (!fin.empty())
+    {
+      LA3G_TRY(bfs_retire(E, fin, true, nullptr, nullptr));
+      for (uint32_t l : fin)
+      {
+        Ticket* t = E->lane[l];
+        E->lane[l] = nullptr;
+        busy--;
+        finish_ticket(E->S, t, LA3G_OK);
+      }
+    }
+  }
+}
+
+int sssp_retire(Engine* E, const std::vector<uint32_t>& lanes)
+{
+  DevGraph& g = E->G->g;
+  cudaStream_t s = E->G->stream;
+  const uint32_t N = E->N, L = E->L;
+  for (size_t j0 = 0; j0 < lanes.size(); j0 += kOutChunk)
+  {
+    const uint32_t nl = (uint32_t) std::min<size_t>(kOutChunk, lanes.size() - j0);
+    LA3G_CUDA(cudaMemcpyAsync(E->ret.p, lanes.data() + j0, nl * 4, cudaMemcpyHostToDevice, s));
+    if (g.nsink)
+    {
+      k_ls_sinks<<<kSMs * 8, 256, 0, s>>>(g.in_ptr, g.in_col, g.in_w, g.nreg, g.nsink, L, E->ret.as<uint32_t>(), nl,
+                                          E->rpos.as<uint32_t>(), g.src_base(), g.iso_base(), E->dist.as<uint32_t>());
+      LA3G_LAUNCHED();
+      tls_launches++;
+    }
+    k_ls_out<<<kSMs * 8, 256, 0, s>>>(E->ret.as<uint32_t>(), nl, N, L, g.id_of_pos, E->dist.as<uint32_t>(),
+                                      E->staging.as<uint32_t>());
+    LA3G_LAUNCHED();
+    tls_launches++;
+    for (uint32_t j = 0; j < nl; j++)
+    {
+      Ticket* t = E->lane[lanes[j0 + j]];
+      if (t->q.out)
+        LA3G_CUDA(cudaMemcpyAsync(t->q.out, E->staging.as<uint32_t>() + (size_t) j * N, (size_t) N * 4,
+                                  cudaMemcpyDeviceToHost, s));
+    }
+    LA3G_CUDA(cudaStreamSynchronize(s));
+  }
+  return LA3G_OK;
+}
+
+int sssp_loop(Engine* E)
+{
+  DevGraph& g = E->G->g;
+  cudaStream_t s = E->G->stream;
+  const uint32_t N = E->N, W = E->W, L = E->L;
+  unsigned long long* ctr = E->ctr.as<unsigned long long>();
+  PairList PL[2];
+  for (int c = 0; c < 2; c++)
+    PL[c] = PairList{E->small[c].as<uint32_t>(), E->hub[c].as<uint32_t>(), E->hub_t0[c].as<uint32_t>(), ctr + c,
+                     ctr + 2 + c};
+  uint32_t busy = 0;
+  int cur = 0;
+  std::vector<Ticket*> got;
+  std::vector<uint32_t> adm, fin;
+  for (;;)
+  {
+    got.clear();
+    if (!take_work(E, busy, L - busy, got)) return LA3G_OK;
+    LA3G_TRY(admit(E, got, busy, adm, 0));
+    if (!adm.empty())
+    {
+      const uint32_t n = (uint32_t) adm.size() / 2;
+      LA3G_CUDA(cudaMemcpyAsync(E->adm.p, adm.data(), adm.size() * 4, cudaMemcpyHostToDevice, s));
+      k_ls_admit<<<grid_for(n, 128), 128, 0, s>>>(E->adm.as<uint32_t>(), n, L, W, g.out_ptr,
+                                                 E->reg_end.as<uint32_t>(), g.nreg, g.src_base(), g.iso_base(),
+                                                 E->dist.as<uint32_t>(), E->msg.as<uint32_t>(),
+                                                 E->sfront[cur].as<uint64_t>(), E->rpos.as<uint32_t>(), PL[cur]);
+      LA3G_LAUNCHED();
+      tls_launches++;
+    }
+    if (busy == 0) continue;
+    // one relaxation step for every occupied lane
+    LA3G_CUDA(cudaMemsetAsync(E->alive[0].p, 0, W * 8, s));
+    {
+      ProfileScope p("serve_sssp_relax", s, 0.0);
+      k_bs_relax<<<kSMs * 16, 256, 0, s>>>(g.out_ptr, E->reg_end.as<uint32_t>(), g.out_row, g.out_w, L, W,
+                                           E->sfront[cur].as<uint64_t>(), PL[cur], E->sfront[cur ^ 1].as<uint64_t>(),
+                                           E->msg.as<uint32_t>(), E->dist.as<uint32_t>());
+      LA3G_LAUNCHED();
+    }
+    LA3G_CUDA(cudaMemsetAsync(ctr + (cur ^ 1), 0, 8, s));
+    LA3G_CUDA(cudaMemsetAsync(ctr + 2 + (cur ^ 1), 0, 8, s));
+    k_bs_apply<<<kSMs * 8, 256, 0, s>>>(N, L, W, g.out_ptr, E->reg_end.as<uint32_t>(), E->sfront[cur ^ 1].as<uint64_t>(),
+                                        E->dist.as<uint32_t>(), E->msg.as<uint32_t>(), PL[cur ^ 1],
+                                        E->sfront[cur].as<uint64_t>(), PL[cur], E->alive[0].as<uint64_t>());
+    LA3G_LAUNCHED();
+    tls_launches += 2;
+    LA3G_CUDA(cudaMemcpyAsync(E->hctr, E->alive[0].p, W * 8, cudaMemcpyDeviceToHost, s));
+    LA3G_CUDA(cudaStreamSynchronize(s));
+    cur ^= 1;
+    fin.clear();
+    for (uint32_t l = 0; l < L; l++)
+      if (E->lane[l] && !((E->hctr[l / 64] >> (l % 64)) & 1ull)) fin.push_back(l);
+    if (!fin.empty())
+    {
+      LA3G_TRY(sssp_retire(E, fin));
+      for (uint32_t l : fin)
+      {
+        Ticket* t = E->lane[l];
+        E->lane[l] = nullptr;
+        busy--;
+        finish_ticket(E->S, t, LA3G_OK);
+      }
+    }
+  }
+}
+
+int bm25_loop(Engine* E)
+{
+  std::vector<Ticket*> got;
+  for (;;)
+  {
+    got.clear();
+    if (!take_work(E, 0, 1, got)) return LA3G_OK;
+    for (Ticket* t : got)
+    {
+      t->start_ms = wall_ms();
+      t->in_flight = 1;
+      uint32_t nout = 0;
+      const int st = la3g_bm25_query(E->G, t->terms.data(), (uint32_t) t->terms.size(), t->q.k, (uint32_t*) t->q.out,
+                                     t->q.scores_out, &nout, nullptr, nullptr, nullptr);
+      t->nout = nout;
+      finish_ticket(E->S, t, st);
+    }
+  }
+}
+
+void worker(Engine* E)
+{
+  int st = LA3G_OK;
+  if (E->kind == kEngBfs) st = bfs_loop(E);
+  else if (E->kind == kEngSssp) st = sssp_loop(E);
+  else st = bm25_loop(E);
+  if (st != LA3G_OK) engine_fail(E, st);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ ABI
+
+extern "C" int la3g_server_create(uint64_t budget_bytes, uint32_t bfs_lanes, uint32_t sssp_lanes, la3g_server** out)
+{
+  if (!out) return set_error(LA3G_EINVAL, "out is null");
+  *out = nullptr;
+  if (bfs_lanes == 0) bfs_lanes = 128;
+  if (sssp_lanes == 0) sssp_lanes = 64;
+  if (bfs_lanes % 64 || sssp_lanes % 64 || bfs_lanes > 4096 || sssp_lanes > 4096)
+    return set_error(LA3G_EINVAL, "lane counts must be multiples of 64, at most 4096");
+  la3g_server* S = new (std::nothrow) la3g_server();
+  if (!S) return set_error(LA3G_ENOMEM, "out of host memory");
+  S->budget = budget_bytes;
+  S->bfs_lanes = bfs_lanes;
+  S->sssp_lanes = sssp_lanes;
+  *out = S;
+  return LA3G_OK;
+}
+
+extern "C" int la3g_server_add_graph(la3g_server* S, la3g_graph* G, uint32_t* graph_id)
+{
+  if (!S || !G) return set_error(LA3G_EINVAL, "null server or graph");
+  DevGraph& g = G->g;
+  int kind = 0;
+  if (g.flags & LA3G_BIPARTITE) kind = kEngBm25;
+  else if (!g.directed()) kind = kEngBfs;
+  else if (g.weighted() && !(g.flags & (LA3G_REVERSE | LA3G_ACYCLIC))) kind = kEngSssp;
+  else return set_error(LA3G_EINVAL, "serve graphs loaded undirected (BFS), DIRECTED|WEIGHTED (SSSP) or BIPARTITE (BM25)");
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    for (Engine* e : S->engines)
+      if (e->G == G) return set_error(LA3G_EINVAL, "graph already served");
+  }
+  if (kind == kEngSssp) LA3G_TRY(build_push_csr(G));
+  if (kind == kEngBm25 && !G->slot[kSlotBm25]) LA3G_TRY(la3g_bm25_prepare(G, nullptr, nullptr, nullptr));
+  const uint32_t N = g.nslots;
+  uint32_t L = kind == kEngBfs ? S->bfs_lanes : (kind == kEngSssp ? S->sssp_lanes : 0);
+  auto need = [&](uint32_t lanes) -> uint64_t {
+    if (kind == kEngBfs) return bfs_lane_bytes(N, lanes);
+    if (kind == kEngSssp) return sssp_lane_bytes(N, lanes);
+    return 0;
+  };
+  uint64_t eng_bytes = 0;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    const uint64_t left = S->budget > S->used ? S->budget - S->used : 0;
+    while (L > 64 && G->device_bytes + need(L) > left) L /= 2;
+    eng_bytes = need(L);
+    if (G->device_bytes + eng_bytes > left)
+      return set_error(LA3G_EBUDGET, "graph and its lane state exceed the server's HBM budget");
+    S->used += G->device_bytes + eng_bytes;  // reserved before allocation
+  }
+  Engine* E = new (std::nothrow) Engine();
+  if (!E)
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->used -= G->device_bytes + eng_bytes;
+    return set_error(LA3G_ENOMEM, "out of host memory");
+  }
+  E->S = S;
+  E->G = G;
+  E->kind = kind;
+  E->N = N;
+  E->L = L;
+  E->W = L / 64;
+  E->bytes = eng_bytes;
+  E->lane.assign(L, nullptr);
+  E->base_h.assign(L, 0);
+  int st = LA3G_OK;
+  if (kind != kEngBm25)
+  {
+    E->pos_of_id.resize(N);
+    st = la3g_graph_positions(G, E->pos_of_id.data(), nullptr);
+    if (st == LA3G_OK && cudaHostAlloc(&E->hctr, 64 * 8 + E->W * 8, cudaHostAllocDefault) != cudaSuccess)
+      st = set_error(LA3G_ECUDA, "pinned counter allocation failed");
+    if (st == LA3G_OK) st = kind == kEngBfs ? bfs_engine_init(E) : sssp_engine_init(E);
+    if (st == LA3G_OK && cudaStreamSynchronize(G->stream) != cudaSuccess)
+      st = set_error(LA3G_ECUDA, "engine initialisation failed");
+  }
+  if (st != LA3G_OK)
+  {
+    if (E->hctr) cudaFreeHost(E->hctr);
+    delete E;
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->used -= G->device_bytes + eng_bytes;
+    return st;
+  }
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    E->id = (uint32_t) S->engines.size();
+    S->engines.push_back(E);
+  }
+  E->th = std::thread(worker, E);
+  if (graph_id) *graph_id = E->id;
+  return LA3G_OK;
+}
+
+extern "C" int la3g_server_submit(la3g_server* S, const la3g_query* q, uint64_t* ticket)
+{
+  if (!S || !q || !ticket) return set_error(LA3G_EINVAL, "null argument");
+  Ticket* t = new (std::nothrow) Ticket();
+  if (!t) return set_error(LA3G_ENOMEM, "out of host memory");
+  t->q = *q;
+  t->submit_ms = wall_ms();
+  std::lock_guard<std::mutex> lk(S->mu);
+  if (q->graph >= S->engines.size())
+  {
+    delete t;
+    return set_error(LA3G_EINVAL, "no such graph id");
+  }
+  Engine* E = S->engines[q->graph];
+  const int want = q->kind == LA3G_QUERY_BFS ? kEngBfs : q->kind == LA3G_QUERY_SSSP ? kEngSssp
+                                                    : q->kind == LA3G_QUERY_BM25 ? kEngBm25 : -1;
+  if (want != E->kind)
+  {
+    delete t;
+    return set_error(LA3G_EINVAL, "query kind does not match the graph");
+  }
+  if (E->error != LA3G_OK)
+  {
+    delete t;
+    return set_error(E->error, "the graph's engine failed: %s", E->error_msg.c_str());
+  }
+  if (want == kEngBm25)
+  {
+    if (!q->terms || q->nterms == 0 || q->k == 0)
+    {
+      delete t;
+      return set_error(LA3G_EINVAL, "bm25 queries need terms and k > 0");
+    }
+    t->terms.assign(q->terms, q->terms + q->nterms);
+    t->q.terms = nullptr;
+  }
+  const uint64_t id = S->next_ticket++;
+  S->tickets[id] = t;
+  E->queue.push_back(t);
+  E->cv.notify_one();
+  *ticket = id;
+  return LA3G_OK;
+}
+
+extern "C" int la3g_server_poll(la3g_server* S, uint64_t ticket, int timeout_ms, la3g_query_result* res)
+{
+  if (!S) return set_error(LA3G_EINVAL, "null server");
+  std::unique_lock<std::mutex> lk(S->mu);
+  auto it = S->tickets.find(ticket);
+  if (it == S->tickets.end()) return set_error(LA3G_EINVAL, "unknown ticket");
+  Ticket* t = it->second;
+  if (t->status < 0 && timeout_ms != 0)
+  {
+    auto pred = [&] { return t->status >= 0; };
+    if (timeout_ms < 0) S->done_cv.wait(lk, pred);
+    else S->done_cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), pred);
+  }
+  if (t->status < 0) return LA3G_EBUSY;
+  if (res)
+  {
+    res->status = t->status;
+    res->kind = t->q.kind;
+    res->queue_ms = t->start_ms - t->submit_ms;
+    res->latency_ms = t->done_ms - t->submit_ms;
+    res->in_flight = t->in_flight;
+    res->nout = t->nout;
+  }
+  S->tickets.erase(it);
+  delete t;
+  return LA3G_OK;
+}
+
+extern "C" int la3g_server_info(la3g_server* S, la3g_server_stats* out)
+{
+  if (!S || !out) return set_error(LA3G_EINVAL, "null argument");
+  std::lock_guard<std::mutex> lk(S->mu);
+  std::memset(out, 0, sizeof(*out));
+  out->budget_bytes = S->budget;
+  out->used_bytes = S->used;
+  out->ngraphs = (uint32_t) S->engines.size();
+  out->completed = S->completed.load();
+  uint64_t pend = 0;
+  for (Engine* e : S->engines) pend += e->queue.size();
+  out->queued = pend;
+  out->pending = S->tickets.size();
+  return LA3G_OK;
+}
+
+extern "C" int la3g_server_lanes(la3g_server* S, uint32_t graph_id, uint32_t* lanes)
+{
+  if (!S || !lanes) return set_error(LA3G_EINVAL, "null argument");
+  std::lock_guard<std::mutex> lk(S->mu);
+  if (graph_id >= S->engines.size()) return set_error(LA3G_EINVAL, "no such graph id");
+  *lanes = S->engines[graph_id]->L;
+  return LA3G_OK;
+}
+
+extern "C" void la3g_server_free(la3g_server* S)
+{
+  if (!S) return;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    for (Engine* e : S->engines)
+    {
+      e->stop = true;
+      e->cv.notify_all();
+    }
+  }
+  for (Engine* e : S->engines)
+    if (e->th.joinable()) e->th.join();
+  // every worker synchronises its stream before it waits for work, so once
+  // the threads are joined no engine work is in flight (the graphs are not
+  // touched here: they may already be gone)
+  for (Engine* e : S->engines)
+  {
+    if (e->hctr) cudaFreeHost(e->hctr);
+    delete e;
+  }
+  for (auto& kv : S->tickets) delete kv.second;
+  delete S;
+}

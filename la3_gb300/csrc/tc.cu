@@ -41,6 +41,7 @@ struct TcScratch
   unsigned int* next = nullptr;  // dynamic work counter
   unsigned long long* total = nullptr;
   double work = 0;               // sum over x of |N+(x)| + sum_y |N+(y)| (list elements read)
+  double work_mid = 0, work_big = 0;  // the part of it in the block-per-x and the global-search classes
 };
 
 static void tc_scratch_free(void* p) { delete (TcScratch*) p; }
@@ -102,6 +103,7 @@ __global__ void k_tc_work(const uint32_t* __restrict__ ptr, const uint32_t* __re
     if (e - b > kTcCap)
     {
       big[atomicAdd(&counts[1], 1ull)] = x;
+      atomicAdd(&counts[5], (unsigned long long) w);
     }
     else
     {
@@ -111,7 +113,11 @@ __global__ void k_tc_work(const uint32_t* __restrict__ ptr, const uint32_t* __re
       const uint32_t wq = (uint32_t) (w < 0x7FFFFFFFull ? w : 0x7FFFFFFFull);
       wkey[slot] = (cls << 31) | (0x7FFFFFFFu - wq);
       wid[slot] = x;
-      if (cls) atomicAdd(&counts[3], 1ull);
+      if (cls)
+      {
+        atomicAdd(&counts[3], 1ull);
+        atomicAdd(&counts[4], (unsigned long long) w);
+      }
     }
     atomicAdd(&counts[2], (unsigned long long) w);
   }
@@ -430,20 +436,22 @@ static int tc_prepare(la3g_graph* G, TcScratch* ts)
   LA3G_TRY(wkey.alloc((size_t) N * 4));
   LA3G_TRY(wid.alloc((size_t) N * 4));
   LA3G_TRY(wkey2.alloc((size_t) N * 4));
-  LA3G_TRY(cnt.alloc(4 * 8));
+  LA3G_TRY(cnt.alloc(8 * 8));
   LA3G_TRY(galloc(G, &ts->order, N));
   LA3G_TRY(galloc(G, &ts->big, N));
-  LA3G_CUDA(cudaMemsetAsync(cnt.p, 0, 32, s));
+  LA3G_CUDA(cudaMemsetAsync(cnt.p, 0, 64, s));
   k_tc_work<<<grid_for(N, 256), 256, 0, s>>>(ts->plus_ptr, ts->plus_col, N, wkey.as<uint32_t>(), wid.as<uint32_t>(),
                                              ts->big, cnt.as<unsigned long long>());
   LA3G_LAUNCHED();
-  unsigned long long hc[4];
-  LA3G_CUDA(cudaMemcpyAsync(hc, cnt.p, 32, cudaMemcpyDeviceToHost, s));
+  unsigned long long hc[8];
+  LA3G_CUDA(cudaMemcpyAsync(hc, cnt.p, 64, cudaMemcpyDeviceToHost, s));
   LA3G_CUDA(cudaStreamSynchronize(s));
   ts->nmid = (uint32_t) hc[3];
   ts->norder = (uint32_t) hc[0];  // small + mid, sorted: small first
   ts->nbig = (uint32_t) hc[1];
   ts->work = (double) hc[2];
+  ts->work_mid = (double) hc[4];
+  ts->work_big = (double) hc[5];
   if (ts->norder)
   {
     size_t tb = 0;
@@ -489,14 +497,15 @@ extern "C" int la3g_tc(la3g_graph* G, uint64_t* total_out, uint32_t* per_vertex_
   LA3G_CUDA(cudaMemsetAsync(ts->next, 0, 8, s));
   if (ts->nmid)
   {
-    ProfileScope p("tc_rank_mid", s, 0.0);
+    // list reads (N+(x) once, N+(y) per oriented edge) + the x's two offsets
+    ProfileScope p("tc_rank_mid", s, 4.0 * ts->work_mid + 8.0 * ts->nmid);
     k_tc_rank_block<kTcCap, 256><<<kSMs * 8, 256, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->order_mid, ts->nmid,
                                                           ts->next + 1, ts->ntri);
     LA3G_LAUNCHED();
   }
   if (ts->norder)
   {
-    ProfileScope p("tc_rank", s, 4.0 * ts->work + 8.0 * N);
+    ProfileScope p("tc_rank", s, 4.0 * (ts->work - ts->work_mid - ts->work_big) + 8.0 * ts->norder);
     k_tc_rank<kTcSmall, 8><<<kSMs * 8, 8 * 32, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->order, ts->norder, ts->next,
                                                        ts->ntri);
     LA3G_LAUNCHED();
