@@ -385,7 +385,16 @@ k_prf_pull(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, c
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
-  if (lane == 0 && local != 0.0) atomicAdd(resid, local);
+  // one FP64 atomic per block (per-warp atomics on one word serialise)
+  __shared__ double wsum[8];
+  if (lane == 0) wsum[threadIdx.x >> 5] = local;
+  __syncthreads();
+  if (threadIdx.x == 0)
+  {
+    double t = 0.0;
+    for (int w = 0; w < (int) (blockDim.x >> 5); w++) t += wsum[w];
+    if (t != 0.0) atomicAdd(resid, t);
+  }
 }
 
 }  // namespace la3g
