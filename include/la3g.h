@@ -250,7 +250,10 @@ typedef struct la3g_server_stats
 } la3g_server_stats;
 
 /* A server with an HBM budget (bytes).  bfs_lanes / sssp_lanes: queries one
- * BFS / SSSP engine holds at once (multiples of 64; 0 = 128 / 64). */
+ * BFS / SSSP engine holds at once (multiples of 64; 0 = 256 / 64).  A BFS
+ * engine admits queries 64 at a time into free 64-lane words (queries that
+ * are queued when a word frees up start together); an SSSP engine admits
+ * them into any free lane. */
 int la3g_server_create(uint64_t budget_bytes, uint32_t bfs_lanes, uint32_t sssp_lanes, la3g_server** out);
 /* Makes a loaded graph resident in the server: undirected graphs serve BFS,
  * DIRECTED|WEIGHTED graphs SSSP, BIPARTITE graphs BM25 (prepared here if

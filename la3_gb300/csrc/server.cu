@@ -12,6 +12,11 @@
 //    worker retires lanes whose frontier emptied (their results are copied
 //    out and the lane's state reset) and admits queued queries into free
 //    lanes.  Continuous batching: a query never waits for a batch to drain.
+//    SSSP queries take any free lane.  BFS queries are admitted a word (64
+//    lanes) at a time: the queries queued when a word frees up start
+//    together, so each word runs a level-synchronous multi-source BFS whose
+//    direction (push or pull) is chosen per word and per level, while the
+//    engine's words sit at different levels.
 //    Each lane's arithmetic is that of the single-root call, and lanes never
 //    read one another's bits, so a result does not depend on the mix.
 //  * BM25 engines run their queries one after another on their corpus.
@@ -55,9 +60,18 @@ struct Ticket
 
 // ------------------------------------------------------------------ BFS lanes
 
+// BFS engine words: the 64 lanes of a word are admitted together and share
+// the word's level, so every word runs a level-synchronous multi-source BFS
+// (direction chosen per word) while different words sit at different
+// levels.  Words are bit w of the `words` masks below (W <= 64).
+struct WordHops
+{
+  uint8_t h[64];  // hop value written at this level, per word
+};
+
 __global__ void k_lb_admit(const uint32_t* __restrict__ adm, uint32_t n, uint32_t N, uint32_t W,
-                           const uint32_t* __restrict__ ptr, uint32_t level, uint64_t* vis, uint64_t* front,
-                           uint8_t* hops, uint32_t* lane_base, uint64_t* alive, unsigned long long* front_deg)
+                           const uint32_t* __restrict__ ptr, uint64_t* vis, uint64_t* front, uint8_t* hops,
+                           uint64_t* alive, unsigned long long* fdeg)
 {
   for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
   {
@@ -68,34 +82,43 @@ __global__ void k_lb_admit(const uint32_t* __restrict__ adm, uint32_t n, uint32_
     atomicOr((unsigned long long*) &front[(uint64_t) p * W + w], bit);
     atomicOr((unsigned long long*) &alive[w], bit);
     hops[(uint64_t) l * N + p] = 0;
-    lane_base[l] = level;
-    atomicAdd(front_deg, (unsigned long long) (ptr[p + 1] - ptr[p]));
+    atomicAdd(&fdeg[w], (unsigned long long) (ptr[p + 1] - ptr[p]));
   }
 }
 
-__device__ __forceinline__ void lb_record(uint64_t nb, uint32_t v, uint32_t w, uint32_t N, uint32_t level,
-                                          const uint32_t* __restrict__ lane_base, uint8_t* hops)
+__device__ __forceinline__ void lb_record(uint64_t nb, uint32_t v, uint32_t w, uint32_t N, uint8_t hop, uint8_t* hops)
 {
   while (nb)
   {
     const int b = __ffsll((long long) nb) - 1;
     nb &= nb - 1;
-    const uint32_t l = w * 64 + b;
-    hops[(uint64_t) l * N + v] = (uint8_t) (level - lane_base[l] + 1);
+    hops[(uint64_t) (w * 64 + b) * N + v] = hop;
   }
 }
 
-// Bottom-up step over (vertex, word) pairs for the lanes in alive_cur.
-__global__ void k_lb_pull(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, uint32_t nrows,
-                          uint32_t N, uint32_t W, uint64_t* vis, const uint64_t* __restrict__ front, uint64_t* next,
-                          const uint64_t* __restrict__ alive_cur, uint64_t* alive_next, uint8_t* hops,
-                          const uint32_t* __restrict__ lane_base, uint32_t level, unsigned long long* front_deg)
+// Per-word frontier degree sums, gathered per block in shared memory.
+__device__ __forceinline__ void lb_deg_flush(unsigned long long* sdeg, uint32_t W, unsigned long long* fdeg)
 {
-  unsigned long long deg = 0;
+  __syncthreads();
+  for (uint32_t w = threadIdx.x; w < W; w += blockDim.x)
+    if (sdeg[w]) atomicAdd(&fdeg[w], sdeg[w]);
+}
+
+// Bottom-up step over (vertex, word) pairs of the pull words.
+__global__ void __launch_bounds__(256)
+k_lb_pull(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, uint32_t nrows, uint32_t N, uint32_t W,
+          uint64_t* vis, const uint64_t* __restrict__ front, uint64_t* next, const uint64_t* __restrict__ alive_cur,
+          uint64_t* alive_next, uint8_t* hops, WordHops hop, uint64_t words, unsigned long long* fdeg)
+{
+  __shared__ unsigned long long sdeg[64];
+  for (uint32_t w = threadIdx.x; w < W; w += blockDim.x) sdeg[w] = 0;
+  __syncthreads();
   const uint64_t NW = (uint64_t) nrows * W;
   for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < NW; i += (uint64_t) gridDim.x * blockDim.x)
   {
-    const uint32_t v = (uint32_t) (i / W), w = (uint32_t) (i % W);
+    const uint32_t w = (uint32_t) (i % W);
+    if (!((words >> w) & 1ull)) continue;
+    const uint32_t v = (uint32_t) (i / W);
     const uint64_t seen = vis[i];
     const uint64_t want = ~seen & alive_cur[w];
     uint64_t nb = 0;
@@ -113,25 +136,26 @@ __global__ void k_lb_pull(const uint32_t* __restrict__ ptr, const uint32_t* __re
     if (nb)
     {
       vis[i] = seen | nb;
-      deg += ptr[v + 1] - ptr[v];
+      atomicAdd(&sdeg[w], (unsigned long long) (ptr[v + 1] - ptr[v]));
       atomicOr((unsigned long long*) &alive_next[w], (unsigned long long) nb);
-      lb_record(nb, v, w, N, level, lane_base, hops);
+      lb_record(nb, v, w, N, hop.h[w], hops);
     }
   }
-  for (int o = 16; o > 0; o >>= 1) deg += __shfl_xor_sync(0xffffffffu, deg, o);
-  if ((threadIdx.x & 31) == 0 && deg) atomicAdd(front_deg, deg);
+  lb_deg_flush(sdeg, W, fdeg);
 }
 
-__global__ void k_lb_clear(uint64_t n, uint64_t* buf)
-{
-  for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t) gridDim.x * blockDim.x)
-    buf[i] = 0;
-}
-
-__global__ void k_lb_list(uint64_t NW, const uint64_t* __restrict__ front, uint32_t* active, unsigned long long* n)
+// Clears the frontier words of the given words (after a pull consumed them).
+__global__ void k_lb_clear(uint64_t NW, uint32_t W, uint64_t* buf, uint64_t words)
 {
   for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < NW; i += (uint64_t) gridDim.x * blockDim.x)
-    if (front[i]) active[atomicAdd(n, 1ull)] = (uint32_t) i;
+    if ((words >> (i % W)) & 1ull) buf[i] = 0;
+}
+
+__global__ void k_lb_list(uint64_t NW, uint32_t W, const uint64_t* __restrict__ front, uint64_t words, uint32_t* active,
+                          unsigned long long* n)
+{
+  for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < NW; i += (uint64_t) gridDim.x * blockDim.x)
+    if (((words >> (i % W)) & 1ull) && front[i]) active[atomicAdd(n, 1ull)] = (uint32_t) i;
 }
 
 // Top-down step: one warp per listed frontier word, ORing it into the
@@ -158,16 +182,20 @@ __global__ void k_lb_push(const uint32_t* __restrict__ ptr, const uint32_t* __re
   }
 }
 
-// After a push: new bits = next & ~visited; the old frontier words are
-// cleared so that the buffer can serve as the next "next".
-__global__ void k_lb_apply(const uint32_t* __restrict__ ptr, uint32_t nrows, uint32_t N, uint32_t W, uint64_t* vis,
-                           uint64_t* front, uint64_t* next, uint64_t* alive_next, uint8_t* hops,
-                           const uint32_t* __restrict__ lane_base, uint32_t level, unsigned long long* front_deg)
+// After a push: new bits = next & ~visited; the old frontier words of the
+// push words are cleared so that the buffer can serve as the next "next".
+__global__ void __launch_bounds__(256)
+k_lb_apply(const uint32_t* __restrict__ ptr, uint32_t nrows, uint32_t N, uint32_t W, uint64_t* vis, uint64_t* front,
+           uint64_t* next, uint64_t* alive_next, uint8_t* hops, WordHops hop, uint64_t words, unsigned long long* fdeg)
 {
-  unsigned long long deg = 0;
+  __shared__ unsigned long long sdeg[64];
+  for (uint32_t w = threadIdx.x; w < W; w += blockDim.x) sdeg[w] = 0;
+  __syncthreads();
   const uint64_t NW = (uint64_t) nrows * W;
   for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < NW; i += (uint64_t) gridDim.x * blockDim.x)
   {
+    const uint32_t w = (uint32_t) (i % W);
+    if (!((words >> w) & 1ull)) continue;
     front[i] = 0;
     const uint64_t x = next[i];
     if (!x) continue;
@@ -175,15 +203,14 @@ __global__ void k_lb_apply(const uint32_t* __restrict__ ptr, uint32_t nrows, uin
     next[i] = nb;
     if (nb)
     {
-      const uint32_t v = (uint32_t) (i / W), w = (uint32_t) (i % W);
+      const uint32_t v = (uint32_t) (i / W);
       vis[i] |= nb;
-      deg += ptr[v + 1] - ptr[v];
+      atomicAdd(&sdeg[w], (unsigned long long) (ptr[v + 1] - ptr[v]));
       atomicOr((unsigned long long*) &alive_next[w], (unsigned long long) nb);
-      lb_record(nb, v, w, N, level, lane_base, hops);
+      lb_record(nb, v, w, N, hop.h[w], hops);
     }
   }
-  for (int o = 16; o > 0; o >>= 1) deg += __shfl_xor_sync(0xffffffffu, deg, o);
-  if ((threadIdx.x & 31) == 0 && deg) atomicAdd(front_deg, deg);
+  lb_deg_flush(sdeg, W, fdeg);
 }
 
 // Retiring lanes: hops by id into the staging rows, hops reset to 255.
@@ -320,10 +347,11 @@ struct Engine
   // lanes
   uint32_t L = 0, W = 0, N = 0;
   std::vector<Ticket*> lane;
-  std::vector<uint32_t> base_h;     // BFS: level at which the lane was admitted
+  std::vector<uint32_t> wlevel;     // BFS: levels each word has run since its admission
+  std::vector<uint32_t> wbusy;      // BFS: occupied lanes per word
   std::vector<uint32_t> pos_of_id;  // host copy
   bool exact_lanes = true;          // SSSP: max weight * N < INF
-  DevBuf vis, buf[2], hops, lane_base, alive[2], active, ctr, adm, ret, mask, staging;
+  DevBuf vis, buf[2], hops, alive[2], active, ctr, adm, ret, mask, staging, fdeg;
   // SSSP
   DevBuf dist, msg, sfront[2], small[2], hub[2], hub_t0[2], reg_end, rpos;
   unsigned long long* hctr = nullptr;  // pinned: counters + alive words
@@ -334,7 +362,7 @@ struct Engine
 struct la3g_server
 {
   uint64_t budget = 0, used = 0;
-  uint32_t bfs_lanes = 128, sssp_lanes = 64;
+  uint32_t bfs_lanes = 256, sssp_lanes = 64;
   std::mutex mu;
   std::condition_variable done_cv;
   std::unordered_map<uint64_t, Ticket*> tickets;
@@ -413,7 +441,6 @@ int bfs_engine_init(Engine* E)
   LA3G_TRY(E->buf[0].alloc(NW * 8));
   LA3G_TRY(E->buf[1].alloc(NW * 8));
   LA3G_TRY(E->hops.alloc((uint64_t) L * N));
-  LA3G_TRY(E->lane_base.alloc((uint64_t) L * 4));
   LA3G_TRY(E->alive[0].alloc(W * 8));
   LA3G_TRY(E->alive[1].alloc(W * 8));
   LA3G_TRY(E->active.alloc(NW * 4));
@@ -421,7 +448,9 @@ int bfs_engine_init(Engine* E)
   LA3G_TRY(E->adm.alloc((uint64_t) L * 8));
   LA3G_TRY(E->ret.alloc((uint64_t) L * 4));
   LA3G_TRY(E->mask.alloc(W * 8));
+  LA3G_TRY(E->fdeg.alloc(W * 8));
   LA3G_TRY(E->staging.alloc((uint64_t) kOutChunk * N));
+  LA3G_CUDA(cudaMemsetAsync(E->fdeg.p, 0, W * 8, s));
   LA3G_CUDA(cudaMemsetAsync(E->vis.p, 0, NW * 8, s));
   LA3G_CUDA(cudaMemsetAsync(E->buf[0].p, 0, NW * 8, s));
   LA3G_CUDA(cudaMemsetAsync(E->buf[1].p, 0, NW * 8, s));
@@ -526,10 +555,23 @@ int run_single(Engine* E, Ticket* t)
   return la3g_sssp(E->G, t->q.root, (uint32_t*) t->q.out, nullptr);
 }
 
-// Admits queued tickets into free lanes; tickets that need no lane (root
-// out of range) or must run alone are completed here.  Returns the
-// (lane, position) pairs to initialise on the device.
-int admit(Engine* E, std::vector<Ticket*>& got, uint32_t& busy, std::vector<uint32_t>& adm, uint32_t level)
+// Completes a ticket whose root has no vertex: nothing is reached
+// (la3g_bfs / la3g_sssp give the same).
+void finish_out_of_range(Engine* E, Ticket* t)
+{
+  if (t->q.out)
+  {
+    if (E->kind == kEngBfs) std::memset(t->q.out, 255, E->N);
+    else
+      for (uint32_t i = 0; i < E->N; i++) ((uint32_t*) t->q.out)[i] = kInfD;
+  }
+  finish_ticket(E->S, t, LA3G_OK);
+}
+
+// SSSP admission: queued tickets take any free lane; tickets that need no
+// lane (root out of range) or must run alone are completed here.  Returns
+// the (lane, position) pairs to initialise on the device.
+int admit(Engine* E, std::vector<Ticket*>& got, uint32_t& busy, std::vector<uint32_t>& adm)
 {
   adm.clear();
   const double now = wall_ms();
@@ -539,14 +581,7 @@ int admit(Engine* E, std::vector<Ticket*>& got, uint32_t& busy, std::vector<uint
     const uint32_t root = t->q.root;
     if (root >= E->N)
     {
-      // no such vertex: nothing is reached (la3g_bfs / la3g_sssp give the same)
-      if (t->q.out)
-      {
-        if (E->kind == kEngBfs) std::memset(t->q.out, 255, E->N);
-        else
-          for (uint32_t i = 0; i < E->N; i++) ((uint32_t*) t->q.out)[i] = kInfD;
-      }
-      finish_ticket(E->S, t, LA3G_OK);
+      finish_out_of_range(E, t);
       continue;
     }
     if (E->kind == kEngSssp && !E->exact_lanes)
@@ -557,7 +592,6 @@ int admit(Engine* E, std::vector<Ticket*>& got, uint32_t& busy, std::vector<uint
     uint32_t l = 0;
     while (E->lane[l]) l++;
     E->lane[l] = t;
-    E->base_h[l] = level;
     busy++;
     t->in_flight = busy;
     adm.push_back(l);
@@ -570,38 +604,74 @@ int bfs_loop(Engine* E)
 {
   DevGraph& g = E->G->g;
   cudaStream_t s = E->G->stream;
-  const uint32_t N = E->N, W = E->W, L = E->L, nrows = g.nrows();
+  const uint32_t N = E->N, W = E->W, nrows = g.nrows();
   const uint64_t NW = (uint64_t) nrows * W;
   unsigned long long* ctr = E->ctr.as<unsigned long long>();
-  uint32_t level = 0, busy = 0;
+  unsigned long long* fdeg = E->fdeg.as<unsigned long long>();
+  uint32_t busy = 0;
+  uint64_t words_busy = 0;  // words with lanes in flight
   int cur = 0;
   std::vector<Ticket*> got;
   std::vector<uint32_t> adm, fin;
+  std::vector<unsigned long long> hdeg(W);
   LA3G_CUDA(cudaMemsetAsync(ctr, 0, 64, s));
   for (;;)
   {
+    // a free word takes up to 64 queued queries at once
+    const uint32_t free_words = W - (uint32_t) __builtin_popcountll(words_busy);
     got.clear();
-    if (!take_work(E, busy, L - busy, got)) return LA3G_OK;
-    LA3G_TRY(admit(E, got, busy, adm, level));
+    if (!take_work(E, busy, free_words * 64, got)) return LA3G_OK;
+    adm.clear();
+    const double now = wall_ms();
+    size_t k = 0;
+    for (uint32_t w = 0; w < W && k < got.size(); w++)
+    {
+      if ((words_busy >> w) & 1ull) continue;
+      uint32_t j = 0;
+      for (; k < got.size() && j < 64; k++)
+      {
+        Ticket* t = got[k];
+        t->start_ms = now;
+        if (t->q.root >= N)
+        {
+          finish_out_of_range(E, t);
+          continue;
+        }
+        const uint32_t l = w * 64 + j++;
+        E->lane[l] = t;
+        busy++;
+        t->in_flight = busy;
+        adm.push_back(l);
+        adm.push_back(E->pos_of_id[t->q.root]);
+      }
+      if (j)
+      {
+        words_busy |= 1ull << w;
+        E->wbusy[w] = j;
+        E->wlevel[w] = 0;
+      }
+    }
+    for (; k < got.size(); k++) finish_out_of_range(E, got[k]);  // only out-of-range ones can be left
     if (!adm.empty())
     {
       const uint32_t n = (uint32_t) adm.size() / 2;
       LA3G_CUDA(cudaMemcpyAsync(E->adm.p, adm.data(), adm.size() * 4, cudaMemcpyHostToDevice, s));
-      k_lb_admit<<<grid_for(n, 128), 128, 0, s>>>(E->adm.as<uint32_t>(), n, N, W, g.in_ptr, level,
-                                                 E->vis.as<uint64_t>(), E->buf[cur].as<uint64_t>(),
-                                                 E->hops.as<uint8_t>(), E->lane_base.as<uint32_t>(),
-                                                 E->alive[cur].as<uint64_t>(), ctr + 1);
+      k_lb_admit<<<grid_for(n, 128), 128, 0, s>>>(E->adm.as<uint32_t>(), n, N, W, g.in_ptr, E->vis.as<uint64_t>(),
+                                                 E->buf[cur].as<uint64_t>(), E->hops.as<uint8_t>(),
+                                                 E->alive[cur].as<uint64_t>(), fdeg);
       LA3G_LAUNCHED();
       tls_launches++;
     }
     if (busy == 0) continue;
     uint64_t* front = E->buf[cur].as<uint64_t>();
     uint64_t* next = E->buf[cur ^ 1].as<uint64_t>();
-    // lanes that would need hop 255 leave for the single-root path, which
-    // follows the reference's uint8 wrap exactly
+    // words whose next hop would be 255 hand their lanes to the single-root
+    // path, which follows the reference's uint8 wrap exactly
     fin.clear();
-    for (uint32_t l = 0; l < L; l++)
-      if (E->lane[l] && level - E->base_h[l] + 1 >= 255) fin.push_back(l);
+    for (uint32_t w = 0; w < W; w++)
+      if (((words_busy >> w) & 1ull) && E->wlevel[w] + 1 >= 255)
+        for (uint32_t l = w * 64; l < w * 64 + 64; l++)
+          if (E->lane[l]) fin.push_back(l);
     if (!fin.empty())
     {
       LA3G_TRY(bfs_retire(E, fin, false, front, E->alive[cur].as<uint64_t>()));
@@ -610,48 +680,59 @@ int bfs_loop(Engine* E)
         Ticket* t = E->lane[l];
         E->lane[l] = nullptr;
         busy--;
+        if (--E->wbusy[l / 64] == 0) words_busy &= ~(1ull << (l / 64));
         finish_ticket(E->S, t, run_single(E, t));
       }
       if (busy == 0) continue;
     }
-    // one level for every occupied lane: push while the frontier's edges
-    // are few, pull otherwise
-    unsigned long long front_deg = 0;
-    LA3G_CUDA(cudaMemcpyAsync(&front_deg, ctr + 1, 8, cudaMemcpyDeviceToHost, s));
+    // one level for every busy word: push while its frontier's edges are
+    // few, pull otherwise (per word, Beamer-style)
+    LA3G_CUDA(cudaMemcpyAsync(hdeg.data(), fdeg, W * 8, cudaMemcpyDeviceToHost, s));
     LA3G_CUDA(cudaStreamSynchronize(s));
-    LA3G_CUDA(cudaMemsetAsync(ctr, 0, 3 * 8, s));
+    LA3G_CUDA(cudaMemsetAsync(fdeg, 0, W * 8, s));
+    LA3G_CUDA(cudaMemsetAsync(ctr + 2, 0, 8, s));
     LA3G_CUDA(cudaMemsetAsync(E->alive[cur ^ 1].p, 0, W * 8, s));
-    const bool push = (double) front_deg * 20.0 < (double) g.nent;
-    if (!push)
+    uint64_t pull_words = 0, push_words = 0;
+    WordHops hop{};
+    for (uint32_t w = 0; w < W; w++)
+    {
+      if (!((words_busy >> w) & 1ull)) continue;
+      hop.h[w] = (uint8_t) (E->wlevel[w] + 1);
+      if ((double) hdeg[w] * 20.0 >= (double) g.nent) pull_words |= 1ull << w;
+      else push_words |= 1ull << w;
+    }
+    if (pull_words)
     {
       k_lb_pull<<<kSMs * 8, 256, 0, s>>>(g.in_ptr, g.in_col, nrows, N, W, E->vis.as<uint64_t>(), front, next,
                                          E->alive[cur].as<uint64_t>(), E->alive[cur ^ 1].as<uint64_t>(),
-                                         E->hops.as<uint8_t>(), E->lane_base.as<uint32_t>(), level, ctr + 1);
+                                         E->hops.as<uint8_t>(), hop, pull_words, fdeg);
       LA3G_LAUNCHED();
-      k_lb_clear<<<kSMs * 8, 256, 0, s>>>(NW, front);
+      k_lb_clear<<<kSMs * 8, 256, 0, s>>>(NW, W, front, pull_words);
       LA3G_LAUNCHED();
       tls_launches += 2;
     }
-    else
+    if (push_words)
     {
-      k_lb_list<<<kSMs * 8, 256, 0, s>>>(NW, front, E->active.as<uint32_t>(), ctr + 2);
+      k_lb_list<<<kSMs * 8, 256, 0, s>>>(NW, W, front, push_words, E->active.as<uint32_t>(), ctr + 2);
       LA3G_LAUNCHED();
       k_lb_push<<<kSMs * 8, 256, 0, s>>>(g.in_ptr, g.in_col, W, front, E->vis.as<uint64_t>(), next,
                                          E->active.as<uint32_t>(), ctr + 2);
       LA3G_LAUNCHED();
       k_lb_apply<<<kSMs * 8, 256, 0, s>>>(g.in_ptr, nrows, N, W, E->vis.as<uint64_t>(), front, next,
-                                          E->alive[cur ^ 1].as<uint64_t>(), E->hops.as<uint8_t>(),
-                                          E->lane_base.as<uint32_t>(), level, ctr + 1);
+                                          E->alive[cur ^ 1].as<uint64_t>(), E->hops.as<uint8_t>(), hop, push_words,
+                                          fdeg);
       LA3G_LAUNCHED();
       tls_launches += 3;
     }
     LA3G_CUDA(cudaMemcpyAsync(E->hctr, E->alive[cur ^ 1].p, W * 8, cudaMemcpyDeviceToHost, s));
     LA3G_CUDA(cudaStreamSynchronize(s));
     cur ^= 1;
-    level++;
-    // a lane that found no new vertex is finished
+    for (uint32_t w = 0; w < W; w++)
+      if ((words_busy >> w) & 1ull) E->wlevel[w]++;
+    // a lane that found no new vertex is finished; a word is free again
+    // when all its lanes are
     fin.clear();
-    for (uint32_t l = 0; l < L; l++)
+    for (uint32_t l = 0; l < E->L; l++)
       if (E->lane[l] && !((E->hctr[l / 64] >> (l % 64)) & 1ull)) fin.push_back(l);
     if (!fin.empty())
     {
@@ -661,6 +742,7 @@ int bfs_loop(Engine* E)
         Ticket* t = E->lane[l];
         E->lane[l] = nullptr;
         busy--;
+        if (--E->wbusy[l / 64] == 0) words_busy &= ~(1ull << (l / 64));
         finish_ticket(E->S, t, LA3G_OK);
       }
     }
@@ -717,7 +799,7 @@ int sssp_loop(Engine* E)
   {
     got.clear();
     if (!take_work(E, busy, L - busy, got)) return LA3G_OK;
-    LA3G_TRY(admit(E, got, busy, adm, 0));
+    LA3G_TRY(admit(E, got, busy, adm));
     if (!adm.empty())
     {
       const uint32_t n = (uint32_t) adm.size() / 2;
@@ -803,7 +885,7 @@ extern "C" int la3g_server_create(uint64_t budget_bytes, uint32_t bfs_lanes, uin
 {
   if (!out) return set_error(LA3G_EINVAL, "out is null");
   *out = nullptr;
-  if (bfs_lanes == 0) bfs_lanes = 128;
+  if (bfs_lanes == 0) bfs_lanes = 256;
   if (sssp_lanes == 0) sssp_lanes = 64;
   if (bfs_lanes % 64 || sssp_lanes % 64 || bfs_lanes > 4096 || sssp_lanes > 4096)
     return set_error(LA3G_EINVAL, "lane counts must be multiples of 64, at most 4096");
@@ -864,7 +946,8 @@ extern "C" int la3g_server_add_graph(la3g_server* S, la3g_graph* G, uint32_t* gr
   E->W = L / 64;
   E->bytes = eng_bytes;
   E->lane.assign(L, nullptr);
-  E->base_h.assign(L, 0);
+  E->wlevel.assign(E->W, 0);
+  E->wbusy.assign(E->W, 0);
   int st = LA3G_OK;
   if (kind != kEngBm25)
   {
