@@ -133,6 +133,31 @@ int la3g_graph_set_stream(la3g_graph* g, void* cuda_stream);
  * array may be NULL. */
 int la3g_graph_positions(const la3g_graph* g, uint32_t* pos_of_id, uint32_t* id_of_pos);
 
+/* Device view of a loaded graph, for vertex programs compiled against the
+ * template engine in la3g_vp.cuh (the reference's VertexProgram runs on its
+ * own Graph's tiles, src/vprogram/vertex_program.h:99-180).  All pointers
+ * are device pointers owned by the graph; positions follow
+ * la3g_graph_positions.  row_ptr / col / weight: in-edges of every position
+ * (rows = regular then sink positions), each row's columns in the order the
+ * reference's SpMV visits them (source columns first, then regular, each
+ * ascending).  weight is NULL for unweighted graphs. */
+typedef struct la3g_device_graph
+{
+  const uint32_t* row_ptr;      /* [nslots + 1] */
+  const uint32_t* col;          /* [nentries] column positions */
+  const uint32_t* weight;       /* [nentries] or NULL */
+  const uint32_t* hash_of_pos;  /* [nslots] hashed id passed as Edge src / dst */
+  const uint32_t* id_of_pos;    /* [nslots] original vertex id */
+  const uint32_t* pos_of_id;    /* [nslots] */
+  uint32_t nslots, nregular, nsink, nsource;
+  uint32_t flags;
+  uint32_t reserved;
+  uint64_t nentries;
+  void* stream;                 /* cudaStream_t the graph's calls run on */
+} la3g_device_graph;
+
+int la3g_graph_device_view(la3g_graph* g, la3g_device_graph* out);
+
 /* ---- apps (replace the six app run() functions) ------------------------ */
 
 /* PageRank, FP64, un-normalised, alpha = 0.15: the reference pr app

@@ -100,6 +100,25 @@ class ServerStats(C.Structure):
     ]
 
 
+class DeviceGraph(C.Structure):
+    _fields_ = [
+        ("row_ptr", C.c_void_p),
+        ("col", C.c_void_p),
+        ("weight", C.c_void_p),
+        ("hash_of_pos", C.c_void_p),
+        ("id_of_pos", C.c_void_p),
+        ("pos_of_id", C.c_void_p),
+        ("nslots", C.c_uint32),
+        ("nregular", C.c_uint32),
+        ("nsink", C.c_uint32),
+        ("nsource", C.c_uint32),
+        ("flags", C.c_uint32),
+        ("reserved", C.c_uint32),
+        ("nentries", C.c_uint64),
+        ("stream", C.c_void_p),
+    ]
+
+
 _P = C.c_void_p
 _u32p = C.POINTER(C.c_uint32)
 _u8p = C.POINTER(C.c_uint8)
@@ -119,6 +138,7 @@ SIGNATURES = {
     "la3g_graph_info_get": (C.c_int, [_P, C.POINTER(GraphInfo)]),
     "la3g_graph_set_stream": (C.c_int, [_P, _P]),
     "la3g_graph_positions": (C.c_int, [_P, _u32p, _u32p]),
+    "la3g_graph_device_view": (C.c_int, [_P, C.POINTER(DeviceGraph)]),
     "la3g_pr": (C.c_int, [_P, C.c_uint32, _f64p, _u32p, _statp]),
     "la3g_pr_f32": (C.c_int, [_P, C.c_uint32, C.c_double, _f64p, _f64p, _statp]),
     "la3g_bfs": (C.c_int, [_P, C.c_uint32, _u8p, _u32p, _statp]),

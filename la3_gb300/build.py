@@ -5,7 +5,8 @@
 
 Everything is compiled for sm_103a only (`-gencode arch=compute_103a,
 code=sm_103a`); translation units compile in parallel and link into
-`la3_gb300/_build/libla3g.so`.  The drivers (`pr`, `bfs`, `sssp`, `cc`, `tc`,
+`la3_gb300/_build/libla3g.so`; the vertex programs of `la3_gb300/programs/`
+(written against `include/la3g_vp.cuh`) link into `libla3g_programs.so`.  The drivers (`pr`, `bfs`, `sssp`, `cc`, `tc`,
 `bm25`, `la3g_tool`) go to `la3_gb300/bin/`.  Floating-point contraction is
 disabled library-wide (`--fmad=false`, `-ffp-contract=off`) because the apps
 reproduce the reference's arithmetic operation by operation.
@@ -24,10 +25,12 @@ PKG = Path(__file__).resolve().parent
 ROOT = PKG.parent
 CSRC = PKG / "csrc"
 DRIVERS = PKG / "drivers"
+PROGRAMS = PKG / "programs"
 BUILD = PKG / "_build"
 BIN = PKG / "bin"
 INCLUDE = ROOT / "include"
 LIB = BUILD / "libla3g.so"
+PROGRAMS_LIB = BUILD / "libla3g_programs.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
@@ -86,8 +89,20 @@ def build(verbose: bool = False) -> Path:
             fut.result()
     if _stale(LIB, objs):
         _run([nvcc()] + ARCH + ["-shared", "-o", str(LIB)] + [str(o) for o in objs] + ["-lpthread"])
+    build_programs()
     build_drivers()
     return LIB
+
+
+def build_programs() -> None:
+    """Vertex programs written against include/la3g_vp.cuh, linked to libla3g."""
+    srcs = sorted(PROGRAMS.glob("*.cu"))
+    if not srcs:
+        return
+    deps = srcs + [LIB, INCLUDE / "la3g.h", INCLUDE / "la3g_vp.cuh"]
+    if _stale(PROGRAMS_LIB, deps):
+        _run([nvcc()] + NVCC_FLAGS + ["-shared", "-o", str(PROGRAMS_LIB)] + [str(x) for x in srcs]
+             + ["-L", str(BUILD), "-lla3g", "-Xlinker", "-rpath,$ORIGIN"])
 
 
 def build_drivers() -> None:
@@ -103,7 +118,7 @@ def build_drivers() -> None:
         if _stale(out, deps):
             jobs.append(["g++", "-O2", "-std=c++17", "-I", str(INCLUDE), "-I", str(DRIVERS), str(src)]
                         + [str(c) for c in common]
-                        + ["-o", str(out), "-L", str(BUILD), "-lla3g", "-Wl,-rpath," + str(BUILD), "-pthread"])
+                        + ["-o", str(out), "-L", str(BUILD), "-lla3g", "-Wl,-rpath,$ORIGIN/../_build", "-pthread"])
     with cf.ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 2)) as ex:
         for f in [ex.submit(_run, c) for c in jobs]:
             f.result()

@@ -565,3 +565,24 @@ extern "C" int la3g_graph_positions(const la3g_graph* G, uint32_t* pos_of_id, ui
   if (id_of_pos) LA3G_CUDA(cudaMemcpy(id_of_pos, g.id_of_pos, (size_t) g.nslots * 4, cudaMemcpyDeviceToHost));
   return LA3G_OK;
 }
+
+extern "C" int la3g_graph_device_view(la3g_graph* G, la3g_device_graph* out)
+{
+  if (!G || !out) return set_error(LA3G_EINVAL, "null graph or output");
+  const DevGraph& g = G->g;
+  std::memset(out, 0, sizeof(*out));
+  out->row_ptr = g.in_ptr;
+  out->col = g.in_col;
+  out->weight = g.weighted() ? g.in_w : nullptr;
+  out->hash_of_pos = g.hash_of_pos;
+  out->id_of_pos = g.id_of_pos;
+  out->pos_of_id = g.pos_of_id;
+  out->nslots = g.nslots;
+  out->nregular = g.nreg;
+  out->nsink = g.nsink;
+  out->nsource = g.nsrc;
+  out->flags = g.flags;
+  out->nentries = g.nent;
+  out->stream = (void*) G->stream;
+  return LA3G_OK;
+}

@@ -1,0 +1,119 @@
+"""The vertex-program API (include/la3g_vp.cuh): the reference's apps written
+as device-functor programs (la3_gb300/programs/vp_apps.cu) and run by the
+generic engine must give the reference's results bit for bit: the golden
+cases, and seeded graphs against the oracle."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import GOLD
+
+DATA = GOLD / "data"
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def progs(gpu):
+    import la3_gb300.build as B
+    lib = C.CDLL(str(B.PROGRAMS_LIB))
+    P = C.c_void_p
+    u8p, u32p, f64p = C.POINTER(C.c_uint8), C.POINTER(C.c_uint32), C.POINTER(C.c_double)
+    lib.la3gp_pagerank.argtypes = [P, P, C.c_uint32, f64p, u32p]
+    lib.la3gp_bfs.argtypes = [P, C.c_uint32, u8p, u32p, u32p]
+    lib.la3gp_sssp.argtypes = [P, C.c_uint32, u32p, u32p]
+    lib.la3gp_cc.argtypes = [P, u32p, u32p]
+    lib.la3gp_degree.argtypes = [P, u32p]
+    return lib
+
+
+def _p(a, t):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+def _pr(L, progs, path, n, iters):
+    g = L.Graph.load_directed(path, n)
+    gr = L.Graph.load_directed(path, n, reverse_edges=True)
+    rank = np.empty(g.nslots, np.float64)
+    deg = np.empty(g.nslots, np.uint32)
+    assert progs.la3gp_pagerank(g._h, gr._h, iters, _p(rank, C.c_double), _p(deg, C.c_uint32)) == 0
+    return rank, deg
+
+
+def _bfs(L, progs, g, root):
+    hops = np.empty(g.nslots, np.uint8)
+    par = np.empty(g.nslots, np.uint32)
+    it = C.c_uint32()
+    assert progs.la3gp_bfs(g._h, root, _p(hops, C.c_uint8), _p(par, C.c_uint32), C.byref(it)) == 0
+    return hops, par, it.value
+
+
+def _sssp(L, progs, g, root):
+    d = np.empty(g.nslots, np.uint32)
+    it = C.c_uint32()
+    assert progs.la3gp_sssp(g._h, root, _p(d, C.c_uint32), C.byref(it)) == 0
+    return d, it.value
+
+
+def _cc(L, progs, g):
+    lab = np.empty(g.nslots, np.uint32)
+    it = C.c_uint32()
+    assert progs.la3gp_cc(g._h, _p(lab, C.c_uint32), C.byref(it)) == 0
+    return lab, it.value
+
+
+def _cases(golden, app):
+    return sorted(k for k, v in golden.items() if v["app"] == app)
+
+
+def test_programs_golden(gpu, progs, golden):
+    L = gpu
+    for name in _cases(golden, "pr"):
+        c = golden[name]
+        ref = np.load(GOLD / f"{name}.npz")
+        rank, deg = _pr(L, progs, DATA / c["file"], c["n"], c["iters"])
+        assert np.array_equal(deg, ref["degree"]), name
+        assert np.array_equal(rank.view(np.uint64), ref["rank"].view(np.uint64)), name
+    for name in _cases(golden, "bfs"):
+        c = golden[name]
+        ref = np.load(GOLD / f"{name}.npz")
+        hops, par, _ = _bfs(L, progs, L.Graph.load_undirected(DATA / c["file"], c["n"]), c["root"])
+        assert np.array_equal(hops, ref["hops"]) and np.array_equal(par, ref["parent"]), name
+    for name in _cases(golden, "sssp"):
+        c = golden[name]
+        ref = np.load(GOLD / f"{name}.npz")
+        d, _ = _sssp(L, progs, L.Graph.load_directed(DATA / c["file"], c["n"], weighted=True), c["root"])
+        assert np.array_equal(d, ref["dist"]), name
+    for name in _cases(golden, "cc"):
+        c = golden[name]
+        ref = np.load(GOLD / f"{name}.npz")
+        lab, _ = _cc(L, progs, L.Graph.load_undirected(DATA / c["file"], c["n"]))
+        assert np.array_equal(lab, ref["label"]), name
+
+
+def test_programs_vs_oracle_rmat(gpu, progs, oracle, tmp_path):
+    L = gpu
+    e = L.EdgeList.rmat(13, 16, seed=41)
+    ew = L.EdgeList.rmat(13, 16, seed=41, weighted=True, wseed=42)
+    p, pw, n = tmp_path / "g.bin", tmp_path / "g.w.bin", 1 << 13
+    e.write(p)
+    ew.write(pw)
+    rank, deg = _pr(L, progs, p, n, 10)
+    orank, odeg = oracle.OracleGraph(p, n, oracle.DIRECTED).pagerank(10)
+    assert np.array_equal(deg, odeg)
+    assert np.array_equal(rank.view(np.uint64), orank.view(np.uint64))
+    gu = L.Graph.load_undirected(p, n)
+    ou = oracle.OracleGraph(p, n, 0)
+    for r in (1, 77, 4000):
+        hops, par, it = _bfs(L, progs, gu, r)
+        oh, opar, oit = ou.bfs(r)
+        assert np.array_equal(hops, oh) and np.array_equal(par, opar) and it == oit, r
+    gw = L.Graph.load_directed(pw, n, weighted=True)
+    ow = oracle.OracleGraph(pw, n, oracle.DIRECTED | oracle.WEIGHTED)
+    for r in (1, 77, 4000):
+        d, it = _sssp(L, progs, gw, r)
+        od, oit = ow.sssp(r)
+        assert np.array_equal(d, od) and it == oit, r
+    lab, it = _cc(L, progs, gu)
+    olab, oit = ou.cc()
+    assert np.array_equal(lab, olab) and it == oit
