@@ -16,7 +16,9 @@
 // iteration is min(old, min over messages) exactly as apply computes it,
 // and a row is activated iff some relaxation lowered it.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
+#include <vector>
 
 #include "frontier.cuh"
 #include "la3g_internal.h"
@@ -24,6 +26,9 @@
 namespace la3g {
 
 static constexpr uint32_t kInf = 0x7FFFFFFFu;
+static constexpr uint32_t kPullLong = 1024;   // pull rows longer than this are cut into tasks
+static constexpr uint32_t kPullChunk = 2048;  // in-edges per long-row task (one warp)
+static constexpr uint32_t kPullLanes = 4;     // lanes per short row in a pull step
 
 // The frontier is two lists: vertices with at most kBigDeg out-edges into
 // regular rows (one warp each) and hubs (their edges shared by the grid).
@@ -41,6 +46,15 @@ struct SsspScratch
   // [4] scratch
   unsigned long long* ctr = nullptr;
   unsigned long long* hctr = nullptr;
+  uint32_t* fmsg = nullptr;       // pull steps: msg of the frontier vertices, INF elsewhere
+  uint32_t* long_rows = nullptr;  // regular rows with more than kPullLong in-edges
+  uint32_t nlong = 0;
+  uint32_t* task_row = nullptr;   // pull tasks over the long rows: kPullChunk in-edges each
+  uint32_t* task_begin = nullptr;
+  uint32_t ntasks = 0;
+  uint32_t* ymin = nullptr;       // [nlong] partial minima of the long rows (INF between steps)
+  uint64_t reg_in = 0;            // in-edges of the regular rows
+  uint32_t max_w = 0;             // largest weight: pull steps need INF + w to stay in uint32
 };
 
 static void sssp_scratch_free(void* p)
@@ -145,10 +159,12 @@ k_sssp_push(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ reg_e
   }
 }
 
-// Activated vertices scatter their new distance and form the next frontier.
+// Activated vertices scatter their new distance and form the next frontier
+// (stamp = this iteration's tag: the pull step finds the frontier by it).
 __global__ void k_sssp_apply(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ reg_end,
                              const uint32_t* __restrict__ raw, const uint32_t* __restrict__ dist, uint32_t* msg,
-                             uint32_t* small, uint32_t* big, uint32_t* big_task0, unsigned long long* ctr)
+                             uint32_t* stamp, uint32_t tag, uint32_t* small, uint32_t* big, uint32_t* big_task0,
+                             unsigned long long* ctr)
 {
   unsigned long long deg = 0;
   const uint32_t n = (uint32_t) ctr[0];
@@ -156,6 +172,7 @@ __global__ void k_sssp_apply(const uint32_t* __restrict__ ptr, const uint32_t* _
   {
     uint32_t v = raw[i];
     msg[v] = dist[v];
+    stamp[v] = tag;
     uint32_t d = reg_end[v] - ptr[v];
     deg += d;
     if (d > kBigDeg) hub_append(v, d, big, big_task0, &ctr[3]);
@@ -163,6 +180,165 @@ __global__ void k_sssp_apply(const uint32_t* __restrict__ ptr, const uint32_t* _
   }
   for (int o = 16; o > 0; o >>= 1) deg += __shfl_xor_sync(0xffffffffu, deg, o);
   if ((threadIdx.x & 31) == 0 && deg) atomicAdd(&ctr[1], deg);
+}
+
+// Pull step (for large frontiers; the reference's own SpMV direction):
+// every regular row takes the min over its in-neighbours in the frontier
+// (the previous iteration's frontier lists) of msg + w, and is activated if
+// that lowers it.  fmsg holds msg for the frontier and INF for every other
+// vertex, so each edge is one load and one add: INF + w (w <= 2^31) stays
+// above INF in uint32 and never lowers a row.  Short rows are owned by one
+// lane group and long rows are cut into tasks whose minima meet in ymin,
+// so dist needs no atomics; fmsg is not written while the step runs.
+// Sources are frontier vertices only in the first iteration, which always
+// pushes.
+__device__ __forceinline__ void sssp_pull_edge(uint32_t e, const uint32_t* __restrict__ col,
+                                               const uint32_t* __restrict__ w, const uint32_t* __restrict__ fmsg,
+                                               uint32_t& y)
+{
+  y = min(y, fmsg[col[e]] + w[e]);
+}
+
+// fmsg = msg for the frontier lists' vertices (small list, then hub slots).
+__global__ void k_fill_inf(uint32_t n, uint32_t* a)
+{
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a[i] = kInf;
+}
+
+__global__ void k_sssp_fmsg(const uint32_t* __restrict__ small, uint32_t nsmall, const uint32_t* __restrict__ big,
+                            uint32_t nbig, const uint32_t* __restrict__ msg, uint32_t* fmsg)
+{
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nsmall + nbig; i += gridDim.x * blockDim.x)
+  {
+    const uint32_t v = i < nsmall ? small[i] : big[i - nsmall];
+    fmsg[v] = msg[v];
+  }
+}
+
+__global__ void __launch_bounds__(256)
+k_sssp_pull(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ w,
+            uint32_t nreg, const uint32_t* __restrict__ task_row, const uint32_t* __restrict__ task_begin,
+            uint32_t ntasks, uint32_t task_warps, uint32_t* ymin, const uint32_t* __restrict__ fmsg,
+            const uint32_t* __restrict__ msg, uint32_t* dist, uint32_t* raw, unsigned long long* ctr)
+{
+  const int lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (warp < task_warps)
+  {
+    // long rows: each task's minimum goes to the row's partial slot
+    for (uint32_t t = warp; t < ntasks; t += task_warps)
+    {
+      const uint32_t k = task_row[t];  // index into the long-row list
+      const uint32_t b = task_begin[t], e = task_begin[ntasks + t];  // [begins | ends]
+      uint32_t y = kInf;
+      for (uint32_t i = b + lane; i < e; i += 32) sssp_pull_edge(i, col, w, fmsg, y);
+      for (int o = 16; o > 0; o >>= 1) y = min(y, __shfl_xor_sync(0xffffffffu, y, o));
+      if (lane == 0 && y < kInf) atomicMin(&ymin[k], y);
+    }
+    return;
+  }
+  // short rows: a group of kPullLanes lanes per row; each lane keeps four
+  // independent loads in flight per step (indices, then frontier words,
+  // then messages), since the step is bound by memory latency
+  constexpr uint32_t G = kPullLanes;
+  const uint32_t sub = lane & (G - 1);
+  const uint32_t group = (((blockIdx.x * blockDim.x + threadIdx.x) >> 5) - task_warps) * (32 / G) + lane / G;
+  const uint32_t ngroups = (((gridDim.x * blockDim.x) >> 5) - task_warps) * (32 / G);
+  const uint32_t rounds = (nreg + ngroups - 1) / ngroups;
+  for (uint32_t k = 0; k < rounds; k++)
+  {
+    const uint32_t v = group + k * ngroups;
+    uint32_t y = kInf;
+    bool mine = false;
+    if (v < nreg)
+    {
+      const uint32_t b = ptr[v], e = ptr[v + 1];
+      mine = e - b <= kPullLong;
+      if (mine)
+        for (uint32_t i = b + sub; i < e; i += 4 * G)
+        {
+          uint32_t c[4], ww[4], m[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++)
+          {
+            const bool ok = i + u * G < e;
+            c[u] = ok ? col[i + u * G] : 0u;
+            ww[u] = ok ? w[i + u * G] : kInf;
+          }
+#pragma unroll
+          for (int u = 0; u < 4; u++) m[u] = fmsg[c[u]];
+#pragma unroll
+          for (int u = 0; u < 4; u++) y = min(y, m[u] + ww[u]);
+        }
+    }
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) y = min(y, __shfl_xor_sync(0xffffffffu, y, o));
+    const bool low = mine && sub == 0 && y < dist[v];
+    if (low) dist[v] = y;
+    const unsigned m = __ballot_sync(0xffffffffu, low);
+    if (m)
+    {
+      uint32_t base = 0;
+      if (lane == 0) base = (uint32_t) atomicAdd(&ctr[0], (unsigned long long) __popc(m));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (low) raw[base + __popc(m & ((1u << lane) - 1))] = v;
+    }
+  }
+}
+
+// Long rows after a pull step: apply the partial minimum, reset it.
+__global__ void k_sssp_pull_long(const uint32_t* __restrict__ long_rows, uint32_t nlong, uint32_t* ymin, uint32_t* dist,
+                                 uint32_t* raw, unsigned long long* ctr)
+{
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nlong; k += gridDim.x * blockDim.x)
+  {
+    const uint32_t y = ymin[k];
+    if (y == kInf) continue;
+    ymin[k] = kInf;
+    const uint32_t v = long_rows[k];
+    if (y < dist[v])
+    {
+      dist[v] = y;
+      raw[atomicAdd(&ctr[0], 1ull)] = v;
+    }
+  }
+}
+
+__global__ void k_sssp_long_rows(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ w, uint32_t nreg,
+                                 uint32_t* list, unsigned long long* n, unsigned long long* edges, unsigned int* maxw)
+{
+  unsigned long long s = 0;
+  unsigned int mw = 0;
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nreg; v += gridDim.x * blockDim.x)
+  {
+    const uint32_t d = ptr[v + 1] - ptr[v];
+    s += d;
+    for (uint32_t i = ptr[v]; i < ptr[v + 1]; i++) mw = max(mw, w[i]);
+    if (d > kPullLong) list[atomicAdd(n, 1ull)] = v;
+  }
+  for (int o = 16; o > 0; o >>= 1)
+  {
+    s += __shfl_xor_sync(0xffffffffu, s, o);
+    mw = max(mw, __shfl_xor_sync(0xffffffffu, mw, o));
+  }
+  if ((threadIdx.x & 31) == 0)
+  {
+    if (s) atomicAdd(edges, s);
+    if (mw) atomicMax(maxw, mw);
+  }
+}
+
+// Frontier degree sums above this fraction of the regular rows' in-edges
+// pull (LA3G_SSSP_PULL overrides the divisor, for tuning; 0 = never pull).
+static double sssp_pull_divisor()
+{
+  static double d = -1;
+  if (d < 0)
+  {
+    const char* e = std::getenv("LA3G_SSSP_PULL");
+    d = e ? std::atof(e) : 4.0;
+  }
+  return d;
 }
 
 // Sink pass: y = min over in-neighbours (regular: final dist; the root if it
@@ -227,6 +403,49 @@ static int sssp_scratch(la3g_graph* G, SsspScratch** out)
   LA3G_CUDA(cudaHostAlloc(&ss->hctr, 8 * sizeof(unsigned long long), cudaHostAllocDefault));
   k_sssp_reg_end<<<grid_for(N, 256), 256, 0, G->stream>>>(G->g.out_ptr, G->g.out_row, N, G->g.nreg, ss->reg_end);
   LA3G_LAUNCHED();
+  LA3G_TRY(galloc(G, &ss->long_rows, std::max<uint32_t>(G->g.nreg, 1)));
+  LA3G_TRY(galloc(G, &ss->fmsg, N));
+  LA3G_CUDA(cudaMemsetAsync(ss->ctr, 0, 8 * sizeof(unsigned long long), G->stream));
+  k_sssp_long_rows<<<grid_for(G->g.nreg, 256), 256, 0, G->stream>>>(G->g.in_ptr, G->g.in_w, G->g.nreg, ss->long_rows,
+                                                                     ss->ctr, ss->ctr + 1, (unsigned int*) (ss->ctr + 2));
+  LA3G_LAUNCHED();
+  LA3G_CUDA(cudaMemcpyAsync(ss->hctr, ss->ctr, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, G->stream));
+  LA3G_CUDA(cudaStreamSynchronize(G->stream));
+  ss->nlong = (uint32_t) ss->hctr[0];
+  ss->reg_in = ss->hctr[1];
+  ss->max_w = (uint32_t) ss->hctr[2];
+  if (ss->nlong)
+  {
+    // cut the long rows into tasks of kPullChunk in-edges (host side: few rows)
+    std::vector<uint32_t> rows(ss->nlong), b(ss->nlong), e(ss->nlong);
+    LA3G_CUDA(cudaMemcpy(rows.data(), ss->long_rows, ss->nlong * 4, cudaMemcpyDeviceToHost));
+    for (uint32_t k = 0; k < ss->nlong; k++)
+    {
+      LA3G_CUDA(cudaMemcpy(&b[k], G->g.in_ptr + rows[k], 4, cudaMemcpyDeviceToHost));
+      LA3G_CUDA(cudaMemcpy(&e[k], G->g.in_ptr + rows[k] + 1, 4, cudaMemcpyDeviceToHost));
+    }
+    std::vector<uint32_t> trow, tbeg;
+    for (uint32_t k = 0; k < ss->nlong; k++)
+      for (uint32_t x = b[k]; x < e[k]; x += kPullChunk)
+      {
+        trow.push_back(k);
+        tbeg.push_back(x);
+      }
+    ss->ntasks = (uint32_t) trow.size();
+    LA3G_TRY(galloc(G, &ss->task_row, trow.size()));
+    LA3G_TRY(galloc(G, &ss->task_begin, 2 * trow.size()));  // [begins | ends]
+    LA3G_TRY(galloc(G, &ss->ymin, ss->nlong));
+    std::vector<uint32_t> be(2 * trow.size());
+    for (size_t t = 0; t < trow.size(); t++)
+    {
+      be[t] = tbeg[t];
+      be[trow.size() + t] = std::min<uint32_t>(tbeg[t] + kPullChunk, e[trow[t]]);
+    }
+    LA3G_CUDA(cudaMemcpy(ss->task_row, trow.data(), trow.size() * 4, cudaMemcpyHostToDevice));
+    LA3G_CUDA(cudaMemcpy(ss->task_begin, be.data(), be.size() * 4, cudaMemcpyHostToDevice));
+    std::vector<uint32_t> inf(ss->nlong, kInf);
+    LA3G_CUDA(cudaMemcpy(ss->ymin, inf.data(), ss->nlong * 4, cudaMemcpyHostToDevice));
+  }
   *out = ss;
   return LA3G_OK;
 }
@@ -274,16 +493,44 @@ static int sssp_run(la3g_graph* G, SsspScratch* ss, uint32_t root, la3g_stats* s
     iter++;
     if (nsmall + nbig == 0) break;
     LA3G_CUDA(cudaMemsetAsync(ss->ctr, 0, 4 * sizeof(unsigned long long), s));
+    const double pdiv = sssp_pull_divisor();
+    if (iter > 1 && pdiv > 0 && ss->max_w <= 0x80000000u && (double) front_deg * pdiv > (double) ss->reg_in)
+    {
+      // in-edges of every regular row (index + weight), stamps and
+      // messages of their columns, one dist read per row
+      ProfileScope p("sssp_pull", s, 8.0 * ss->reg_in + 8.0 * ss->reg_in + 8.0 * g.nreg);
+      const uint32_t task_warps = std::min<uint32_t>(ss->ntasks, kSMs * 8 * 8 / 4);
+      k_fill_inf<<<grid_for(N, 256), 256, 0, s>>>(N, ss->fmsg);
+      LA3G_LAUNCHED();
+      k_sssp_fmsg<<<grid_for(nsmall + nbig, 256), 256, 0, s>>>(ss->small[cur], (uint32_t) nsmall, ss->big[cur],
+                                                               (uint32_t) nbig, ss->msg, ss->fmsg);
+      LA3G_LAUNCHED();
+      tls_launches += 2;
+      k_sssp_pull<<<kSMs * 8, 256, 0, s>>>(g.in_ptr, g.in_col, g.in_w, g.nreg, ss->task_row, ss->task_begin,
+                                            ss->ntasks, task_warps, ss->ymin, ss->fmsg, ss->msg, ss->dist, ss->raw,
+                                            ss->ctr);
+      LA3G_LAUNCHED();
+      tls_launches++;
+      if (ss->nlong)
+      {
+        k_sssp_pull_long<<<grid_for(ss->nlong, 256), 256, 0, s>>>(ss->long_rows, ss->nlong, ss->ymin, ss->dist,
+                                                                  ss->raw, ss->ctr);
+        LA3G_LAUNCHED();
+        tls_launches++;
+      }
+      examined += ss->reg_in;
+    }
+    else
     {
       ProfileScope p("sssp_push", s, 8.0 * front_deg + 12.0 * (nsmall + nbig));
       k_sssp_push<<<blocks, 256, 0, s>>>(g.out_ptr, ss->reg_end, g.out_row, g.out_w, ss->small[cur], (uint32_t) nsmall,
                                          ss->big[cur], ss->big_task0[cur], (uint32_t) nbig, (uint32_t) ntasks, ss->msg,
                                          ss->dist, ss->stamp, iter, ss->raw, ss->ctr);
       LA3G_LAUNCHED();
+      examined += front_deg;
     }
-    examined += front_deg;
-    k_sssp_apply<<<kSMs * 4, 256, 0, s>>>(g.out_ptr, ss->reg_end, ss->raw, ss->dist, ss->msg, ss->small[cur ^ 1],
-                                         ss->big[cur ^ 1], ss->big_task0[cur ^ 1], ss->ctr);
+    k_sssp_apply<<<kSMs * 4, 256, 0, s>>>(g.out_ptr, ss->reg_end, ss->raw, ss->dist, ss->msg, ss->stamp, iter,
+                                         ss->small[cur ^ 1], ss->big[cur ^ 1], ss->big_task0[cur ^ 1], ss->ctr);
     LA3G_LAUNCHED();
     tls_launches++;
     LA3G_CUDA(cudaMemcpyAsync(ss->hctr, ss->ctr, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));

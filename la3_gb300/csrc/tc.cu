@@ -19,6 +19,8 @@
 // short (max |N+| is about sqrt(2m)), which is what makes this fast on
 // skewed graphs.
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <cub/device/device_radix_sort.cuh>
 
@@ -123,6 +125,141 @@ __global__ void k_tc_work(const uint32_t* __restrict__ ptr, const uint32_t* __re
   }
 }
 
+// Shared-memory set of N+(x) for O(1) membership: open addressing with
+// linear probing over a power-of-two table of at least 2 |N+(x)| slots;
+// each slot holds a vertex id and its index in N+(x).
+static constexpr uint32_t kEmpty = 0xFFFFFFFFu;
+
+__device__ __forceinline__ uint32_t tc_slot(uint32_t w, int lg) { return (w * 0x9E3779B1u) >> (32 - lg); }
+
+__host__ __device__ constexpr uint32_t tc_pow2(uint32_t v) { return v <= 32 ? 32 : 2 * tc_pow2((v + 1) / 2); }
+
+__device__ __forceinline__ int tc_lg(uint32_t d)
+{
+  int lg = 5;
+  while ((1u << lg) < 2 * d) lg++;
+  return lg;
+}
+
+// Counts the triangle {x, y, w} (w found at index pw of N+(x), y at index
+// jy) at its middle id: x through cx, the others through their counters.
+__device__ __forceinline__ void tc_attribute(uint32_t x, uint32_t y, uint32_t w, uint32_t jy, uint32_t pw,
+                                             uint32_t* Cn, uint32_t* cx)
+{
+  const uint32_t mn = min(x, y), mx = max(x, y);
+  if (w < mn) atomicAdd(mn == x ? cx : &Cn[jy], 1u);
+  else if (w > mx) atomicAdd(mx == x ? cx : &Cn[jy], 1u);
+  else atomicAdd(&Cn[pw], 1u);
+}
+
+// x's walk with lane groups of G lanes: group g takes y = L[jy] for jy = g,
+// g + ngroups, ...; its lanes walk N+(y) (coalesced loads, each element
+// probed in the hash set of N+(x)) unless N+(y) is more than walk_factor
+// times longer than N+(x), in which case they walk N+(x) and binary-search
+// each element in N+(y).
+template <int G, class IDX>
+__device__ __forceinline__ void tc_walk(uint32_t x, uint32_t d, const uint32_t* L, uint32_t* Cn, const uint32_t* key,
+                                        const IDX* idx, int lg, uint32_t* cx, const uint32_t* __restrict__ ptr,
+                                        const uint32_t* __restrict__ col, uint32_t walk_factor, uint32_t g,
+                                        uint32_t ngroups, uint32_t glane)
+{
+  const uint32_t mask = (1u << lg) - 1;
+  for (uint32_t jy = g; jy < d; jy += ngroups)
+  {
+    const uint32_t y = L[jy];
+    const uint32_t yb = ptr[y], ylen = ptr[y + 1] - yb;
+    if (ylen <= walk_factor * d)
+    {
+      for (uint32_t r = glane; r < ylen; r += G)
+      {
+        const uint32_t w = col[yb + r];
+        uint32_t sl = tc_slot(w, lg);
+        for (;;)
+        {
+          const uint32_t kk = key[sl];
+          if (kk == w)
+          {
+            tc_attribute(x, y, w, jy, idx[sl], Cn, cx);
+            break;
+          }
+          if (kk == kEmpty) break;
+          sl = (sl + 1) & mask;
+        }
+      }
+    }
+    else
+    {
+      for (uint32_t r = glane; r < d; r += G)
+      {
+        const uint32_t w = L[r];
+        uint32_t a = yb, c = yb + ylen;
+        while (a < c)
+        {
+          const uint32_t mid = (a + c) >> 1;
+          if (col[mid] < w) a = mid + 1;
+          else c = mid;
+        }
+        if (a < yb + ylen && col[a] == w) tc_attribute(x, y, w, jy, r, Cn, cx);
+      }
+    }
+  }
+}
+
+template <class IDX>
+__device__ __forceinline__ void tc_insert_t(uint32_t* key, IDX* idx, int lg, uint32_t w, uint32_t j)
+{
+  const uint32_t mask = (1u << lg) - 1;
+  uint32_t sl = tc_slot(w, lg);
+  while (atomicCAS(&key[sl], kEmpty, w) != kEmpty) sl = (sl + 1) & mask;
+  idx[sl] = (IDX) j;
+}
+
+// One warp per vertex x (fetched dynamically, heaviest first) with
+// |N+(x)| <= CAP; the warp's lanes form groups of G.
+template <uint32_t CAP, int WARPS, int G>
+__global__ void __launch_bounds__(WARPS * 32)
+k_tc_rank(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ order,
+          uint32_t norder, unsigned int* next, uint32_t* ntri, uint32_t walk_factor)
+{
+  constexpr uint32_t H = tc_pow2(2 * CAP);
+  static_assert(CAP < 256, "uint8 indexes");
+  __shared__ uint32_t s_L[WARPS][CAP], s_C[WARPS][CAP], s_key[WARPS][H];
+  __shared__ uint8_t s_idx[WARPS][H];
+  __shared__ uint32_t s_x[WARPS];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  uint32_t* L = s_L[wib];
+  uint32_t* Cn = s_C[wib];
+  uint32_t* key = s_key[wib];
+  uint8_t* idx = s_idx[wib];
+  for (;;)
+  {
+    uint32_t k = 0;
+    if (lane == 0) k = atomicAdd(next, 1u);
+    k = __shfl_sync(0xffffffffu, k, 0);
+    if (k >= norder) break;
+    const uint32_t x = order[k];
+    const uint32_t xb = ptr[x], d = ptr[x + 1] - xb;
+    const int lg = tc_lg(d);
+    for (uint32_t i = lane; i < (1u << lg); i += 32) key[i] = kEmpty;
+    if (lane == 0) s_x[wib] = 0;
+    __syncwarp();
+    for (uint32_t j = lane; j < d; j += 32)
+    {
+      const uint32_t y = col[xb + j];
+      L[j] = y;
+      Cn[j] = 0;
+      tc_insert_t(key, idx, lg, y, j);
+    }
+    __syncwarp();
+    tc_walk<G>(x, d, L, Cn, key, idx, lg, &s_x[wib], ptr, col, walk_factor, lane / G, 32 / G, lane % G);
+    __syncwarp();
+    for (uint32_t j = lane; j < d; j += 32)
+      if (Cn[j]) atomicAdd(&ntri[L[j]], Cn[j]);
+    if (lane == 0 && s_x[wib]) atomicAdd(&ntri[x], s_x[wib]);
+    __syncwarp();
+  }
+}
+
 __device__ __forceinline__ uint32_t lower_bound_s(const uint32_t* s, uint32_t n, uint32_t key)
 {
   uint32_t lo = 0, hi = n;
@@ -144,7 +281,7 @@ __device__ __forceinline__ uint32_t lower_bound_s(const uint32_t* s, uint32_t n,
 // is counted at its middle id.
 template <uint32_t CAP, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32)
-k_tc_rank(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ order,
+k_tc_rank_flat(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ order,
           uint32_t norder, unsigned int* next, uint32_t* ntri)
 {
   __shared__ uint32_t s_list[WARPS][CAP];
@@ -247,20 +384,16 @@ k_tc_rank(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, co
   }
 }
 
-// Heavy vertices (kTcSmall < |N+(x)| <= kTcCap): the same walk with a whole
-// block per x.
-template <uint32_t CAP, int THREADS>
+// Heavy vertices (kTcSmall < |N+(x)| <= kTcCap): a whole block per x, its
+// threads in groups of G lanes.
+template <uint32_t CAP, int THREADS, int G>
 __global__ void __launch_bounds__(THREADS)
 k_tc_rank_block(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ order,
-                uint32_t norder, unsigned int* next, uint32_t* ntri)
+                uint32_t norder, unsigned int* next, uint32_t* ntri, uint32_t walk_factor)
 {
-  constexpr int PER = (CAP + THREADS - 1) / THREADS;
-  __shared__ uint32_t L[CAP];
-  __shared__ uint32_t O[CAP + 1];
-  __shared__ uint32_t Cn[CAP];
-  __shared__ uint32_t s_warp[THREADS / 32];
+  __shared__ uint32_t L[CAP], Cn[CAP], key[2 * CAP];
+  __shared__ uint16_t idx[2 * CAP];
   __shared__ uint32_t s_k, s_x;
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   for (;;)
   {
     if (threadIdx.x == 0) s_k = atomicAdd(next, 1u);
@@ -269,88 +402,19 @@ k_tc_rank_block(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ c
     if (k >= norder) break;
     const uint32_t x = order[k];
     const uint32_t xb = ptr[x], d = ptr[x + 1] - xb;
-    // stage: thread i owns elements [i * PER, i * PER + PER)
-    uint32_t len[PER];
-    uint32_t mine = 0;
-#pragma unroll
-    for (int q = 0; q < PER; q++)
-    {
-      const uint32_t j = threadIdx.x * PER + q;
-      len[q] = 0;
-      if (j < d)
-      {
-        const uint32_t y = col[xb + j];
-        len[q] = min(ptr[y + 1] - ptr[y], d);
-        L[j] = y;
-        Cn[j] = 0;
-      }
-      mine += len[q];
-    }
-    uint32_t incl = mine;
-    for (int o = 1; o < 32; o <<= 1)
-    {
-      uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += t;
-    }
-    if (lane == 31) s_warp[wib] = incl;
+    const int lg = tc_lg(d);
+    for (uint32_t i = threadIdx.x; i < (1u << lg); i += THREADS) key[i] = kEmpty;
     if (threadIdx.x == 0) s_x = 0;
     __syncthreads();
-    uint32_t wbase = 0;
-    for (int w = 0; w < wib; w++) wbase += s_warp[w];
-    uint32_t run = wbase + incl - mine;
-#pragma unroll
-    for (int q = 0; q < PER; q++)
+    for (uint32_t j = threadIdx.x; j < d; j += THREADS)
     {
-      const uint32_t j = threadIdx.x * PER + q;
-      if (j < d) O[j] = run;
-      run += len[q];
+      const uint32_t y = col[xb + j];
+      L[j] = y;
+      Cn[j] = 0;
+      tc_insert_t(key, idx, lg, y, j);
     }
-    uint32_t total = 0;
-    for (int w = 0; w < THREADS / 32; w++) total += s_warp[w];
-    if (threadIdx.x == 0) O[d] = total;
     __syncthreads();
-    for (uint32_t t = threadIdx.x; t < total; t += THREADS)
-    {
-      uint32_t lo = 0, hi = d;
-      while (hi - lo > 1)
-      {
-        uint32_t mid = (lo + hi) >> 1;
-        if (O[mid] <= t) lo = mid;
-        else hi = mid;
-      }
-      const uint32_t jy = lo;
-      const uint32_t y = L[jy];
-      const uint32_t yb = ptr[y], ylen = ptr[y + 1] - yb;
-      const uint32_t r = t - O[jy];
-      uint32_t w, pw;
-      bool hit;
-      if (ylen <= d)
-      {
-        w = col[yb + r];
-        pw = lower_bound_s(L, d, w);
-        hit = pw < d && L[pw] == w;
-      }
-      else
-      {
-        pw = r;
-        w = L[r];
-        uint32_t a = yb, c = yb + ylen;
-        while (a < c)
-        {
-          uint32_t mid = (a + c) >> 1;
-          if (col[mid] < w) a = mid + 1;
-          else c = mid;
-        }
-        hit = a < yb + ylen && col[a] == w;
-      }
-      if (hit)
-      {
-        const uint32_t mn = min(x, y), mx = max(x, y);
-        if (w < mn) { if (mn == x) atomicAdd(&s_x, 1u); else atomicAdd(&Cn[jy], 1u); }
-        else if (w > mx) { if (mx == x) atomicAdd(&s_x, 1u); else atomicAdd(&Cn[jy], 1u); }
-        else atomicAdd(&Cn[pw], 1u);
-      }
-    }
+    tc_walk<G>(x, d, L, Cn, key, idx, lg, &s_x, ptr, col, walk_factor, threadIdx.x / G, THREADS / G, threadIdx.x % G);
     __syncthreads();
     for (uint32_t j = threadIdx.x; j < d; j += THREADS)
       if (Cn[j]) atomicAdd(&ntri[L[j]], Cn[j]);
@@ -398,6 +462,35 @@ __global__ void k_tc_sum(uint32_t N, const uint32_t* __restrict__ ntri, unsigned
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < N; v += gridDim.x * blockDim.x) s += ntri[v];
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   if ((threadIdx.x & 31) == 0 && s) atomicAdd(total, s);
+}
+
+// N+(y) is walked unless it is longer than this many times |N+(x)|
+// (LA3G_TC_WALK overrides it, for tuning).
+static uint32_t tc_walk_factor()
+{
+  static uint32_t f = 0;
+  if (!f)
+  {
+    const char* e = std::getenv("LA3G_TC_WALK");
+    f = e ? (uint32_t) std::max(1, std::atoi(e)) : 16u;
+  }
+  return f;
+}
+
+// Lane-group sizes of the two kernels (LA3G_TC_GROUPS="small,mid"
+// overrides them, for tuning).
+static int tc_variant(int which)
+{
+  static int g[2] = {0, 0};
+  static bool init = false;
+  if (!init)
+  {
+    init = true;
+    g[0] = 0;  // 0: the flattened kernel
+    g[1] = 32;
+    if (const char* e = std::getenv("LA3G_TC_GROUPS")) std::sscanf(e, "%d,%d", &g[0], &g[1]);
+  }
+  return g[which];
 }
 
 static int tc_prepare(la3g_graph* G, TcScratch* ts)
@@ -495,19 +588,37 @@ extern "C" int la3g_tc(la3g_graph* G, uint64_t* total_out, uint32_t* per_vertex_
   LA3G_CUDA(cudaMemsetAsync(ts->ntri, 0, (size_t) N * 4, s));
   LA3G_CUDA(cudaMemsetAsync(ts->total, 0, 8, s));
   LA3G_CUDA(cudaMemsetAsync(ts->next, 0, 8, s));
+  const uint32_t wf = tc_walk_factor();
   if (ts->nmid)
   {
     // list reads (N+(x) once, N+(y) per oriented edge) + the x's two offsets
     ProfileScope p("tc_rank_mid", s, 4.0 * ts->work_mid + 8.0 * ts->nmid);
-    k_tc_rank_block<kTcCap, 256><<<kSMs * 8, 256, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->order_mid, ts->nmid,
-                                                          ts->next + 1, ts->ntri);
+    if (tc_variant(1) == 16)
+      k_tc_rank_block<kTcCap, 256, 16><<<kSMs * 8, 256, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->order_mid, ts->nmid,
+                                                                ts->next + 1, ts->ntri, wf);
+    else
+      k_tc_rank_block<kTcCap, 256, 32><<<kSMs * 8, 256, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->order_mid, ts->nmid,
+                                                                ts->next + 1, ts->ntri, wf);
     LA3G_LAUNCHED();
   }
   if (ts->norder)
   {
     ProfileScope p("tc_rank", s, 4.0 * (ts->work - ts->work_mid - ts->work_big) + 8.0 * ts->norder);
-    k_tc_rank<kTcSmall, 8><<<kSMs * 8, 8 * 32, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->order, ts->norder, ts->next,
-                                                       ts->ntri);
+    switch (tc_variant(0))
+    {
+      case 8:
+        k_tc_rank<kTcSmall, 8, 8><<<kSMs * 6, 256, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->order, ts->norder,
+                                                            ts->next, ts->ntri, wf);
+        break;
+      case 32:
+        k_tc_rank<kTcSmall, 8, 32><<<kSMs * 6, 256, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->order, ts->norder,
+                                                             ts->next, ts->ntri, wf);
+        break;
+      default:
+        // short lists: the flattened walk keeps all 32 lanes busy across the y's
+        k_tc_rank_flat<kTcSmall, 8><<<kSMs * 8, 8 * 32, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->order, ts->norder,
+                                                                ts->next, ts->ntri);
+    }
     LA3G_LAUNCHED();
   }
   if (ts->nbig)
