@@ -700,7 +700,7 @@ def serve_line(args, rank, world, local) -> dict | None:
         return arr, qs
 
     budget = int(200e9)
-    S = L.Server(budget, bfs_lanes=128, sssp_lanes=64)
+    S = L.Server(budget)  # default lanes: 256 BFS (four 64-lane words), 64 SSSP
     gid = []
     for sc, gu, gw in graphs:
         gid.append((S.add_graph(gu), S.add_graph(gw)))
@@ -780,7 +780,7 @@ def serve_line(args, rank, world, local) -> dict | None:
     results = []
     with ClockSampler(local) as clocks:
         for rate in rates:
-            nq = int(min(max(rate * args.serve_seconds, 200), 50_000))
+            nq = int(min(max(rate * args.serve_seconds, 200), 20_000))
             arr, qs = make_stream(rate, nq)
             sv, _ = served(arr, qs)
             pl = plain(arr, qs)

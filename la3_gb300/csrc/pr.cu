@@ -325,9 +325,9 @@ __device__ __forceinline__ double prf_finish(uint32_t r, float acc, float* __res
 // FP32 SpMV with FP32 accumulation (any order inside a row is allowed
 // here).  The first `long_blocks` blocks take the rows longer than
 // kLongRow, one block per row with a shared-memory reduction; the others
-// give each row of at most kLongRow edges a group of 8 lanes (four rows per
-// warp), so average-degree rows keep the lanes busy.  The L1 residual is
-// reduced in FP64.
+// give each row of at most kLongRow edges a group of 4 lanes (eight rows
+// per warp), so average-degree rows keep the lanes busy.  The L1 residual
+// is reduced in FP64.
 __global__ void __launch_bounds__(256)
 k_prf_pull(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const float* __restrict__ x,
            float* __restrict__ xnext, float* __restrict__ rankf, double* __restrict__ rank,
@@ -360,11 +360,14 @@ k_prf_pull(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, c
     if (threadIdx.x == 0 && local != 0.0) atomicAdd(resid, local);
     return;
   }
-  const uint32_t sub = lane & 7;
-  const uint32_t group = ((blockIdx.x - long_blocks) * blockDim.x + threadIdx.x) >> 3;
-  const uint32_t ngroups = ((gridDim.x - long_blocks) * blockDim.x) >> 3;
+  // short rows: 4 lanes per row, each keeping four independent loads in
+  // flight per step (the step is bound by memory latency)
+  constexpr uint32_t G = 4;
+  const uint32_t sub = lane & (G - 1);
+  const uint32_t group = ((blockIdx.x - long_blocks) * blockDim.x + threadIdx.x) / G;
+  const uint32_t ngroups = ((gridDim.x - long_blocks) * blockDim.x) / G;
   const uint32_t nrows = row_hi - row_lo;
-  // all 8-lane groups of a warp run the same number of rounds
+  // all groups of a warp run the same number of rounds
   const uint32_t rounds = (nrows + ngroups - 1) / ngroups;
   for (uint32_t k = 0; k < rounds; k++)
   {
@@ -376,11 +379,20 @@ k_prf_pull(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, c
       const uint32_t b = ptr[r], e = ptr[r + 1];
       mine = (e - b) <= kLongRow;
       if (mine)
-        for (uint32_t i = b + sub; i < e; i += 8) acc += x[col[i]];
+        for (uint32_t i = b + sub; i < e; i += 4 * G)
+        {
+          uint32_t c[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++) c[u] = i + u * G < e ? col[i + u * G] : 0xFFFFFFFFu;
+          float v[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++) v[u] = c[u] != 0xFFFFFFFFu ? x[c[u]] : 0.0f;
+#pragma unroll
+          for (int u = 0; u < 4; u++) acc += v[u];
+        }
     }
-    acc += __shfl_xor_sync(0xffffffffu, acc, 4);
-    acc += __shfl_xor_sync(0xffffffffu, acc, 2);
-    acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (mine && sub == 0) local += prf_finish(r, acc, xnext, rankf, rank, deg, write_x);
   }
 #pragma unroll
@@ -497,7 +509,7 @@ extern "C" int la3g_pr_f32(la3g_graph* G, uint32_t iters, double tol, double* ra
   uint32_t it = 0;
   double res = 0.0;
   const uint32_t long_blocks = ps->nlong ? std::min<uint32_t>(ps->nlong, kSMs * 2) : 0;
-  const unsigned blocks = long_blocks + std::max<uint32_t>(grid_for((uint64_t) g.nreg * 8, 256, kSMs * 8), 1);
+  const unsigned blocks = long_blocks + std::max<uint32_t>(grid_for((uint64_t) g.nreg * 4, 256, kSMs * 8), 1);
   // algorithmic bytes per iteration (FP32 form of the FP64 count): column
   // index per edge, row offsets, x read, rank read + write, next x write
   const double it_bytes = 4.0 * g.nent + 4.0 * (g.nreg + 1) + 4.0 * N + 8.0 * g.nreg + 8.0 * g.nreg + 4.0 * g.nreg;
@@ -523,7 +535,7 @@ extern "C" int la3g_pr_f32(la3g_graph* G, uint32_t iters, double tol, double* ra
   if (tol <= 0) LA3G_CUDA(cudaMemcpyAsync(&res, ps->resid, 8, cudaMemcpyDeviceToHost, s));
   if (g.nsink)
   {
-    const unsigned sb = long_blocks + std::max<uint32_t>(grid_for((uint64_t) g.nsink * 8, 256, kSMs * 8), 1);
+    const unsigned sb = long_blocks + std::max<uint32_t>(grid_for((uint64_t) g.nsink * 4, 256, kSMs * 8), 1);
     LA3G_CUDA(cudaMemsetAsync(ps->resid, 0, 8, s));
     k_prf_pull<<<sb, 256, 0, s>>>(g.in_ptr, g.in_col, ps->xf[cur], ps->xf[cur ^ 1], ps->rankf, ps->rank, ps->deg,
                                   ps->long_rows, ps->nlong, long_blocks, g.nreg, g.nreg + g.nsink, ps->resid, 0);
