@@ -173,10 +173,12 @@ def ref_bench_bin() -> Path:
     return ROOT / "oracle" / "_ref" / "bin" / "bench_ref"
 
 
-def run_reference_sample(steps: int, scale: int, tc_scale: int, nroots: int = 4, seed: int = 99) -> dict:
+def run_reference_sample(steps: int, scale: int, tc_scale: int, nroots: int = 4, seed: int = 99,
+                         threads: int = 0) -> dict:
     """Runs the reference's own CPU implementation (built from its sources with
-    the single-rank MPI stand-in; np = 1, OMP_NUM_THREADS = 2) on a seeded
-    R-MAT sample, ingest untimed, execute() windows timed."""
+    the single-rank MPI stand-in; np = 1, OMP_NUM_THREADS = threads, all host
+    cores by default) on a seeded R-MAT sample, ingest untimed, execute()
+    windows timed."""
     import numpy as np
     import la3_gb300 as L
     exe = ref_bench_bin()
@@ -194,7 +196,7 @@ def run_reference_sample(steps: int, scale: int, tc_scale: int, nroots: int = 4,
         # roots with out-edges, so that the directed SSSP from them does work too
         cand = np.unique(src[src != dst])
         roots = rank_roots(cand, nroots, 0, seed)
-        env = dict(os.environ, OMP_NUM_THREADS="2")
+        env = dict(os.environ, OMP_NUM_THREADS=str(threads or os.cpu_count() or 1))
         t0 = time.time()
         r = subprocess.run([str(exe), str(d / "g.bin"), str(d / "g.w.bin"), str(n), str(d / "t.bin"), str(ntc),
                             str(steps)] + [str(x) for x in roots], capture_output=True, text=True, env=env, check=True)
@@ -202,7 +204,8 @@ def run_reference_sample(steps: int, scale: int, tc_scale: int, nroots: int = 4,
     out = [json.loads(l) for l in r.stdout.splitlines() if l.startswith("{")]
     summ = [o for o in out if o.get("summary")][-1]
     per_step = [o for o in out if "step" in o]
-    return {"summary": summ, "steps": per_step, "wall_s": wall, "roots": roots}
+    return {"summary": summ, "steps": per_step, "wall_s": wall, "roots": roots,
+            "threads": int(env["OMP_NUM_THREADS"])}
 
 
 def cpu_threads_note() -> str:
@@ -222,7 +225,7 @@ def reference_line(args) -> dict:
     v = e / t / 1e9
     apps = {a: sum(s[f"{a}_e"] for s in steps) / max(1e-12, sum(s[f"{a}_s"] for s in steps)) / 1e9
             for a in ("bfs", "sssp", "cc", "tc")}
-    sample = (f"reference apps (np=1, OMP_NUM_THREADS=2; one tile so SpMV runs on one thread) on R-MAT "
+    sample = (f"reference apps (np=1, OMP_NUM_THREADS={res['threads']}; one tile, so its SpMV runs on one thread) on R-MAT "
               f"s{CPU_SAMPLE_SCALE} (BFS/SSSP/CC) + s{CPU_SAMPLE_TC_SCALE} (TC); execute() windows only; "
               f"host {cpu_threads_note()}")
     return {"metric": METRIC, "value": v, "unit": "GTEPS", "impl": "reference", "n_gpus": args.gpus,
@@ -232,7 +235,7 @@ def reference_line(args) -> dict:
             "config": {"workload": f"plain BFS+SSSP+CC R-MAT s{CPU_SAMPLE_SCALE} + TC s{CPU_SAMPLE_TC_SCALE} "
                                    f"(bounded CPU sample of the s{SCALE}/s{TC_SCALE} workload)",
                        "apps_gteps": apps},
-            "cpu_baseline": {"value": v, "unit": "GTEPS", "cores": 2, "kind": "reference", "sample": sample},
+            "cpu_baseline": {"value": v, "unit": "GTEPS", "cores": res["threads"], "kind": "reference", "sample": sample},
             "e2e": {"value": v, "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -422,10 +425,11 @@ def gpu_line(args, rank: int, world: int, local: int) -> dict | None:
             e_ = s["bfs_e"] + s["sssp_e"] + s["cc_e"] + s["tc_e"]
             t_ = s["bfs_s"] + s["sssp_s"] + s["cc_s"] + s["tc_s"]
             line["cpu_baseline"] = {
-                "value": e_ / t_ / 1e9, "unit": "GTEPS", "cores": 2, "kind": "reference",
+                "value": e_ / t_ / 1e9, "unit": "GTEPS", "cores": res["threads"], "kind": "reference",
                 "sample": (f"2 steps of BFS+SSSP+CC on R-MAT s{CPU_SAMPLE_SCALE} + TC on s{CPU_SAMPLE_TC_SCALE}, "
-                           f"reference apps np=1 OMP_NUM_THREADS=2 (one tile: SpMV on one thread), execute() "
-                           f"windows only, host {cpu_threads_note()}, {res['wall_s']:.1f} s wall incl. ingest")}
+                           f"reference apps np=1 OMP_NUM_THREADS={res['threads']} (one tile: its SpMV runs on one "
+                           f"thread), execute() windows only, host {cpu_threads_note()}, {res['wall_s']:.1f} s wall "
+                           f"incl. ingest")}
         except Exception as ex:  # the baseline is reported, never required
             line["cpu_baseline"] = {"value": None, "unit": "GTEPS", "cores": 0, "kind": "reference",
                                     "sample": f"unavailable: {type(ex).__name__}: {ex}"}

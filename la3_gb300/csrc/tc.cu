@@ -23,6 +23,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
 
 #include "la3g_internal.h"
 
@@ -30,6 +31,8 @@ namespace la3g {
 
 static constexpr uint32_t kTcCap = 1024;     // N+(x) held in shared memory up to this length
 static constexpr uint32_t kTcSmall = 192;    // lists up to this length use the high-occupancy variant
+static constexpr uint32_t kTcHubMin = 32;    // N+(y) longer than this (and than N+(x)) is a hub list:
+static constexpr uint32_t kTcHubCap = 1024;  // ... small x's pairs with it go to the hub kernel, up to this length
 
 struct TcScratch
 {
@@ -44,6 +47,12 @@ struct TcScratch
   unsigned long long* total = nullptr;
   double work = 0;               // sum over x of |N+(x)| + sum_y |N+(y)| (list elements read)
   double work_mid = 0, work_big = 0;  // the part of it in the block-per-x and the global-search classes
+  // hub-centric pairs: small x with y in N+(x), |N+(y)| > max(|N+(x)|, kTcHubMin)
+  uint32_t* hub_ptr = nullptr;   // [nslots + 1] by id of y
+  uint32_t* hub_x = nullptr;     // the x's of each hub y
+  uint32_t* hubs = nullptr;      // hub ids, heaviest first
+  uint32_t nhubs = 0;
+  double hub_items = 0;          // sum over hub pairs of |N+(x)|
 };
 
 static void tc_scratch_free(void* p) { delete (TcScratch*) p; }
@@ -146,10 +155,10 @@ __device__ __forceinline__ int tc_lg(uint32_t d)
 __device__ __forceinline__ void tc_attribute(uint32_t x, uint32_t y, uint32_t w, uint32_t jy, uint32_t pw,
                                              uint32_t* Cn, uint32_t* cx)
 {
+  // the middle id of {x, y, w}: w itself, or the larger / smaller of x, y
   const uint32_t mn = min(x, y), mx = max(x, y);
-  if (w < mn) atomicAdd(mn == x ? cx : &Cn[jy], 1u);
-  else if (w > mx) atomicAdd(mx == x ? cx : &Cn[jy], 1u);
-  else atomicAdd(&Cn[pw], 1u);
+  const uint32_t mid = w < mn ? mn : (w > mx ? mx : w);
+  atomicAdd(mid == x ? cx : &Cn[mid == w ? pw : jy], 1u);
 }
 
 // x's walk with lane groups of G lanes: group g takes y = L[jy] for jy = g,
@@ -157,22 +166,42 @@ __device__ __forceinline__ void tc_attribute(uint32_t x, uint32_t y, uint32_t w,
 // probed in the hash set of N+(x)) unless N+(y) is more than walk_factor
 // times longer than N+(x), in which case they walk N+(x) and binary-search
 // each element in N+(y).
+// A pair (x, y) of a list N+(x) (at most kTcCap long) with a longer list
+// N+(y) of moderate length: instead of walking N+(y) against N+(x), or
+// binary-searching N+(y) in global memory for every element of N+(x), the
+// pair is handled hub-centrically (k_tc_hub walks the shorter N+(x)).
+__device__ __forceinline__ bool tc_is_hub_pair(uint32_t d, uint32_t ylen)
+{
+  return ylen > d && ylen > kTcHubMin && ylen <= kTcHubCap;
+}
+
+// Bloom bits of N+(x) (one hash, kBloomBits bits): most candidates that
+// are not in N+(x) are rejected by one shared load, before the probe loop.
+static constexpr uint32_t kBloomBits = 1u << 16;
+__device__ __forceinline__ uint32_t tc_bloom(uint32_t w) { return (w * 0x85EBCA6Bu) >> 16; }
+
 template <int G, class IDX>
 __device__ __forceinline__ void tc_walk(uint32_t x, uint32_t d, const uint32_t* L, uint32_t* Cn, const uint32_t* key,
                                         const IDX* idx, int lg, uint32_t* cx, const uint32_t* __restrict__ ptr,
                                         const uint32_t* __restrict__ col, uint32_t walk_factor, uint32_t g,
-                                        uint32_t ngroups, uint32_t glane)
+                                        uint32_t ngroups, uint32_t glane, const uint32_t* bloom = nullptr)
 {
   const uint32_t mask = (1u << lg) - 1;
   for (uint32_t jy = g; jy < d; jy += ngroups)
   {
     const uint32_t y = L[jy];
     const uint32_t yb = ptr[y], ylen = ptr[y + 1] - yb;
+    if (tc_is_hub_pair(d, ylen)) continue;  // k_tc_hub walks this pair
     if (ylen <= walk_factor * d)
     {
       for (uint32_t r = glane; r < ylen; r += G)
       {
         const uint32_t w = col[yb + r];
+        if (bloom)
+        {
+          const uint32_t bb = tc_bloom(w);
+          if (!((bloom[bb >> 5] >> (bb & 31)) & 1u)) continue;
+        }
         uint32_t sl = tc_slot(w, lg);
         for (;;)
         {
@@ -279,6 +308,141 @@ __device__ __forceinline__ uint32_t lower_bound_s(const uint32_t* s, uint32_t n,
 // search into N+(x), or a global one into N+(y)); lanes share the
 // concatenated work of all y.  A hit w closes the triangle {x, y, w}, which
 // is counted at its middle id.
+// Counts, per hub y, the x's (|N+(x)| <= kTcCap) pointing at it and their
+// list lengths.
+__global__ void k_tc_hub_count(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, uint32_t N,
+                               uint32_t* cnt, unsigned long long* work)
+{
+  for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < N; x += gridDim.x * blockDim.x)
+  {
+    const uint32_t b = ptr[x], d = ptr[x + 1] - b;
+    if (d == 0 || d > kTcCap) continue;
+    for (uint32_t i = b; i < b + d; i++)
+    {
+      const uint32_t y = col[i];
+      if (tc_is_hub_pair(d, ptr[y + 1] - ptr[y]))
+      {
+        atomicAdd(&cnt[y], 1u);
+        atomicAdd(&work[y], (unsigned long long) d);
+      }
+    }
+  }
+}
+
+__global__ void k_tc_hub_fill(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, uint32_t N,
+                              const uint32_t* __restrict__ hub_ptr, uint32_t* fill, uint32_t* hub_x)
+{
+  for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < N; x += gridDim.x * blockDim.x)
+  {
+    const uint32_t b = ptr[x], d = ptr[x + 1] - b;
+    if (d == 0 || d > kTcCap) continue;
+    for (uint32_t i = b; i < b + d; i++)
+    {
+      const uint32_t y = col[i];
+      if (tc_is_hub_pair(d, ptr[y + 1] - ptr[y])) hub_x[hub_ptr[y] + atomicAdd(&fill[y], 1u)] = x;
+    }
+  }
+}
+
+// Hub keys for sorting: ~work so that heavier hubs come first.
+__global__ void k_tc_hub_keys(uint32_t N, const uint32_t* __restrict__ cnt, const unsigned long long* __restrict__ work,
+                              uint32_t* keys, uint32_t* ids, unsigned long long* n)
+{
+  for (uint32_t y = blockIdx.x * blockDim.x + threadIdx.x; y < N; y += gridDim.x * blockDim.x)
+    if (cnt[y])
+    {
+      const unsigned long long k = atomicAdd(n, 1ull);
+      const unsigned long long w = work[y];
+      keys[k] = 0xFFFFFFFFu - (uint32_t) (w < 0xFFFFFFFFull ? w : 0xFFFFFFFFull);
+      ids[k] = y;
+    }
+}
+
+// One block per hub y (heaviest first): N+(y) is staged in shared memory
+// with a hash set and Bloom bits; warps take the x's pointing at y, their
+// lanes walk N+(x) (coalesced) and probe N+(y).  A hit w closes the
+// triangle {x, y, w}, counted at its middle id: y and w in shared counters
+// (flushed once per hub), x through a warp sum per x.  (A flattened walk
+// over chunks of x's, which fills the lanes better for short N+(x), measured
+// slower: its staging and barriers cost more than the idle lanes.)
+template <uint32_t CAP, int THREADS>
+__global__ void __launch_bounds__(THREADS)
+k_tc_hub(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ hubs,
+         uint32_t nhubs, const uint32_t* __restrict__ hub_ptr, const uint32_t* __restrict__ hub_x, unsigned int* next,
+         uint32_t* ntri)
+{
+  constexpr int NW = THREADS / 32;
+  __shared__ uint32_t L[CAP], Cn[CAP], key[2 * CAP];
+  __shared__ uint16_t idx[2 * CAP];
+  __shared__ uint32_t bloom[kBloomBits / 32];
+  __shared__ uint32_t s_k, s_y;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  for (uint32_t i = threadIdx.x; i < kBloomBits / 32; i += THREADS) bloom[i] = 0;
+  for (;;)
+  {
+    if (threadIdx.x == 0) s_k = atomicAdd(next, 1u);
+    __syncthreads();
+    const uint32_t k = s_k;
+    if (k >= nhubs) break;
+    const uint32_t y = hubs[k];
+    const uint32_t yb = ptr[y], d = ptr[y + 1] - yb;
+    const int lg = tc_lg(d);
+    const uint32_t mask = (1u << lg) - 1;
+    for (uint32_t i = threadIdx.x; i < (1u << lg); i += THREADS) key[i] = kEmpty;
+    if (threadIdx.x == 0) s_y = 0;
+    __syncthreads();
+    for (uint32_t j = threadIdx.x; j < d; j += THREADS)
+    {
+      const uint32_t w = col[yb + j];
+      L[j] = w;
+      Cn[j] = 0;
+      tc_insert_t(key, idx, lg, w, j);
+      const uint32_t bb = tc_bloom(w);
+      atomicOr(&bloom[bb >> 5], 1u << (bb & 31));
+    }
+    __syncthreads();
+    const uint32_t h0 = hub_ptr[y], h1 = hub_ptr[y + 1];
+    for (uint32_t h = h0 + wib; h < h1; h += NW)
+    {
+      const uint32_t x = hub_x[h];
+      const uint32_t xb = ptr[x], xd = ptr[x + 1] - xb;
+      const uint32_t mn = min(x, y), mx = max(x, y);
+      uint32_t cnt_x = 0;
+      for (uint32_t r = lane; r < xd; r += 32)
+      {
+        const uint32_t w = col[xb + r];
+        const uint32_t bb = tc_bloom(w);
+        if (!((bloom[bb >> 5] >> (bb & 31)) & 1u)) continue;
+        uint32_t sl = tc_slot(w, lg);
+        for (;;)
+        {
+          const uint32_t kk = key[sl];
+          if (kk == w)
+          {
+            const uint32_t mid = w < mn ? mn : (w > mx ? mx : w);
+            if (mid == x) cnt_x++;
+            else atomicAdd(mid == y ? &s_y : &Cn[idx[sl]], 1u);
+            break;
+          }
+          if (kk == kEmpty) break;
+          sl = (sl + 1) & mask;
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1) cnt_x += __shfl_xor_sync(0xffffffffu, cnt_x, o);
+      if (lane == 0 && cnt_x) atomicAdd(&ntri[x], cnt_x);
+    }
+    __syncthreads();
+    for (uint32_t j = threadIdx.x; j < d; j += THREADS)
+    {
+      if (Cn[j]) atomicAdd(&ntri[L[j]], Cn[j]);
+      const uint32_t bb = tc_bloom(L[j]);
+      bloom[bb >> 5] = 0;
+    }
+    if (threadIdx.x == 0 && s_y) atomicAdd(&ntri[y], s_y);
+    __syncthreads();
+  }
+}
+
 template <uint32_t CAP, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32)
 k_tc_rank_flat(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ order,
@@ -309,7 +473,9 @@ k_tc_rank_flat(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ co
       if (j < d)
       {
         const uint32_t y = col[xb + j];
-        len = min(ptr[y + 1] - ptr[y], d);
+        const uint32_t ylen = ptr[y + 1] - ptr[y];
+        // pairs with a hub list are walked by k_tc_hub instead
+        len = tc_is_hub_pair(d, ylen) ? 0u : min(ylen, d);
         L[j] = y;
         Cn[j] = 0;
       }
@@ -393,7 +559,9 @@ k_tc_rank_block(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ c
 {
   __shared__ uint32_t L[CAP], Cn[CAP], key[2 * CAP];
   __shared__ uint16_t idx[2 * CAP];
+  __shared__ uint32_t bloom[kBloomBits / 32];
   __shared__ uint32_t s_k, s_x;
+  for (uint32_t i = threadIdx.x; i < kBloomBits / 32; i += THREADS) bloom[i] = 0;
   for (;;)
   {
     if (threadIdx.x == 0) s_k = atomicAdd(next, 1u);
@@ -412,12 +580,19 @@ k_tc_rank_block(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ c
       L[j] = y;
       Cn[j] = 0;
       tc_insert_t(key, idx, lg, y, j);
+      const uint32_t bb = tc_bloom(y);
+      atomicOr(&bloom[bb >> 5], 1u << (bb & 31));
     }
     __syncthreads();
-    tc_walk<G>(x, d, L, Cn, key, idx, lg, &s_x, ptr, col, walk_factor, threadIdx.x / G, THREADS / G, threadIdx.x % G);
+    tc_walk<G>(x, d, L, Cn, key, idx, lg, &s_x, ptr, col, walk_factor, threadIdx.x / G, THREADS / G, threadIdx.x % G,
+               bloom);
     __syncthreads();
     for (uint32_t j = threadIdx.x; j < d; j += THREADS)
+    {
       if (Cn[j]) atomicAdd(&ntri[L[j]], Cn[j]);
+      const uint32_t bb = tc_bloom(L[j]);
+      bloom[bb >> 5] = 0;  // clears the words this x set (others are zero already)
+    }
     if (threadIdx.x == 0 && s_x) atomicAdd(&ntri[x], s_x);
     __syncthreads();
   }
@@ -503,7 +678,7 @@ static int tc_prepare(la3g_graph* G, TcScratch* ts)
   LA3G_TRY(galloc(G, &ts->plus_col, m + 1));
   LA3G_TRY(galloc(G, &ts->ntri, N));
   LA3G_TRY(galloc(G, &ts->total, 1));
-  LA3G_TRY(galloc(G, &ts->next, 2));
+  LA3G_TRY(galloc(G, &ts->next, 4));
   DevBuf deg, k1, k2, tmp, wkey, wid, wkey2, cnt;
   LA3G_TRY(deg.alloc((size_t) N * 4));
   LA3G_TRY(k1.alloc(m * 8 + 8));
@@ -558,6 +733,59 @@ static int tc_prepare(la3g_graph* G, TcScratch* ts)
   LA3G_CUDA(cudaStreamSynchronize(s));
   ts->order_mid = ts->order + (ts->norder - ts->nmid);
   ts->norder -= ts->nmid;
+
+  // hub-centric pairs (small x, moderate hub y): CSR by y, hubs heaviest first
+  DevBuf hcnt, hwork, hkeys, hkeys2, hids, hn;
+  LA3G_TRY(hcnt.alloc((size_t) (N + 1) * 4));
+  LA3G_TRY(hwork.alloc((size_t) N * 8));
+  LA3G_CUDA(cudaMemsetAsync(hcnt.p, 0, (size_t) (N + 1) * 4, s));
+  LA3G_CUDA(cudaMemsetAsync(hwork.p, 0, (size_t) N * 8, s));
+  k_tc_hub_count<<<grid_for(N, 256), 256, 0, s>>>(ts->plus_ptr, ts->plus_col, N, hcnt.as<uint32_t>(),
+                                                  hwork.as<unsigned long long>());
+  LA3G_LAUNCHED();
+  LA3G_TRY(galloc(G, &ts->hub_ptr, N + 1));
+  {
+    size_t tb = 0;
+    LA3G_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tb, hcnt.as<uint32_t>(), ts->hub_ptr, N + 1, s));
+    DevBuf t;
+    LA3G_TRY(t.alloc(tb));
+    LA3G_CUDA(cub::DeviceScan::ExclusiveSum(t.p, tb, hcnt.as<uint32_t>(), ts->hub_ptr, N + 1, s));
+  }
+  uint32_t npairs = 0;
+  LA3G_CUDA(cudaMemcpyAsync(&npairs, ts->hub_ptr + N, 4, cudaMemcpyDeviceToHost, s));
+  LA3G_CUDA(cudaStreamSynchronize(s));
+  LA3G_TRY(galloc(G, &ts->hub_x, std::max<uint32_t>(npairs, 1)));
+  LA3G_TRY(galloc(G, &ts->hubs, N));
+  if (npairs)
+  {
+    DevBuf fill;
+    LA3G_TRY(fill.alloc((size_t) N * 4));
+    LA3G_CUDA(cudaMemsetAsync(fill.p, 0, (size_t) N * 4, s));
+    k_tc_hub_fill<<<grid_for(N, 256), 256, 0, s>>>(ts->plus_ptr, ts->plus_col, N, ts->hub_ptr, fill.as<uint32_t>(),
+                                                   ts->hub_x);
+    LA3G_LAUNCHED();
+    LA3G_TRY(hkeys.alloc((size_t) N * 4));
+    LA3G_TRY(hkeys2.alloc((size_t) N * 4));
+    LA3G_TRY(hids.alloc((size_t) N * 4));
+    LA3G_TRY(hn.alloc(8));
+    LA3G_CUDA(cudaMemsetAsync(hn.p, 0, 8, s));
+    k_tc_hub_keys<<<grid_for(N, 256), 256, 0, s>>>(N, hcnt.as<uint32_t>(), hwork.as<unsigned long long>(),
+                                                   hkeys.as<uint32_t>(), hids.as<uint32_t>(),
+                                                   hn.as<unsigned long long>());
+    LA3G_LAUNCHED();
+    unsigned long long nh = 0;
+    LA3G_CUDA(cudaMemcpyAsync(&nh, hn.p, 8, cudaMemcpyDeviceToHost, s));
+    LA3G_CUDA(cudaStreamSynchronize(s));
+    ts->nhubs = (uint32_t) nh;
+    size_t tb = 0;
+    LA3G_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tb, hkeys.as<uint32_t>(), hkeys2.as<uint32_t>(),
+                                              hids.as<uint32_t>(), ts->hubs, ts->nhubs, 0, 32, s));
+    DevBuf t;
+    LA3G_TRY(t.alloc(tb));
+    LA3G_CUDA(cub::DeviceRadixSort::SortPairs(t.p, tb, hkeys.as<uint32_t>(), hkeys2.as<uint32_t>(),
+                                              hids.as<uint32_t>(), ts->hubs, ts->nhubs, 0, 32, s));
+  }
+  LA3G_CUDA(cudaStreamSynchronize(s));
   return LA3G_OK;
 }
 
@@ -587,7 +815,7 @@ extern "C" int la3g_tc(la3g_graph* G, uint64_t* total_out, uint32_t* per_vertex_
   T.device_begin();
   LA3G_CUDA(cudaMemsetAsync(ts->ntri, 0, (size_t) N * 4, s));
   LA3G_CUDA(cudaMemsetAsync(ts->total, 0, 8, s));
-  LA3G_CUDA(cudaMemsetAsync(ts->next, 0, 8, s));
+  LA3G_CUDA(cudaMemsetAsync(ts->next, 0, 16, s));
   const uint32_t wf = tc_walk_factor();
   if (ts->nmid)
   {
@@ -619,6 +847,13 @@ extern "C" int la3g_tc(la3g_graph* G, uint64_t* total_out, uint32_t* per_vertex_
         k_tc_rank_flat<kTcSmall, 8><<<kSMs * 8, 8 * 32, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->order, ts->norder,
                                                                 ts->next, ts->ntri);
     }
+    LA3G_LAUNCHED();
+  }
+  if (ts->nhubs)
+  {
+    ProfileScope p("tc_hub", s, 0.0);
+    k_tc_hub<kTcHubCap, 256><<<kSMs * 6, 256, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->hubs, ts->nhubs, ts->hub_ptr,
+                                                      ts->hub_x, ts->next + 2, ts->ntri);
     LA3G_LAUNCHED();
   }
   if (ts->nbig)
