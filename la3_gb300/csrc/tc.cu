@@ -34,6 +34,15 @@ static constexpr uint32_t kTcSmall = 192;    // lists up to this length use the 
 static constexpr uint32_t kTcHubMin = 32;    // N+(y) longer than this (and than N+(x)) is a hub list:
 static constexpr uint32_t kTcHubCap = 1024;  // ... small x's pairs with it go to the hub kernel, up to this length
 
+// A pair (x, y) of a list N+(x) (at most kTcCap long) with a longer list
+// N+(y) of moderate length: instead of walking N+(y) against N+(x), or
+// binary-searching N+(y) in global memory for every element of N+(x), the
+// pair is handled hub-centrically (k_tc_hub walks the shorter N+(x)).
+__device__ __forceinline__ bool tc_is_hub_pair(uint32_t d, uint32_t ylen)
+{
+  return ylen > d && ylen > kTcHubMin && ylen <= kTcHubCap;
+}
+
 struct TcScratch
 {
   uint32_t* plus_ptr = nullptr;  // [nslots + 1] by original id
@@ -52,7 +61,9 @@ struct TcScratch
   uint32_t* hub_x = nullptr;     // the x's of each hub y
   uint32_t* hubs = nullptr;      // hub ids, heaviest first
   uint32_t nhubs = 0;
+  uint32_t hub_pairs = 0;
   double hub_items = 0;          // sum over hub pairs of |N+(x)|
+  double hub_lists = 0;          // sum over hubs of |N+(y)|
 };
 
 static void tc_scratch_free(void* p) { delete (TcScratch*) p; }
@@ -110,7 +121,14 @@ __global__ void k_tc_work(const uint32_t* __restrict__ ptr, const uint32_t* __re
     const uint32_t b = ptr[x], e = ptr[x + 1];
     if (b == e) continue;
     uint64_t w = e - b;
-    for (uint32_t i = b; i < e; i++) w += ptr[col[i] + 1] - ptr[col[i]];
+    const uint32_t d = e - b;
+    for (uint32_t i = b; i < e; i++)
+    {
+      const uint32_t ylen = ptr[col[i] + 1] - ptr[col[i]];
+      // a hub pair is walked by k_tc_hub (|N+(x)| elements, counted there)
+      if (d <= kTcCap && tc_is_hub_pair(d, ylen)) continue;
+      w += ylen;
+    }
     if (e - b > kTcCap)
     {
       big[atomicAdd(&counts[1], 1ull)] = x;
@@ -166,15 +184,6 @@ __device__ __forceinline__ void tc_attribute(uint32_t x, uint32_t y, uint32_t w,
 // probed in the hash set of N+(x)) unless N+(y) is more than walk_factor
 // times longer than N+(x), in which case they walk N+(x) and binary-search
 // each element in N+(y).
-// A pair (x, y) of a list N+(x) (at most kTcCap long) with a longer list
-// N+(y) of moderate length: instead of walking N+(y) against N+(x), or
-// binary-searching N+(y) in global memory for every element of N+(x), the
-// pair is handled hub-centrically (k_tc_hub walks the shorter N+(x)).
-__device__ __forceinline__ bool tc_is_hub_pair(uint32_t d, uint32_t ylen)
-{
-  return ylen > d && ylen > kTcHubMin && ylen <= kTcHubCap;
-}
-
 // Bloom bits of N+(x) (one hash, kBloomBits bits): most candidates that
 // are not in N+(x) are rejected by one shared load, before the probe loop.
 static constexpr uint32_t kBloomBits = 1u << 16;
@@ -341,6 +350,30 @@ __global__ void k_tc_hub_fill(const uint32_t* __restrict__ ptr, const uint32_t* 
       const uint32_t y = col[i];
       if (tc_is_hub_pair(d, ptr[y + 1] - ptr[y])) hub_x[hub_ptr[y] + atomicAdd(&fill[y], 1u)] = x;
     }
+  }
+}
+
+// Totals for the algorithmic byte count: sum of |N+(x)| over hub pairs and
+// of |N+(y)| over hubs.
+__global__ void k_tc_hub_sums(const uint32_t* __restrict__ ptr, uint32_t N, const uint32_t* __restrict__ cnt,
+                              const unsigned long long* __restrict__ work, unsigned long long* out)
+{
+  unsigned long long a = 0, b = 0;
+  for (uint32_t y = blockIdx.x * blockDim.x + threadIdx.x; y < N; y += gridDim.x * blockDim.x)
+    if (cnt[y])
+    {
+      a += work[y];
+      b += ptr[y + 1] - ptr[y];
+    }
+  for (int o = 16; o > 0; o >>= 1)
+  {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+  if ((threadIdx.x & 31) == 0)
+  {
+    if (a) atomicAdd(&out[0], a);
+    if (b) atomicAdd(&out[1], b);
   }
 }
 
@@ -755,6 +788,7 @@ static int tc_prepare(la3g_graph* G, TcScratch* ts)
   LA3G_CUDA(cudaMemcpyAsync(&npairs, ts->hub_ptr + N, 4, cudaMemcpyDeviceToHost, s));
   LA3G_CUDA(cudaStreamSynchronize(s));
   LA3G_TRY(galloc(G, &ts->hub_x, std::max<uint32_t>(npairs, 1)));
+  ts->hub_pairs = npairs;
   LA3G_TRY(galloc(G, &ts->hubs, N));
   if (npairs)
   {
@@ -773,10 +807,20 @@ static int tc_prepare(la3g_graph* G, TcScratch* ts)
                                                    hkeys.as<uint32_t>(), hids.as<uint32_t>(),
                                                    hn.as<unsigned long long>());
     LA3G_LAUNCHED();
+    DevBuf hsum;
+    LA3G_TRY(hsum.alloc(16));
+    LA3G_CUDA(cudaMemsetAsync(hsum.p, 0, 16, s));
+    k_tc_hub_sums<<<grid_for(N, 256), 256, 0, s>>>(ts->plus_ptr, N, hcnt.as<uint32_t>(), hwork.as<unsigned long long>(),
+                                                   hsum.as<unsigned long long>());
+    LA3G_LAUNCHED();
+    unsigned long long hs[2] = {0, 0};
+    LA3G_CUDA(cudaMemcpyAsync(hs, hsum.p, 16, cudaMemcpyDeviceToHost, s));
     unsigned long long nh = 0;
     LA3G_CUDA(cudaMemcpyAsync(&nh, hn.p, 8, cudaMemcpyDeviceToHost, s));
     LA3G_CUDA(cudaStreamSynchronize(s));
     ts->nhubs = (uint32_t) nh;
+    ts->hub_items = (double) hs[0];
+    ts->hub_lists = (double) hs[1];
     size_t tb = 0;
     LA3G_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tb, hkeys.as<uint32_t>(), hkeys2.as<uint32_t>(),
                                               hids.as<uint32_t>(), ts->hubs, ts->nhubs, 0, 32, s));
@@ -851,7 +895,8 @@ extern "C" int la3g_tc(la3g_graph* G, uint64_t* total_out, uint32_t* per_vertex_
   }
   if (ts->nhubs)
   {
-    ProfileScope p("tc_hub", s, 0.0);
+    // N+(x) of every hub pair + each hub's N+(y) once + two offsets per pair
+    ProfileScope p("tc_hub", s, 4.0 * ts->hub_items + 4.0 * ts->hub_lists + 8.0 * (double) ts->hub_pairs);
     k_tc_hub<kTcHubCap, 256><<<kSMs * 6, 256, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->hubs, ts->nhubs, ts->hub_ptr,
                                                       ts->hub_x, ts->next + 2, ts->ntri);
     LA3G_LAUNCHED();
