@@ -26,8 +26,8 @@
 namespace la3g {
 
 static constexpr uint32_t kInf = 0x7FFFFFFFu;
-static constexpr uint32_t kPullLong = 1024;   // pull rows longer than this are cut into tasks
-static constexpr uint32_t kPullChunk = 2048;  // in-edges per long-row task (one warp)
+static constexpr uint32_t kPullLong = 64;     // pull rows longer than this are cut into tasks
+static constexpr uint32_t kPullChunk = 512;   // in-edges per long-row task (one warp)
 static constexpr uint32_t kPullLanes = 4;     // lanes per short row in a pull step
 
 // The frontier is two lists: vertices with at most kBigDeg out-edges into
@@ -52,6 +52,7 @@ struct SsspScratch
   uint32_t* task_row = nullptr;   // pull tasks over the long rows: kPullChunk in-edges each
   uint32_t* task_begin = nullptr;
   uint32_t ntasks = 0;
+  uint64_t task_edges = 0;        // in-edges of the long rows
   uint32_t* ymin = nullptr;       // [nlong] partial minima of the long rows (INF between steps)
   uint64_t reg_in = 0;            // in-edges of the regular rows
   uint32_t max_w = 0;             // largest weight: pull steps need INF + w to stay in uint32
@@ -417,20 +418,24 @@ static int sssp_scratch(la3g_graph* G, SsspScratch** out)
   if (ss->nlong)
   {
     // cut the long rows into tasks of kPullChunk in-edges (host side: few rows)
-    std::vector<uint32_t> rows(ss->nlong), b(ss->nlong), e(ss->nlong);
+    std::vector<uint32_t> rows(ss->nlong), b(ss->nlong), e(ss->nlong), ptr((size_t) G->g.nreg + 1);
     LA3G_CUDA(cudaMemcpy(rows.data(), ss->long_rows, ss->nlong * 4, cudaMemcpyDeviceToHost));
+    LA3G_CUDA(cudaMemcpy(ptr.data(), G->g.in_ptr, ptr.size() * 4, cudaMemcpyDeviceToHost));
     for (uint32_t k = 0; k < ss->nlong; k++)
     {
-      LA3G_CUDA(cudaMemcpy(&b[k], G->g.in_ptr + rows[k], 4, cudaMemcpyDeviceToHost));
-      LA3G_CUDA(cudaMemcpy(&e[k], G->g.in_ptr + rows[k] + 1, 4, cudaMemcpyDeviceToHost));
+      b[k] = ptr[rows[k]];
+      e[k] = ptr[rows[k] + 1];
     }
     std::vector<uint32_t> trow, tbeg;
     for (uint32_t k = 0; k < ss->nlong; k++)
+    {
+      ss->task_edges += e[k] - b[k];
       for (uint32_t x = b[k]; x < e[k]; x += kPullChunk)
       {
         trow.push_back(k);
         tbeg.push_back(x);
       }
+    }
     ss->ntasks = (uint32_t) trow.size();
     LA3G_TRY(galloc(G, &ss->task_row, trow.size()));
     LA3G_TRY(galloc(G, &ss->task_begin, 2 * trow.size()));  // [begins | ends]
@@ -499,7 +504,13 @@ static int sssp_run(la3g_graph* G, SsspScratch* ss, uint32_t root, la3g_stats* s
       // in-edges of every regular row (index + weight), stamps and
       // messages of their columns, one dist read per row
       ProfileScope p("sssp_pull", s, 8.0 * ss->reg_in + 8.0 * ss->reg_in + 8.0 * g.nreg);
-      const uint32_t task_warps = std::min<uint32_t>(ss->ntasks, kSMs * 8 * 8 / 4);
+      // warps split between long-row tasks and short rows in proportion to their in-edges
+      const uint32_t all_warps = kSMs * 8 * 8;
+      const uint32_t task_warps =
+          ss->ntasks ? std::min<uint32_t>(ss->ntasks, std::max<uint32_t>(1, (uint32_t) ((double) all_warps *
+                                                                                          ss->task_edges /
+                                                                                          std::max<uint64_t>(ss->reg_in, 1))))
+                     : 0;
       k_fill_inf<<<grid_for(N, 256), 256, 0, s>>>(N, ss->fmsg);
       LA3G_LAUNCHED();
       k_sssp_fmsg<<<grid_for(nsmall + nbig, 256), 256, 0, s>>>(ss->small[cur], (uint32_t) nsmall, ss->big[cur],
