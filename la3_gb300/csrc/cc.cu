@@ -71,15 +71,16 @@ __device__ __forceinline__ void cc_union(uint32_t* parent, uint32_t a, uint32_t 
   }
 }
 
-// Afforest-style sampling: every row unites with its first `k` neighbours.
+// Afforest-style sampling round r: every row unites with its r-th
+// neighbour (rounds are separated by a full path compression, which keeps
+// the finds of the next round short).
 __global__ void k_cc_sample(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col,
-                            const uint32_t* __restrict__ id_of_pos, uint32_t nrows, uint32_t k, uint32_t* parent)
+                            const uint32_t* __restrict__ id_of_pos, uint32_t nrows, uint32_t r, uint32_t* parent)
 {
   for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < nrows; u += gridDim.x * blockDim.x)
   {
-    const uint32_t b = ptr[u], e = min(ptr[u + 1], ptr[u] + k);
-    const uint32_t iu = id_of_pos[u];
-    for (uint32_t i = b; i < e; i++) cc_union(parent, iu, id_of_pos[col[i]]);
+    const uint32_t i = ptr[u] + r;
+    if (i < ptr[u + 1]) cc_union(parent, id_of_pos[u], id_of_pos[col[i]]);
   }
 }
 
@@ -217,15 +218,19 @@ extern "C" int la3g_cc(la3g_graph* G, uint32_t* label_out, la3g_stats* st)
     k_cc_init<<<grid_for(N, 256), 256, 0, s>>>(N, cs->label);
     LA3G_LAUNCHED();
     tls_launches++;
+    for (uint32_t r = 0; r < k; r++)
     {
-      ProfileScope p("cc_sample", s, 8.0 * nrows + 12.0 * nrows);
-      k_cc_sample<<<grid_for(nrows, 256), 256, 0, s>>>(g.in_ptr, g.in_col, g.id_of_pos, nrows, k, cs->label);
-      LA3G_LAUNCHED();
-    }
-    {
-      ProfileScope p("cc_flatten", s, 8.0 * N);
-      k_cc_flatten<<<grid_for(N, 256), 256, 0, s>>>(N, cs->label);
-      LA3G_LAUNCHED();
+      {
+        // row offsets, one index, two ids, and the two finds' parents
+        ProfileScope p("cc_sample", s, 8.0 * nrows + 4.0 * nrows + 8.0 * nrows + 8.0 * nrows);
+        k_cc_sample<<<grid_for(nrows, 256), 256, 0, s>>>(g.in_ptr, g.in_col, g.id_of_pos, nrows, r, cs->label);
+        LA3G_LAUNCHED();
+      }
+      {
+        ProfileScope p("cc_flatten", s, 8.0 * N);
+        k_cc_flatten<<<grid_for(N, 256), 256, 0, s>>>(N, cs->label);
+        LA3G_LAUNCHED();
+      }
     }
     if (!cs->probe) LA3G_TRY(galloc(G, &cs->probe, nsamples));
     k_cc_probe<<<4, 256, 0, s>>>(g.id_of_pos, nrows, nsamples, 0x5A3Dull, cs->label, cs->probe);
