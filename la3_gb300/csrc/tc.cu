@@ -171,12 +171,14 @@ __device__ __forceinline__ int tc_lg(uint32_t d)
 // Counts the triangle {x, y, w} (w found at index pw of N+(x), y at index
 // jy) at its middle id: x through cx, the others through their counters.
 __device__ __forceinline__ void tc_attribute(uint32_t x, uint32_t y, uint32_t w, uint32_t jy, uint32_t pw,
-                                             uint32_t* Cn, uint32_t* cx)
+                                             uint32_t* Cn, uint32_t& cx)
 {
-  // the middle id of {x, y, w}: w itself, or the larger / smaller of x, y
+  // the middle id of {x, y, w}: w itself, or the larger / smaller of x, y;
+  // x's count stays in a register (one shared word would serialise lanes)
   const uint32_t mn = min(x, y), mx = max(x, y);
   const uint32_t mid = w < mn ? mn : (w > mx ? mx : w);
-  atomicAdd(mid == x ? cx : &Cn[mid == w ? pw : jy], 1u);
+  if (mid == x) cx++;
+  else atomicAdd(&Cn[mid == w ? pw : jy], 1u);
 }
 
 // x's walk with lane groups of G lanes: group g takes y = L[jy] for jy = g,
@@ -196,6 +198,7 @@ __device__ __forceinline__ void tc_walk(uint32_t x, uint32_t d, const uint32_t* 
                                         uint32_t ngroups, uint32_t glane, const uint32_t* bloom = nullptr)
 {
   const uint32_t mask = (1u << lg) - 1;
+  uint32_t cxr = 0;  // triangles counted at x by this lane
   for (uint32_t jy = g; jy < d; jy += ngroups)
   {
     const uint32_t y = L[jy];
@@ -203,25 +206,34 @@ __device__ __forceinline__ void tc_walk(uint32_t x, uint32_t d, const uint32_t* 
     if (tc_is_hub_pair(d, ylen)) continue;  // k_tc_hub walks this pair
     if (ylen <= walk_factor * d)
     {
-      for (uint32_t r = glane; r < ylen; r += G)
+      // four independent list loads in flight per lane, then the probes
+      for (uint32_t r0 = glane; r0 < ylen; r0 += 4 * G)
       {
-        const uint32_t w = col[yb + r];
-        if (bloom)
+        uint32_t wv[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) wv[u] = r0 + u * G < ylen ? col[yb + r0 + u * G] : kEmpty;
+#pragma unroll
+        for (int u = 0; u < 4; u++)
         {
-          const uint32_t bb = tc_bloom(w);
-          if (!((bloom[bb >> 5] >> (bb & 31)) & 1u)) continue;
-        }
-        uint32_t sl = tc_slot(w, lg);
-        for (;;)
-        {
-          const uint32_t kk = key[sl];
-          if (kk == w)
+          const uint32_t w = wv[u];
+          if (w == kEmpty) continue;
+          if (bloom)
           {
-            tc_attribute(x, y, w, jy, idx[sl], Cn, cx);
-            break;
+            const uint32_t bb = tc_bloom(w);
+            if (!((bloom[bb >> 5] >> (bb & 31)) & 1u)) continue;
           }
-          if (kk == kEmpty) break;
-          sl = (sl + 1) & mask;
+          uint32_t sl = tc_slot(w, lg);
+          for (;;)
+          {
+            const uint32_t kk = key[sl];
+            if (kk == w)
+            {
+              tc_attribute(x, y, w, jy, idx[sl], Cn, cxr);
+              break;
+            }
+            if (kk == kEmpty) break;
+            sl = (sl + 1) & mask;
+          }
         }
       }
     }
@@ -237,10 +249,12 @@ __device__ __forceinline__ void tc_walk(uint32_t x, uint32_t d, const uint32_t* 
           if (col[mid] < w) a = mid + 1;
           else c = mid;
         }
-        if (a < yb + ylen && col[a] == w) tc_attribute(x, y, w, jy, r, Cn, cx);
+        if (a < yb + ylen && col[a] == w) tc_attribute(x, y, w, jy, r, Cn, cxr);
       }
     }
   }
+  for (int o = 16; o > 0; o >>= 1) cxr += __shfl_xor_sync(0xffffffffu, cxr, o);
+  if ((threadIdx.x & 31) == 0 && cxr) atomicAdd(cx, cxr);
 }
 
 template <class IDX>
@@ -440,29 +454,46 @@ k_tc_hub(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, con
       const uint32_t x = hub_x[h];
       const uint32_t xb = ptr[x], xd = ptr[x + 1] - xb;
       const uint32_t mn = min(x, y), mx = max(x, y);
-      uint32_t cnt_x = 0;
-      for (uint32_t r = lane; r < xd; r += 32)
+      uint32_t cnt_x = 0, cnt_y = 0;
+      for (uint32_t r0 = lane; r0 < xd; r0 += 4 * 32)
       {
-        const uint32_t w = col[xb + r];
-        const uint32_t bb = tc_bloom(w);
-        if (!((bloom[bb >> 5] >> (bb & 31)) & 1u)) continue;
-        uint32_t sl = tc_slot(w, lg);
-        for (;;)
+        uint32_t wv[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) wv[u] = r0 + u * 32 < xd ? col[xb + r0 + u * 32] : kEmpty;
+#pragma unroll
+        for (int u = 0; u < 4; u++)
         {
-          const uint32_t kk = key[sl];
-          if (kk == w)
+          const uint32_t w = wv[u];
+          if (w == kEmpty) continue;
+          const uint32_t bb = tc_bloom(w);
+          if (!((bloom[bb >> 5] >> (bb & 31)) & 1u)) continue;
+          uint32_t sl = tc_slot(w, lg);
+          for (;;)
           {
-            const uint32_t mid = w < mn ? mn : (w > mx ? mx : w);
-            if (mid == x) cnt_x++;
-            else atomicAdd(mid == y ? &s_y : &Cn[idx[sl]], 1u);
-            break;
+            const uint32_t kk = key[sl];
+            if (kk == w)
+            {
+              const uint32_t mid = w < mn ? mn : (w > mx ? mx : w);
+              if (mid == x) cnt_x++;
+              else if (mid == y) cnt_y++;
+              else atomicAdd(&Cn[idx[sl]], 1u);
+              break;
+            }
+            if (kk == kEmpty) break;
+            sl = (sl + 1) & mask;
           }
-          if (kk == kEmpty) break;
-          sl = (sl + 1) & mask;
         }
       }
-      for (int o = 16; o > 0; o >>= 1) cnt_x += __shfl_xor_sync(0xffffffffu, cnt_x, o);
-      if (lane == 0 && cnt_x) atomicAdd(&ntri[x], cnt_x);
+      for (int o = 16; o > 0; o >>= 1)
+      {
+        cnt_x += __shfl_xor_sync(0xffffffffu, cnt_x, o);
+        cnt_y += __shfl_xor_sync(0xffffffffu, cnt_y, o);
+      }
+      if (lane == 0)
+      {
+        if (cnt_x) atomicAdd(&ntri[x], cnt_x);
+        if (cnt_y) atomicAdd(&s_y, cnt_y);
+      }
     }
     __syncthreads();
     for (uint32_t j = threadIdx.x; j < d; j += THREADS)
