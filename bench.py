@@ -493,7 +493,7 @@ def batched_line(args, rank, world, local) -> dict | None:
         gu.set_stream(stream.cuda_stream)
         gw.set_stream(stream.cuda_stream)
     sizes_b, sizes_s = (64, 256, 1024), (64, 256)
-    sweep, depth_hist = {}, {}
+    sweep, depth_hist, tune = {}, {}, {}
     roots_of = {}
     for name, (gu, gw) in graphs.items():
         _, ids = gu.positions()
@@ -505,6 +505,9 @@ def batched_line(args, rank, world, local) -> dict | None:
         rb = rank_roots(cand_b, max(sizes_b), rank, seed=7)
         rs = rank_roots(cand_s, max(sizes_s), rank, seed=8)
         roots_of[name] = (rb, rs)
+        # the project autotuner picks level mode, block size and push threshold
+        # for this graph and each batch size (untimed setup, separate root draws)
+        tune[name] = {R: L.batch_autotune(gu, rank_roots(cand_b, R, rank, seed=17 + R)) for R in sizes_b}
         # single-root numerators and times (outside every timed batch)
         tb, ts, eb, es, lv = [], [], {}, {}, []
         for r in rb:
@@ -581,6 +584,8 @@ def batched_line(args, rank, world, local) -> dict | None:
         "config": {"workload": f"batched BFS (1024 roots) + SSSP (256 roots) on R-MAT s{args.scale}; sweep on R-MAT "
                                f"and ER 2^{args.scale} (deg 16)", "l2": "256 MB L2 flush before every step",
                    "sweep": sweep, "bfs_depth_histogram": depth_hist,
+                   "autotune_best": {g: {R: min(t, key=lambda c: c["ms"]) for R, t in tr.items()}
+                                     for g, tr in tune.items()},
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "e2e": {"value": (eb + es) / e2e_s / 1e9, "unit": "GTEPS", "h2d_bytes_per_step": 4 * (len(rb) + len(rs)),
                 "d2h_bytes_per_step": int(hb.nbytes + ds.nbytes)},

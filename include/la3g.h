@@ -224,12 +224,15 @@ int la3g_sssp_batch(la3g_graph* g, const uint32_t* roots, uint32_t nroots, uint3
 
 /* Tunes the batched BFS for this graph (level mode: per-level CUDA graph or
  * persistent kernel; block size; push/pull threshold) by timing each
- * combination on the given roots; the best is kept on the graph handle.
- * report (nullable) receives a JSON list of the timings. */
+ * combination on the given roots (best of two runs); the best is kept on the
+ * graph handle for batches of the same number of 64-root words (batches of
+ * other sizes use the nearest tuned size).  report (nullable) receives a
+ * JSON list of the timings. */
 int la3g_batch_autotune(la3g_graph* g, const uint32_t* roots, uint32_t nroots, char* report, size_t cap);
 
-/* Sets the batched-BFS configuration by hand: mode 0 = per-level CUDA graph,
- * 1 = persistent kernel; block 128 / 256 / 512; push_frac in [0, 1]. */
+/* Sets the batched-BFS configuration by hand (dropping tuned ones): mode 0 =
+ * per-level CUDA graph, 1 = persistent kernel; block 128 / 256 / 512;
+ * push_frac in [0, 1]. */
 int la3g_batch_config(la3g_graph* g, int mode, int block, double push_frac);
 
 /* ---- serving loop (no reference counterpart; the reference answers one
