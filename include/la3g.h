@@ -298,6 +298,11 @@ int la3g_server_submit(la3g_server* s, const la3g_query* q, uint64_t* ticket);
  * it is still pending.  Thread-safe. */
 int la3g_server_poll(la3g_server* s, uint64_t ticket, int timeout_ms, la3g_query_result* res);
 int la3g_server_info(la3g_server* s, la3g_server_stats* out);
+/* Adaptive batching: an engine with no lanes in flight answers queries one at
+ * a time through the single-root entry point while at most this many wait
+ * (defaults 16 for BFS, 4 for SSSP); deeper queues use lanes.  0 = always
+ * lanes.  Results are the same either way. */
+int la3g_server_set_solo(la3g_server* s, uint32_t bfs_depth, uint32_t sssp_depth);
 /* Lanes the engine of graph_id was given (after budget halving). */
 int la3g_server_lanes(la3g_server* s, uint32_t graph_id, uint32_t* lanes);
 /* Stops the workers (queries still queued are dropped) and frees the

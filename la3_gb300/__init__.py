@@ -276,6 +276,10 @@ class Server:
         G._servers.append(weakref.ref(self))
         return gid.value
 
+    def set_solo(self, bfs_depth: int, sssp_depth: int) -> None:
+        """Adaptive batching depths (0, 0 = always lanes)."""
+        N.check(N.lib().la3g_server_set_solo(self._h, bfs_depth, sssp_depth))
+
     def lanes(self, gid: int) -> int:
         n = C.c_uint32()
         N.check(N.lib().la3g_server_lanes(self._h, gid, C.byref(n)))

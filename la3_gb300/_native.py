@@ -165,6 +165,7 @@ SIGNATURES = {
     "la3g_server_poll": (C.c_int, [_P, C.c_uint64, C.c_int, C.POINTER(QueryResult)]),
     "la3g_server_info": (C.c_int, [_P, C.POINTER(ServerStats)]),
     "la3g_server_lanes": (C.c_int, [_P, C.c_uint32, _u32p]),
+    "la3g_server_set_solo": (C.c_int, [_P, C.c_uint32, C.c_uint32]),
     "la3g_server_free": (None, [_P]),
     "la3g_profile_enable": (None, [C.c_int]),
     "la3g_profile_reset": (None, []),

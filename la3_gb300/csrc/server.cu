@@ -19,6 +19,10 @@
 //    engine's words sit at different levels.
 //    Each lane's arithmetic is that of the single-root call, and lanes never
 //    read one another's bits, so a result does not depend on the mix.
+//    Adaptive batching: an engine with no lanes in flight and only a few
+//    queries waiting answers them one at a time through the single-root
+//    entry point (faster per query at low load); lanes take over when the
+//    queue is deeper.
 //  * BM25 engines run their queries one after another on their corpus.
 //
 // Admission by HBM budget: a graph joins only if its device bytes plus the
@@ -28,6 +32,7 @@
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <mutex>
@@ -364,6 +369,7 @@ struct la3g_server
 {
   uint64_t budget = 0, used = 0;
   uint32_t bfs_lanes = 256, sssp_lanes = 64;
+  uint32_t solo_bfs = 16, solo_sssp = 4;  // adaptive batching depths
   std::mutex mu;
   std::condition_variable done_cv;
   std::unordered_map<uint64_t, Ticket*> tickets;
@@ -373,6 +379,11 @@ struct la3g_server
 };
 
 namespace {
+
+uint32_t solo_depth(const Engine* E)
+{
+  return E->kind == kEngBfs ? E->S->solo_bfs : E->S->solo_sssp;
+}
 
 uint64_t bfs_lane_bytes(uint32_t N, uint32_t L)
 {
@@ -418,11 +429,26 @@ void engine_fail(Engine* E, int st)
 
 // Pops up to `free_lanes` queued tickets (waits while there is no work).
 // Returns false when the engine stops.
-bool take_work(Engine* E, uint32_t busy, uint32_t free_lanes, std::vector<Ticket*>& got)
+// Adaptive batching: an engine with no lanes in flight and at most
+// solo_depth queries waiting answers them one at a time through the
+// single-root path, which is faster per query at low load; lanes take over
+// above it (la3g_server_set_solo sets the depths; 0 = lanes only).
+uint32_t solo_depth(const Engine* E);
+
+// Waits for work.  With no lanes in flight and a short queue, pops one
+// ticket into *solo; otherwise pops up to `free_lanes` into got.  Returns
+// false when the engine stops.
+bool take_work(Engine* E, uint32_t busy, uint32_t free_lanes, std::vector<Ticket*>& got, Ticket** solo = nullptr)
 {
   std::unique_lock<std::mutex> lk(E->S->mu);
   while (!E->stop && busy == 0 && E->queue.empty()) E->cv.wait(lk);
   if (E->stop) return false;
+  if (solo && busy == 0 && E->queue.size() <= solo_depth(E))
+  {
+    *solo = E->queue.front();
+    E->queue.pop_front();
+    return true;
+  }
   while (free_lanes && !E->queue.empty())
   {
     got.push_back(E->queue.front());
@@ -430,6 +456,18 @@ bool take_work(Engine* E, uint32_t busy, uint32_t free_lanes, std::vector<Ticket
     free_lanes--;
   }
   return true;
+}
+
+int run_single(Engine* E, Ticket* t);
+void finish_out_of_range(Engine* E, Ticket* t);
+
+// A query answered alone (adaptive batching): the single-root entry point.
+void run_solo(Engine* E, Ticket* t)
+{
+  t->start_ms = wall_ms();
+  t->in_flight = 1;
+  if (t->q.root >= E->N) finish_out_of_range(E, t);
+  else finish_ticket(E->S, t, run_single(E, t));
 }
 
 int bfs_engine_init(Engine* E)
@@ -621,7 +659,13 @@ int bfs_loop(Engine* E)
     // a free word takes up to 64 queued queries at once
     const uint32_t free_words = W - (uint32_t) __builtin_popcountll(words_busy);
     got.clear();
-    if (!take_work(E, busy, free_words * 64, got)) return LA3G_OK;
+    Ticket* solo = nullptr;
+    if (!take_work(E, busy, free_words * 64, got, &solo)) return LA3G_OK;
+    if (solo)
+    {
+      run_solo(E, solo);
+      continue;
+    }
     adm.clear();
     const double now = wall_ms();
     size_t k = 0;
@@ -804,7 +848,13 @@ int sssp_loop(Engine* E)
   for (;;)
   {
     got.clear();
-    if (!take_work(E, busy, L - busy, got)) return LA3G_OK;
+    Ticket* solo = nullptr;
+    if (!take_work(E, busy, L - busy, got, E->exact_lanes ? &solo : nullptr)) return LA3G_OK;
+    if (solo)
+    {
+      run_solo(E, solo);
+      continue;
+    }
     LA3G_TRY(admit(E, got, busy, adm));
     if (!adm.empty())
     {
@@ -1081,6 +1131,15 @@ extern "C" int la3g_server_info(la3g_server* S, la3g_server_stats* out)
   for (Engine* e : S->engines) pend += e->queue.size();
   out->queued = pend;
   out->pending = S->tickets.size();
+  return LA3G_OK;
+}
+
+extern "C" int la3g_server_set_solo(la3g_server* S, uint32_t bfs_depth, uint32_t sssp_depth)
+{
+  if (!S) return set_error(LA3G_EINVAL, "null server");
+  std::lock_guard<std::mutex> lk(S->mu);
+  S->solo_bfs = bfs_depth;
+  S->solo_sssp = sssp_depth;
   return LA3G_OK;
 }
 

@@ -24,13 +24,17 @@ def _roots(G, k, seed):
     return [int(x) for x in np.random.default_rng(seed).choice(cand, k)]
 
 
-@pytest.fixture
-def servers(gpu):
-    """Creates servers and frees them at teardown, before their graphs."""
+@pytest.fixture(params=["lanes", "adaptive"])
+def servers(gpu, request):
+    """Creates servers and frees them at teardown, before their graphs.  Every
+    test runs twice: lanes only (every query in a lane), and with adaptive
+    batching (queries arriving at an idle engine answered alone)."""
     made = []
 
     def make(*a, **k):
         S = gpu.Server(*a, **k)
+        if request.param == "lanes":
+            S.set_solo(0, 0)
         made.append(S)
         return S
 
