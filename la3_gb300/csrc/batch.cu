@@ -74,7 +74,6 @@ struct BatchScratch
   uint32_t* shub[2] = {nullptr, nullptr};    // pairs of high-degree vertices, N*W each
   uint32_t* shub_t0[2] = {nullptr, nullptr}; // their first task numbers
   uint32_t* reg_end = nullptr;
-  LanePullTasks pull;
   uint32_t max_w = 0;
   bool max_w_known = false;
 };
@@ -742,24 +741,10 @@ static int sssp_batch_chunk(la3g_graph* G, BatchScratch* b, const uint32_t* root
   k_bs_list<<<kSMs * 8, 256, 0, s>>>((uint64_t) N * W, W, g.out_ptr, b->reg_end, b->sfront[0], L[0]);
   LA3G_LAUNCHED();
   tls_launches++;
-  LA3G_TRY(lane_pull_tasks(G, &b->pull));
-  const uint32_t reg_in = b->pull.reg_in;
-  const uint32_t task_warps = std::min<uint32_t>(b->pull.n * W, kSMs * 8 * 8 / 4);
-  unsigned long long degsum = 0;
-  const double pdiv = lanes_pull_divisor();
   for (;;)
   {
     if (iters > 1000000) return set_error(LA3G_ETIMEOUT, "batched sssp did not converge");
     iters++;
-    if (iters > 1 && pdiv > 0 && (double) degsum * pdiv > (double) reg_in * W)
-    {
-      ProfileScope p("sssp_batch_pull", s, 0.0);
-      k_bs_pull<<<kSMs * 8, 256, 0, s>>>(g.in_ptr, g.in_col, g.in_w, g.nreg, R, W, b->sfront[cur],
-                                         b->sfront[cur ^ 1], b->smsg, b->sdist, b->pull.row, b->pull.b, b->pull.e,
-                                         b->pull.n, task_warps);
-      LA3G_LAUNCHED();
-    }
-    else
     {
       ProfileScope p("sssp_batch_relax", s, 0.0);
       k_bs_relax<<<kSMs * 16, 256, 0, s>>>(g.out_ptr, b->reg_end, g.out_row, g.out_w, R, W, b->sfront[cur], L[cur],
@@ -768,16 +753,14 @@ static int sssp_batch_chunk(la3g_graph* G, BatchScratch* b, const uint32_t* root
     }
     LA3G_CUDA(cudaMemsetAsync(b->ctr + (cur ^ 1), 0, 8, s));
     LA3G_CUDA(cudaMemsetAsync(b->ctr + 2 + (cur ^ 1), 0, 8, s));
-    LA3G_CUDA(cudaMemsetAsync(b->ctr + 4, 0, 8, s));
     k_bs_apply<<<kSMs * 8, 256, 0, s>>>(N, R, W, g.out_ptr, b->reg_end, b->sfront[cur ^ 1], b->sdist, b->smsg,
-                                        L[cur ^ 1], b->sfront[cur], L[cur], nullptr, b->ctr + 4);
+                                        L[cur ^ 1], b->sfront[cur], L[cur]);
     LA3G_LAUNCHED();
     tls_launches += 2;
-    unsigned long long act[5] = {0, 0, 0, 0, 0};
-    LA3G_CUDA(cudaMemcpyAsync(act, b->ctr, 5 * 8, cudaMemcpyDeviceToHost, s));
+    unsigned long long act[4] = {0, 0, 0, 0};
+    LA3G_CUDA(cudaMemcpyAsync(act, b->ctr, 4 * 8, cudaMemcpyDeviceToHost, s));
     LA3G_CUDA(cudaStreamSynchronize(s));
     cur ^= 1;
-    degsum = act[4];
     if (!act[cur] && !act[2 + cur]) break;
   }
   if (g.nsink)

@@ -359,7 +359,6 @@ struct Engine
   DevBuf vis, buf[2], hops, alive[2], active, ctr, adm, ret, mask, staging, fdeg;
   // SSSP
   DevBuf dist, msg, sfront[2], small[2], hub[2], hub_t0[2], reg_end, rpos;
-  LanePullTasks pull;
   unsigned long long* hctr = nullptr;  // pinned: counters + alive words
 };
 
@@ -840,11 +839,6 @@ int sssp_loop(Engine* E)
   int cur = 0;
   std::vector<Ticket*> got;
   std::vector<uint32_t> adm, fin;
-  LA3G_TRY(lane_pull_tasks(E->G, &E->pull));
-  const uint32_t reg_in = E->pull.reg_in;
-  const uint32_t task_warps = std::min<uint32_t>(E->pull.n * W, kSMs * 8 * 8 / 4);
-  unsigned long long degsum = 0;  // out-degree sum of the active pairs (from the last apply)
-  const double pdiv = lanes_pull_divisor();
   for (;;)
   {
     got.clear();
@@ -868,19 +862,8 @@ int sssp_loop(Engine* E)
       tls_launches++;
     }
     if (busy == 0) continue;
-    // one BSP step for every occupied lane: push while the active pairs'
-    // edges are few, pull otherwise (the same result either way)
+    // one relaxation step for every occupied lane
     LA3G_CUDA(cudaMemsetAsync(E->alive[0].p, 0, W * 8, s));
-    if (pdiv > 0 && (double) degsum * pdiv > (double) reg_in * W)
-    {
-      ProfileScope p("serve_sssp_pull", s, 0.0);
-      k_bs_pull<<<kSMs * 8, 256, 0, s>>>(g.in_ptr, g.in_col, g.in_w, g.nreg, L, W, E->sfront[cur].as<uint64_t>(),
-                                         E->sfront[cur ^ 1].as<uint64_t>(), E->msg.as<uint32_t>(),
-                                         E->dist.as<uint32_t>(), E->pull.row, E->pull.b, E->pull.e, E->pull.n,
-                                         task_warps);
-      LA3G_LAUNCHED();
-    }
-    else
     {
       ProfileScope p("serve_sssp_relax", s, 0.0);
       k_bs_relax<<<kSMs * 16, 256, 0, s>>>(g.out_ptr, E->reg_end.as<uint32_t>(), g.out_row, g.out_w, L, W,
@@ -890,14 +873,12 @@ int sssp_loop(Engine* E)
     }
     LA3G_CUDA(cudaMemsetAsync(ctr + (cur ^ 1), 0, 8, s));
     LA3G_CUDA(cudaMemsetAsync(ctr + 2 + (cur ^ 1), 0, 8, s));
-    LA3G_CUDA(cudaMemsetAsync(ctr + 4, 0, 8, s));
     k_bs_apply<<<kSMs * 8, 256, 0, s>>>(N, L, W, g.out_ptr, E->reg_end.as<uint32_t>(), E->sfront[cur ^ 1].as<uint64_t>(),
                                         E->dist.as<uint32_t>(), E->msg.as<uint32_t>(), PL[cur ^ 1],
-                                        E->sfront[cur].as<uint64_t>(), PL[cur], E->alive[0].as<uint64_t>(), ctr + 4);
+                                        E->sfront[cur].as<uint64_t>(), PL[cur], E->alive[0].as<uint64_t>());
     LA3G_LAUNCHED();
     tls_launches += 2;
     LA3G_CUDA(cudaMemcpyAsync(E->hctr, E->alive[0].p, W * 8, cudaMemcpyDeviceToHost, s));
-    LA3G_CUDA(cudaMemcpyAsync(&degsum, ctr + 4, 8, cudaMemcpyDeviceToHost, s));
     LA3G_CUDA(cudaStreamSynchronize(s));
     cur ^= 1;
     fin.clear();

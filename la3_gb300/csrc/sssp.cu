@@ -329,18 +329,9 @@ __global__ void k_sssp_long_rows(const uint32_t* __restrict__ ptr, const uint32_
   }
 }
 
-// Frontier degree sums above this fraction of the regular rows' in-edges
-// pull (LA3G_SSSP_PULL overrides the divisor, for tuning; 0 = never pull).
-static double sssp_pull_divisor()
-{
-  static double d = -1;
-  if (d < 0)
-  {
-    const char* e = std::getenv("LA3G_SSSP_PULL");
-    d = e ? std::atof(e) : 4.0;
-  }
-  return d;
-}
+// A step pulls when its frontier's out-degree sum exceeds the regular rows'
+// in-edges / kPullDivisor (measured on R-MAT s22: 2 and 4 are best).
+static constexpr double kPullDivisor = 4.0;
 
 // Sink pass: y = min over in-neighbours (regular: final dist; the root if it
 // is a source: its message 0) of msg + w; dist = min(dist, y).
@@ -498,8 +489,7 @@ static int sssp_run(la3g_graph* G, SsspScratch* ss, uint32_t root, la3g_stats* s
     iter++;
     if (nsmall + nbig == 0) break;
     LA3G_CUDA(cudaMemsetAsync(ss->ctr, 0, 4 * sizeof(unsigned long long), s));
-    const double pdiv = sssp_pull_divisor();
-    if (iter > 1 && pdiv > 0 && ss->max_w <= 0x80000000u && (double) front_deg * pdiv > (double) ss->reg_in)
+    if (iter > 1 && ss->max_w <= 0x80000000u && (double) front_deg * kPullDivisor > (double) ss->reg_in)
     {
       // in-edges of every regular row (index + weight), stamps and
       // messages of their columns, one dist read per row

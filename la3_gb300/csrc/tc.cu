@@ -31,6 +31,7 @@ namespace la3g {
 
 static constexpr uint32_t kTcCap = 1024;     // N+(x) held in shared memory up to this length
 static constexpr uint32_t kTcSmall = 192;    // lists up to this length use the high-occupancy variant
+static constexpr uint32_t kTcWalkFactor = 16;  // heavy x: N+(y) is walked unless > 16 |N+(x)| (then searched)
 static constexpr uint32_t kTcHubMin = 32;    // N+(y) longer than this (and than N+(x)) is a hub list:
 static constexpr uint32_t kTcHubCap = 1024;  // ... small x's pairs with it go to the hub kernel, up to this length
 
@@ -264,52 +265,6 @@ __device__ __forceinline__ void tc_insert_t(uint32_t* key, IDX* idx, int lg, uin
   uint32_t sl = tc_slot(w, lg);
   while (atomicCAS(&key[sl], kEmpty, w) != kEmpty) sl = (sl + 1) & mask;
   idx[sl] = (IDX) j;
-}
-
-// One warp per vertex x (fetched dynamically, heaviest first) with
-// |N+(x)| <= CAP; the warp's lanes form groups of G.
-template <uint32_t CAP, int WARPS, int G>
-__global__ void __launch_bounds__(WARPS * 32)
-k_tc_rank(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ order,
-          uint32_t norder, unsigned int* next, uint32_t* ntri, uint32_t walk_factor)
-{
-  constexpr uint32_t H = tc_pow2(2 * CAP);
-  static_assert(CAP < 256, "uint8 indexes");
-  __shared__ uint32_t s_L[WARPS][CAP], s_C[WARPS][CAP], s_key[WARPS][H];
-  __shared__ uint8_t s_idx[WARPS][H];
-  __shared__ uint32_t s_x[WARPS];
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  uint32_t* L = s_L[wib];
-  uint32_t* Cn = s_C[wib];
-  uint32_t* key = s_key[wib];
-  uint8_t* idx = s_idx[wib];
-  for (;;)
-  {
-    uint32_t k = 0;
-    if (lane == 0) k = atomicAdd(next, 1u);
-    k = __shfl_sync(0xffffffffu, k, 0);
-    if (k >= norder) break;
-    const uint32_t x = order[k];
-    const uint32_t xb = ptr[x], d = ptr[x + 1] - xb;
-    const int lg = tc_lg(d);
-    for (uint32_t i = lane; i < (1u << lg); i += 32) key[i] = kEmpty;
-    if (lane == 0) s_x[wib] = 0;
-    __syncwarp();
-    for (uint32_t j = lane; j < d; j += 32)
-    {
-      const uint32_t y = col[xb + j];
-      L[j] = y;
-      Cn[j] = 0;
-      tc_insert_t(key, idx, lg, y, j);
-    }
-    __syncwarp();
-    tc_walk<G>(x, d, L, Cn, key, idx, lg, &s_x[wib], ptr, col, walk_factor, lane / G, 32 / G, lane % G);
-    __syncwarp();
-    for (uint32_t j = lane; j < d; j += 32)
-      if (Cn[j]) atomicAdd(&ntri[L[j]], Cn[j]);
-    if (lane == 0 && s_x[wib]) atomicAdd(&ntri[x], s_x[wib]);
-    __syncwarp();
-  }
 }
 
 __device__ __forceinline__ uint32_t lower_bound_s(const uint32_t* s, uint32_t n, uint32_t key)
@@ -703,35 +658,6 @@ __global__ void k_tc_sum(uint32_t N, const uint32_t* __restrict__ ntri, unsigned
   if ((threadIdx.x & 31) == 0 && s) atomicAdd(total, s);
 }
 
-// N+(y) is walked unless it is longer than this many times |N+(x)|
-// (LA3G_TC_WALK overrides it, for tuning).
-static uint32_t tc_walk_factor()
-{
-  static uint32_t f = 0;
-  if (!f)
-  {
-    const char* e = std::getenv("LA3G_TC_WALK");
-    f = e ? (uint32_t) std::max(1, std::atoi(e)) : 16u;
-  }
-  return f;
-}
-
-// Lane-group sizes of the two kernels (LA3G_TC_GROUPS="small,mid"
-// overrides them, for tuning).
-static int tc_variant(int which)
-{
-  static int g[2] = {0, 0};
-  static bool init = false;
-  if (!init)
-  {
-    init = true;
-    g[0] = 0;  // 0: the flattened kernel
-    g[1] = 32;
-    if (const char* e = std::getenv("LA3G_TC_GROUPS")) std::sscanf(e, "%d,%d", &g[0], &g[1]);
-  }
-  return g[which];
-}
-
 static int tc_prepare(la3g_graph* G, TcScratch* ts)
 {
   DevGraph& g = G->g;
@@ -891,37 +817,20 @@ extern "C" int la3g_tc(la3g_graph* G, uint64_t* total_out, uint32_t* per_vertex_
   LA3G_CUDA(cudaMemsetAsync(ts->ntri, 0, (size_t) N * 4, s));
   LA3G_CUDA(cudaMemsetAsync(ts->total, 0, 8, s));
   LA3G_CUDA(cudaMemsetAsync(ts->next, 0, 16, s));
-  const uint32_t wf = tc_walk_factor();
   if (ts->nmid)
   {
     // list reads (N+(x) once, N+(y) per oriented edge) + the x's two offsets
     ProfileScope p("tc_rank_mid", s, 4.0 * ts->work_mid + 8.0 * ts->nmid);
-    if (tc_variant(1) == 16)
-      k_tc_rank_block<kTcCap, 256, 16><<<kSMs * 8, 256, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->order_mid, ts->nmid,
-                                                                ts->next + 1, ts->ntri, wf);
-    else
-      k_tc_rank_block<kTcCap, 256, 32><<<kSMs * 8, 256, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->order_mid, ts->nmid,
-                                                                ts->next + 1, ts->ntri, wf);
+    k_tc_rank_block<kTcCap, 256, 32><<<kSMs * 8, 256, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->order_mid, ts->nmid,
+                                                              ts->next + 1, ts->ntri, kTcWalkFactor);
     LA3G_LAUNCHED();
   }
   if (ts->norder)
   {
     ProfileScope p("tc_rank", s, 4.0 * (ts->work - ts->work_mid - ts->work_big) + 8.0 * ts->norder);
-    switch (tc_variant(0))
-    {
-      case 8:
-        k_tc_rank<kTcSmall, 8, 8><<<kSMs * 6, 256, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->order, ts->norder,
-                                                            ts->next, ts->ntri, wf);
-        break;
-      case 32:
-        k_tc_rank<kTcSmall, 8, 32><<<kSMs * 6, 256, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->order, ts->norder,
-                                                             ts->next, ts->ntri, wf);
-        break;
-      default:
-        // short lists: the flattened walk keeps all 32 lanes busy across the y's
-        k_tc_rank_flat<kTcSmall, 8><<<kSMs * 8, 8 * 32, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->order, ts->norder,
-                                                                ts->next, ts->ntri);
-    }
+    // short lists: the flattened walk keeps all 32 lanes busy across the y's
+    k_tc_rank_flat<kTcSmall, 8><<<kSMs * 8, 8 * 32, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->order, ts->norder, ts->next,
+                                                            ts->ntri);
     LA3G_LAUNCHED();
   }
   if (ts->nhubs)
