@@ -782,6 +782,27 @@ def serve_line(args, rank, world, local) -> dict | None:
         t_end = time.perf_counter() - t0
         return {"qps": n / t_end, "p50_ms": _pct(lat, 50), "p99_ms": _pct(lat, 99)}
 
+    # BM25 alone: device time per query and the term kernel's algorithmic
+    # GB/s (postings' doc id + tf, touched docs' K(d) and score) vs the peak
+    bm_q = [sorted(set(int(D + 1 + t) for t in rng.choice(T, int(rng.integers(2, 9)), p=zipf_w))) for _ in range(300)]
+    for q in bm_q[:20]:
+        bm.query(q, 10)
+    L.profile_reset()
+    L.profile(True)
+    bm_ms, bm_post = [], 0
+    for q in bm_q:
+        _, _, _, st = bm.query(q, 10)
+        bm_ms.append(st.device_ms)
+        bm_post += st.edges_examined
+    L.profile(False)
+    prof = L.profile_report().get("bm25_term", {"ms": 0.0, "bytes": 0.0, "launches": 0})
+    peaks = measured_peaks()
+    bm25_gbs = prof["bytes"] / (prof["ms"] / 1e3) / 1e9 if prof["ms"] else None
+    bm25 = {"queries": len(bm_q), "device_ms_mean": statistics.mean(bm_ms), "device_ms_p50": _pct(bm_ms, 50),
+            "postings_per_query": bm_post / len(bm_q), "term_kernel_gbs": bm25_gbs,
+            "term_kernel_frac": (bm25_gbs / peaks["hbm_gbs"]) if bm25_gbs else None,
+            "term_kernel_launches": prof["launches"]}
+
     # warm both arms (allocations, first launches)
     arr, qs = make_stream(2000.0, 200)
     served(arr, qs)
@@ -807,6 +828,7 @@ def serve_line(args, rank, world, local) -> dict | None:
         "config": {"workload": f"served stream: BFS/SSSP over R-MAT s{scales[0]}/s{scales[1]}/s{scales[2]} + BM25 "
                                f"top-10 over {D} docs x {T} terms ({postings} postings); Poisson arrivals",
                    "rates": results, "lanes": lanes, "hbm_budget_bytes": budget, "hbm_used_bytes": info["used_bytes"],
+                   "bm25_alone": bm25,
                    "setup_s": round(setup_s, 1),
                    "p50_ms_at_top_rate": top["served"]["p50_ms"], "p99_ms_at_top_rate": top["served"]["p99_ms"]},
         "e2e": None, "clocks": clocks.summary(),

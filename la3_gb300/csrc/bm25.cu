@@ -143,6 +143,7 @@ __global__ void k_bm25_term(const uint32_t* __restrict__ ptr, const uint32_t* __
   const uint32_t t = qpos[1 + j];                          // j-th smallest pushed index
   const float idf = __uint_as_float(qpos[1 + nq + j]);     // value of slot j
   const uint32_t b = ptr[t], e = ptr[t + 1];
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ctr[2], (unsigned long long) (e - b));  // postings walked
   const float k1p1 = __fadd_rn(kK1, 1.0f);
   for (uint32_t i = b + blockIdx.x * blockDim.x + threadIdx.x; i < e; i += gridDim.x * blockDim.x)
   {
@@ -382,6 +383,7 @@ extern "C" int la3g_bm25_query(la3g_graph* G, const uint32_t* term_vids, uint32_
   T.device_begin();
   if (nterms) LA3G_CUDA(cudaMemcpyAsync(b->qin, term_vids, (size_t) nterms * 4, cudaMemcpyHostToDevice, s));
   LA3G_CUDA(cudaMemsetAsync(b->ctr, 0, 8, s));
+  LA3G_CUDA(cudaMemsetAsync(b->ctr + 2, 0, 8, s));
   LA3G_CUDA(cudaMemsetAsync(b->qpos, 0, 4, s));
   if (nterms)
   {
@@ -407,8 +409,9 @@ extern "C" int la3g_bm25_query(la3g_graph* G, const uint32_t* term_vids, uint32_
     tls_launches += 2;
   }
   T.device_end();
-  unsigned long long ntouched = 0;
+  unsigned long long ntouched = 0, postings = 0;
   LA3G_CUDA(cudaMemcpyAsync(&ntouched, b->ctr, 8, cudaMemcpyDeviceToHost, s));
+  LA3G_CUDA(cudaMemcpyAsync(&postings, b->ctr + 2, 8, cudaMemcpyDeviceToHost, s));
   unsigned long long best[kTopKMax];
   if (kk > 0) LA3G_CUDA(cudaMemcpyAsync(best, b->best, (size_t) kk * 8, cudaMemcpyDeviceToHost, s));
   if (all_scores_out || active_out)
@@ -434,10 +437,16 @@ extern "C" int la3g_bm25_query(la3g_graph* G, const uint32_t* term_vids, uint32_
     if (scores_out) scores_out[i] = sc;
   }
   if (nout) *nout = n;
+  // algorithmic bytes: doc id + tf per posting walked, K(d) read and score
+  // written per touched doc, the top-k pass over the touched docs
+  const double bytes = 8.0 * (double) postings + 12.0 * (double) ntouched;
+  profile_add_bytes("bm25_term", bytes);
   if (st)
   {
     st->iterations = 1;
     st->teps_edges = ntouched;
+    st->edges_examined = postings;
+    st->algo_bytes = (uint64_t) bytes;
   }
   return LA3G_OK;
 }

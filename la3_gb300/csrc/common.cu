@@ -88,6 +88,13 @@ ProfileScope::~ProfileScope()
   k.bytes += bytes;
 }
 
+void profile_add_bytes(const char* name, double bytes)
+{
+  if (!prof_on) return;
+  std::lock_guard<std::mutex> lock(prof_mu);
+  prof_table[name].bytes += bytes;
+}
+
 CallTimer::CallTimer(la3g_graph* G_, la3g_stats* st_) : G(G_), st(st_), t0(now_ms()), launches0(tls_launches)
 {
   if (st) std::memset(st, 0, sizeof *st);

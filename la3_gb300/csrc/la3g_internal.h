@@ -92,6 +92,10 @@ struct ProfileScope
   ~ProfileScope();
 };
 
+// Adds algorithmic bytes to a kernel's profile entry when they are known
+// only after its launches (e.g. from a count the kernels produced).
+void profile_add_bytes(const char* name, double bytes);
+
 extern thread_local uint32_t tls_launches;
 
 // Scoped device buffer for temporaries.
