@@ -49,6 +49,7 @@ struct Bm25Scratch
   unsigned long long* cand = nullptr;  // kTopBlocks * kTopKMax candidates
   unsigned long long* best = nullptr;  // kTopKMax
   uint32_t qcap = 0;
+  uint32_t term_row0 = 0;       // first regular position of a term (docs come first)
   uint32_t query_id = 0;
   uint64_t tokens = 0;
   float avg = 0.0f;
@@ -133,10 +134,13 @@ __global__ void k_bm25_pair(const uint32_t* __restrict__ q, uint32_t nq, uint32_
 
 // One term: every doc of the term adds its contribution; a doc appears once
 // per term, so there are no races inside a launch.
+// gather reads the row's mirror state, taken when the TFIDF program was
+// first initialised: docs hold K(d); terms (not active then) hold zero.  A
+// term row is reached only by a query that names a document vertex.
 __global__ void k_bm25_term(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col,
                             const uint32_t* __restrict__ w, const uint32_t* __restrict__ qpos, uint32_t nq,
-                            uint32_t j, const float* __restrict__ length, float* score, uint32_t* stamp,
-                            uint32_t qid, uint32_t* touched, unsigned long long* ctr)
+                            uint32_t j, const float* __restrict__ length, uint32_t term_row0, float* score,
+                            uint32_t* stamp, uint32_t qid, uint32_t* touched, unsigned long long* ctr)
 {
   const uint32_t cnt = qpos[0];
   if (j >= cnt) return;
@@ -149,7 +153,8 @@ __global__ void k_bm25_term(const uint32_t* __restrict__ ptr, const uint32_t* __
   {
     const uint32_t d = col[i];
     const float wf = (float) w[i];
-    const float c = __fmul_rn(__fdiv_rn(__fmul_rn(wf, k1p1), __fadd_rn(wf, length[d])), idf);
+    const float kd = d < term_row0 ? length[d] : 0.0f;
+    const float c = __fmul_rn(__fdiv_rn(__fmul_rn(wf, k1p1), __fadd_rn(wf, kd)), idf);
     if (stamp[d] != qid)
     {
       stamp[d] = qid;
@@ -314,6 +319,7 @@ extern "C" int la3g_bm25_prepare(la3g_graph* G, uint64_t* ntokens_out, float* av
   LA3G_CUDA(cudaStreamSynchronize(s));
   uint32_t tb = 0;
   LA3G_TRY(first_term_row(G, &tb));
+  b->term_row0 = tb;
   LA3G_CUDA(cudaMemsetAsync(b->length, 0, (size_t) N * 4, s));
   LA3G_CUDA(cudaMemsetAsync(b->ctr, 0, 4 * 8, s));
   {
@@ -368,7 +374,7 @@ extern "C" int la3g_bm25_query(la3g_graph* G, const uint32_t* term_vids, uint32_
   cudaStream_t s = G->stream;
   const uint32_t N = g.nslots;
   CallTimer T(G, st);
-  if (nterms > b->qcap)
+  if (nterms > b->qcap || !b->qpos)
   {
     uint32_t cap = std::max<uint32_t>(64, nterms);
     LA3G_TRY(galloc(G, &b->qin, cap));
@@ -395,8 +401,8 @@ extern "C" int la3g_bm25_query(la3g_graph* G, const uint32_t* term_vids, uint32_
   for (uint32_t j = 0; j < nterms; j++)
   {
     ProfileScope p("bm25_term", s, 0.0);
-    k_bm25_term<<<kSMs * 4, 256, 0, s>>>(g.in_ptr, g.in_col, g.in_w, b->qpos, nterms, j, b->length, b->score,
-                                        b->stamp, b->query_id, b->touched, b->ctr);
+    k_bm25_term<<<kSMs * 4, 256, 0, s>>>(g.in_ptr, g.in_col, g.in_w, b->qpos, nterms, j, b->length, b->term_row0,
+                                        b->score, b->stamp, b->query_id, b->touched, b->ctr);
     LA3G_LAUNCHED();
   }
   const int kk = (int) k;
