@@ -83,3 +83,22 @@ def test_bm25_degenerate_queries(gpu, oracle, tmp_path):
         ids, sc, _, _ = b.query(q, k)
         oids, osc, _, _ = ob.query(q, k)
         assert ids.tolist() == oids.tolist() and np.array_equal(sc, osc), (q, k)
+
+
+def test_header_format_matches_plain(gpu, tmp_path):
+    """n = 0 takes the vertex count from the 16-byte header
+    (graph.hpp:89-117); the graph equals the headerless one with n given."""
+    L = gpu
+    e = L.EdgeList.rmat(10, 8, seed=12, weighted=True, wseed=13)
+    ph, pp = tmp_path / "h.bin", tmp_path / "p.bin"
+    e.write(ph, header=True)
+    e.write(pp, header=False)
+    n = 1 << 10
+    a = L.Graph.load_directed(ph, 0, weighted=True)
+    b = L.Graph.load_directed(pp, n, weighted=True)
+    assert a.nslots == b.nslots == n + 1
+    assert a.info.nentries == b.info.nentries
+    assert np.array_equal(L.sssp(a, 3)[0], L.sssp(b, 3)[0])
+    au = L.Graph.load_undirected(ph, 0, weighted=True)
+    bu = L.Graph.load_undirected(pp, n, weighted=True)
+    assert np.array_equal(L.bfs(au, 3)[0], L.bfs(bu, 3)[0])
