@@ -37,39 +37,62 @@ static __device__ __forceinline__ void bs_list_pair(uint32_t i, uint32_t deg, co
 // Relaxes edges [k0, k1) of the vertex of pair i: lane l handles roots
 // 64w + l and 64w + l + 32, so the distances of one edge's target are read
 // contiguously; the roots an edge improved are ORed into the target's
-// next-frontier word at once.
+// next-frontier word at once.  Edges go 8 at a time (targets and weights
+// loaded by 8 lanes and broadcast) so that up to 16 target reads per lane are
+// in flight.  A root's bit is set when its candidate is below the distance
+// read through L2: distances only fall, so that read is at most the value
+// the iteration started with and the bit means "lowered in this iteration",
+// exactly as an atomic's returned old value would; the minimum itself is
+// therefore a reduction whose result nobody waits for.
 static __device__ __forceinline__ void bs_relax_range(uint32_t i, uint32_t k0, uint32_t k1, int lane, uint32_t R, uint32_t W,
                                                const uint32_t* __restrict__ row, const uint32_t* __restrict__ wgt,
                                                const uint64_t* __restrict__ front, uint64_t* next,
                                                const uint32_t* __restrict__ msg, uint32_t* dist)
 {
+  constexpr int G = 8;
   const uint32_t u = i / W, w = i % W;
   const uint64_t f = front[i];
   const uint32_t r0 = w * 64 + lane, r1 = r0 + 32;
   const bool h0 = (f >> lane) & 1ull, h1 = (f >> (lane + 32)) & 1ull;
   const uint32_t m0 = h0 ? msg[(uint64_t) u * R + r0] : 0, m1 = h1 ? msg[(uint64_t) u * R + r1] : 0;
-  for (uint32_t k = k0; k < k1; k++)
+  for (uint32_t kb = k0; kb < k1; kb += G)
   {
-    const uint32_t v = row[k], wt = wgt[k];
-    bool i0 = false, i1 = false;
-    if (h0)
+    const uint32_t cnt = min((uint32_t) G, k1 - kb);
+    uint32_t lv = 0, lw = 0;
+    if ((uint32_t) lane < cnt)
     {
-      const uint32_t cand = m0 + wt;
-      uint32_t* p = &dist[(uint64_t) v * R + r0];
-      i0 = cand < *p && cand < atomicMin(p, cand);
+      lv = row[kb + lane];
+      lw = wgt[kb + lane];
     }
-    if (h1)
+    uint32_t v[G];
+#pragma unroll
+    for (int j = 0; j < G; j++) v[j] = __shfl_sync(0xffffffffu, lv, j);
+    uint32_t d0[G], d1[G];
+#pragma unroll
+    for (int j = 0; j < G; j++)
     {
-      const uint32_t cand = m1 + wt;
-      uint32_t* p = &dist[(uint64_t) v * R + r1];
-      i1 = cand < *p && cand < atomicMin(p, cand);
+      const bool live = (uint32_t) j < cnt;
+      d0[j] = live && h0 ? __ldcg(&dist[(uint64_t) v[j] * R + r0]) : 0u;
+      d1[j] = live && h1 ? __ldcg(&dist[(uint64_t) v[j] * R + r1]) : 0u;
     }
-    const uint64_t mask = (uint64_t) __ballot_sync(0xffffffffu, i0) | ((uint64_t) __ballot_sync(0xffffffffu, i1) << 32);
-    if (lane == 0 && mask) atomicOr((unsigned long long*) &next[(uint64_t) v * W + w], (unsigned long long) mask);
+    // lane j keeps edge j's new bits and ORs them into next once
+    uint64_t mine = 0;
+#pragma unroll
+    for (int j = 0; j < G; j++)
+    {
+      if ((uint32_t) j >= cnt) break;
+      const uint32_t wt = __shfl_sync(0xffffffffu, lw, j), c0 = m0 + wt, c1 = m1 + wt;
+      const bool i0 = h0 && c0 < d0[j], i1 = h1 && c1 < d1[j];
+      if (i0) atomicMin(&dist[(uint64_t) v[j] * R + r0], c0);
+      if (i1) atomicMin(&dist[(uint64_t) v[j] * R + r1], c1);
+      const uint64_t mask = (uint64_t) __ballot_sync(0xffffffffu, i0) | ((uint64_t) __ballot_sync(0xffffffffu, i1) << 32);
+      if (lane == j) mine = mask;
+    }
+    if (mine) atomicOr((unsigned long long*) &next[(uint64_t) lv * W + w], (unsigned long long) mine);
   }
 }
 
-static __global__ void __launch_bounds__(256)
+static __global__ void __launch_bounds__(256, 4)
 k_bs_relax(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ reg_end, const uint32_t* __restrict__ row,
            const uint32_t* __restrict__ wgt, uint32_t R, uint32_t W, const uint64_t* __restrict__ front, PairList L,
            uint64_t* next, const uint32_t* __restrict__ msg, uint32_t* dist)
@@ -128,15 +151,6 @@ static __global__ void k_bs_apply(uint32_t N, uint32_t R, uint32_t W, const uint
   }
 }
 
-// Pull step over (regular vertex, word) pairs, for large frontiers: one warp
-// per pair, lane l holding roots 64w + l and 64w + l + 32.  For each
-// in-edge (u, v) whose frontier word has bits, every lane whose root is in
-// u's frontier takes msg(u) + weight; the pair's new bits (roots lowered)
-// are written to next directly (each pair has one writer), so no atomics are
-// needed.  Edges go 8 at a time (indices, weights and frontier words loaded
-// by 8 lanes and broadcast), so each lane has up to 16 independent message
-// loads in flight.  The result per (vertex, root) is the min over the same
-// messages a push step relaxes, so both directions give the same iteration.
 // Initial active list: the nonzero words of the root frontier.
 static __global__ void k_bs_list(uint64_t NW, uint32_t W, const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ reg_end,
                           const uint64_t* __restrict__ front, PairList out)
