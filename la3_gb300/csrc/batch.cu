@@ -68,7 +68,6 @@ struct BatchScratch
   // SSSP
   uint32_t cap_sr = 0;
   uint32_t* sdist = nullptr;   // [N][R]
-  uint32_t* smsg = nullptr;    // [N][R]
   uint64_t* sfront[2] = {nullptr, nullptr};  // [N][W]
   uint32_t* sact[2] = {nullptr, nullptr};    // active (vertex, word) pairs, N*W each
   uint32_t* shub[2] = {nullptr, nullptr};    // pairs of high-degree vertices, N*W each
@@ -535,14 +534,13 @@ __global__ void k_bs_init(uint64_t n, uint32_t* dist, uint64_t nw, uint64_t* f0,
 }
 
 __global__ void k_bs_roots(const uint32_t* __restrict__ rpos, uint32_t R, uint32_t N, uint32_t W, uint32_t nreg,
-                           uint32_t src_base, uint32_t iso_base, uint32_t* dist, uint32_t* msg, uint64_t* front)
+                           uint32_t src_base, uint32_t iso_base, uint32_t* dist, uint64_t* front)
 {
   for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < R; r += gridDim.x * blockDim.x)
   {
     const uint32_t p = rpos[r];
     if (p >= N) continue;
     dist[(uint64_t) p * R + r] = 0;
-    msg[(uint64_t) p * R + r] = 0;
     if (p < nreg || (p >= src_base && p < iso_base))
       atomicOr((unsigned long long*) &front[(uint64_t) p * W + r / 64], 1ull << (r % 64));
   }
@@ -710,7 +708,6 @@ static int sssp_batch_chunk(la3g_graph* G, BatchScratch* b, const uint32_t* root
   if (R > b->cap_sr)
   {
     LA3G_TRY(galloc(G, &b->sdist, (size_t) N * R));
-    LA3G_TRY(galloc(G, &b->smsg, (size_t) N * R));
     LA3G_TRY(galloc(G, &b->sfront[0], (size_t) N * W));
     LA3G_TRY(galloc(G, &b->sfront[1], (size_t) N * W));
     LA3G_TRY(galloc(G, &b->sact[0], (size_t) N * W));
@@ -727,7 +724,7 @@ static int sssp_batch_chunk(la3g_graph* G, BatchScratch* b, const uint32_t* root
   LA3G_LAUNCHED();
   k_bs_init<<<kSMs * 8, 256, 0, s>>>((uint64_t) N * R, b->sdist, (uint64_t) N * W, b->sfront[0], b->sfront[1]);
   LA3G_LAUNCHED();
-  k_bs_roots<<<grid_for(R, 256), 256, 0, s>>>(b->rpos, R, N, W, g.nreg, g.src_base(), g.iso_base(), b->sdist, b->smsg,
+  k_bs_roots<<<grid_for(R, 256), 256, 0, s>>>(b->rpos, R, N, W, g.nreg, g.src_base(), g.iso_base(), b->sdist,
                                               b->sfront[0]);
   LA3G_LAUNCHED();
   tls_launches += 3;
@@ -748,13 +745,13 @@ static int sssp_batch_chunk(la3g_graph* G, BatchScratch* b, const uint32_t* root
     {
       ProfileScope p("sssp_batch_relax", s, 0.0);
       k_bs_relax<<<kSMs * 16, 256, 0, s>>>(g.out_ptr, b->reg_end, g.out_row, g.out_w, R, W, b->sfront[cur], L[cur],
-                                           b->sfront[cur ^ 1], b->smsg, b->sdist);
+                                           b->sfront[cur ^ 1], b->sdist);
       LA3G_LAUNCHED();
     }
     LA3G_CUDA(cudaMemsetAsync(b->ctr + (cur ^ 1), 0, 8, s));
     LA3G_CUDA(cudaMemsetAsync(b->ctr + 2 + (cur ^ 1), 0, 8, s));
-    k_bs_apply<<<kSMs * 8, 256, 0, s>>>(N, R, W, g.out_ptr, b->reg_end, b->sfront[cur ^ 1], b->sdist, b->smsg,
-                                        L[cur ^ 1], b->sfront[cur], L[cur]);
+    k_bs_apply<<<kSMs * 8, 256, 0, s>>>(N, W, g.out_ptr, b->reg_end, b->sfront[cur ^ 1], L[cur ^ 1], b->sfront[cur],
+                                        L[cur]);
     LA3G_LAUNCHED();
     tls_launches += 2;
     unsigned long long act[4] = {0, 0, 0, 0};

@@ -37,7 +37,11 @@ static __device__ __forceinline__ void bs_list_pair(uint32_t i, uint32_t deg, co
 // Relaxes edges [k0, k1) of the vertex of pair i: lane l handles roots
 // 64w + l and 64w + l + 32, so the distances of one edge's target are read
 // contiguously; the roots an edge improved are ORed into the target's
-// next-frontier word at once.  Edges go 8 at a time (targets and weights
+// next-frontier word at once.  A source's distances are read when its pair is
+// taken, not as of the iteration's start: a value lowered earlier in the same
+// iteration reaches its targets at once (Gauss-Seidel order), and the source
+// is in the next frontier anyway.  Every order of relaxation ends at the same
+// shortest distances.  Edges go 8 at a time (targets and weights
 // loaded by 8 lanes and broadcast) so that up to 16 target reads per lane are
 // in flight.  A root's bit is set when its candidate is below the distance
 // read through L2: distances only fall, so that read is at most the value
@@ -46,15 +50,14 @@ static __device__ __forceinline__ void bs_list_pair(uint32_t i, uint32_t deg, co
 // therefore a reduction whose result nobody waits for.
 static __device__ __forceinline__ void bs_relax_range(uint32_t i, uint32_t k0, uint32_t k1, int lane, uint32_t R, uint32_t W,
                                                const uint32_t* __restrict__ row, const uint32_t* __restrict__ wgt,
-                                               const uint64_t* __restrict__ front, uint64_t* next,
-                                               const uint32_t* __restrict__ msg, uint32_t* dist)
+                                               const uint64_t* __restrict__ front, uint64_t* next, uint32_t* dist)
 {
   constexpr int G = 8;
   const uint32_t u = i / W, w = i % W;
   const uint64_t f = front[i];
   const uint32_t r0 = w * 64 + lane, r1 = r0 + 32;
   const bool h0 = (f >> lane) & 1ull, h1 = (f >> (lane + 32)) & 1ull;
-  const uint32_t m0 = h0 ? msg[(uint64_t) u * R + r0] : 0, m1 = h1 ? msg[(uint64_t) u * R + r1] : 0;
+  const uint32_t m0 = h0 ? __ldcg(&dist[(uint64_t) u * R + r0]) : 0, m1 = h1 ? __ldcg(&dist[(uint64_t) u * R + r1]) : 0;
   for (uint32_t kb = k0; kb < k1; kb += G)
   {
     const uint32_t cnt = min((uint32_t) G, k1 - kb);
@@ -95,7 +98,7 @@ static __device__ __forceinline__ void bs_relax_range(uint32_t i, uint32_t k0, u
 static __global__ void __launch_bounds__(256, 4)
 k_bs_relax(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ reg_end, const uint32_t* __restrict__ row,
            const uint32_t* __restrict__ wgt, uint32_t R, uint32_t W, const uint64_t* __restrict__ front, PairList L,
-           uint64_t* next, const uint32_t* __restrict__ msg, uint32_t* dist)
+           uint64_t* next, uint32_t* dist)
 {
   const int lane = threadIdx.x & 31;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -110,24 +113,23 @@ k_bs_relax(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ reg_en
       const uint32_t slot = hub_of_task(L.hub_t0, nbig, a);
       const uint32_t i = L.hub[slot], u = i / W;
       const uint32_t k0 = ptr[u] + (a - L.hub_t0[slot]) * kHubTask;
-      bs_relax_range(i, k0, min(k0 + kHubTask, reg_end[u]), lane, R, W, row, wgt, front, next, msg, dist);
+      bs_relax_range(i, k0, min(k0 + kHubTask, reg_end[u]), lane, R, W, row, wgt, front, next, dist);
     }
     else
     {
       const uint32_t i = L.small[a - ntasks], u = i / W;
-      bs_relax_range(i, ptr[u], reg_end[u], lane, R, W, row, wgt, front, next, msg, dist);
+      bs_relax_range(i, ptr[u], reg_end[u], lane, R, W, row, wgt, front, next, dist);
     }
   }
 }
 
 // After a relaxation: the old frontier words are cleared (they become the
-// next "next" buffer); messages = current distances of the newly lowered
-// roots; the words holding them form the next active list.  alive (W words,
-// optional) collects the roots that still have a frontier.
-static __global__ void k_bs_apply(uint32_t N, uint32_t R, uint32_t W, const uint32_t* __restrict__ ptr,
+// next "next" buffer) and the words holding newly lowered roots form the next
+// active list.  alive (W words, optional) collects the roots that still have
+// a frontier.
+static __global__ void k_bs_apply(uint32_t N, uint32_t W, const uint32_t* __restrict__ ptr,
                                   const uint32_t* __restrict__ reg_end, const uint64_t* __restrict__ next,
-                                  const uint32_t* __restrict__ dist, uint32_t* msg, PairList out, uint64_t* front_old,
-                                  PairList old, uint64_t* alive = nullptr)
+                                  PairList out, uint64_t* front_old, PairList old, uint64_t* alive = nullptr)
 {
   const uint64_t tid = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x, nth = (uint64_t) gridDim.x * blockDim.x;
   const uint64_t ns = *old.nsmall, nb = hub_count(*old.packed);
@@ -136,18 +138,11 @@ static __global__ void k_bs_apply(uint32_t N, uint32_t R, uint32_t W, const uint
   const uint64_t NW = (uint64_t) N * W;
   for (uint64_t i = tid; i < NW; i += nth)
   {
-    uint64_t f = next[i];
+    const uint64_t f = next[i];
     if (!f) continue;
     const uint32_t v = (uint32_t) (i / W), w = (uint32_t) (i % W);
     bs_list_pair((uint32_t) i, reg_end[v] - ptr[v], out);
     if (alive && (alive[w] & f) != f) atomicOr((unsigned long long*) &alive[w], (unsigned long long) f);
-    while (f)
-    {
-      const int bpos = __ffsll((long long) f) - 1;
-      f &= f - 1;
-      const uint64_t j = (uint64_t) v * R + w * 64 + bpos;
-      msg[j] = dist[j];
-    }
   }
 }
 

@@ -259,14 +259,13 @@ __global__ void k_ls_fill_u32(uint64_t n, uint32_t* p, uint32_t v)
 
 __global__ void k_ls_admit(const uint32_t* __restrict__ adm, uint32_t n, uint32_t L, uint32_t W,
                            const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ reg_end, uint32_t nreg,
-                           uint32_t src_base, uint32_t iso_base, uint32_t* dist, uint32_t* msg, uint64_t* front,
+                           uint32_t src_base, uint32_t iso_base, uint32_t* dist, uint64_t* front,
                            uint32_t* rpos, PairList list)
 {
   for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
   {
     const uint32_t l = adm[2 * j], p = adm[2 * j + 1];
     dist[(uint64_t) p * L + l] = 0;
-    msg[(uint64_t) p * L + l] = 0;
     rpos[l] = p;
     if (p < nreg || (p >= src_base && p < iso_base))
     {
@@ -358,7 +357,7 @@ struct Engine
   bool exact_lanes = true;          // SSSP: max weight * N < INF
   DevBuf vis, buf[2], hops, alive[2], active, ctr, adm, ret, mask, staging, fdeg;
   // SSSP
-  DevBuf dist, msg, sfront[2], small[2], hub[2], hub_t0[2], reg_end, rpos;
+  DevBuf dist, sfront[2], small[2], hub[2], hub_t0[2], reg_end, rpos;
   unsigned long long* hctr = nullptr;  // pinned: counters + alive words
 };
 
@@ -393,7 +392,7 @@ uint64_t bfs_lane_bytes(uint32_t N, uint32_t L)
 uint64_t sssp_lane_bytes(uint32_t N, uint32_t L)
 {
   const uint64_t W = L / 64;
-  return (uint64_t) N * L * 4 * 2 + (uint64_t) N * W * 8 * 2 + (uint64_t) N * W * 4 * 6 + (uint64_t) N * 4 +
+  return (uint64_t) N * L * 4 + (uint64_t) N * W * 8 * 2 + (uint64_t) N * W * 4 * 6 + (uint64_t) N * 4 +
          (uint64_t) kOutChunk * N * 4 + 4096 + L * 16;
 }
 
@@ -507,7 +506,6 @@ int sssp_engine_init(Engine* E)
   const uint32_t N = E->N, W = E->W, L = E->L;
   const uint64_t NW = (uint64_t) N * W;
   LA3G_TRY(E->dist.alloc((uint64_t) N * L * 4));
-  LA3G_TRY(E->msg.alloc((uint64_t) N * L * 4));
   for (int c = 0; c < 2; c++)
   {
     LA3G_TRY(E->sfront[c].alloc(NW * 8));
@@ -856,7 +854,7 @@ int sssp_loop(Engine* E)
       LA3G_CUDA(cudaMemcpyAsync(E->adm.p, adm.data(), adm.size() * 4, cudaMemcpyHostToDevice, s));
       k_ls_admit<<<grid_for(n, 128), 128, 0, s>>>(E->adm.as<uint32_t>(), n, L, W, g.out_ptr,
                                                  E->reg_end.as<uint32_t>(), g.nreg, g.src_base(), g.iso_base(),
-                                                 E->dist.as<uint32_t>(), E->msg.as<uint32_t>(),
+                                                 E->dist.as<uint32_t>(),
                                                  E->sfront[cur].as<uint64_t>(), E->rpos.as<uint32_t>(), PL[cur]);
       LA3G_LAUNCHED();
       tls_launches++;
@@ -868,14 +866,14 @@ int sssp_loop(Engine* E)
       ProfileScope p("serve_sssp_relax", s, 0.0);
       k_bs_relax<<<kSMs * 16, 256, 0, s>>>(g.out_ptr, E->reg_end.as<uint32_t>(), g.out_row, g.out_w, L, W,
                                            E->sfront[cur].as<uint64_t>(), PL[cur], E->sfront[cur ^ 1].as<uint64_t>(),
-                                           E->msg.as<uint32_t>(), E->dist.as<uint32_t>());
+                                           E->dist.as<uint32_t>());
       LA3G_LAUNCHED();
     }
     LA3G_CUDA(cudaMemsetAsync(ctr + (cur ^ 1), 0, 8, s));
     LA3G_CUDA(cudaMemsetAsync(ctr + 2 + (cur ^ 1), 0, 8, s));
-    k_bs_apply<<<kSMs * 8, 256, 0, s>>>(N, L, W, g.out_ptr, E->reg_end.as<uint32_t>(), E->sfront[cur ^ 1].as<uint64_t>(),
-                                        E->dist.as<uint32_t>(), E->msg.as<uint32_t>(), PL[cur ^ 1],
-                                        E->sfront[cur].as<uint64_t>(), PL[cur], E->alive[0].as<uint64_t>());
+    k_bs_apply<<<kSMs * 8, 256, 0, s>>>(N, W, g.out_ptr, E->reg_end.as<uint32_t>(), E->sfront[cur ^ 1].as<uint64_t>(),
+                                        PL[cur ^ 1], E->sfront[cur].as<uint64_t>(), PL[cur],
+                                        E->alive[0].as<uint64_t>());
     LA3G_LAUNCHED();
     tls_launches += 2;
     LA3G_CUDA(cudaMemcpyAsync(E->hctr, E->alive[0].p, W * 8, cudaMemcpyDeviceToHost, s));
