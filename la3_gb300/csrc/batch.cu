@@ -53,7 +53,7 @@ struct BatchScratch
   uint64_t* vis = nullptr;   // [N][W]
   uint64_t* buf[2] = {nullptr, nullptr};  // frontier / next, [N][W]
   uint64_t* alive[2] = {nullptr, nullptr};  // [W] per-word "discovered something" masks
-  uint8_t* hops = nullptr;   // [R][N] by position
+  uint8_t* hops = nullptr;   // [N][W * 64] by position (vertex-major)
   uint32_t* rpos = nullptr;  // root positions
   uint32_t* active = nullptr;  // push: active (vertex, word) pairs
   unsigned long long* ctr = nullptr;  // [0] new bits, [1] active pairs, [2] frontier edges*words, [3] level
@@ -87,8 +87,7 @@ static void batch_scratch_free(void* p)
 
 // ------------------------------------------------------------------ BFS
 
-__global__ void k_ms_init(uint32_t N, uint32_t W, uint32_t R, uint64_t* vis, uint64_t* front, uint64_t* next,
-                          uint8_t* hops)
+__global__ void k_ms_init(uint32_t N, uint32_t W, uint32_t R, uint64_t* vis, uint64_t* front, uint64_t* next)
 {
   const uint64_t NW = (uint64_t) N * W;
   for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < NW; i += (uint64_t) gridDim.x * blockDim.x)
@@ -102,9 +101,6 @@ __global__ void k_ms_init(uint32_t N, uint32_t W, uint32_t R, uint64_t* vis, uin
     front[i] = 0;
     next[i] = 0;
   }
-  const uint64_t RN = (uint64_t) R * N;
-  for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < RN; i += (uint64_t) gridDim.x * blockDim.x)
-    hops[i] = 255;
 }
 
 __global__ void k_ms_roots(const uint32_t* __restrict__ rpos, uint32_t R, uint32_t N, uint32_t W, uint64_t* vis,
@@ -119,17 +115,7 @@ __global__ void k_ms_roots(const uint32_t* __restrict__ rpos, uint32_t R, uint32
     atomicOr((unsigned long long*) &vis[(uint64_t) p * W + w], (unsigned long long) bit);
     atomicOr((unsigned long long*) &front[(uint64_t) p * W + w], (unsigned long long) bit);
     atomicOr((unsigned long long*) &alive[w], (unsigned long long) bit);
-    hops[(uint64_t) r * N + p] = 0;
-  }
-}
-
-__device__ __forceinline__ void ms_record(uint64_t nb, uint32_t v, uint32_t w, uint32_t N, uint8_t hop, uint8_t* hops)
-{
-  while (nb)
-  {
-    const int b = __ffsll((long long) nb) - 1;
-    nb &= nb - 1;
-    hops[(uint64_t) (w * 64 + b) * N + v] = hop;
+    hops[((uint64_t) p * W + w) * 64 + r % 64] = 0;
   }
 }
 
@@ -170,7 +156,7 @@ __device__ __forceinline__ void ms_pull_body(const uint32_t* __restrict__ ptr, c
       vis[i] = seen | nb;
       cnt += __popcll(nb);
       atomicOr((unsigned long long*) &alive_next[w], (unsigned long long) nb);
-      ms_record(nb, v, w, N, hop, hops);
+      hops_record(hops + i * 64, nb, hop);
     }
   }
   for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
@@ -254,7 +240,7 @@ __global__ void k_ms_apply(uint32_t nrows, uint32_t N, uint32_t W, uint64_t* vis
       vis[i] |= nb;
       cnt += __popcll(nb);
       atomicOr((unsigned long long*) &alive_next[i % W], (unsigned long long) nb);
-      ms_record(nb, (uint32_t) (i / W), (uint32_t) (i % W), N, hop, hops);
+      hops_record(hops + i * 64, nb, hop);
     }
   }
   for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
@@ -341,14 +327,30 @@ __global__ void k_ms_persistent(const uint32_t* __restrict__ ptr, const uint32_t
   }
 }
 
-__global__ void k_ms_out(uint32_t N, uint32_t R, const uint32_t* __restrict__ id_of_pos, const uint8_t* __restrict__ hops,
-                         uint8_t* out)
+// Hops by position, [N][W * 64], to out[root][id]: 32 ids x 32 roots per
+// tile through shared memory, so reads and writes both move 32-byte runs.
+__global__ void __launch_bounds__(256) k_ms_out(uint32_t N, uint32_t R, uint32_t W, const uint32_t* __restrict__ pos_of_id,
+                                                const uint8_t* __restrict__ hops, uint8_t* out)
 {
-  const uint64_t RN = (uint64_t) R * N;
-  for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < RN; i += (uint64_t) gridDim.x * blockDim.x)
+  __shared__ uint8_t t[32][33];
+  const uint32_t tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const uint32_t nid = (N + 31) / 32, nr = (R + 31) / 32;
+  const uint64_t RW = (uint64_t) W * 64;
+  for (uint64_t tile = blockIdx.x; tile < (uint64_t) nid * nr; tile += gridDim.x)
   {
-    const uint32_t r = (uint32_t) (i / N), p = (uint32_t) (i % N);
-    out[(uint64_t) r * N + id_of_pos[p]] = hops[i];
+    const uint32_t id0 = (uint32_t) (tile % nid) * 32, r0 = (uint32_t) (tile / nid) * 32;
+    for (uint32_t k = ty; k < 32; k += 8)
+    {
+      const uint32_t id = id0 + k;
+      t[k][tx] = id < N && r0 + tx < R ? hops[(uint64_t) pos_of_id[id] * RW + r0 + tx] : 255;
+    }
+    __syncthreads();
+    for (uint32_t k = ty; k < 32; k += 8)
+    {
+      const uint32_t r = r0 + k, id = id0 + tx;
+      if (r < R && id < N) out[(uint64_t) r * N + id] = t[tx][k];
+    }
+    __syncthreads();
   }
 }
 
@@ -380,7 +382,7 @@ static int ms_bfs_alloc(la3g_graph* G, BatchScratch* b, uint32_t R)
   LA3G_TRY(galloc(G, &b->buf[1], (size_t) N * W));
   LA3G_TRY(galloc(G, &b->alive[0], W));
   LA3G_TRY(galloc(G, &b->alive[1], W));
-  LA3G_TRY(galloc(G, &b->hops, (size_t) R * N));
+  LA3G_TRY(galloc(G, &b->hops, (size_t) N * W * 64));
   LA3G_TRY(galloc(G, &b->rpos, R));
   LA3G_TRY(galloc(G, &b->active, (size_t) N * W));
   b->cap_r = R;
@@ -412,8 +414,9 @@ static int ms_bfs_run(la3g_graph* G, BatchScratch* b, const uint32_t* roots_host
   LA3G_CUDA(cudaMemcpyAsync(b->active, roots_host, (size_t) R * 4, cudaMemcpyHostToDevice, s));
   k_root_pos<<<grid_for(R, 256), 256, 0, s>>>(b->active, R, N, g.pos_of_id, b->rpos);
   LA3G_LAUNCHED();
-  k_ms_init<<<kSMs * 8, 256, 0, s>>>(N, W, R, b->vis, b->buf[0], b->buf[1], b->hops);
+  k_ms_init<<<kSMs * 8, 256, 0, s>>>(N, W, R, b->vis, b->buf[0], b->buf[1]);
   LA3G_LAUNCHED();
+  LA3G_CUDA(cudaMemsetAsync(b->hops, 0xFF, (size_t) N * W * 64, s));
   LA3G_CUDA(cudaMemsetAsync(b->alive[0], 0, (size_t) W * 8, s));
   LA3G_CUDA(cudaMemsetAsync(b->alive[1], 0, (size_t) W * 8, s));
   LA3G_CUDA(cudaMemsetAsync(b->ctr, 0, 8 * 8, s));
@@ -621,7 +624,7 @@ extern "C" int la3g_bfs_batch(la3g_graph* G, const uint32_t* roots, uint32_t nro
   {
     DevBuf tmp;
     LA3G_TRY(tmp.alloc((size_t) nroots * N));
-    k_ms_out<<<kSMs * 8, 256, 0, s>>>(N, nroots, g.id_of_pos, b->hops, tmp.as<uint8_t>());
+    k_ms_out<<<kSMs * 8, 256, 0, s>>>(N, nroots, (nroots + 63) / 64, g.pos_of_id, b->hops, tmp.as<uint8_t>());
     LA3G_LAUNCHED();
     LA3G_CUDA(cudaMemcpyAsync(hops_out, tmp.p, (size_t) nroots * N, cudaMemcpyDeviceToHost, s));
     LA3G_CUDA(cudaStreamSynchronize(s));

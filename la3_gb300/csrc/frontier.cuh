@@ -56,6 +56,34 @@ __device__ __forceinline__ uint32_t hub_of_task(const uint32_t* __restrict__ tas
   return lo;
 }
 
+// Multi-source BFS hop bytes are kept vertex-major: the 64 roots of frontier
+// word w of vertex v own bytes [64 (v W + w), 64 (v W + w) + 64), so the
+// thread that owns a (vertex, word) pair writes its newly reached roots with
+// at most eight aligned 8-byte read-modify-writes inside one 64-byte block.
+// Byte k of group g takes `hop` when bit 8g + k of nb is set.
+__device__ __forceinline__ uint64_t spread_bits_to_bytes(uint32_t m)
+{
+  uint64_t x = m & 0xFFu;
+  x = (x | (x << 28)) & 0x0000000F0000000Full;
+  x = (x | (x << 14)) & 0x0003000300030003ull;
+  x = (x | (x << 7)) & 0x0101010101010101ull;
+  return x * 0xFFu;
+}
+
+__device__ __forceinline__ void hops_record(uint8_t* block, uint64_t nb, uint8_t hop)
+{
+  uint64_t* q = reinterpret_cast<uint64_t*>(block);
+  const uint64_t hx = 0x0101010101010101ull * hop;
+#pragma unroll
+  for (int g = 0; g < 8; g++)
+  {
+    const uint32_t m = (uint32_t) (nb >> (8 * g)) & 0xFFu;
+    if (!m) continue;
+    const uint64_t M = spread_bits_to_bytes(m);
+    q[g] = (q[g] & ~M) | (hx & M);
+  }
+}
+
 }  // namespace la3g
 
 #endif
