@@ -119,8 +119,9 @@ __global__ void k_ms_roots(const uint32_t* __restrict__ rpos, uint32_t R, uint32
   }
 }
 
-// Bottom-up level over (vertex, word) pairs: G lanes per vertex.  Reads the
-// level from ctr[3]; front / next alternate with its parity.
+// Bottom-up level over (vertex, word) pairs (pull_scan: a lane per pair,
+// the warp for long in-edge lists).  Reads the level from ctr[3]; front /
+// next alternate with its parity.  tid / nthreads count whole warps.
 __device__ __forceinline__ void ms_pull_body(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col,
                                              uint32_t nrows, uint32_t N, uint32_t W, uint64_t* vis, uint64_t* const* buf,
                                              uint64_t* const* alive, uint8_t* hops, unsigned long long* ctr,
@@ -134,22 +135,17 @@ __device__ __forceinline__ void ms_pull_body(const uint32_t* __restrict__ ptr, c
   const uint8_t hop = (uint8_t) (level + 1);
   unsigned long long cnt = 0;
   const uint64_t NW = (uint64_t) nrows * W;
-  for (uint64_t i = tid; i < NW; i += nthreads)
+  // a warp takes 32 consecutive pairs at a time (pull_scan is warp-collective)
+  const int lane = threadIdx.x & 31;
+  for (uint64_t base = (tid >> 5) * 32; base < NW; base += (nthreads >> 5) * 32)
   {
-    const uint32_t v = (uint32_t) (i / W), w = (uint32_t) (i % W);
-    const uint64_t seen = vis[i];
-    uint64_t nb = 0;
-    const uint64_t want = ~seen & alive_now[w];
-    if (want)
-    {
-      uint64_t acc = 0;
-      for (uint32_t e = ptr[v]; e < ptr[v + 1]; e++)
-      {
-        acc |= front[(uint64_t) col[e] * W + w];
-        if ((acc & want) == want) break;
-      }
-      nb = acc & want;
-    }
+    const uint64_t i = base + lane;
+    const bool ok = i < NW;
+    const uint32_t v = ok ? (uint32_t) (i / W) : 0, w = ok ? (uint32_t) (i % W) : 0;
+    const uint64_t seen = ok ? vis[i] : ~0ull;
+    const uint64_t want = ok ? ~seen & alive_now[w] : 0;
+    const uint64_t nb = pull_scan(v, w, W, want, ptr, col, front, lane);
+    if (!ok) continue;
     next[i] = nb;
     if (nb)
     {
@@ -327,30 +323,44 @@ __global__ void k_ms_persistent(const uint32_t* __restrict__ ptr, const uint32_t
   }
 }
 
-// Hops by position, [N][W * 64], to out[root][id]: 32 ids x 32 roots per
-// tile through shared memory, so reads and writes both move 32-byte runs.
-__global__ void __launch_bounds__(256) k_ms_out(uint32_t N, uint32_t R, uint32_t W, const uint32_t* __restrict__ pos_of_id,
-                                                const uint8_t* __restrict__ hops, uint8_t* out)
+// Hops to out[root][id] in two passes, so that no pass gathers across the
+// whole [N][W * 64] array: a tiled transpose by position (32 positions x 32
+// roots per tile through shared memory; reads and writes move 32-byte runs)
+// into tpos[root][position], then a gather by id inside one root's N-byte
+// row, which stays in L2.
+__global__ void __launch_bounds__(256) k_ms_out_pos(uint32_t N, uint32_t R, uint32_t W, const uint8_t* __restrict__ hops,
+                                                    uint8_t* tpos)
 {
   __shared__ uint8_t t[32][33];
   const uint32_t tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  const uint32_t nid = (N + 31) / 32, nr = (R + 31) / 32;
+  const uint32_t np = (N + 31) / 32, nr = (R + 31) / 32;
   const uint64_t RW = (uint64_t) W * 64;
-  for (uint64_t tile = blockIdx.x; tile < (uint64_t) nid * nr; tile += gridDim.x)
+  for (uint64_t tile = blockIdx.x; tile < (uint64_t) np * nr; tile += gridDim.x)
   {
-    const uint32_t id0 = (uint32_t) (tile % nid) * 32, r0 = (uint32_t) (tile / nid) * 32;
+    const uint32_t p0 = (uint32_t) (tile % np) * 32, r0 = (uint32_t) (tile / np) * 32;
     for (uint32_t k = ty; k < 32; k += 8)
     {
-      const uint32_t id = id0 + k;
-      t[k][tx] = id < N && r0 + tx < R ? hops[(uint64_t) pos_of_id[id] * RW + r0 + tx] : 255;
+      const uint32_t p = p0 + k;
+      t[k][tx] = p < N && r0 + tx < R ? hops[(uint64_t) p * RW + r0 + tx] : 255;
     }
     __syncthreads();
     for (uint32_t k = ty; k < 32; k += 8)
     {
-      const uint32_t r = r0 + k, id = id0 + tx;
-      if (r < R && id < N) out[(uint64_t) r * N + id] = t[tx][k];
+      const uint32_t r = r0 + k, p = p0 + tx;
+      if (r < R && p < N) tpos[(uint64_t) r * N + p] = t[tx][k];
     }
     __syncthreads();
+  }
+}
+
+__global__ void k_ms_out_id(uint32_t N, uint32_t R, const uint32_t* __restrict__ pos_of_id, const uint8_t* __restrict__ tpos,
+                            uint8_t* out)
+{
+  const uint64_t RN = (uint64_t) R * N;
+  for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < RN; i += (uint64_t) gridDim.x * blockDim.x)
+  {
+    const uint64_t r = i / N;
+    out[i] = tpos[r * N + pos_of_id[i - r * N]];
   }
 }
 
@@ -622,11 +632,15 @@ extern "C" int la3g_bfs_batch(la3g_graph* G, const uint32_t* roots, uint32_t nro
   cudaStream_t s = G->stream;
   if (hops_out)
   {
-    DevBuf tmp;
-    LA3G_TRY(tmp.alloc((size_t) nroots * N));
-    k_ms_out<<<kSMs * 8, 256, 0, s>>>(N, nroots, (nroots + 63) / 64, g.pos_of_id, b->hops, tmp.as<uint8_t>());
+    // the by-id rows go into the hop array itself (N x W x 64 >= nroots x N
+    // bytes), which the next batch re-initialises
+    DevBuf tpos;
+    LA3G_TRY(tpos.alloc((size_t) nroots * N));
+    k_ms_out_pos<<<kSMs * 8, 256, 0, s>>>(N, nroots, (nroots + 63) / 64, b->hops, tpos.as<uint8_t>());
     LA3G_LAUNCHED();
-    LA3G_CUDA(cudaMemcpyAsync(hops_out, tmp.p, (size_t) nroots * N, cudaMemcpyDeviceToHost, s));
+    k_ms_out_id<<<kSMs * 8, 256, 0, s>>>(N, nroots, g.pos_of_id, tpos.as<uint8_t>(), b->hops);
+    LA3G_LAUNCHED();
+    LA3G_CUDA(cudaMemcpyAsync(hops_out, b->hops, (size_t) nroots * N, cudaMemcpyDeviceToHost, s));
     LA3G_CUDA(cudaStreamSynchronize(s));
   }
   LA3G_TRY(T.finish());

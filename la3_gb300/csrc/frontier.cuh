@@ -84,6 +84,66 @@ __device__ __forceinline__ void hops_record(uint8_t* block, uint64_t nb, uint8_t
   }
 }
 
+// Bottom-up scan of one (vertex, word) pair of a multi-source BFS: the OR of
+// the frontier words front[u W + w] over the in-neighbours u of v, stopping
+// once every bit of `want` is found.  Called by all 32 lanes of a warp with
+// one pair each (want = 0 for lanes without work).  A lane scans its own
+// first kPullOwn edges, four independent loads at a time; pairs still short
+// of bits after that are finished one after another by the whole warp, 32
+// edges a step with an OR-reduction, so a hub's list never sits on a single
+// thread.  Returns acc & want.
+static constexpr uint32_t kPullOwn = 32;
+
+__device__ __forceinline__ uint64_t warp_or64(uint64_t a)
+{
+  const uint32_t lo = __reduce_or_sync(0xffffffffu, (uint32_t) a);
+  const uint32_t hi = __reduce_or_sync(0xffffffffu, (uint32_t) (a >> 32));
+  return ((uint64_t) hi << 32) | lo;
+}
+
+__device__ __forceinline__ uint64_t pull_scan(uint32_t v, uint32_t w, uint32_t W, uint64_t want,
+                                              const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col,
+                                              const uint64_t* __restrict__ front, int lane)
+{
+  uint64_t acc = 0;
+  uint32_t e = 0, end = 0;
+  if (want)
+  {
+    e = ptr[v];
+    end = ptr[v + 1];
+  }
+  const uint32_t own = min(end, e + kPullOwn);
+  while (e < own && (acc & want) != want)
+  {
+    uint32_t c[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) c[u] = e + u < own ? col[e + u] : 0xFFFFFFFFu;
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+      if (c[u] != 0xFFFFFFFFu) acc |= front[(uint64_t) c[u] * W + w];
+    e += 4;
+  }
+  unsigned m = __ballot_sync(0xffffffffu, (acc & want) != want && own < end);
+  while (m)
+  {
+    const int src = __ffs(m) - 1;
+    m &= m - 1;
+    const uint32_t ws = __shfl_sync(0xffffffffu, w, src);
+    const uint32_t b0 = __shfl_sync(0xffffffffu, own, src), b1 = __shfl_sync(0xffffffffu, end, src);
+    const uint64_t wants = __shfl_sync(0xffffffffu, want, src), accs = __shfl_sync(0xffffffffu, acc, src);
+    uint64_t a = 0, tot = accs;
+    for (uint32_t kb = b0; kb < b1; kb += 32)
+    {
+      const uint32_t k = kb + lane;
+      if (k < b1) a |= front[(uint64_t) col[k] * W + ws];
+      tot = accs | warp_or64(a);
+      if ((tot & wants) == wants) break;
+    }
+    if (lane == src) acc = tot;
+  }
+  return acc & want;
+}
+
 }  // namespace la3g
 
 #endif

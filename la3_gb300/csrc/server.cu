@@ -86,18 +86,8 @@ __global__ void k_lb_admit(const uint32_t* __restrict__ adm, uint32_t n, uint32_
     atomicOr((unsigned long long*) &vis[(uint64_t) p * W + w], bit);
     atomicOr((unsigned long long*) &front[(uint64_t) p * W + w], bit);
     atomicOr((unsigned long long*) &alive[w], bit);
-    hops[(uint64_t) l * N + p] = 0;
+    hops[((uint64_t) p * W + w) * 64 + l % 64] = 0;
     atomicAdd(&fdeg[w], (unsigned long long) (ptr[p + 1] - ptr[p]));
-  }
-}
-
-__device__ __forceinline__ void lb_record(uint64_t nb, uint32_t v, uint32_t w, uint32_t N, uint8_t hop, uint8_t* hops)
-{
-  while (nb)
-  {
-    const int b = __ffsll((long long) nb) - 1;
-    nb &= nb - 1;
-    hops[(uint64_t) (w * 64 + b) * N + v] = hop;
   }
 }
 
@@ -119,31 +109,26 @@ k_lb_pull(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, ui
   for (uint32_t w = threadIdx.x; w < W; w += blockDim.x) sdeg[w] = 0;
   __syncthreads();
   const uint64_t NW = (uint64_t) nrows * W;
-  for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < NW; i += (uint64_t) gridDim.x * blockDim.x)
+  const int lane = threadIdx.x & 31;
+  const uint64_t warp = ((uint64_t) blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t) gridDim.x * blockDim.x) >> 5;
+  for (uint64_t base = warp * 32; base < NW; base += nwarps * 32)
   {
-    const uint32_t w = (uint32_t) (i % W);
-    if (!((words >> w) & 1ull)) continue;
-    const uint32_t v = (uint32_t) (i / W);
-    const uint64_t seen = vis[i];
-    const uint64_t want = ~seen & alive_cur[w];
-    uint64_t nb = 0;
-    if (want)
-    {
-      uint64_t acc = 0;
-      for (uint32_t e = ptr[v]; e < ptr[v + 1]; e++)
-      {
-        acc |= front[(uint64_t) col[e] * W + w];
-        if ((acc & want) == want) break;
-      }
-      nb = acc & want;
-    }
+    const uint64_t i = base + lane;
+    const uint32_t w = i < NW ? (uint32_t) (i % W) : 0;
+    const bool ok = i < NW && ((words >> w) & 1ull);
+    const uint32_t v = ok ? (uint32_t) (i / W) : 0;
+    const uint64_t seen = ok ? vis[i] : ~0ull;
+    const uint64_t want = ok ? ~seen & alive_cur[w] : 0;
+    const uint64_t nb = pull_scan(v, w, W, want, ptr, col, front, lane);
+    if (!ok) continue;
     next[i] = nb;
     if (nb)
     {
       vis[i] = seen | nb;
       atomicAdd(&sdeg[w], (unsigned long long) (ptr[v + 1] - ptr[v]));
       atomicOr((unsigned long long*) &alive_next[w], (unsigned long long) nb);
-      lb_record(nb, v, w, N, hop.h[w], hops);
+      hops_record(hops + i * 64, nb, hop.h[w]);
     }
   }
   lb_deg_flush(sdeg, W, fdeg);
@@ -212,23 +197,38 @@ k_lb_apply(const uint32_t* __restrict__ ptr, uint32_t nrows, uint32_t N, uint32_
       vis[i] |= nb;
       atomicAdd(&sdeg[w], (unsigned long long) (ptr[v + 1] - ptr[v]));
       atomicOr((unsigned long long*) &alive_next[w], (unsigned long long) nb);
-      lb_record(nb, v, w, N, hop.h[w], hops);
+      hops_record(hops + i * 64, nb, hop.h[w]);
     }
   }
   lb_deg_flush(sdeg, W, fdeg);
 }
 
-// Retiring lanes: hops by id into the staging rows, hops reset to 255.
-__global__ void k_lb_out(const uint32_t* __restrict__ lanes, uint32_t nl, uint32_t N,
-                         const uint32_t* __restrict__ id_of_pos, uint8_t* hops, uint8_t* staging)
+// Retiring lanes, in two passes so that no pass gathers across the whole
+// [N][L] hop array: first by position (hop rows read in order) into tmp[j][p],
+// resetting the bytes to 255; then by id, staging[j][id] = tmp[j][pos(id)],
+// a gather inside one lane's N-byte row, which stays in L2.
+__global__ void k_lb_out_pos(const uint32_t* __restrict__ lanes, uint32_t nl, uint32_t N, uint32_t L, uint8_t* hops,
+                             uint8_t* tmp)
 {
-  const uint64_t n = (uint64_t) nl * N;
-  for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t) gridDim.x * blockDim.x)
+  for (uint64_t p = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; p < N; p += (uint64_t) gridDim.x * blockDim.x)
   {
-    const uint32_t j = (uint32_t) (i / N), p = (uint32_t) (i % N);
-    uint8_t* h = &hops[(uint64_t) lanes[j] * N + p];
-    staging[(uint64_t) j * N + id_of_pos[p]] = *h;
-    *h = 255;
+    uint8_t* row = hops + p * L;
+    for (uint32_t j = 0; j < nl; j++)
+    {
+      const uint32_t l = lanes[j];
+      tmp[(uint64_t) j * N + p] = row[l];
+      row[l] = 255;
+    }
+  }
+}
+
+__global__ void k_lb_out_id(uint32_t nl, uint32_t N, const uint32_t* __restrict__ pos_of_id, const uint8_t* __restrict__ tmp,
+                            uint8_t* staging)
+{
+  for (uint64_t id = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; id < N; id += (uint64_t) gridDim.x * blockDim.x)
+  {
+    const uint32_t p = pos_of_id[id];
+    for (uint32_t j = 0; j < nl; j++) staging[(uint64_t) j * N + id] = tmp[(uint64_t) j * N + p];
   }
 }
 
@@ -355,7 +355,7 @@ struct Engine
   std::vector<uint32_t> wbusy;      // BFS: occupied lanes per word
   std::vector<uint32_t> pos_of_id;  // host copy
   bool exact_lanes = true;          // SSSP: max weight * N < INF
-  DevBuf vis, buf[2], hops, alive[2], active, ctr, adm, ret, mask, staging, fdeg;
+  DevBuf vis, buf[2], hops, alive[2], active, ctr, adm, ret, mask, staging, outpos, fdeg;
   // SSSP
   DevBuf dist, sfront[2], small[2], hub[2], hub_t0[2], reg_end, rpos;
   unsigned long long* hctr = nullptr;  // pinned: counters + alive words
@@ -386,7 +386,8 @@ uint32_t solo_depth(const Engine* E)
 uint64_t bfs_lane_bytes(uint32_t N, uint32_t L)
 {
   const uint64_t W = L / 64;
-  return (uint64_t) N * W * 8 * 3 + (uint64_t) N * L + (uint64_t) N * W * 4 + (uint64_t) kOutChunk * N + 4096 + L * 16;
+  return (uint64_t) N * W * 8 * 3 + (uint64_t) N * L + (uint64_t) N * W * 4 + (uint64_t) kOutChunk * N * 2 + 4096 +
+         L * 16;
 }
 
 uint64_t sssp_lane_bytes(uint32_t N, uint32_t L)
@@ -487,6 +488,7 @@ int bfs_engine_init(Engine* E)
   LA3G_TRY(E->mask.alloc(W * 8));
   LA3G_TRY(E->fdeg.alloc(W * 8));
   LA3G_TRY(E->staging.alloc((uint64_t) kOutChunk * N));
+  LA3G_TRY(E->outpos.alloc((uint64_t) kOutChunk * N));
   LA3G_CUDA(cudaMemsetAsync(E->fdeg.p, 0, W * 8, s));
   LA3G_CUDA(cudaMemsetAsync(E->vis.p, 0, NW * 8, s));
   LA3G_CUDA(cudaMemsetAsync(E->buf[0].p, 0, NW * 8, s));
@@ -555,10 +557,12 @@ int bfs_retire(Engine* E, const std::vector<uint32_t>& lanes, bool deliver, uint
   {
     const uint32_t nl = (uint32_t) std::min<size_t>(kOutChunk, lanes.size() - j0);
     LA3G_CUDA(cudaMemcpyAsync(E->ret.p, lanes.data() + j0, nl * 4, cudaMemcpyHostToDevice, s));
-    k_lb_out<<<kSMs * 8, 256, 0, s>>>(E->ret.as<uint32_t>(), nl, N, g.id_of_pos, E->hops.as<uint8_t>(),
-                                      E->staging.as<uint8_t>());
+    k_lb_out_pos<<<kSMs * 8, 256, 0, s>>>(E->ret.as<uint32_t>(), nl, N, E->L, E->hops.as<uint8_t>(),
+                                          E->outpos.as<uint8_t>());
     LA3G_LAUNCHED();
-    tls_launches++;
+    k_lb_out_id<<<kSMs * 8, 256, 0, s>>>(nl, N, g.pos_of_id, E->outpos.as<uint8_t>(), E->staging.as<uint8_t>());
+    LA3G_LAUNCHED();
+    tls_launches += 2;
     for (uint32_t j = 0; deliver && j < nl; j++)
     {
       Ticket* t = E->lane[lanes[j0 + j]];
