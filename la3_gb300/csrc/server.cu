@@ -29,6 +29,7 @@
 // engine's lane state fit in what is left of the budget (the lane count is
 // halved down to 64 before LA3G_EBUDGET is returned); queries then wait for a
 // free lane of their graph's engine.
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
@@ -46,7 +47,7 @@
 namespace la3g {
 namespace {
 
-constexpr uint32_t kOutChunk = 16;  // lanes retired per output pass (staging size)
+constexpr uint32_t kOutChunk = 64;  // lanes retired per output pass (staging size)
 
 double wall_ms()
 {
@@ -206,20 +207,33 @@ k_lb_apply(const uint32_t* __restrict__ ptr, uint32_t nrows, uint32_t N, uint32_
 // Retiring lanes, in two passes so that no pass gathers across the whole
 // [N][L] hop array: first by position (hop rows read in order) into tmp[j][p],
 // resetting the bytes to 255; then by id, staging[j][id] = tmp[j][pos(id)],
-// a gather inside one lane's N-byte row, which stays in L2.
-__global__ void k_lb_out_pos(const uint32_t* __restrict__ lanes, uint32_t nl, uint32_t N, uint32_t L, uint8_t* hops,
-                             uint8_t* tmp)
+// a gather inside one lane's N-byte row, which stays in L2.  The retiring
+// lanes of a pass are given per word (wmask[w]; wbase[w] = index j of the
+// word's first one); a thread loads the 8-byte groups of a (position, word)
+// block that hold them at once and writes the 255s back with masked words.
+__global__ void k_lb_out_pos(const uint64_t* __restrict__ wmask, const uint32_t* __restrict__ wbase, uint32_t N, uint32_t W,
+                             uint8_t* hops, uint8_t* tmp)
 {
   for (uint64_t p = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; p < N; p += (uint64_t) gridDim.x * blockDim.x)
-  {
-    uint8_t* row = hops + p * L;
-    for (uint32_t j = 0; j < nl; j++)
+    for (uint32_t w = 0; w < W; w++)
     {
-      const uint32_t l = lanes[j];
-      tmp[(uint64_t) j * N + p] = row[l];
-      row[l] = 255;
+      const uint64_t mw = wmask[w];
+      if (!mw) continue;
+      uint64_t* blk = reinterpret_cast<uint64_t*>(hops + (p * W + w) * 64);
+      uint64_t q[8];
+#pragma unroll
+      for (int g = 0; g < 8; g++) q[g] = ((mw >> (8 * g)) & 0xFFu) ? blk[g] : 0;
+      uint32_t j = wbase[w];
+#pragma unroll
+      for (int g = 0; g < 8; g++)
+      {
+        const uint32_t m8 = (uint32_t) (mw >> (8 * g)) & 0xFFu;
+        if (!m8) continue;
+        for (uint32_t m = m8; m; m &= m - 1)
+          tmp[(uint64_t) j++ * N + p] = (uint8_t) (q[g] >> (8 * (__ffs(m) - 1)));
+        blk[g] = q[g] | spread_bits_to_bytes(m8);
+      }
     }
-  }
 }
 
 __global__ void k_lb_out_id(uint32_t nl, uint32_t N, const uint32_t* __restrict__ pos_of_id, const uint8_t* __restrict__ tmp,
@@ -548,17 +562,29 @@ int sssp_engine_init(Engine* E)
 // Copies each retiring lane's result into its ticket's output (when
 // `deliver`) and frees the lane: its bits leave the visited bitmap and, for
 // lanes leaving early, the current frontier and alive mask as well.
-int bfs_retire(Engine* E, const std::vector<uint32_t>& lanes, bool deliver, uint64_t* front, uint64_t* alive)
+int bfs_retire(Engine* E, const std::vector<uint32_t>& lanes_in, bool deliver, uint64_t* front, uint64_t* alive)
 {
   DevGraph& g = E->G->g;
   cudaStream_t s = E->G->stream;
   const uint32_t N = E->N, W = E->W;
+  std::vector<uint32_t> lanes(lanes_in);
+  std::sort(lanes.begin(), lanes.end());  // staging row j = j-th retiring lane in lane order
   for (size_t j0 = 0; j0 < lanes.size(); j0 += kOutChunk)
   {
     const uint32_t nl = (uint32_t) std::min<size_t>(kOutChunk, lanes.size() - j0);
-    LA3G_CUDA(cudaMemcpyAsync(E->ret.p, lanes.data() + j0, nl * 4, cudaMemcpyHostToDevice, s));
-    k_lb_out_pos<<<kSMs * 8, 256, 0, s>>>(E->ret.as<uint32_t>(), nl, N, E->L, E->hops.as<uint8_t>(),
-                                          E->outpos.as<uint8_t>());
+    // per-word masks of this pass's lanes (ascending, so lane order = j order)
+    std::vector<uint64_t> wm(W, 0);
+    std::vector<uint32_t> wb(W, 0);
+    for (uint32_t j = nl; j-- > 0;)
+    {
+      const uint32_t l = lanes[j0 + j];
+      wm[l / 64] |= 1ull << (l % 64);
+      wb[l / 64] = j;
+    }
+    LA3G_CUDA(cudaMemcpyAsync(E->ret.p, wm.data(), W * 8, cudaMemcpyHostToDevice, s));
+    LA3G_CUDA(cudaMemcpyAsync(E->ret.as<uint8_t>() + W * 8, wb.data(), W * 4, cudaMemcpyHostToDevice, s));
+    k_lb_out_pos<<<kSMs * 8, 256, 0, s>>>(E->ret.as<uint64_t>(), (const uint32_t*) (E->ret.as<uint8_t>() + W * 8), N, W,
+                                          E->hops.as<uint8_t>(), E->outpos.as<uint8_t>());
     LA3G_LAUNCHED();
     k_lb_out_id<<<kSMs * 8, 256, 0, s>>>(nl, N, g.pos_of_id, E->outpos.as<uint8_t>(), E->staging.as<uint8_t>());
     LA3G_LAUNCHED();
