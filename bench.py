@@ -709,7 +709,7 @@ def serve_line(args, rank, world, local) -> dict | None:
         return arr, qs
 
     budget = int(200e9)
-    S = L.Server(budget)  # default lanes: 256 BFS (four 64-lane words), 64 SSSP
+    S = L.Server(budget)  # default lanes: 256 BFS (four 64-lane words), 256 SSSP
     gid = []
     for sc, gu, gw in graphs:
         gid.append((S.add_graph(gu), S.add_graph(gw)))

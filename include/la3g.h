@@ -278,7 +278,7 @@ typedef struct la3g_server_stats
 } la3g_server_stats;
 
 /* A server with an HBM budget (bytes).  bfs_lanes / sssp_lanes: queries one
- * BFS / SSSP engine holds at once (multiples of 64; 0 = 256 / 64).  A BFS
+ * BFS / SSSP engine holds at once (multiples of 64; 0 = 256 / 256).  A BFS
  * engine admits queries 64 at a time into free 64-lane words (queries that
  * are queued when a word frees up start together); an SSSP engine admits
  * them into any free lane. */

@@ -47,7 +47,8 @@
 namespace la3g {
 namespace {
 
-constexpr uint32_t kOutChunk = 64;  // lanes retired per output pass (staging size)
+constexpr uint32_t kOutChunk = 64;   // BFS lanes retired per output pass (staging rows)
+constexpr uint32_t kOutChunkS = 16;  // SSSP lanes retired per output pass (staging rows)
 
 double wall_ms()
 {
@@ -380,7 +381,7 @@ struct Engine
 struct la3g_server
 {
   uint64_t budget = 0, used = 0;
-  uint32_t bfs_lanes = 256, sssp_lanes = 64;
+  uint32_t bfs_lanes = 256, sssp_lanes = 256;
   uint32_t solo_bfs = 16, solo_sssp = 4;  // adaptive batching depths
   std::mutex mu;
   std::condition_variable done_cv;
@@ -408,7 +409,7 @@ uint64_t sssp_lane_bytes(uint32_t N, uint32_t L)
 {
   const uint64_t W = L / 64;
   return (uint64_t) N * L * 4 + (uint64_t) N * W * 8 * 2 + (uint64_t) N * W * 4 * 6 + (uint64_t) N * 4 +
-         (uint64_t) kOutChunk * N * 4 + 4096 + L * 16;
+         (uint64_t) kOutChunkS * N * 4 + 4096 + L * 16;
 }
 
 void finish_ticket(la3g_server* S, Ticket* t, int status)
@@ -536,7 +537,7 @@ int sssp_engine_init(Engine* E)
   LA3G_TRY(E->ctr.alloc(8 * 8));
   LA3G_TRY(E->adm.alloc((uint64_t) L * 8));
   LA3G_TRY(E->ret.alloc((uint64_t) L * 4));
-  LA3G_TRY(E->staging.alloc((uint64_t) kOutChunk * N * 4));
+  LA3G_TRY(E->staging.alloc((uint64_t) kOutChunkS * N * 4));
   LA3G_CUDA(cudaMemsetAsync(E->ctr.p, 0, 64, s));
   k_ls_fill_u32<<<kSMs * 8, 256, 0, s>>>((uint64_t) N * L, E->dist.as<uint32_t>(), kInfD);
   LA3G_LAUNCHED();
@@ -826,9 +827,9 @@ int sssp_retire(Engine* E, const std::vector<uint32_t>& lanes)
   DevGraph& g = E->G->g;
   cudaStream_t s = E->G->stream;
   const uint32_t N = E->N, L = E->L;
-  for (size_t j0 = 0; j0 < lanes.size(); j0 += kOutChunk)
+  for (size_t j0 = 0; j0 < lanes.size(); j0 += kOutChunkS)
   {
-    const uint32_t nl = (uint32_t) std::min<size_t>(kOutChunk, lanes.size() - j0);
+    const uint32_t nl = (uint32_t) std::min<size_t>(kOutChunkS, lanes.size() - j0);
     LA3G_CUDA(cudaMemcpyAsync(E->ret.p, lanes.data() + j0, nl * 4, cudaMemcpyHostToDevice, s));
     if (g.nsink)
     {
@@ -964,7 +965,7 @@ extern "C" int la3g_server_create(uint64_t budget_bytes, uint32_t bfs_lanes, uin
   if (!out) return set_error(LA3G_EINVAL, "out is null");
   *out = nullptr;
   if (bfs_lanes == 0) bfs_lanes = 256;
-  if (sssp_lanes == 0) sssp_lanes = 64;
+  if (sssp_lanes == 0) sssp_lanes = 256;
   if (bfs_lanes % 64 || sssp_lanes % 64 || bfs_lanes > 4096 || sssp_lanes > 4096)
     return set_error(LA3G_EINVAL, "lane counts must be multiples of 64, at most 4096");
   la3g_server* S = new (std::nothrow) la3g_server();
