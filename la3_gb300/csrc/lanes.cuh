@@ -34,27 +34,84 @@ static __device__ __forceinline__ void bs_list_pair(uint32_t i, uint32_t deg, co
   else hub_append(i, deg, L.hub, L.hub_t0, L.packed);
 }
 
-// Relaxes edges [k0, k1) of the vertex of pair i: lane l handles roots
-// 64w + l and 64w + l + 32, so the distances of one edge's target are read
-// contiguously; the roots an edge improved are ORed into the target's
-// next-frontier word at once.  A source's distances are read when its pair is
-// taken, not as of the iteration's start: a value lowered earlier in the same
-// iteration reaches its targets at once (Gauss-Seidel order), and the source
-// is in the next frontier anyway.  Every order of relaxation ends at the same
-// shortest distances.  Edges go 8 at a time (targets and weights
-// loaded by 8 lanes and broadcast) so that up to 16 target reads per lane are
-// in flight.  A root's bit is set when its candidate is below the distance
-// read through L2: distances only fall, so that read is at most the value
-// the iteration started with and the bit means "lowered in this iteration",
-// exactly as an atomic's returned old value would; the minimum itself is
-// therefore a reduction whose result nobody waits for.
-static __device__ __forceinline__ void bs_relax_range(uint32_t i, uint32_t k0, uint32_t k1, int lane, uint32_t R, uint32_t W,
+// Position of the s-th (from 0) set bit of f; s < popcount(f).
+static __device__ __forceinline__ int nth_set_bit(uint64_t f, int s)
+{
+  int pos = 0;
+  uint32_t x = (uint32_t) f;
+  int c = __popc(x);
+  if (s >= c)
+  {
+    s -= c;
+    x = (uint32_t) (f >> 32);
+    pos = 32;
+  }
+  c = __popc(x & 0xFFFFu);
+  if (s >= c) { s -= c; x >>= 16; pos += 16; }
+  c = __popc(x & 0xFFu);
+  if (s >= c) { s -= c; x >>= 8; pos += 8; }
+  c = __popc(x & 0xFu);
+  if (s >= c) { s -= c; x >>= 4; pos += 4; }
+  c = __popc(x & 0x3u);
+  if (s >= c) { s -= c; x >>= 2; pos += 2; }
+  if (s >= (int) (x & 1u)) pos += 1;
+  return pos;
+}
+
+// Pairs with at most 32 active roots: the k active roots are packed into
+// groups of S = next power of two >= k lanes, so a warp step covers 32 / S
+// edges (four steps unrolled, their target reads in flight together); a
+// lowered root ORs its own bit into the target's next word.
+static __device__ __forceinline__ void bs_relax_sparse(uint32_t k0, uint32_t k1, int lane, uint32_t R, uint32_t W,
+                                                const uint32_t* __restrict__ row, const uint32_t* __restrict__ wgt,
+                                                uint32_t u, uint32_t w, uint64_t f, int k, uint64_t* next, uint32_t* dist)
+{
+  const int S = k <= 1 ? 1 : 1 << (32 - __clz(k - 1));
+  const uint32_t E = 32 / S;
+  const int slot = lane & (S - 1);
+  const uint32_t e = (uint32_t) lane / S;
+  const bool act = slot < k;
+  const int b = act ? nth_set_bit(f, slot) : 0;
+  const uint32_t r = w * 64 + b;
+  const uint32_t m = act ? __ldcg(&dist[(uint64_t) u * R + r]) : 0;
+  const unsigned long long bit = 1ull << b;
+  for (uint32_t kb = k0; kb < k1; kb += 4 * E)
+  {
+    uint32_t v[4], wt[4], d[4];
+    bool live[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+    {
+      const uint32_t ke = kb + q * E + e;
+      live[q] = act && ke < k1;
+      v[q] = live[q] ? row[ke] : 0;
+      wt[q] = live[q] ? wgt[ke] : 0;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) d[q] = live[q] ? __ldcg(&dist[(uint64_t) v[q] * R + r]) : 0;
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+    {
+      const uint32_t c = m + wt[q];
+      if (live[q] && c < d[q])
+      {
+        atomicMin(&dist[(uint64_t) v[q] * R + r], c);
+        atomicOr((unsigned long long*) &next[(uint64_t) v[q] * W + w], bit);
+      }
+    }
+  }
+}
+
+// Pairs with more than 32 active roots: lane l handles roots 64w + l and
+// 64w + l + 32, so the distances of one edge's target are read contiguously;
+// the roots an edge lowered are ORed into the target's next-frontier word at
+// once.  Edges go 8 at a time (targets and weights loaded by 8 lanes and
+// broadcast) so that up to 16 target reads per lane are in flight.
+static __device__ __forceinline__ void bs_relax_dense(uint32_t k0, uint32_t k1, int lane, uint32_t R, uint32_t W,
                                                const uint32_t* __restrict__ row, const uint32_t* __restrict__ wgt,
-                                               const uint64_t* __restrict__ front, uint64_t* next, uint32_t* dist)
+                                               uint32_t u, uint32_t w, uint64_t f, uint64_t* next, uint32_t* dist)
 {
   constexpr int G = 8;
-  const uint32_t u = i / W, w = i % W;
-  const uint64_t f = front[i];
   const uint32_t r0 = w * 64 + lane, r1 = r0 + 32;
   const bool h0 = (f >> lane) & 1ull, h1 = (f >> (lane + 32)) & 1ull;
   const uint32_t m0 = h0 ? __ldcg(&dist[(uint64_t) u * R + r0]) : 0, m1 = h1 ? __ldcg(&dist[(uint64_t) u * R + r1]) : 0;
@@ -93,6 +150,27 @@ static __device__ __forceinline__ void bs_relax_range(uint32_t i, uint32_t k0, u
     }
     if (mine) atomicOr((unsigned long long*) &next[(uint64_t) lv * W + w], (unsigned long long) mine);
   }
+}
+
+// Relaxes edges [k0, k1) of the vertex of pair i (a warp, all lanes).  A
+// source's distances are read when its pair is taken, not as of the
+// iteration's start: a value lowered earlier in the same iteration reaches its
+// targets at once (Gauss-Seidel order), and the source is in the next frontier
+// anyway; every order of relaxation ends at the same shortest distances.  A
+// root's bit is set when its candidate is below the distance read through L2:
+// distances only fall, so that read is at most the value the iteration
+// started with and the bit means "lowered in this iteration", exactly as an
+// atomic's returned old value would; the minimum itself is therefore a
+// reduction whose result nobody waits for.
+static __device__ __forceinline__ void bs_relax_range(uint32_t i, uint32_t k0, uint32_t k1, int lane, uint32_t R, uint32_t W,
+                                               const uint32_t* __restrict__ row, const uint32_t* __restrict__ wgt,
+                                               const uint64_t* __restrict__ front, uint64_t* next, uint32_t* dist)
+{
+  const uint32_t u = i / W, w = i % W;
+  const uint64_t f = front[i];
+  const int k = __popcll(f);
+  if (k > 32) bs_relax_dense(k0, k1, lane, R, W, row, wgt, u, w, f, next, dist);
+  else bs_relax_sparse(k0, k1, lane, R, W, row, wgt, u, w, f, k, next, dist);
 }
 
 static __global__ void __launch_bounds__(256, 4)
