@@ -48,7 +48,6 @@ namespace la3g {
 namespace {
 
 constexpr uint32_t kOutChunk = 64;   // BFS lanes retired per output pass (staging rows)
-constexpr uint32_t kOutChunkS = 16;  // SSSP lanes retired per output pass (staging rows)
 
 double wall_ms()
 {
@@ -319,16 +318,44 @@ __global__ void k_ls_sinks(const uint32_t* __restrict__ ptr, const uint32_t* __r
   }
 }
 
-__global__ void k_ls_out(const uint32_t* __restrict__ lanes, uint32_t nl, uint32_t N, uint32_t L,
-                         const uint32_t* __restrict__ id_of_pos, uint32_t* dist, uint32_t* staging)
+// Retiring SSSP lanes in two passes: by position, a thread per vertex loads
+// the retiring lanes' distances of its row (all in flight together), writes
+// them to tmp[j][p] (coalesced per lane) and resets them to INF; then by id,
+// staging[j][id] = tmp[j][pos(id)], a gather inside one lane's N-entry row,
+// which stays in L2 (a scatter by id straight from the rows would spread
+// partial-sector writes over all nl rows at once).
+static constexpr uint32_t kOutChunkS = 16;  // SSSP lanes retired per output pass (staging rows)
+
+__global__ void k_ls_out_pos(const uint32_t* __restrict__ lanes, uint32_t nl, uint32_t N, uint32_t L, uint32_t* dist,
+                             uint32_t* __restrict__ tmp)
+{
+  uint32_t ln[kOutChunkS];
+#pragma unroll
+  for (uint32_t j = 0; j < kOutChunkS; j++) ln[j] = j < nl ? lanes[j] : 0;
+  for (uint64_t p = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; p < N; p += (uint64_t) gridDim.x * blockDim.x)
+  {
+    uint32_t* row = dist + p * L;
+    uint32_t x[kOutChunkS];
+#pragma unroll
+    for (uint32_t j = 0; j < kOutChunkS; j++) x[j] = j < nl ? __ldcg(&row[ln[j]]) : 0;
+#pragma unroll
+    for (uint32_t j = 0; j < kOutChunkS; j++)
+      if (j < nl)
+      {
+        tmp[(uint64_t) j * N + p] = x[j];
+        row[ln[j]] = kInfD;
+      }
+  }
+}
+
+__global__ void k_ls_out_id(uint32_t nl, uint32_t N, const uint32_t* __restrict__ pos_of_id, const uint32_t* __restrict__ tmp,
+                            uint32_t* __restrict__ staging)
 {
   const uint64_t n = (uint64_t) nl * N;
   for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t) gridDim.x * blockDim.x)
   {
-    const uint32_t j = (uint32_t) (i % nl), p = (uint32_t) (i / nl);
-    uint32_t* d = &dist[(uint64_t) p * L + lanes[j]];
-    staging[(uint64_t) j * N + id_of_pos[p]] = *d;
-    *d = kInfD;
+    const uint64_t j = i / N;
+    staging[i] = tmp[j * N + pos_of_id[i - j * N]];
   }
 }
 
@@ -409,7 +436,7 @@ uint64_t sssp_lane_bytes(uint32_t N, uint32_t L)
 {
   const uint64_t W = L / 64;
   return (uint64_t) N * L * 4 + (uint64_t) N * W * 8 * 2 + (uint64_t) N * W * 4 * 6 + (uint64_t) N * 4 +
-         (uint64_t) kOutChunkS * N * 4 + 4096 + L * 16;
+         (uint64_t) kOutChunkS * N * 4 * 2 + 4096 + L * 16;
 }
 
 void finish_ticket(la3g_server* S, Ticket* t, int status)
@@ -538,6 +565,7 @@ int sssp_engine_init(Engine* E)
   LA3G_TRY(E->adm.alloc((uint64_t) L * 8));
   LA3G_TRY(E->ret.alloc((uint64_t) L * 4));
   LA3G_TRY(E->staging.alloc((uint64_t) kOutChunkS * N * 4));
+  LA3G_TRY(E->outpos.alloc((uint64_t) kOutChunkS * N * 4));
   LA3G_CUDA(cudaMemsetAsync(E->ctr.p, 0, 64, s));
   k_ls_fill_u32<<<kSMs * 8, 256, 0, s>>>((uint64_t) N * L, E->dist.as<uint32_t>(), kInfD);
   LA3G_LAUNCHED();
@@ -584,6 +612,7 @@ int bfs_retire(Engine* E, const std::vector<uint32_t>& lanes_in, bool deliver, u
     }
     LA3G_CUDA(cudaMemcpyAsync(E->ret.p, wm.data(), W * 8, cudaMemcpyHostToDevice, s));
     LA3G_CUDA(cudaMemcpyAsync(E->ret.as<uint8_t>() + W * 8, wb.data(), W * 4, cudaMemcpyHostToDevice, s));
+    ProfileScope prof("serve_bfs_out", s, 0.0);
     k_lb_out_pos<<<kSMs * 8, 256, 0, s>>>(E->ret.as<uint64_t>(), (const uint32_t*) (E->ret.as<uint8_t>() + W * 8), N, W,
                                           E->hops.as<uint8_t>(), E->outpos.as<uint8_t>());
     LA3G_LAUNCHED();
@@ -776,6 +805,7 @@ int bfs_loop(Engine* E)
     }
     if (pull_words)
     {
+      ProfileScope prof("serve_bfs_pull", s, 0.0);
       k_lb_pull<<<kSMs * 8, 256, 0, s>>>(g.in_ptr, g.in_col, nrows, N, W, E->vis.as<uint64_t>(), front, next,
                                          E->alive[cur].as<uint64_t>(), E->alive[cur ^ 1].as<uint64_t>(),
                                          E->hops.as<uint8_t>(), hop, pull_words, fdeg);
@@ -786,6 +816,7 @@ int bfs_loop(Engine* E)
     }
     if (push_words)
     {
+      ProfileScope prof("serve_bfs_push", s, 0.0);
       k_lb_list<<<kSMs * 8, 256, 0, s>>>(NW, W, front, push_words, E->active.as<uint32_t>(), ctr + 2);
       LA3G_LAUNCHED();
       k_lb_push<<<kSMs * 8, 256, 0, s>>>(g.in_ptr, g.in_col, W, front, E->vis.as<uint64_t>(), next,
@@ -831,6 +862,7 @@ int sssp_retire(Engine* E, const std::vector<uint32_t>& lanes)
   {
     const uint32_t nl = (uint32_t) std::min<size_t>(kOutChunkS, lanes.size() - j0);
     LA3G_CUDA(cudaMemcpyAsync(E->ret.p, lanes.data() + j0, nl * 4, cudaMemcpyHostToDevice, s));
+    ProfileScope prof("serve_sssp_out", s, 0.0);
     if (g.nsink)
     {
       k_ls_sinks<<<kSMs * 8, 256, 0, s>>>(g.in_ptr, g.in_col, g.in_w, g.nreg, g.nsink, L, E->ret.as<uint32_t>(), nl,
@@ -838,10 +870,12 @@ int sssp_retire(Engine* E, const std::vector<uint32_t>& lanes)
       LA3G_LAUNCHED();
       tls_launches++;
     }
-    k_ls_out<<<kSMs * 8, 256, 0, s>>>(E->ret.as<uint32_t>(), nl, N, L, g.id_of_pos, E->dist.as<uint32_t>(),
-                                      E->staging.as<uint32_t>());
+    k_ls_out_pos<<<kSMs * 8, 256, 0, s>>>(E->ret.as<uint32_t>(), nl, N, L, E->dist.as<uint32_t>(),
+                                          E->outpos.as<uint32_t>());
     LA3G_LAUNCHED();
-    tls_launches++;
+    k_ls_out_id<<<kSMs * 8, 256, 0, s>>>(nl, N, g.pos_of_id, E->outpos.as<uint32_t>(), E->staging.as<uint32_t>());
+    LA3G_LAUNCHED();
+    tls_launches += 2;
     for (uint32_t j = 0; j < nl; j++)
     {
       Ticket* t = E->lane[lanes[j0 + j]];
