@@ -55,8 +55,11 @@ struct BatchScratch
   uint64_t* alive[2] = {nullptr, nullptr};  // [W] per-word "discovered something" masks
   uint8_t* hops = nullptr;   // [N][W * 64] by position (vertex-major)
   uint32_t* rpos = nullptr;  // root positions
-  uint32_t* active = nullptr;  // push: active (vertex, word) pairs
-  unsigned long long* ctr = nullptr;  // [0] new bits, [1] active pairs, [2] frontier edges*words, [3] level
+  uint32_t* active = nullptr;  // push: active (vertex, word) pairs of small vertices
+  uint32_t* phub = nullptr;    // push: pairs of hub vertices, and their first task numbers
+  uint32_t* phub_t0 = nullptr;
+  unsigned long long* ctr = nullptr;  // [0] new bits, [1] small pairs, [2] frontier edges*words, [3] level,
+                                      // [4] levels that found something, [5] hub slots / tasks (packed)
   unsigned long long* hctr = nullptr;
   unsigned int* bar = nullptr;        // grid barrier: count, generation
   int* err = nullptr;
@@ -183,39 +186,25 @@ __global__ void k_ms_advance(uint32_t W, BufPair alive, unsigned long long* ctr)
 
 // Top-down level: list the nonzero frontier words, push them to neighbours
 // (masked by visited), then apply.
-__global__ void k_ms_list(uint32_t nrows, uint32_t W, BufPair buf, const uint32_t* __restrict__ ptr, uint32_t* active,
-                          unsigned long long* ctr)
+__global__ void k_ms_list(uint32_t nrows, uint32_t W, BufPair buf, const uint32_t* __restrict__ ptr, PairList out,
+                          const unsigned long long* __restrict__ ctr)
 {
   const uint32_t level = (uint32_t) ctr[3];
   const uint64_t* front = buf.p[level & 1];
   const uint64_t NW = (uint64_t) nrows * W;
   for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < NW; i += (uint64_t) gridDim.x * blockDim.x)
-    if (front[i]) active[atomicAdd(&ctr[1], 1ull)] = (uint32_t) i;
+    if (front[i])
+    {
+      const uint32_t v = (uint32_t) (i / W);
+      bs_list_pair((uint32_t) i, ptr[v + 1] - ptr[v], out);
+    }
 }
 
 __global__ void k_ms_push(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, uint32_t W, BufPair buf,
-                          const uint64_t* __restrict__ vis, const uint32_t* __restrict__ active,
-                          unsigned long long* ctr)
+                          const uint64_t* __restrict__ vis, PairList list, const unsigned long long* __restrict__ ctr)
 {
   const uint32_t level = (uint32_t) ctr[3];
-  const uint64_t* front = buf.p[level & 1];
-  uint64_t* next = buf.p[(level + 1) & 1];
-  const uint32_t n = (uint32_t) ctr[1];
-  const int lane = threadIdx.x & 31;
-  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t a = warp; a < n; a += nwarps)
-  {
-    const uint32_t i = active[a];
-    const uint32_t u = i / W, w = i % W;
-    const uint64_t f = front[i];
-    for (uint32_t e = ptr[u] + lane; e < ptr[u + 1]; e += 32)
-    {
-      const uint64_t j = (uint64_t) col[e] * W + w;
-      const uint64_t nb = f & ~vis[j];
-      if (nb && (next[j] & nb) != nb) atomicOr((unsigned long long*) &next[j], (unsigned long long) nb);
-    }
-  }
+  ms_push_pairs(ptr, col, W, buf.p[level & 1], vis, buf.p[(level + 1) & 1], list);
 }
 
 __global__ void k_ms_apply(uint32_t nrows, uint32_t N, uint32_t W, uint64_t* vis, BufPair buf, BufPair alive,
@@ -395,6 +384,8 @@ static int ms_bfs_alloc(la3g_graph* G, BatchScratch* b, uint32_t R)
   LA3G_TRY(galloc(G, &b->hops, (size_t) N * W * 64));
   LA3G_TRY(galloc(G, &b->rpos, R));
   LA3G_TRY(galloc(G, &b->active, (size_t) N * W));
+  LA3G_TRY(galloc(G, &b->phub, (size_t) N * W));
+  LA3G_TRY(galloc(G, &b->phub_t0, (size_t) N * W));
   b->cap_r = R;
   if (b->pull_exec)
   {
@@ -508,9 +499,11 @@ static int ms_bfs_run(la3g_graph* G, BatchScratch* b, const uint32_t* roots_host
     if (push)
     {
       ProfileScope p("msbfs_push", s, 0.0);
+      const PairList pl{b->active, b->phub, b->phub_t0, b->ctr + 1, b->ctr + 5};
+      LA3G_CUDA(cudaMemsetAsync(b->ctr + 5, 0, 8, s));
       k_ms_clear<<<blocks, cfg.block, 0, s>>>((uint64_t) N * W, buf, b->ctr);
-      k_ms_list<<<blocks, cfg.block, 0, s>>>(nrows, W, buf, g.in_ptr, b->active, b->ctr);
-      k_ms_push<<<blocks, cfg.block, 0, s>>>(g.in_ptr, g.in_col, W, buf, b->vis, b->active, b->ctr);
+      k_ms_list<<<blocks, cfg.block, 0, s>>>(nrows, W, buf, g.in_ptr, pl, b->ctr);
+      k_ms_push<<<blocks, cfg.block, 0, s>>>(g.in_ptr, g.in_col, W, buf, b->vis, pl, b->ctr);
       k_ms_apply<<<blocks, cfg.block, 0, s>>>(nrows, N, W, b->vis, buf, alive, b->hops, b->ctr);
       k_ms_advance<<<1, 256, 0, s>>>(W, alive, b->ctr);
       LA3G_LAUNCHED();

@@ -224,6 +224,49 @@ static __global__ void k_bs_apply(uint32_t N, uint32_t W, const uint32_t* __rest
   }
 }
 
+// Top-down step of a multi-source BFS over a split list of frontier
+// (vertex, word) pairs (small pairs a warp each, hub edges as kHubTask-edge
+// tasks): each edge's target gets the word's bits that it has not visited,
+// ORed into its next word (skipped when already there).
+static __device__ __forceinline__ void ms_push_pairs(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col,
+                                                     uint32_t W, const uint64_t* __restrict__ front,
+                                                     const uint64_t* __restrict__ vis, uint64_t* next, const PairList& L)
+{
+  const int lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t ns = (uint32_t) *L.nsmall;
+  const unsigned long long pk = *L.packed;
+  const uint32_t nbig = hub_count(pk), ntasks = hub_tasks(pk);
+  for (uint32_t a = warp; a < ntasks + ns; a += nwarps)
+  {
+    uint32_t i, k0, k1;
+    if (a < ntasks)
+    {
+      const uint32_t slot = hub_of_task(L.hub_t0, nbig, a);
+      i = L.hub[slot];
+      const uint32_t u = i / W;
+      k0 = ptr[u] + (a - L.hub_t0[slot]) * kHubTask;
+      k1 = min(k0 + kHubTask, ptr[u + 1]);
+    }
+    else
+    {
+      i = L.small[a - ntasks];
+      const uint32_t u = i / W;
+      k0 = ptr[u];
+      k1 = ptr[u + 1];
+    }
+    const uint32_t w = i % W;
+    const uint64_t f = front[i];
+    for (uint32_t e = k0 + lane; e < k1; e += 32)
+    {
+      const uint64_t j = (uint64_t) col[e] * W + w;
+      const uint64_t nb = f & ~vis[j];
+      if (nb && (next[j] & nb) != nb) atomicOr((unsigned long long*) &next[j], (unsigned long long) nb);
+    }
+  }
+}
+
 // Initial active list: the nonzero words of the root frontier.
 static __global__ void k_bs_list(uint64_t NW, uint32_t W, const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ reg_end,
                           const uint64_t* __restrict__ front, PairList out)

@@ -142,35 +142,24 @@ __global__ void k_lb_clear(uint64_t NW, uint32_t W, uint64_t* buf, uint64_t word
     if ((words >> (i % W)) & 1ull) buf[i] = 0;
 }
 
-__global__ void k_lb_list(uint64_t NW, uint32_t W, const uint64_t* __restrict__ front, uint64_t words, uint32_t* active,
-                          unsigned long long* n)
+__global__ void k_lb_list(uint64_t NW, uint32_t W, const uint32_t* __restrict__ ptr, const uint64_t* __restrict__ front,
+                          uint64_t words, PairList out)
 {
   for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < NW; i += (uint64_t) gridDim.x * blockDim.x)
-    if (((words >> (i % W)) & 1ull) && front[i]) active[atomicAdd(n, 1ull)] = (uint32_t) i;
+    if (((words >> (i % W)) & 1ull) && front[i])
+    {
+      const uint32_t v = (uint32_t) (i / W);
+      bs_list_pair((uint32_t) i, ptr[v + 1] - ptr[v], out);
+    }
 }
 
-// Top-down step: one warp per listed frontier word, ORing it into the
-// neighbours' next words (masked by visited).
+// Top-down step over the listed frontier words (ms_push_pairs: small pairs a
+// warp each, hub edges as tasks), ORing them into the neighbours' next words
+// (masked by visited).
 __global__ void k_lb_push(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, uint32_t W,
-                          const uint64_t* __restrict__ front, const uint64_t* __restrict__ vis, uint64_t* next,
-                          const uint32_t* __restrict__ active, const unsigned long long* __restrict__ nactive)
+                          const uint64_t* __restrict__ front, const uint64_t* __restrict__ vis, uint64_t* next, PairList list)
 {
-  const uint32_t n = (uint32_t) *nactive;
-  const int lane = threadIdx.x & 31;
-  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t a = warp; a < n; a += nwarps)
-  {
-    const uint32_t i = active[a];
-    const uint32_t u = i / W, w = i % W;
-    const uint64_t f = front[i];
-    for (uint32_t e = ptr[u] + lane; e < ptr[u + 1]; e += 32)
-    {
-      const uint64_t j = (uint64_t) col[e] * W + w;
-      const uint64_t nb = f & ~vis[j];
-      if (nb && (next[j] & nb) != nb) atomicOr((unsigned long long*) &next[j], (unsigned long long) nb);
-    }
-  }
+  ms_push_pairs(ptr, col, W, front, vis, next, list);
 }
 
 // After a push: new bits = next & ~visited; the old frontier words of the
@@ -428,7 +417,7 @@ uint32_t solo_depth(const Engine* E)
 uint64_t bfs_lane_bytes(uint32_t N, uint32_t L)
 {
   const uint64_t W = L / 64;
-  return (uint64_t) N * W * 8 * 3 + (uint64_t) N * L + (uint64_t) N * W * 4 + (uint64_t) kOutChunk * N * 2 + 4096 +
+  return (uint64_t) N * W * 8 * 3 + (uint64_t) N * L + (uint64_t) N * W * 4 * 3 + (uint64_t) kOutChunk * N * 2 + 4096 +
          L * 16;
 }
 
@@ -524,6 +513,8 @@ int bfs_engine_init(Engine* E)
   LA3G_TRY(E->alive[0].alloc(W * 8));
   LA3G_TRY(E->alive[1].alloc(W * 8));
   LA3G_TRY(E->active.alloc(NW * 4));
+  LA3G_TRY(E->hub[0].alloc(NW * 4));
+  LA3G_TRY(E->hub_t0[0].alloc(NW * 4));
   LA3G_TRY(E->ctr.alloc(8 * 8));
   LA3G_TRY(E->adm.alloc((uint64_t) L * 8));
   LA3G_TRY(E->ret.alloc((uint64_t) L * 4));
@@ -817,10 +808,11 @@ int bfs_loop(Engine* E)
     if (push_words)
     {
       ProfileScope prof("serve_bfs_push", s, 0.0);
-      k_lb_list<<<kSMs * 8, 256, 0, s>>>(NW, W, front, push_words, E->active.as<uint32_t>(), ctr + 2);
+      const PairList pl{E->active.as<uint32_t>(), E->hub[0].as<uint32_t>(), E->hub_t0[0].as<uint32_t>(), ctr + 2, ctr + 4};
+      LA3G_CUDA(cudaMemsetAsync(ctr + 4, 0, 8, s));
+      k_lb_list<<<kSMs * 8, 256, 0, s>>>(NW, W, g.in_ptr, front, push_words, pl);
       LA3G_LAUNCHED();
-      k_lb_push<<<kSMs * 8, 256, 0, s>>>(g.in_ptr, g.in_col, W, front, E->vis.as<uint64_t>(), next,
-                                         E->active.as<uint32_t>(), ctr + 2);
+      k_lb_push<<<kSMs * 8, 256, 0, s>>>(g.in_ptr, g.in_col, W, front, E->vis.as<uint64_t>(), next, pl);
       LA3G_LAUNCHED();
       k_lb_apply<<<kSMs * 8, 256, 0, s>>>(g.in_ptr, nrows, N, W, E->vis.as<uint64_t>(), front, next,
                                           E->alive[cur ^ 1].as<uint64_t>(), E->hops.as<uint8_t>(), hop, push_words,

@@ -165,7 +165,7 @@ def test_budget_admission(gpu, servers):
     S.free()
     # the graph fits with fewer lanes: the engine is halved to 64
     N = gu.nslots
-    lane128 = N * 2 * 8 * 3 + N * 128 + N * 2 * 4 + 2 * 64 * N + 4096 + 128 * 16
+    lane128 = N * 2 * 8 * 3 + N * 128 + N * 2 * 4 * 3 + 2 * 64 * N + 4096 + 128 * 16
     S = servers(need + lane128 - 1, bfs_lanes=128)
     gid = S.add_graph(gu)
     assert S.lanes(gid) == 64
