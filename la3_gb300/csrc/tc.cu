@@ -48,6 +48,7 @@ struct TcScratch
 {
   uint32_t* plus_ptr = nullptr;  // [nslots + 1] by original id
   uint32_t* plus_col = nullptr;  // [nent] ids, each row ascending
+  uint32_t* plus_col_r = nullptr;  // [nent] the same rows ordered by rank (ids stored)
   uint32_t* order = nullptr;     // ids with 0 < |N+| <= kTcSmall, heaviest first
   uint32_t* order_mid = nullptr; // ids with kTcSmall < |N+| <= kTcCap, heaviest first
   uint32_t* big = nullptr;       // ids with |N+| > kTcCap
@@ -60,10 +61,11 @@ struct TcScratch
   // hub-centric pairs: small x with y in N+(x), |N+(y)| > max(|N+(x)|, kTcHubMin)
   uint32_t* hub_ptr = nullptr;   // [nslots + 1] by id of y
   uint32_t* hub_x = nullptr;     // the x's of each hub y
+  uint32_t* hub_j = nullptr;     // ... and the index of y in x's rank-ordered row
   uint32_t* hubs = nullptr;      // hub ids, heaviest first
   uint32_t nhubs = 0;
   uint32_t hub_pairs = 0;
-  double hub_items = 0;          // sum over hub pairs of |N+(x)|
+  double hub_items = 0;          // sum over hub pairs of the part of N+(x) ranked above y
   double hub_lists = 0;          // sum over hubs of |N+(y)|
 };
 
@@ -111,6 +113,40 @@ __global__ void k_tc_rows(const uint64_t* __restrict__ k, uint64_t m, uint32_t N
     int64_t rp = i == 0 ? -1 : (int64_t) (k[i - 1] >> 32);
     for (int64_t q = rp + 1; q <= r; q++) ptr[q] = (uint32_t) i;
   }
+}
+
+// Vertex ranks for the rank-ordered rows: keys (degree, id) sorted give
+// rank -> id; rank_of_id is its inverse.
+__global__ void k_tc_vkeys(uint32_t N, const uint32_t* __restrict__ deg, uint64_t* keys)
+{
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < N; v += gridDim.x * blockDim.x)
+    keys[v] = (uint64_t) deg[v] << 32 | v;
+}
+
+__global__ void k_tc_ranks(uint32_t N, const uint64_t* __restrict__ sorted, uint32_t* rank_of_id, uint32_t* id_of_rank)
+{
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < N; r += gridDim.x * blockDim.x)
+  {
+    const uint32_t v = (uint32_t) sorted[r];
+    rank_of_id[v] = r;
+    id_of_rank[r] = v;
+  }
+}
+
+// (x, id) keys of the id-ordered rows -> (x, rank) keys, and back to ids
+// once sorted.
+__global__ void k_tc_rank_keys(const uint64_t* __restrict__ k, uint64_t m, const uint32_t* __restrict__ rank_of_id,
+                               uint64_t* out)
+{
+  for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (uint64_t) gridDim.x * blockDim.x)
+    out[i] = (k[i] & 0xFFFFFFFF00000000ull) | rank_of_id[(uint32_t) k[i]];
+}
+
+__global__ void k_tc_rank_ids(const uint64_t* __restrict__ k, uint64_t m, const uint32_t* __restrict__ id_of_rank,
+                              uint32_t* col)
+{
+  for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (uint64_t) gridDim.x * blockDim.x)
+    col[i] = id_of_rank[(uint32_t) k[i]];
 }
 
 // Work estimate per vertex and the lists of vertices to process.
@@ -286,9 +322,10 @@ __device__ __forceinline__ uint32_t lower_bound_s(const uint32_t* s, uint32_t n,
 // search into N+(x), or a global one into N+(y)); lanes share the
 // concatenated work of all y.  A hit w closes the triangle {x, y, w}, which
 // is counted at its middle id.
-// Counts, per hub y, the x's (|N+(x)| <= kTcCap) pointing at it and their
-// list lengths.
-__global__ void k_tc_hub_count(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, uint32_t N,
+// Counts, per hub y, the x's (|N+(x)| <= kTcCap) pointing at it and the
+// part of their rows a walk reads: only the elements ranked above y (after y
+// in the rank-ordered row) can lie in N+(y).
+__global__ void k_tc_hub_count(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ colr, uint32_t N,
                                uint32_t* cnt, unsigned long long* work)
 {
   for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < N; x += gridDim.x * blockDim.x)
@@ -297,18 +334,18 @@ __global__ void k_tc_hub_count(const uint32_t* __restrict__ ptr, const uint32_t*
     if (d == 0 || d > kTcCap) continue;
     for (uint32_t i = b; i < b + d; i++)
     {
-      const uint32_t y = col[i];
+      const uint32_t y = colr[i];
       if (tc_is_hub_pair(d, ptr[y + 1] - ptr[y]))
       {
         atomicAdd(&cnt[y], 1u);
-        atomicAdd(&work[y], (unsigned long long) d);
+        atomicAdd(&work[y], (unsigned long long) (b + d - i - 1));
       }
     }
   }
 }
 
-__global__ void k_tc_hub_fill(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, uint32_t N,
-                              const uint32_t* __restrict__ hub_ptr, uint32_t* fill, uint32_t* hub_x)
+__global__ void k_tc_hub_fill(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ colr, uint32_t N,
+                              const uint32_t* __restrict__ hub_ptr, uint32_t* fill, uint32_t* hub_x, uint32_t* hub_j)
 {
   for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < N; x += gridDim.x * blockDim.x)
   {
@@ -316,8 +353,13 @@ __global__ void k_tc_hub_fill(const uint32_t* __restrict__ ptr, const uint32_t* 
     if (d == 0 || d > kTcCap) continue;
     for (uint32_t i = b; i < b + d; i++)
     {
-      const uint32_t y = col[i];
-      if (tc_is_hub_pair(d, ptr[y + 1] - ptr[y])) hub_x[hub_ptr[y] + atomicAdd(&fill[y], 1u)] = x;
+      const uint32_t y = colr[i];
+      if (tc_is_hub_pair(d, ptr[y + 1] - ptr[y]))
+      {
+        const uint32_t slot = hub_ptr[y] + atomicAdd(&fill[y], 1u);
+        hub_x[slot] = x;
+        hub_j[slot] = i - b;
+      }
     }
   }
 }
@@ -362,16 +404,17 @@ __global__ void k_tc_hub_keys(uint32_t N, const uint32_t* __restrict__ cnt, cons
 
 // One block per hub y (heaviest first): N+(y) is staged in shared memory
 // with a hash set and Bloom bits; warps take the x's pointing at y, their
-// lanes walk N+(x) (coalesced) and probe N+(y).  A hit w closes the
+// lanes walk the part of x's rank-ordered row after y (coalesced; the rest
+// is ranked below y and cannot lie in N+(y)) and probe N+(y).  A hit w closes the
 // triangle {x, y, w}, counted at its middle id: y and w in shared counters
 // (flushed once per hub), x through a warp sum per x.  (A flattened walk
 // over chunks of x's, which fills the lanes better for short N+(x), measured
 // slower: its staging and barriers cost more than the idle lanes.)
 template <uint32_t CAP, int THREADS>
 __global__ void __launch_bounds__(THREADS)
-k_tc_hub(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ hubs,
-         uint32_t nhubs, const uint32_t* __restrict__ hub_ptr, const uint32_t* __restrict__ hub_x, unsigned int* next,
-         uint32_t* ntri)
+k_tc_hub(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ colr,
+         const uint32_t* __restrict__ hubs, uint32_t nhubs, const uint32_t* __restrict__ hub_ptr,
+         const uint32_t* __restrict__ hub_x, const uint32_t* __restrict__ hub_j, unsigned int* next, uint32_t* ntri)
 {
   constexpr int NW = THREADS / 32;
   __shared__ uint32_t L[CAP], Cn[CAP], key[2 * CAP];
@@ -407,14 +450,15 @@ k_tc_hub(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, con
     for (uint32_t h = h0 + wib; h < h1; h += NW)
     {
       const uint32_t x = hub_x[h];
-      const uint32_t xb = ptr[x], xd = ptr[x + 1] - xb;
+      const uint32_t j1 = hub_j[h] + 1;
+      const uint32_t xb = ptr[x] + j1, xd = ptr[x + 1] - xb;
       const uint32_t mn = min(x, y), mx = max(x, y);
       uint32_t cnt_x = 0, cnt_y = 0;
       for (uint32_t r0 = lane; r0 < xd; r0 += 4 * 32)
       {
         uint32_t wv[4];
 #pragma unroll
-        for (int u = 0; u < 4; u++) wv[u] = r0 + u * 32 < xd ? col[xb + r0 + u * 32] : kEmpty;
+        for (int u = 0; u < 4; u++) wv[u] = r0 + u * 32 < xd ? colr[xb + r0 + u * 32] : kEmpty;
 #pragma unroll
         for (int u = 0; u < 4; u++)
         {
@@ -688,7 +732,30 @@ static int tc_prepare(la3g_graph* G, TcScratch* ts)
     LA3G_CUDA(cub::DeviceRadixSort::SortKeys(tmp.p, tb, k1.as<uint64_t>(), k2.as<uint64_t>(), m, 0, end_bit, s));
     k_tc_split_keys<<<grid_for(m, 256), 256, 0, s>>>(k2.as<uint64_t>(), m, ts->plus_col);
     LA3G_LAUNCHED();
+    // the same rows ordered by rank (degree, id), for the hub walks
+    DevBuf vk, vk2, rk, ir, k3, t3;
+    LA3G_TRY(vk.alloc((size_t) N * 8));
+    LA3G_TRY(vk2.alloc((size_t) N * 8));
+    LA3G_TRY(rk.alloc((size_t) N * 4));
+    LA3G_TRY(ir.alloc((size_t) N * 4));
+    LA3G_TRY(k3.alloc(m * 8 + 8));
+    k_tc_vkeys<<<grid_for(N, 256), 256, 0, s>>>(N, deg.as<uint32_t>(), vk.as<uint64_t>());
+    LA3G_LAUNCHED();
+    size_t tv = 0;
+    LA3G_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, tv, vk.as<uint64_t>(), vk2.as<uint64_t>(), N, 0, 64, s));
+    LA3G_TRY(t3.alloc(std::max(tv, tb)));
+    LA3G_CUDA(cub::DeviceRadixSort::SortKeys(t3.p, tv, vk.as<uint64_t>(), vk2.as<uint64_t>(), N, 0, 64, s));
+    k_tc_ranks<<<grid_for(N, 256), 256, 0, s>>>(N, vk2.as<uint64_t>(), rk.as<uint32_t>(), ir.as<uint32_t>());
+    LA3G_LAUNCHED();
+    k_tc_rank_keys<<<grid_for(m, 256), 256, 0, s>>>(k2.as<uint64_t>(), m, rk.as<uint32_t>(), k3.as<uint64_t>());
+    LA3G_LAUNCHED();
+    LA3G_CUDA(cub::DeviceRadixSort::SortKeys(t3.p, tb, k3.as<uint64_t>(), k1.as<uint64_t>(), m, 0, end_bit, s));
+    LA3G_TRY(galloc(G, &ts->plus_col_r, m + 1));
+    k_tc_rank_ids<<<grid_for(m, 256), 256, 0, s>>>(k1.as<uint64_t>(), m, ir.as<uint32_t>(), ts->plus_col_r);
+    LA3G_LAUNCHED();
+    LA3G_CUDA(cudaStreamSynchronize(s));
   }
+  else LA3G_TRY(galloc(G, &ts->plus_col_r, 1));
   k_tc_rows<<<grid_for(m + 1, 256), 256, 0, s>>>(k2.as<uint64_t>(), m, N, ts->plus_ptr);
   LA3G_LAUNCHED();
   LA3G_TRY(wkey.alloc((size_t) N * 4));
@@ -730,7 +797,7 @@ static int tc_prepare(la3g_graph* G, TcScratch* ts)
   LA3G_TRY(hwork.alloc((size_t) N * 8));
   LA3G_CUDA(cudaMemsetAsync(hcnt.p, 0, (size_t) (N + 1) * 4, s));
   LA3G_CUDA(cudaMemsetAsync(hwork.p, 0, (size_t) N * 8, s));
-  k_tc_hub_count<<<grid_for(N, 256), 256, 0, s>>>(ts->plus_ptr, ts->plus_col, N, hcnt.as<uint32_t>(),
+  k_tc_hub_count<<<grid_for(N, 256), 256, 0, s>>>(ts->plus_ptr, ts->plus_col_r, N, hcnt.as<uint32_t>(),
                                                   hwork.as<unsigned long long>());
   LA3G_LAUNCHED();
   LA3G_TRY(galloc(G, &ts->hub_ptr, N + 1));
@@ -745,6 +812,7 @@ static int tc_prepare(la3g_graph* G, TcScratch* ts)
   LA3G_CUDA(cudaMemcpyAsync(&npairs, ts->hub_ptr + N, 4, cudaMemcpyDeviceToHost, s));
   LA3G_CUDA(cudaStreamSynchronize(s));
   LA3G_TRY(galloc(G, &ts->hub_x, std::max<uint32_t>(npairs, 1)));
+  LA3G_TRY(galloc(G, &ts->hub_j, std::max<uint32_t>(npairs, 1)));
   ts->hub_pairs = npairs;
   LA3G_TRY(galloc(G, &ts->hubs, N));
   if (npairs)
@@ -752,8 +820,8 @@ static int tc_prepare(la3g_graph* G, TcScratch* ts)
     DevBuf fill;
     LA3G_TRY(fill.alloc((size_t) N * 4));
     LA3G_CUDA(cudaMemsetAsync(fill.p, 0, (size_t) N * 4, s));
-    k_tc_hub_fill<<<grid_for(N, 256), 256, 0, s>>>(ts->plus_ptr, ts->plus_col, N, ts->hub_ptr, fill.as<uint32_t>(),
-                                                   ts->hub_x);
+    k_tc_hub_fill<<<grid_for(N, 256), 256, 0, s>>>(ts->plus_ptr, ts->plus_col_r, N, ts->hub_ptr, fill.as<uint32_t>(),
+                                                   ts->hub_x, ts->hub_j);
     LA3G_LAUNCHED();
     LA3G_TRY(hkeys.alloc((size_t) N * 4));
     LA3G_TRY(hkeys2.alloc((size_t) N * 4));
@@ -835,10 +903,11 @@ extern "C" int la3g_tc(la3g_graph* G, uint64_t* total_out, uint32_t* per_vertex_
   }
   if (ts->nhubs)
   {
-    // N+(x) of every hub pair + each hub's N+(y) once + two offsets per pair
-    ProfileScope p("tc_hub", s, 4.0 * ts->hub_items + 4.0 * ts->hub_lists + 8.0 * (double) ts->hub_pairs);
-    k_tc_hub<kTcHubCap, 256><<<kSMs * 6, 256, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->hubs, ts->nhubs, ts->hub_ptr,
-                                                      ts->hub_x, ts->next + 2, ts->ntri);
+    // the walked part of N+(x) of every hub pair + each hub's N+(y) once + the
+    // pair's x, index and two offsets
+    ProfileScope p("tc_hub", s, 4.0 * ts->hub_items + 4.0 * ts->hub_lists + 16.0 * (double) ts->hub_pairs);
+    k_tc_hub<kTcHubCap, 256><<<kSMs * 6, 256, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->plus_col_r, ts->hubs, ts->nhubs,
+                                                      ts->hub_ptr, ts->hub_x, ts->hub_j, ts->next + 2, ts->ntri);
     LA3G_LAUNCHED();
   }
   if (ts->nbig)
