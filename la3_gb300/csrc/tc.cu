@@ -34,6 +34,7 @@ static constexpr uint32_t kTcSmall = 192;    // lists up to this length use the 
 static constexpr uint32_t kTcWalkFactor = 16;  // heavy x: N+(y) is walked unless > 16 |N+(x)| (then searched)
 static constexpr uint32_t kTcHubMin = 32;    // N+(y) longer than this (and than N+(x)) is a hub list:
 static constexpr uint32_t kTcHubCap = 1024;  // ... small x's pairs with it go to the hub kernel, up to this length
+static constexpr int kTcHubLanes = 8;        // lanes per hub pair in k_tc_hub
 
 // A pair (x, y) of a list N+(x) (at most kTcCap long) with a longer list
 // N+(y) of moderate length: instead of walking N+(y) against N+(x), or
@@ -410,18 +411,17 @@ __global__ void k_tc_hub_keys(uint32_t N, const uint32_t* __restrict__ cnt, cons
 // (flushed once per hub), x through a warp sum per x.  (A flattened walk
 // over chunks of x's, which fills the lanes better for short N+(x), measured
 // slower: its staging and barriers cost more than the idle lanes.)
-template <uint32_t CAP, int THREADS>
+template <uint32_t CAP, int THREADS, int G>
 __global__ void __launch_bounds__(THREADS)
 k_tc_hub(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ colr,
          const uint32_t* __restrict__ hubs, uint32_t nhubs, const uint32_t* __restrict__ hub_ptr,
          const uint32_t* __restrict__ hub_x, const uint32_t* __restrict__ hub_j, unsigned int* next, uint32_t* ntri)
 {
-  constexpr int NW = THREADS / 32;
   __shared__ uint32_t L[CAP], Cn[CAP], key[2 * CAP];
   __shared__ uint16_t idx[2 * CAP];
   __shared__ uint32_t bloom[kBloomBits / 32];
   __shared__ uint32_t s_k, s_y;
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
   for (uint32_t i = threadIdx.x; i < kBloomBits / 32; i += THREADS) bloom[i] = 0;
   for (;;)
   {
@@ -447,18 +447,22 @@ k_tc_hub(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, con
     }
     __syncthreads();
     const uint32_t h0 = hub_ptr[y], h1 = hub_ptr[y + 1];
-    for (uint32_t h = h0 + wib; h < h1; h += NW)
+    // G lanes per pair (THREADS / G pairs at a time): the walked suffixes are
+    // short, so whole warps per pair left most lanes idle
+    const int gl = lane % G;
+    const unsigned gmask = (G == 32 ? 0xffffffffu : ((1u << G) - 1) << (lane - gl));
+    for (uint32_t h = h0 + threadIdx.x / G; h < h1; h += THREADS / G)
     {
       const uint32_t x = hub_x[h];
       const uint32_t j1 = hub_j[h] + 1;
       const uint32_t xb = ptr[x] + j1, xd = ptr[x + 1] - xb;
       const uint32_t mn = min(x, y), mx = max(x, y);
       uint32_t cnt_x = 0, cnt_y = 0;
-      for (uint32_t r0 = lane; r0 < xd; r0 += 4 * 32)
+      for (uint32_t r0 = gl; r0 < xd; r0 += 4 * G)
       {
         uint32_t wv[4];
 #pragma unroll
-        for (int u = 0; u < 4; u++) wv[u] = r0 + u * 32 < xd ? colr[xb + r0 + u * 32] : kEmpty;
+        for (int u = 0; u < 4; u++) wv[u] = r0 + u * G < xd ? colr[xb + r0 + u * G] : kEmpty;
 #pragma unroll
         for (int u = 0; u < 4; u++)
         {
@@ -483,12 +487,12 @@ k_tc_hub(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, con
           }
         }
       }
-      for (int o = 16; o > 0; o >>= 1)
+      for (int o = G / 2; o > 0; o >>= 1)
       {
-        cnt_x += __shfl_xor_sync(0xffffffffu, cnt_x, o);
-        cnt_y += __shfl_xor_sync(0xffffffffu, cnt_y, o);
+        cnt_x += __shfl_xor_sync(gmask, cnt_x, o);
+        cnt_y += __shfl_xor_sync(gmask, cnt_y, o);
       }
-      if (lane == 0)
+      if (gl == 0)
       {
         if (cnt_x) atomicAdd(&ntri[x], cnt_x);
         if (cnt_y) atomicAdd(&s_y, cnt_y);
@@ -906,7 +910,7 @@ extern "C" int la3g_tc(la3g_graph* G, uint64_t* total_out, uint32_t* per_vertex_
     // the walked part of N+(x) of every hub pair + each hub's N+(y) once + the
     // pair's x, index and two offsets
     ProfileScope p("tc_hub", s, 4.0 * ts->hub_items + 4.0 * ts->hub_lists + 16.0 * (double) ts->hub_pairs);
-    k_tc_hub<kTcHubCap, 256><<<kSMs * 6, 256, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->plus_col_r, ts->hubs, ts->nhubs,
+    k_tc_hub<kTcHubCap, 256, kTcHubLanes><<<kSMs * 6, 256, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->plus_col_r, ts->hubs, ts->nhubs,
                                                       ts->hub_ptr, ts->hub_x, ts->hub_j, ts->next + 2, ts->ntri);
     LA3G_LAUNCHED();
   }
