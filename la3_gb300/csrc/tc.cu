@@ -413,8 +413,7 @@ __global__ void k_tc_hub_keys(uint32_t N, const uint32_t* __restrict__ cnt, cons
 // slower: its staging and barriers cost more than the idle lanes.)
 template <uint32_t CAP, int THREADS, int G>
 __global__ void __launch_bounds__(THREADS)
-k_tc_hub(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ colr,
-         const uint32_t* __restrict__ hubs, uint32_t nhubs, const uint32_t* __restrict__ hub_ptr,
+k_tc_hub(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ colr, const uint32_t* __restrict__ hubs, uint32_t nhubs, const uint32_t* __restrict__ hub_ptr,
          const uint32_t* __restrict__ hub_x, const uint32_t* __restrict__ hub_j, unsigned int* next, uint32_t* ntri)
 {
   __shared__ uint32_t L[CAP], Cn[CAP], key[2 * CAP];
@@ -438,7 +437,7 @@ k_tc_hub(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, con
     __syncthreads();
     for (uint32_t j = threadIdx.x; j < d; j += THREADS)
     {
-      const uint32_t w = col[yb + j];
+      const uint32_t w = colr[yb + j];  // set order is free: read the rows the walks read
       L[j] = w;
       Cn[j] = 0;
       tc_insert_t(key, idx, lg, w, j);
@@ -910,7 +909,7 @@ extern "C" int la3g_tc(la3g_graph* G, uint64_t* total_out, uint32_t* per_vertex_
     // the walked part of N+(x) of every hub pair + each hub's N+(y) once + the
     // pair's x, index and two offsets
     ProfileScope p("tc_hub", s, 4.0 * ts->hub_items + 4.0 * ts->hub_lists + 16.0 * (double) ts->hub_pairs);
-    k_tc_hub<kTcHubCap, 256, kTcHubLanes><<<kSMs * 6, 256, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->plus_col_r, ts->hubs, ts->nhubs,
+    k_tc_hub<kTcHubCap, 256, kTcHubLanes><<<kSMs * 6, 256, 0, s>>>(ts->plus_ptr, ts->plus_col_r, ts->hubs, ts->nhubs,
                                                       ts->hub_ptr, ts->hub_x, ts->hub_j, ts->next + 2, ts->ntri);
     LA3G_LAUNCHED();
   }
