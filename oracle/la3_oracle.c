@@ -979,12 +979,11 @@ static int iv_cmp(const void* a, const void* b)
   return x->id < y->id ? -1 : x->id > y->id;
 }
 
-int og_bm25_query(og_bm25* b, const uint32_t* term_vids, uint32_t nterms, uint32_t k,
-                  float* scores, uint8_t* active, uint32_t* topk_ids, float* topk_scores,
-                  uint32_t* ntopk)
+/* One query of the BM25 / LM TFIDF program over the shared states S. */
+static int ir_query(const og_graph* g, og_vp* vp, const dt_state* S, const uint32_t* term_vids, uint32_t nterms,
+                    uint32_t k, float* scores, uint8_t* active, uint32_t* topk_ids, float* topk_scores,
+                    uint32_t* ntopk)
 {
-  const og_graph* g = b->g;
-  og_vp* vp = &b->vp;
   /* reset() then initialize(vids) (vertex_program.hpp:51-63, 177-259): each
    * listed vertex is initialised in list order; regular ones push their
    * scatter.  The pushes go through the StreamingArray, so a list that is
@@ -1018,8 +1017,8 @@ int og_bm25_query(og_bm25* b, const uint32_t* term_vids, uint32_t nterms, uint32
     if (!vp->active[i]) continue;
     uint32_t o = hb_unhash(g, g->hash_of_pos[i]);
     ivs[j].id = o;
-    ivs[j].score = b->S[i].score;
-    if (scores) scores[o] = b->S[i].score;
+    ivs[j].score = S[i].score;
+    if (scores) scores[o] = S[i].score;
     if (active) active[o] = 1;
     j++;
   }
@@ -1032,11 +1031,125 @@ int og_bm25_query(og_bm25* b, const uint32_t* term_vids, uint32_t nterms, uint32
   }
   if (ntopk) *ntopk = kk;
   free(ivs);
-  memset(vp->active, 0, g->nslots);  /* tfidf.reset_activity() (bm25.cpp:79) */
+  memset(vp->active, 0, g->nslots);  /* tfidf.reset_activity() (bm25.cpp:79, lm.cpp:86) */
   return OG_OK;
 }
 
+int og_bm25_query(og_bm25* b, const uint32_t* term_vids, uint32_t nterms, uint32_t k,
+                  float* scores, uint8_t* active, uint32_t* topk_ids, float* topk_scores,
+                  uint32_t* ntopk)
+{
+  return ir_query(b->g, &b->vp, b->S, term_vids, nterms, k, scores, active, topk_ids, topk_scores, ntopk);
+}
+
 void og_bm25_free(og_bm25* b)
+{
+  if (!b) return;
+  vp_free(&b->vp);
+  free(b->S);
+  free(b);
+}
+
+/* ---------------------------------------------------------------------- */
+/* LM: query likelihood with Dirichlet smoothing (lm.h:16-75,             */
+/* lm.cpp:8-144).                                                          */
+/* ---------------------------------------------------------------------- */
+
+static const float LM_MU = 2000.0f;
+
+struct og_lm
+{
+  const og_graph* g;
+  dt_state* S;
+  og_vp vp;       /* TFIDF program */
+  og_prog prog;
+  uint32_t query_nterms;
+};
+
+static bool tl_apply(void* c, const void* y, void* s, uint32_t iter)
+{
+  /* s.length = y / collection_ntokens (lm.h:55): the uint64 count converts to
+   * float, then a float divide */
+  uint64_t ntok = *(const uint64_t*) c;
+  ((dt_state*) s)->length = *(const float*) y / (float) ntok;
+  return true;
+}
+static void lm_gather(void* c, uint32_t src, uint32_t dst, uint32_t w, const void* m, const void* ds, void* a)
+{
+  /* log10(1.0 + w / (mu * msg)) (lm.h:71): the quotient is float, 1.0
+   * promotes it to double, log10 is the double function and the result is
+   * stored as float */
+  float q = (float) w / (LM_MU * *(const float*) m);
+  *(float*) a = (float) log10(1.0 + (double) q);
+}
+static bool lm_apply(void* c, const void* y, void* s, uint32_t iter)
+{
+  /* s.score = y + query_nterms * log10(mu / (s.length + mu)) (lm.h:73-74):
+   * the argument is float, so log10 resolves to the float overload (log10f
+   * of the platform's libm, which is not correctly rounded), and the rest is
+   * float arithmetic */
+  uint32_t nq = *(const uint32_t*) c;
+  dt_state* st = (dt_state*) s;
+  float t = log10f(LM_MU / (st->length + LM_MU));
+  st->score = *(const float*) y + (float) nq * t;
+  return true;
+}
+
+int og_lm_prepare(const og_graph* g, og_lm** out, uint64_t* collection_ntokens, float* length)
+{
+  *out = NULL;
+  if (!(g->flags & OG_BIPARTITE) || (g->flags & OG_DIRECTED))
+    return og_fail(OG_EINVAL, "lm needs load_bipartite(directed=false)");
+  og_lm* b = (og_lm*) calloc(1, sizeof(og_lm));
+  dt_state* S = (dt_state*) calloc(g->nslots, sizeof(dt_state));
+  uint8_t* active = (uint8_t*) calloc(g->nslots, 1);
+  if (!b || !S || !active) { free(b); free(S); free(active); return og_fail(OG_ENOMEM, "out of memory"); }
+  b->g = g;
+  b->S = S;
+  /* Step 1: DL over terms -> docs (lm.cpp:18-22): length(d) = sum of tf. */
+  float avg0 = 0.0f;
+  og_prog pdl = {0, sizeof(float), sizeof(dt_state), true, false, false, &avg0,
+                 empty_scatter, dl_gather, f32_combine, dl_apply, f32_zero};
+  int rc = run_bipartite(g, &pdl, S, false, true, NULL);
+  /* collection_ntokens = sum over every vertex of (uint64) its float length
+   * (lm.cpp:26-29); terms still hold 0 here */
+  uint64_t ntok = 0;
+  for (uint32_t i = 0; i < g->nslots && !rc; i++)
+  {
+    float f = S[i].length;
+    ntok += (f <= -1.0f) ? 0u : (uint64_t) f;
+  }
+  /* Step 2: TL over docs -> terms (lm.cpp:33-39). */
+  og_prog ptl = {0, sizeof(float), sizeof(dt_state), true, false, false, &ntok,
+                 empty_scatter, dl_gather, f32_combine, tl_apply, f32_zero};
+  if (!rc) rc = run_bipartite(g, &ptl, S, true, false, active);
+  if (rc) { free(active); free(S); free(b); return rc; }
+  /* TFIDF program (lm.cpp:46), sharing the states.  Its gather reads no
+   * state, so no mirrors are taken at its first initialize and the activity
+   * the TL pass left (every term it reached) is still set in the first
+   * query's top-k pool (score 0); tfidf.reset_activity() clears it after. */
+  og_prog pt = {sizeof(float), sizeof(float), sizeof(dt_state), false, false, false, &b->query_nterms,
+                tfidf_scatter, lm_gather, f32_combine, lm_apply, f32_zero};
+  b->prog = pt;
+  rc = vp_init(&b->vp, g, &b->prog, (char*) S);
+  if (!rc) memcpy(b->vp.active, active, g->nslots);
+  free(active);
+  if (rc) { og_lm_free(b); return rc; }
+  if (collection_ntokens) *collection_ntokens = ntok;
+  if (length)
+    for (uint32_t i = 0; i < g->nslots; i++) length[hb_unhash(g, g->hash_of_pos[i])] = S[i].length;
+  *out = b;
+  return OG_OK;
+}
+
+int og_lm_query(og_lm* b, const uint32_t* term_vids, uint32_t nterms, uint32_t k, float* scores,
+                uint8_t* active, uint32_t* topk_ids, float* topk_scores, uint32_t* ntopk)
+{
+  b->query_nterms = nterms;  /* tfidf.query_nterms = queries[q].size() (lm.cpp:66) */
+  return ir_query(b->g, &b->vp, b->S, term_vids, nterms, k, scores, active, topk_ids, topk_scores, ntopk);
+}
+
+void og_lm_free(og_lm* b)
 {
   if (!b) return;
   vp_free(&b->vp);

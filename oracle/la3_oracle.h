@@ -9,7 +9,7 @@
  * SimpleBucketHasher, vertex classification, locators, per-tile dedup + CSC),
  * its BSP execution engine (VertexProgram::execute and its optimizable /
  * non-optimizable / single-iteration paths) and the six apps (pr, bfs, sssp,
- * cc, tc, bm25).  Every result is indexed by ORIGINAL vertex id 0..nslots-1.
+ * cc, tc, bm25, lm).  Every result is indexed by ORIGINAL vertex id 0..nslots-1.
  * Function comments cite the reference file:line each one follows.
  *
  * Parity is pinned against the reference itself: the same sources are built
@@ -81,6 +81,14 @@ int og_bm25_query(og_bm25* b, const uint32_t* term_vids, uint32_t nterms, uint32
                   float* scores, uint8_t* active, uint32_t* topk_ids, float* topk_scores,
                   uint32_t* ntopk);
 void og_bm25_free(og_bm25* b);
+
+/* LM (lm.cpp:8-144), same graph and query conventions as BM25.  length:
+ * length(d) for docs, length(t) for terms after the TL pass. */
+typedef struct og_lm og_lm;
+int og_lm_prepare(const og_graph* g, og_lm** out, uint64_t* collection_ntokens, float* length /* nullable */);
+int og_lm_query(og_lm* b, const uint32_t* term_vids, uint32_t nterms, uint32_t k, float* scores,
+                uint8_t* active, uint32_t* topk_ids, float* topk_scores, uint32_t* ntopk);
+void og_lm_free(og_lm* b);
 
 const char* og_last_error(void);
 

@@ -53,6 +53,9 @@ def lib() -> C.CDLL:
             "og_bm25_prepare": (C.c_int, [P, C.POINTER(P), u64p, f32p, f32p]),
             "og_bm25_query": (C.c_int, [P, u32p, C.c_uint32, C.c_uint32, f32p, u8p, u32p, f32p, u32p]),
             "og_bm25_free": (None, [P]),
+            "og_lm_prepare": (C.c_int, [P, C.POINTER(P), u64p, f32p]),
+            "og_lm_query": (C.c_int, [P, u32p, C.c_uint32, C.c_uint32, f32p, u8p, u32p, f32p, u32p]),
+            "og_lm_free": (None, [P]),
             "og_last_error": (C.c_char_p, []),
         }
         for k, (r, a) in sig.items():
@@ -160,6 +163,39 @@ class OracleBM25:
         try:
             if self.h:
                 lib().og_bm25_free(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+
+class OracleLM:
+    """LM (lm.cpp:8-144) on the oracle's engine: same query interface as
+    OracleBM25."""
+
+    def __init__(self, g: OracleGraph):
+        self.g = g
+        self.h = C.c_void_p()
+        ntok = C.c_uint64()
+        self.length = np.empty(g.nslots, np.float32)
+        _check(lib().og_lm_prepare(g.h, C.byref(self.h), C.byref(ntok), _p(self.length, C.c_float)))
+        self.collection_ntokens = ntok.value
+
+    def query(self, term_vids: Sequence[int], k: int):
+        q = np.ascontiguousarray(np.asarray(term_vids, np.uint32))
+        n = self.g.nslots
+        scores = np.empty(n, np.float32)
+        active = np.empty(n, np.uint8)
+        ids = np.empty(max(k, 1), np.uint32)
+        sc = np.empty(max(k, 1), np.float32)
+        nk = C.c_uint32()
+        _check(lib().og_lm_query(self.h, _p(q, C.c_uint32), q.size, k, _p(scores, C.c_float), _p(active, C.c_uint8),
+                                 _p(ids, C.c_uint32), _p(sc, C.c_float), C.byref(nk)))
+        return ids[:nk.value].copy(), sc[:nk.value].copy(), scores, active
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib().og_lm_free(self.h)
                 self.h = None
         except Exception:
             pass

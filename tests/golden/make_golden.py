@@ -55,6 +55,7 @@ def write_records(path: Path, recs: list[tuple], weighted: bool) -> None:
 
 
 def main() -> None:
+    only_lm = "--only-lm" in sys.argv  # regenerate the LM cases alone (other fixtures untouched)
     if not (REF_BIN / "dump_pr").exists():
         sys.exit("build the reference first: make -C oracle stage ref")
     from la3_gb300 import EdgeList  # host-side generators; no GPU needed
@@ -97,6 +98,17 @@ def main() -> None:
     qlines += ["t9 t3", "t3 t9", "t5 t5 t2", "t400 t1 t200", "tnope t7"]
     (DATA / "bip.queries").write_text("\n".join(qlines) + "\n")
 
+    # LM corpus whose doc and term token sums pass 2^24, where the order of
+    # the float additions shows in the result
+    brng = np.random.default_rng(13)
+    brecs = []
+    for d in range(1, 61):
+        for t in sorted(set(int(x) for x in brng.integers(1, 25, 9))):
+            brecs.append((d, t, int(brng.integers(1, 3_000_000))))
+    write_records(DATA / "bigtf.w.bp.bin", brecs, True)
+    (DATA / "bigtf.term.labels").write_text("".join(f"b{i} {i}\n" for i in range(1, 25)))
+    (DATA / "bigtf.queries").write_text("b1 b2\nb24 b7 b3\nb5\nb9 b9 b11\nb20 b1 b14 b6\n")
+
     cases = {}
     tmp = Path(tempfile.mkdtemp())
 
@@ -132,9 +144,9 @@ def main() -> None:
         np.savez_compressed(GOLD / f"{name}.npz", ntri=load(o, ".ntri.u32", np.uint32))
         cases[name] = {"app": "tc", "file": f, "n": n, **meta}
 
-    def bm25_case(name, f, labels_f, ndocs, nterms, queries_f, k):
+    def bm25_case(name, f, labels_f, ndocs, nterms, queries_f, k, app="bm25"):
         o = tmp / name
-        meta = run_dump([REF_BIN / "dump_bm25", DATA / f, DATA / labels_f, ndocs, nterms, DATA / queries_f, k, o])
+        meta = run_dump([REF_BIN / f"dump_{app}", DATA / f, DATA / labels_f, ndocs, nterms, DATA / queries_f, k, o])
         raw = np.fromfile(str(o) + ".queries.bin", dtype=np.uint32)
         i = 0
         arrays = {"length": load(o, ".length.f32", np.float32)}
@@ -150,8 +162,22 @@ def main() -> None:
             arrays[f"q{nq}_topk_scores"] = tk[:, 1].copy().view(np.float32)
             nq += 1
         np.savez_compressed(GOLD / f"{name}.npz", **arrays)
-        cases[name] = {"app": "bm25", "file": f, "labels": labels_f, "queries": queries_f, "ndocs": ndocs,
+        cases[name] = {"app": app, "file": f, "labels": labels_f, "queries": queries_f, "ndocs": ndocs,
                        "nterms": nterms, "k": k, **meta}
+
+    def lm_cases():
+        bm25_case("g2_lm", "g2_7_7_17.w.bp.bin", "g2_7_7_17.term.labels", 7, 7, "g2_7_7_17.queries", 3, app="lm")
+        bm25_case("bip_lm", "bip.w.bp.bin", "bip.term.labels", ndocs, nterms, "bip.queries", 10, app="lm")
+        bm25_case("bigtf_lm", "bigtf.w.bp.bin", "bigtf.term.labels", 60, 24, "bigtf.queries", 8, app="lm")
+
+    if only_lm:
+        lm_cases()
+        old = json.loads((GOLD / "golden.json").read_text())
+        old.update(cases)
+        (GOLD / "golden.json").write_text(json.dumps(old, indent=1, sort_keys=True) + "\n")
+        shutil.rmtree(tmp)
+        print(f"{len(cases)} LM cases written to {GOLD}")
+        return
 
     pr_case("g1_pr", "g1_8_8_13.bin", 8, 20)
     pr_case("g1_pr_conv", "g1_8_8_13.bin", 8, 0)
@@ -190,6 +216,7 @@ def main() -> None:
     bfs_case("isolated_root_bfs", "rmat10.bin", 1024, 0)
     sssp_case("isolated_root_sssp", "rmat10.w.bin", 1024, 0)
     bm25_case("bip_bm25", "bip.w.bp.bin", "bip.term.labels", ndocs, nterms, "bip.queries", 10)
+    lm_cases()
 
     (GOLD / "golden.json").write_text(json.dumps(cases, indent=1, sort_keys=True) + "\n")
     shutil.rmtree(tmp)

@@ -14,12 +14,12 @@ def _cases(golden, app):
 
 def test_golden_manifest_complete(golden):
     apps = {v["app"] for v in golden.values()}
-    assert apps == {"pr", "bfs", "sssp", "cc", "tc", "bm25"}
+    assert apps == {"pr", "bfs", "sssp", "cc", "tc", "bm25", "lm"}
     for k in golden:
         assert (GOLD / f"{k}.npz").exists(), k
 
 
-@pytest.mark.parametrize("app", ["pr", "bfs", "sssp", "cc", "tc", "bm25"])
+@pytest.mark.parametrize("app", ["pr", "bfs", "sssp", "cc", "tc", "bm25", "lm"])
 def test_oracle_matches_reference(golden, oracle, app):
     O = oracle
     for name in _cases(golden, app):
@@ -53,7 +53,7 @@ def test_oracle_matches_reference(golden, oracle, app):
             assert total == c["triangles"], name
         else:
             g = O.OracleGraph(f, c["ndocs"], O.BIPARTITE | O.WEIGHTED, nright=c["nterms"])
-            b = O.OracleBM25(g)
+            b = O.OracleBM25(g) if app == "bm25" else O.OracleLM(g)
             assert b.collection_ntokens == c["collection_ntokens"], name
             assert np.array_equal(b.length.view(np.uint32), ref["length"].view(np.uint32)), name
             queries = O.read_queries(DATA / c["labels"], DATA / c["queries"], c["ndocs"])
