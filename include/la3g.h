@@ -212,6 +212,22 @@ int la3g_bm25_query(la3g_graph* g, const uint32_t* term_vids, uint32_t nterms, u
                     uint32_t* ids_out, float* scores_out, uint32_t* nout, float* all_scores_out,
                     uint8_t* active_out, la3g_stats* st);
 
+/* LM, query likelihood with Dirichlet smoothing (mu = 2000)
+ * (src/apps/information_retrieval/lm.cpp:8-144, lm.h:16-75), on a graph
+ * loaded with LA3G_BIPARTITE (undirected).  prepare runs the DL and TL
+ * passes; length_out (nslots, nullable) receives length(d) for docs and
+ * length(t) for terms.  The score's per-vertex factor log10f(mu / (length +
+ * mu)) is evaluated here with the platform's log10f, the function the
+ * reference calls (lm.h:74). */
+int la3g_lm_prepare(la3g_graph* g, uint64_t* collection_ntokens_out, float* length_out);
+
+/* One LM query, same conventions as la3g_bm25_query.  As in the reference,
+ * the first query after prepare also ranks the term vertices the TL pass
+ * left active (score 0), since the LM program takes no mirrors. */
+int la3g_lm_query(la3g_graph* g, const uint32_t* term_vids, uint32_t nterms, uint32_t k,
+                  uint32_t* ids_out, float* scores_out, uint32_t* nout, float* all_scores_out,
+                  uint8_t* active_out, la3g_stats* st);
+
 /* ---- batched multi-source forms (no reference counterpart; the reference
  *      runs one root per VertexProgram, bfs.cpp:11-37 / sssp.cpp:11-37) ---- */
 

@@ -229,6 +229,32 @@ class BM25:
         return ids[:n].copy(), scores[:n].copy(), (alls, act), st
 
 
+class LM:
+    """lm.cpp:8-144 (query likelihood, Dirichlet smoothing) over a bipartite
+    graph: prepare once, then query (same interface as BM25)."""
+
+    def __init__(self, G: Graph, want_length: bool = False):
+        self.G = G
+        ntok = C.c_uint64(0)
+        self.length = np.empty(G.nslots, np.float32) if want_length else None
+        N.check(N.lib().la3g_lm_prepare(G._h, C.byref(ntok), _ptr(self.length, C.c_float)))
+        self.collection_ntokens = ntok.value
+
+    def query(self, term_vids: Sequence[int], k: int = 10, full: bool = False):
+        q = np.ascontiguousarray(np.asarray(term_vids, dtype=np.uint32))
+        ids = np.empty(max(k, 1), np.uint32)
+        scores = np.empty(max(k, 1), np.float32)
+        nout = C.c_uint32(0)
+        st = Stats()
+        alls = np.empty(self.G.nslots, np.float32) if full else None
+        act = np.empty(self.G.nslots, np.uint8) if full else None
+        N.check(N.lib().la3g_lm_query(self.G._h, _ptr(q, C.c_uint32), q.size, k, _ptr(ids, C.c_uint32),
+                                      _ptr(scores, C.c_float), C.byref(nout), _ptr(alls, C.c_float),
+                                      _ptr(act, C.c_uint8), C.byref(st)))
+        n = nout.value
+        return ids[:n].copy(), scores[:n].copy(), (alls, act), st
+
+
 def read_queries(labels_path: str, queries_path: str, ndocs: int) -> list[list[int]]:
     """prepare_queries (helpers.hpp:76-123): the label on line i of the term
     labels file is term vertex ndocs + i + 1; each query line is a list of
@@ -455,5 +481,5 @@ def profile_report() -> dict:
 
 
 __all__ = ["Graph", "EdgeList", "BM25", "LA3GError", "Stats", "pagerank", "pagerank_f32", "bfs", "sssp", "cc", "tc",
-           "bfs_batch", "sssp_batch", "batch_autotune", "batch_config", "read_queries", "profile", "profile_reset", "profile_report", "DIRECTED", "REVERSE", "ACYCLIC",
+           "LM", "bfs_batch", "sssp_batch", "batch_autotune", "batch_config", "read_queries", "profile", "profile_reset", "profile_report", "DIRECTED", "REVERSE", "ACYCLIC",
            "BIPARTITE", "WEIGHTED", "SSSP_INF", "BFS_INF"]

@@ -28,14 +28,13 @@
 #include <vector>
 
 #include "la3g_internal.h"
+#include "ir.cuh"
 
 namespace la3g {
 
+static_assert(kTopBlocks == 2 * kSMs, "two partial top-k blocks per SM");
 static constexpr float kK1 = 1.2f;
 static constexpr float kB = 0.75f;
-static constexpr int kTopKMax = 64;
-static constexpr int kTopBlocks = 2 * kSMs;
-static constexpr int kTopThreads = 128;
 
 struct Bm25Scratch
 {
@@ -286,7 +285,7 @@ static int bm25_scratch(la3g_graph* G, Bm25Scratch** out)
 }
 
 // First term row: positions ascend with ids, docs (ids <= D) come first.
-static int first_term_row(la3g_graph* G, uint32_t* out)
+int bipartite_first_term_row(la3g_graph* G, uint32_t* out)
 {
   DevGraph& g = G->g;
   // binary search over id_of_pos[0, nreg) for the first id > nleft
@@ -318,7 +317,7 @@ extern "C" int la3g_bm25_prepare(la3g_graph* G, uint64_t* ntokens_out, float* av
   const uint32_t N = g.nslots;
   LA3G_CUDA(cudaStreamSynchronize(s));
   uint32_t tb = 0;
-  LA3G_TRY(first_term_row(G, &tb));
+  LA3G_TRY(bipartite_first_term_row(G, &tb));
   b->term_row0 = tb;
   LA3G_CUDA(cudaMemsetAsync(b->length, 0, (size_t) N * 4, s));
   LA3G_CUDA(cudaMemsetAsync(b->ctr, 0, 4 * 8, s));

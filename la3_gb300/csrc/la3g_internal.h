@@ -161,7 +161,7 @@ struct DevGraph
 };
 
 // Per-app device scratch cached on a graph handle (allocated on first use).
-enum AppSlot { kSlotPr = 0, kSlotBfs, kSlotSssp, kSlotCc, kSlotTc, kSlotBm25, kSlotBatch, kSlotVp, kSlotCount };
+enum AppSlot { kSlotPr = 0, kSlotBfs, kSlotSssp, kSlotCc, kSlotTc, kSlotBm25, kSlotBatch, kSlotVp, kSlotLm, kSlotCount };
 
 }  // namespace la3g
 
@@ -188,6 +188,8 @@ int galloc(la3g_graph* G, T** p, size_t count)
 }
 
 int build_push_csr(la3g_graph* G);
+// Bipartite corpus: the position of the first term row (docs come first).
+int bipartite_first_term_row(la3g_graph* G, uint32_t* out);
 
 // Bracket an app call: events on the graph's stream and the host clock.
 struct CallTimer

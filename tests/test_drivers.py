@@ -63,11 +63,12 @@ def test_graph_drivers(bins, golden):
         assert abs(_num(out, "Pagerank Checksum") - c["pr_checksum"]) <= 5e-7, name
 
 
-def test_bm25_driver(bins, golden):
-    for name in _cases(golden, "bm25"):
+@pytest.mark.parametrize("app", ["bm25", "lm"])
+def test_ir_driver(bins, golden, app):
+    for name in _cases(golden, app):
         c = golden[name]
         ref = np.load(GOLD / f"{name}.npz")
-        out = _run(bins / "bm25", DATA / c["file"], DATA / c["labels"], c["ndocs"], c["nterms"],
+        out = _run(bins / app, DATA / c["file"], DATA / c["labels"], c["ndocs"], c["nterms"],
                    DATA / c["queries"], c["k"])
         assert _num(out, "Collection.Tokens") == c["collection_ntokens"], name
         blocks = re.split(r"^q \d+ \(", out, flags=re.M)[1:]

@@ -159,13 +159,14 @@ def test_out_of_range_ids_rejected(gpu, tmp_path):
     assert ei.value.status == 1
 
 
-def test_bm25_golden(gpu, golden):
+@pytest.mark.parametrize("app", ["bm25", "lm"])
+def test_ir_golden(gpu, golden, app):
     L = gpu
-    for name in _cases(golden, "bm25"):
+    for name in _cases(golden, app):
         c = golden[name]
         ref = np.load(GOLD / f"{name}.npz")
         g = L.Graph.load_bipartite(DATA / c["file"], c["ndocs"], c["nterms"])
-        b = L.BM25(g, want_length=True)
+        b = L.BM25(g, want_length=True) if app == "bm25" else L.LM(g, want_length=True)
         assert b.collection_ntokens == c["collection_ntokens"], name
         assert np.array_equal(b.length.view(np.uint32), ref["length"].view(np.uint32)), name
         queries = L.read_queries(DATA / c["labels"], DATA / c["queries"], c["ndocs"])
@@ -203,3 +204,35 @@ def test_bm25_corpus_vs_oracle(gpu, oracle, tmp_path):
         assert np.array_equal(act, oact), qi
         assert np.array_equal(alls.view(np.uint32), oscores.view(np.uint32)), qi
         assert ids.tolist() == oids.tolist() and np.array_equal(sc, osc), qi
+
+
+def test_lm_corpus_vs_oracle(gpu, oracle, tmp_path):
+    """LM on a generated corpus against the oracle (same host libm for the
+    score's log10f factor): lengths, active sets and every score bit-exact,
+    including the first query's leftover term vertices."""
+    L = gpu
+    D, T = 20000, 3000
+    e = L.EdgeList.bipartite(D, T, 30, seed=78)
+    p = tmp_path / "c.w.bp.bin"
+    e.write(p)
+    g = L.Graph.load_bipartite(p, D, T)
+    b = L.LM(g, want_length=True)
+    og = oracle.OracleGraph(p, D, oracle.BIPARTITE | oracle.WEIGHTED, nright=T)
+    ob = oracle.OracleLM(og)
+    assert b.collection_ntokens == ob.collection_ntokens
+    assert np.array_equal(b.length.view(np.uint32), ob.length.view(np.uint32))
+    rng = np.random.default_rng(4)
+    for qi in range(30):
+        q = sorted(set(int(x) for x in rng.integers(D + 1, D + T + 1, int(rng.integers(2, 9)))))
+        if qi % 5 == 4:
+            q = q[::-1] + [q[0]]  # not ascending, with a repeat: the reference's pairing
+        if qi == 7:
+            q = [3, D + 5, 0]  # a doc vertex and vertex 0 in the list
+        ids, sc, (alls, act), _ = b.query(q, 20, full=True)
+        oids, osc, oscores, oact = ob.query(q, 20)
+        assert np.array_equal(act, oact), qi
+        assert np.array_equal(alls.view(np.uint32), oscores.view(np.uint32)), qi
+        assert ids.tolist() == oids.tolist() and np.array_equal(sc, osc), qi
+        if qi == 0:
+            assert act[D + 1:].sum() > 0  # the TL pass's term activity in the first query
+
