@@ -195,6 +195,21 @@ int la3g_cc(la3g_graph* g, uint32_t* label_out, la3g_stats* st);
  * the reference's accumulator does).  per_vertex_out may be NULL. */
 int la3g_tc(la3g_graph* g, uint64_t* total_out, uint32_t* per_vertex_out, la3g_stats* st);
 
+/* Degrees (src/apps/graph_analytics/degree.cpp:16-46, degree.h:17-35): on a
+ * graph loaded with LA3G_DIRECTED, the in-degree of every vertex (its number
+ * of distinct in-neighbours); loaded with LA3G_DIRECTED | LA3G_REVERSE, the
+ * out-degree (the reference's -o).  degree_out: nslots uint32 by id
+ * (nullable).  The k (<= 64) largest, degree desc, id asc, go to topk_ids /
+ * topk_degrees (nullable; *ntopk = min(k, nslots)). */
+int la3g_degree(la3g_graph* g, uint32_t* degree_out, uint32_t k, uint32_t* topk_ids, uint32_t* topk_degrees,
+                uint32_t* ntopk, la3g_stats* st);
+
+/* Top-k on the device over n uint32 values (a host array, index = id):
+ * the k (<= 64) largest, value desc, index asc (vertex_program.hpp:607-680,
+ * with the tie order fixed). */
+int la3g_topk_u32(const uint32_t* values, uint32_t n, uint32_t k, uint32_t* ids_out, uint32_t* values_out,
+                  uint32_t* nout);
+
 /* BM25 (src/apps/information_retrieval/bm25.cpp:8-114, bm25.h:11-92) on a
  * graph loaded with LA3G_BIPARTITE (undirected).  prepare runs the IDF and
  * the two doc-length passes; length_out (nslots, nullable) receives the

@@ -202,6 +202,31 @@ def tc(G: Graph, want_per_vertex: bool = True):
     return total.value, per, st
 
 
+def degree(G: Graph, k: int = 3):
+    """degree.cpp:16-46: in-degrees (out-degrees on a graph loaded with
+    reverse_edges) by id, and the top k (degree desc, id asc)."""
+    deg = np.empty(G.nslots, np.uint32)
+    ids = np.empty(max(k, 1), np.uint32)
+    vals = np.empty(max(k, 1), np.uint32)
+    n = C.c_uint32(0)
+    st = Stats()
+    N.check(N.lib().la3g_degree(G._h, _ptr(deg, C.c_uint32), k, _ptr(ids, C.c_uint32), _ptr(vals, C.c_uint32),
+                                C.byref(n), C.byref(st)))
+    return deg, ids[:n.value].copy(), vals[:n.value].copy(), st
+
+
+def topk_u32(values: np.ndarray, k: int):
+    """Top k of a uint32 array on the device: (indices, values), value desc,
+    index asc."""
+    v = np.ascontiguousarray(np.asarray(values, np.uint32))
+    ids = np.empty(max(k, 1), np.uint32)
+    vals = np.empty(max(k, 1), np.uint32)
+    n = C.c_uint32(0)
+    N.check(N.lib().la3g_topk_u32(_ptr(v, C.c_uint32), v.size, k, _ptr(ids, C.c_uint32), _ptr(vals, C.c_uint32),
+                                  C.byref(n)))
+    return ids[:n.value].copy(), vals[:n.value].copy()
+
+
 class BM25:
     """bm25.cpp:8-114 over a bipartite graph: prepare once, then query."""
 
@@ -481,5 +506,5 @@ def profile_report() -> dict:
 
 
 __all__ = ["Graph", "EdgeList", "BM25", "LA3GError", "Stats", "pagerank", "pagerank_f32", "bfs", "sssp", "cc", "tc",
-           "LM", "bfs_batch", "sssp_batch", "batch_autotune", "batch_config", "read_queries", "profile", "profile_reset", "profile_report", "DIRECTED", "REVERSE", "ACYCLIC",
+           "LM", "degree", "topk_u32", "bfs_batch", "sssp_batch", "batch_autotune", "batch_config", "read_queries", "profile", "profile_reset", "profile_report", "DIRECTED", "REVERSE", "ACYCLIC",
            "BIPARTITE", "WEIGHTED", "SSSP_INF", "BFS_INF"]

@@ -147,6 +147,8 @@ SIGNATURES = {
     "la3g_tc": (C.c_int, [_P, _u64p, _u32p, _statp]),
     "la3g_bm25_prepare": (C.c_int, [_P, _u64p, _f32p, _f32p]),
     "la3g_bm25_query": (C.c_int, [_P, _u32p, C.c_uint32, C.c_uint32, _u32p, _f32p, _u32p, _f32p, _u8p, _statp]),
+    "la3g_degree": (C.c_int, [_P, _u32p, C.c_uint32, _u32p, _u32p, _u32p, _statp]),
+    "la3g_topk_u32": (C.c_int, [_u32p, C.c_uint32, C.c_uint32, _u32p, _u32p, _u32p]),
     "la3g_lm_prepare": (C.c_int, [_P, _u64p, _f32p]),
     "la3g_lm_query": (C.c_int, [_P, _u32p, C.c_uint32, C.c_uint32, _u32p, _f32p, _u32p, _f32p, _u8p, _statp]),
     "la3g_bfs_batch": (C.c_int, [_P, _u32p, C.c_uint32, _u8p, _statp]),

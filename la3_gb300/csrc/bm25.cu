@@ -177,48 +177,6 @@ __device__ __forceinline__ unsigned long long bm25_key(float s, uint32_t id)
   return ((unsigned long long) u << 32) | (0xFFFFFFFFu - id);
 }
 
-// Block-level top-k of a key stream: each thread keeps its k best keys, the
-// block then extracts the k largest by repeated block-wide max.
-__device__ void block_topk(unsigned long long* mine, int k, unsigned long long* out)
-{
-  __shared__ unsigned long long s_best[kTopThreads];
-  __shared__ int s_who[kTopThreads];
-  for (int r = 0; r < k; r++)
-  {
-    unsigned long long m = 0;
-    int mi = -1;
-    for (int i = 0; i < k; i++)
-      if (mine[i] > m) { m = mine[i]; mi = i; }
-    s_best[threadIdx.x] = m;
-    s_who[threadIdx.x] = threadIdx.x;
-    __syncthreads();
-    for (int o = kTopThreads / 2; o > 0; o >>= 1)
-    {
-      if ((int) threadIdx.x < o && s_best[threadIdx.x + o] > s_best[threadIdx.x])
-      {
-        s_best[threadIdx.x] = s_best[threadIdx.x + o];
-        s_who[threadIdx.x] = s_who[threadIdx.x + o];
-      }
-      __syncthreads();
-    }
-    unsigned long long top = s_best[0];
-    int who = s_who[0];
-    __syncthreads();
-    if (threadIdx.x == 0) out[r] = top;
-    if ((int) threadIdx.x == who && mi >= 0 && top != 0) mine[mi] = 0;
-    __syncthreads();
-  }
-}
-
-__device__ __forceinline__ void keep_best(unsigned long long* mine, int k, unsigned long long key)
-{
-  int mi = 0;
-  unsigned long long mv = mine[0];
-  for (int i = 1; i < k; i++)
-    if (mine[i] < mv) { mv = mine[i]; mi = i; }
-  if (key > mv) mine[mi] = key;
-}
-
 __global__ void __launch_bounds__(kTopThreads)
 k_bm25_top_partial(const uint32_t* __restrict__ touched, const unsigned long long* __restrict__ ctr,
                    const float* __restrict__ score, const uint32_t* __restrict__ id_of_pos, int k,

@@ -1,7 +1,9 @@
-// Kernels shared by the two information-retrieval apps, BM25 (bm25.cu) and
+// Top-k over 64-bit keys (value in the high half, ~id in the low half, so
+// that ties go to the smaller id), used by BM25, LM and the degree app, and
+// the kernels the two information-retrieval apps share, BM25 (bm25.cu) and
 // LM (lm.cu), over a bipartite corpus: docs 1..D then terms D+1..D+T,
 // identity hash, so positions ascend with ids and a term's pull row lists
-// its docs ascending.  Defined in bm25.cu.
+// its docs ascending.  The kernels are defined in bm25.cu.
 #ifndef LA3G_IR_CUH
 #define LA3G_IR_CUH
 
@@ -12,6 +14,48 @@ namespace la3g {
 constexpr int kTopKMax = 64;       // largest k of a top-k query
 constexpr int kTopThreads = 128;   // threads of the top-k blocks
 constexpr int kTopBlocks = 2 * 152;  // partial top-k blocks (two per SM)
+
+// Block-level top-k of a key stream: each thread keeps its k best keys, the
+// block then extracts the k largest by repeated block-wide max.
+static __device__ void block_topk(unsigned long long* mine, int k, unsigned long long* out)
+{
+  __shared__ unsigned long long s_best[kTopThreads];
+  __shared__ int s_who[kTopThreads];
+  for (int r = 0; r < k; r++)
+  {
+    unsigned long long m = 0;
+    int mi = -1;
+    for (int i = 0; i < k; i++)
+      if (mine[i] > m) { m = mine[i]; mi = i; }
+    s_best[threadIdx.x] = m;
+    s_who[threadIdx.x] = threadIdx.x;
+    __syncthreads();
+    for (int o = kTopThreads / 2; o > 0; o >>= 1)
+    {
+      if ((int) threadIdx.x < o && s_best[threadIdx.x + o] > s_best[threadIdx.x])
+      {
+        s_best[threadIdx.x] = s_best[threadIdx.x + o];
+        s_who[threadIdx.x] = s_who[threadIdx.x + o];
+      }
+      __syncthreads();
+    }
+    unsigned long long top = s_best[0];
+    int who = s_who[0];
+    __syncthreads();
+    if (threadIdx.x == 0) out[r] = top;
+    if ((int) threadIdx.x == who && mi >= 0 && top != 0) mine[mi] = 0;
+    __syncthreads();
+  }
+}
+
+static __device__ __forceinline__ void keep_best(unsigned long long* mine, int k, unsigned long long key)
+{
+  int mi = 0;
+  unsigned long long mv = mine[0];
+  for (int i = 1; i < k; i++)
+    if (mine[i] < mv) { mv = mine[i]; mi = i; }
+  if (key > mv) mine[mi] = key;
+}
 
 // Sum of (float) tf over rows [row_lo, row_hi), ascending entry order, then
 // length = sum (avg == 0) or BM25's K(d) (avg > 0).

@@ -18,7 +18,8 @@ def declared_symbols():
 def test_header_declares_the_boundary():
     syms = declared_symbols()
     for s in ["la3g_graph_load", "la3g_pr", "la3g_bfs", "la3g_sssp", "la3g_cc", "la3g_tc", "la3g_bm25_prepare",
-              "la3g_bm25_query", "la3g_lm_prepare", "la3g_lm_query", "la3g_bfs_batch", "la3g_sssp_batch",
+              "la3g_bm25_query", "la3g_lm_prepare", "la3g_lm_query", "la3g_degree", "la3g_topk_u32",
+              "la3g_bfs_batch", "la3g_sssp_batch",
               "la3g_last_error_string"]:
         assert s in syms
 
@@ -107,10 +108,10 @@ def test_load_errors_are_reported(native, tmp_path):
 
 
 def test_drivers_and_programs_are_built(native):
-    """The seven command-line drivers and the vertex-program library exist;
+    """The eight command-line drivers and the vertex-program library exist;
     a driver prints its usage without touching a GPU."""
     import la3_gb300.build as B
-    for d in ("pr", "bfs", "sssp", "cc", "tc", "bm25", "lm"):
+    for d in ("pr", "bfs", "sssp", "cc", "tc", "bm25", "lm", "degree"):
         assert (B.BIN / d).exists(), d
     r = subprocess.run([str(B.BIN / "tc")], capture_output=True, text=True)
     assert r.returncode == 1 and "Usage" in r.stdout
