@@ -227,6 +227,76 @@ def topk_u32(values: np.ndarray, k: int):
     return ids[:n.value].copy(), vals[:n.value].copy()
 
 
+def _strtok(s: str, delims: str):
+    """C strtok on one string: skip leading delimiters, cut at the next one;
+    returns (token or None, rest)."""
+    i = 0
+    while i < len(s) and s[i] in delims:
+        i += 1
+    if i == len(s):
+        return None, ""
+    j = i
+    while j < len(s) and s[j] not in delims:
+        j += 1
+    return s[i:j], s[j + 1:]
+
+
+def read_graphsim_labels(path: str, nvertices: int) -> list[str]:
+    """Data-graph labels (graphsim.cpp:14-40): a first line "[", then one
+    line per vertex 0..nvertices-1 of the form {"key":"label"}, whose label
+    is taken as C strtok takes it (the text after the first ':' minus its
+    first character, up to the next '"'); a first line "null," leaves vertex
+    0 without a label.  Vertex nvertices never has one."""
+    labels = [""] * nvertices
+    with open(path, "rb") as f:
+        lines = f.read().decode("latin-1").split("\n")
+    for i in range(nvertices):
+        line = lines[i + 1].rstrip("\r") if i + 1 < len(lines) else ""
+        line = line[:2047]
+        if i == 0 and line == "null,":
+            continue
+        t, rest = _strtok(line, ":")
+        if t is None:
+            continue
+        t, _ = _strtok(rest, ":")
+        if t is None:
+            continue
+        t, _ = _strtok(t[1:], '"')
+        if t is not None:
+            labels[i] = t
+    return labels
+
+
+def read_graphsim_query(labels_path: str, mtx_path: str) -> tuple[list[str], list[tuple[int, int]]]:
+    """Query graph (graphsim_query.h:17-52): labels are whitespace-separated
+    tokens read with `while (!eof) { fin >> label; push }`, so a file that
+    ends in whitespace, or holds no token, yields one more, empty, label; the
+    matrix file holds pairs "i j" (edge i -> j), kept in file order."""
+    with open(labels_path, "rb") as f:
+        text = f.read().decode("latin-1")
+    toks = text.split()
+    labels = list(toks)
+    if not toks or text[-1:].isspace():
+        labels.append("")
+    with open(mtx_path) as f:
+        nums = [int(x) for x in f.read().split()]
+    edges = [(nums[2 * k], nums[2 * k + 1]) for k in range(len(nums) // 2)]
+    return labels, edges
+
+
+def graphsim_label_ids(vertex_labels: Sequence[str], query_labels: Sequence[str], nslots: int):
+    """Integer label ids, 0 for the empty string (no label), equal strings
+    equal ids: (per-vertex ids, nslots long, and the query's ids)."""
+    ids = {"": 0}
+    def lid(s):
+        return ids.setdefault(s, len(ids))
+    v = np.zeros(nslots, np.uint32)
+    for i, s in enumerate(vertex_labels):
+        v[i] = lid(s)
+    q = np.array([lid(s) for s in query_labels], np.uint32)
+    return v, q
+
+
 class BM25:
     """bm25.cpp:8-114 over a bipartite graph: prepare once, then query."""
 
@@ -506,5 +576,5 @@ def profile_report() -> dict:
 
 
 __all__ = ["Graph", "EdgeList", "BM25", "LA3GError", "Stats", "pagerank", "pagerank_f32", "bfs", "sssp", "cc", "tc",
-           "LM", "degree", "topk_u32", "bfs_batch", "sssp_batch", "batch_autotune", "batch_config", "read_queries", "profile", "profile_reset", "profile_report", "DIRECTED", "REVERSE", "ACYCLIC",
+           "LM", "degree", "topk_u32", "read_graphsim_labels", "read_graphsim_query", "graphsim_label_ids", "bfs_batch", "sssp_batch", "batch_autotune", "batch_config", "read_queries", "profile", "profile_reset", "profile_report", "DIRECTED", "REVERSE", "ACYCLIC",
            "BIPARTITE", "WEIGHTED", "SSSP_INF", "BFS_INF"]

@@ -1156,3 +1156,169 @@ void og_lm_free(og_lm* b)
   free(b->S);
   free(b);
 }
+
+/* ---------------------------------------------------------------------- */
+/* Graph simulation (graphsim.h:60-184, graphsim.cpp:45-90) on the data   */
+/* graph loaded reversed.  Labels are integer ids (equal strings, equal  */
+/* ids; 0 = the empty string); the query has at most 32 vertices, its     */
+/* children lists in file order.                                          */
+/* ---------------------------------------------------------------------- */
+
+#define GS_QMAX 32
+
+typedef struct
+{
+  uint32_t vid, label;
+  int32_t degree, deps;
+  uint32_t mm;           /* temp mismatches, bit i = query vertex i */
+  int32_t pm[GS_QMAX];   /* potential matches */
+  char res[GS_QMAX];     /* 'U' | '0' | '1' */
+} gs_state;
+
+typedef struct
+{
+  uint32_t qsize;
+  const uint32_t* qlabel;
+  const uint32_t* cptr;  /* children of query vertex i: cidx[cptr[i] .. cptr[i + 1]) */
+  const uint32_t* cidx;
+  const uint32_t* vlabel;  /* by vertex id */
+} gs_ctx;
+
+/* InitVertex (graphsim.h:70-92): label and out-degree (in-degree of the
+ * reversed graph), stationary, one pass. */
+static bool gsi_init(void* ctx, uint32_t vid, uint32_t pos, void* s)
+{
+  gs_state* st = (gs_state*) s;
+  st->vid = vid;
+  st->label = ((const gs_ctx*) ctx)->vlabel[vid];
+  return true;
+}
+static void gsi_gather(void* c, uint32_t src, uint32_t dst, uint32_t w, const void* m, const void* ds, void* a)
+{ *(int32_t*) a = 1; }
+static void i32_combine(void* c, const void* y1, void* y2) { *(int32_t*) y2 += *(const int32_t*) y1; }
+static void i32_zero(void* c, void* a) { *(int32_t*) a = 0; }
+static bool gsi_apply(void* c, const void* y, void* s, uint32_t iter)
+{ ((gs_state*) s)->degree = *(const int32_t*) y; return true; }
+
+/* GsVertex (graphsim.h:100-184). */
+static bool gs_init(void* ctx, uint32_t vid, uint32_t pos, void* s)
+{
+  const gs_ctx* q = (const gs_ctx*) ctx;
+  gs_state* st = (gs_state*) s;
+  st->mm = 0;
+  for (uint32_t i = 0; i < q->qsize; i++) { st->res[i] = 'U'; st->pm[i] = -1; }
+  for (uint32_t i = 0; i < q->qsize; i++)
+  {
+    const bool same = st->label == q->qlabel[i];
+    if (same && q->cptr[i] == q->cptr[i + 1]) st->res[i] = '1';
+    else if (same && st->degree > 0)
+    {
+      st->deps++;
+      for (uint32_t e = q->cptr[i]; e < q->cptr[i + 1]; e++) st->pm[q->cidx[e]] = st->degree;
+    }
+    else
+    {
+      st->res[i] = '0';
+      st->mm |= 1u << i;
+    }
+  }
+  return st->mm != 0;
+}
+static void gs_scatter(void* c, const void* s, void* m) { *(uint32_t*) m = ((const gs_state*) s)->mm; }
+static void gs_gather(void* c, uint32_t src, uint32_t dst, uint32_t w, const void* m, const void* ds, void* a)
+{
+  const gs_ctx* q = (const gs_ctx*) c;
+  uint32_t mask = *(const uint32_t*) m;
+  for (uint32_t i = 0; i < q->qsize; i++) ((int32_t*) a)[i] = (mask >> i) & 1u;
+}
+static void gs_combine(void* c, const void* y1, void* y2)
+{
+  const gs_ctx* q = (const gs_ctx*) c;
+  for (uint32_t i = 0; i < q->qsize; i++) ((int32_t*) y2)[i] += ((const int32_t*) y1)[i];
+}
+static void gs_zero(void* c, void* a) { memset(a, 0, (size_t) ((const gs_ctx*) c)->qsize * sizeof(int32_t)); }
+static bool gs_apply(void* c, const void* yv, void* s, uint32_t iter)
+{
+  const gs_ctx* q = (const gs_ctx*) c;
+  const int32_t* y = (const int32_t*) yv;
+  gs_state* st = (gs_state*) s;
+  if (st->label == 0) return false;  /* s.label.empty() */
+  st->mm = 0;
+  for (uint32_t i = 0; i < q->qsize; i++)
+  {
+    if (st->res[i] != 'U') continue;
+    /* only the first undecided query vertex is looked at (the loop breaks
+     * after it, graphsim.h:172) */
+    for (uint32_t e = q->cptr[i]; e < q->cptr[i + 1]; e++)
+    {
+      uint32_t j = q->cidx[e];
+      if (st->pm[j] > 0)
+      {
+        st->pm[j] -= y[j];
+        if (st->pm[j] == 0)
+        {
+          st->res[i] = '0';
+          st->mm |= 1u << i;
+          st->deps--;
+          break;
+        }
+      }
+    }
+    break;
+  }
+  return st->mm != 0;
+}
+
+int og_graphsim(const og_graph* g, const uint32_t* vlabel, uint32_t qsize, const uint32_t* qlabel,
+                const uint32_t* qedges, uint32_t nqedges, uint8_t* matched, char* res, uint32_t* nmatches,
+                uint32_t* niters)
+{
+  if (!(g->flags & OG_DIRECTED) || !(g->flags & OG_REVERSE))
+    return og_fail(OG_EINVAL, "graphsim needs load_directed(..., reverse=true)");
+  if (qsize == 0 || qsize > GS_QMAX) return og_fail(OG_EINVAL, "query size must be 1..32");
+  for (uint32_t e = 0; e < 2 * nqedges; e++)
+    if (qedges[e] >= qsize) return og_fail(OG_EINVAL, "query edge endpoint out of range");
+  uint32_t* cptr = (uint32_t*) calloc(qsize + 1, sizeof(uint32_t));
+  uint32_t* cidx = (uint32_t*) malloc((nqedges ? nqedges : 1) * sizeof(uint32_t));
+  uint32_t* fill = (uint32_t*) calloc(qsize, sizeof(uint32_t));
+  gs_state* S = (gs_state*) calloc(g->nslots, sizeof(gs_state));
+  if (!cptr || !cidx || !fill || !S)
+  { free(cptr); free(cidx); free(fill); free(S); return og_fail(OG_ENOMEM, "out of memory"); }
+  for (uint32_t e = 0; e < nqedges; e++) cptr[qedges[2 * e] + 1]++;
+  for (uint32_t i = 0; i < qsize; i++) cptr[i + 1] += cptr[i];
+  for (uint32_t e = 0; e < nqedges; e++) cidx[cptr[qedges[2 * e]] + fill[qedges[2 * e]]++] = qedges[2 * e + 1];
+  gs_ctx q = {qsize, qlabel, cptr, cidx, vlabel};
+  /* InitVertex vp_init(vp, true); vp_init.execute(1) (graphsim.cpp:55-64) */
+  og_prog pi = {0, sizeof(int32_t), sizeof(gs_state), true, false, false, &q,
+                empty_scatter, gsi_gather, i32_combine, gsi_apply, i32_zero};
+  og_vp vp;
+  int rc = vp_init(&vp, g, &pi, (char*) S);
+  if (!rc) rc = vp_initialize(&vp, gsi_init, &q);
+  if (!rc) vp_execute(&vp, 1);
+  vp_free(&vp);
+  /* vp.execute() until convergence (graphsim.cpp:72) */
+  og_prog pg = {sizeof(uint32_t), qsize * sizeof(int32_t), sizeof(gs_state), false, false, true, &q,
+                gs_scatter, gs_gather, gs_combine, gs_apply, gs_zero};
+  uint32_t it = 0;
+  if (!rc) rc = vp_init(&vp, g, &pg, (char*) S);
+  if (!rc) rc = vp_initialize(&vp, gs_init, &q);
+  if (!rc) it = vp_execute(&vp, 0);
+  vp_free(&vp);
+  if (!rc)
+  {
+    uint32_t nm = 0;
+    for (uint32_t i = 0; i < g->nslots; i++)
+    {
+      uint32_t o = hb_unhash(g, g->hash_of_pos[i]);
+      bool m = false;
+      for (uint32_t k = 0; k < qsize; k++) m |= S[i].res[k] != '0';  /* is_matched (graphsim.h:50-57) */
+      nm += m;
+      if (matched) matched[o] = m;
+      if (res) memcpy(res + (size_t) o * qsize, S[i].res, qsize);
+    }
+    if (nmatches) *nmatches = nm;
+    if (niters) *niters = it;
+  }
+  free(cptr); free(cidx); free(fill); free(S);
+  return rc;
+}

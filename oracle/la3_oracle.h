@@ -90,6 +90,14 @@ int og_lm_query(og_lm* b, const uint32_t* term_vids, uint32_t nterms, uint32_t k
                 uint8_t* active, uint32_t* topk_ids, float* topk_scores, uint32_t* ntopk);
 void og_lm_free(og_lm* b);
 
+/* Graph simulation (graphsim.cpp:45-90).  g: load_directed(..., reverse=1).
+ * vlabel: nslots label ids by vertex id (0 = the empty string, i.e. no
+ * label); the query: qsize (<= 32) label ids and nqedges edges (i, j) in file
+ * order.  matched: nslots bytes (is_matched), res: nslots x qsize chars. */
+int og_graphsim(const og_graph* g, const uint32_t* vlabel, uint32_t qsize, const uint32_t* qlabel,
+                const uint32_t* qedges, uint32_t nqedges, uint8_t* matched, char* res, uint32_t* nmatches,
+                uint32_t* niters);
+
 const char* og_last_error(void);
 
 #ifdef __cplusplus

@@ -50,6 +50,7 @@ def lib() -> C.CDLL:
             "og_sssp": (C.c_int, [P, C.c_uint32, u32p, u32p]),
             "og_cc": (C.c_int, [P, u32p, u32p]),
             "og_tc": (C.c_int, [P, u32p, u64p]),
+            "og_graphsim": (C.c_int, [P, u32p, C.c_uint32, u32p, u32p, C.c_uint32, u8p, C.c_char_p, u32p, u32p]),
             "og_bm25_prepare": (C.c_int, [P, C.POINTER(P), u64p, f32p, f32p]),
             "og_bm25_query": (C.c_int, [P, u32p, C.c_uint32, C.c_uint32, f32p, u8p, u32p, f32p, u32p]),
             "og_bm25_free": (None, [P]),
@@ -126,6 +127,20 @@ class OracleGraph:
         tot = C.c_uint64()
         _check(lib().og_tc(self.h, _p(t, C.c_uint32), C.byref(tot)))
         return tot.value, t
+
+    def graphsim(self, vlabel, qlabel, qedges):
+        """Graph simulation on a graph loaded DIRECTED | REVERSE: (matched
+        flags, res as an nslots x qsize uint8 array, match count, iterations)."""
+        v = np.ascontiguousarray(np.asarray(vlabel, np.uint32))
+        q = np.ascontiguousarray(np.asarray(qlabel, np.uint32))
+        e = np.ascontiguousarray(np.asarray(qedges, np.uint32).reshape(-1))
+        matched = np.empty(self.nslots, np.uint8)
+        res = C.create_string_buffer(self.nslots * q.size)
+        nm, it = C.c_uint32(), C.c_uint32()
+        _check(lib().og_graphsim(self.h, _p(v, C.c_uint32), q.size, _p(q, C.c_uint32), _p(e, C.c_uint32),
+                                 e.size // 2, _p(matched, C.c_uint8), res, C.byref(nm), C.byref(it)))
+        r = np.frombuffer(res.raw, np.uint8).reshape(self.nslots, q.size).copy()
+        return matched, r, nm.value, it.value
 
     def __del__(self):
         try:

@@ -33,6 +33,15 @@ public:
     if (n) is_.read(reinterpret_cast<char*>(v.data()), (std::streamsize) (n * sizeof(U)));
   }
 
+  template <class A>
+  void load(std::vector<bool, A>& v)  // one byte per element
+  {
+    uint64_t n = 0;
+    is_.read(reinterpret_cast<char*>(&n), sizeof(n));
+    v.resize(n);
+    for (uint64_t i = 0; i < n; i++) { char c = 0; is_.read(&c, 1); v[i] = c != 0; }
+  }
+
   template <class T>
   void load(T& v) { load_(v, 0); }
 

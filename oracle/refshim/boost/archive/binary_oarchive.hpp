@@ -35,6 +35,14 @@ public:
     if (n) os_.write(reinterpret_cast<const char*>(v.data()), (std::streamsize) (n * sizeof(U)));
   }
 
+  template <class A>
+  void save(const std::vector<bool, A>& v)  // one byte per element
+  {
+    uint64_t n = v.size();
+    os_.write(reinterpret_cast<const char*>(&n), sizeof(n));
+    for (bool b : v) { char c = b ? 1 : 0; os_.write(&c, 1); }
+  }
+
   template <class T>
   void save(const T& v) { save_(v, 0); }
 

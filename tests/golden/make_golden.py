@@ -56,10 +56,14 @@ def write_records(path: Path, recs: list[tuple], weighted: bool) -> None:
 
 def main() -> None:
     only_lm = "--only-lm" in sys.argv  # regenerate the LM cases alone (other fixtures untouched)
+    only_gs = "--only-gs" in sys.argv  # regenerate the graph-simulation cases alone
     if not (REF_BIN / "dump_pr").exists():
         sys.exit("build the reference first: make -C oracle stage ref")
     from la3_gb300 import EdgeList  # host-side generators; no GPU needed
     DATA.mkdir(parents=True, exist_ok=True)
+    for f in ["graph_simulation/g3_13_13_20.bin", "graph_simulation/g3_13_13_20.labels"] + \
+             [f"graph_simulation/{q}.{x}" for q in ("q1_4_4_6", "q2_4_4_4", "q3_4_4_6") for x in ("labels", "mtx")]:
+        shutil.copy(REFDATA / f, DATA / Path(f).name)
     for f in ["graph_analytics/g1_8_8_13.bin", "graph_analytics/g1_8_8_13.w.bin",
               "information_retrieval/g2_7_7_17.w.bp.bin", "information_retrieval/g2_7_7_17.term.labels",
               "information_retrieval/g2_7_7_17.queries"]:
@@ -109,8 +113,57 @@ def main() -> None:
     (DATA / "bigtf.term.labels").write_text("".join(f"b{i} {i}\n" for i in range(1, 25)))
     (DATA / "bigtf.queries").write_text("b1 b2\nb24 b7 b3\nb5\nb9 b9 b11\nb20 b1 b14 b6\n")
 
+    # graph-simulation inputs: JSON-line labels over a small alphabet (vertex 0
+    # without a label in one file), random small queries, some label files
+    # ending in a newline (the reference then reads one more, empty, label)
+    grng = np.random.default_rng(17)
+    alphabet = ["A", "B", "C", "D", "E"]
+    for gname, n, null0 in (("rmat10", 1024, False), ("er10", 1024, True)):
+        lines = ["["]
+        for i in range(n):
+            lines.append("null," if (null0 and i == 0) else '{"t":"%s"},' % alphabet[int(grng.integers(0, 5))])
+        lines.append("]")
+        (DATA / f"{gname}.gs.labels").write_text("\n".join(lines) + "\n")
+    gs_queries = []
+    for qi in range(6):
+        qn = int(grng.integers(3, 7))
+        labs = [alphabet[int(grng.integers(0, 5))] for _ in range(qn)]
+        if qi == 4:
+            labs[1] = "Z"  # not in the data
+        edges = sorted({(int(grng.integers(0, qn)), int(grng.integers(0, qn))) for _ in range(qn + 2)})
+        edges = [e for e in edges if e[0] != e[1]] or [(0, 1)]
+        trail = "\n" if qi % 2 else ""
+        (DATA / f"gsq{qi}.labels").write_text("\n".join(labs) + trail)
+        (DATA / f"gsq{qi}.mtx").write_text("\n".join(f"{a} {b}" for a, b in edges) + "\n")
+        gs_queries.append(f"gsq{qi}")
+
     cases = {}
     tmp = Path(tempfile.mkdtemp())
+
+    def gs_case(name, labels_f, f, n, ql_f, qm_f):
+        o = tmp / name
+        meta = run_dump([REF_BIN / "dump_graphsim", DATA / labels_f, DATA / f, n, DATA / ql_f, DATA / qm_f, o])
+        q = meta["qsize"]
+        res = np.fromfile(str(o) + ".res.u8", dtype=np.uint8).reshape(-1, q)
+        np.savez_compressed(GOLD / f"{name}.npz", res=res, matched=load(o, ".matched.u8", np.uint8))
+        cases[name] = {"app": "graphsim", "file": f, "labels": labels_f, "n": n, "qlabels": ql_f, "qmtx": qm_f,
+                       **meta}
+
+    def gs_cases():
+        for q in ("q1_4_4_6", "q2_4_4_4", "q3_4_4_6"):
+            gs_case(f"g3_{q}_gs", "g3_13_13_20.labels", "g3_13_13_20.bin", 13, f"{q}.labels", f"{q}.mtx")
+        for k, qn in enumerate(gs_queries):
+            gname = "rmat10" if k % 2 == 0 else "er10"
+            gs_case(f"{gname}_{qn}_gs", f"{gname}.gs.labels", f"{gname}.bin", 1024, f"{qn}.labels", f"{qn}.mtx")
+
+    if only_gs:
+        gs_cases()
+        old = json.loads((GOLD / "golden.json").read_text())
+        old.update(cases)
+        (GOLD / "golden.json").write_text(json.dumps(old, indent=1, sort_keys=True) + "\n")
+        shutil.rmtree(tmp)
+        print(f"{len(cases)} graph-simulation cases written to {GOLD}")
+        return
 
     def pr_case(name, f, n, iters):
         o = tmp / name
@@ -217,6 +270,7 @@ def main() -> None:
     sssp_case("isolated_root_sssp", "rmat10.w.bin", 1024, 0)
     bm25_case("bip_bm25", "bip.w.bp.bin", "bip.term.labels", ndocs, nterms, "bip.queries", 10)
     lm_cases()
+    gs_cases()
 
     (GOLD / "golden.json").write_text(json.dumps(cases, indent=1, sort_keys=True) + "\n")
     shutil.rmtree(tmp)

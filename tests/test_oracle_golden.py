@@ -14,7 +14,7 @@ def _cases(golden, app):
 
 def test_golden_manifest_complete(golden):
     apps = {v["app"] for v in golden.values()}
-    assert apps == {"pr", "bfs", "sssp", "cc", "tc", "bm25", "lm"}
+    assert apps == {"pr", "bfs", "sssp", "cc", "tc", "bm25", "lm", "graphsim"}
     for k in golden:
         assert (GOLD / f"{k}.npz").exists(), k
 
@@ -67,6 +67,27 @@ def test_oracle_matches_reference(golden, oracle, app):
                 # the reference's top-k agrees with the canonical order up to ties
                 tk = ref[f"q{qi}_topk_scores"]
                 assert np.array_equal(np.sort(sc)[::-1].view(np.uint32), np.sort(tk)[::-1].view(np.uint32)), (name, qi)
+
+
+def test_oracle_graphsim_matches_reference(golden, oracle):
+    """Graph simulation: the reference's per-vertex result strings and match
+    flags (its own sample data graph and queries, plus synthetic ones); the
+    inputs are read by the package's readers, which follow the reference's
+    parsing rules."""
+    import la3_gb300 as L
+    O = oracle
+    for name in _cases(golden, "graphsim"):
+        c = golden[name]
+        ref = np.load(GOLD / f"{name}.npz")
+        g = O.OracleGraph(DATA / c["file"], c["n"], O.DIRECTED | O.REVERSE)
+        vl = L.read_graphsim_labels(DATA / c["labels"], c["n"])
+        ql, qe = L.read_graphsim_query(DATA / c["qlabels"], DATA / c["qmtx"])
+        assert len(ql) == c["qsize"], name
+        v, q = L.graphsim_label_ids(vl, ql, g.nslots)
+        matched, res, nm, _ = g.graphsim(v, q, qe)
+        assert nm == c["nmatches"], name
+        assert np.array_equal(matched, ref["matched"]), name
+        assert np.array_equal(res, ref["res"]), name
 
 
 def test_oracle_rejects_out_of_range_ids(oracle, tmp_path):
