@@ -31,8 +31,8 @@
  *     edge after another: combine need not be associative or commutative;
  *   - a touched row applies combine(acc, zero()); activated regular rows (all
  *     touched rows when stationary) scatter into the next iteration;
- *   - source messages are sent in the first iteration only (every iteration
- *     when stationary);
+ *   - regular rows take the sources' messages in the first iteration only
+ *     (every iteration when stationary), sink rows in every iteration;
  *   - directed programs without gather_with_state / apply_with_iteration
  *     ("optimizable", vertex_program.hpp:77) leave sinks out of the
  *     iterations and compute them once afterwards from every regular
@@ -271,7 +271,9 @@ class Engine
         const bool with_src = P::stationary || it == 0;
         ck(cudaMemsetAsync(xra_[cur_ ^ 1], 0, nreg + 1, s_));
         pass(0, nreg, with_src, false, it);
-        if (!optimizable && directed_ && dv_.nsink) pass(nreg, nrows, with_src, false, it);
+        // sink rows take the sources' messages in every iteration
+        // (vertex_program_execute.hpp:464-468)
+        if (!optimizable && directed_ && dv_.nsink) pass(nreg, nrows, true, false, it);
         cur_ ^= 1;
         it++;
         int any = 0;

@@ -99,7 +99,7 @@ def build_programs() -> None:
     srcs = sorted(PROGRAMS.glob("*.cu"))
     if not srcs:
         return
-    deps = srcs + [LIB, INCLUDE / "la3g.h", INCLUDE / "la3g_vp.cuh"]
+    deps = srcs + [LIB, INCLUDE / "la3g.h", INCLUDE / "la3g_vp.cuh", INCLUDE / "la3g_programs.h"]
     if _stale(PROGRAMS_LIB, deps):
         _run([nvcc()] + NVCC_FLAGS + ["-shared", "-o", str(PROGRAMS_LIB)] + [str(x) for x in srcs]
              + ["-L", str(BUILD), "-lla3g", "-Xlinker", "-rpath,$ORIGIN"])
@@ -115,10 +115,15 @@ def build_drivers() -> None:
             continue
         out = BIN / src.stem
         deps = [src, LIB] + common + sorted(DRIVERS.glob("*.h")) + [INCLUDE / "la3g.h"]
+        # drivers of apps written as vertex programs link libla3g_programs too
+        progs = "la3g_programs.h" in src.read_text()
+        if progs:
+            deps += [PROGRAMS_LIB, INCLUDE / "la3g_programs.h"]
         if _stale(out, deps):
             jobs.append(["g++", "-O2", "-std=c++17", "-I", str(INCLUDE), "-I", str(DRIVERS), str(src)]
                         + [str(c) for c in common]
-                        + ["-o", str(out), "-L", str(BUILD), "-lla3g", "-Wl,-rpath,$ORIGIN/../_build", "-pthread"])
+                        + ["-o", str(out), "-L", str(BUILD)] + (["-lla3g_programs"] if progs else [])
+                        + ["-lla3g", "-Wl,-rpath,$ORIGIN/../_build", "-pthread"])
     with cf.ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 2)) as ex:
         for f in [ex.submit(_run, c) for c in jobs]:
             f.result()

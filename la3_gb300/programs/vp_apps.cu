@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "la3g.h"
+#include "la3g_programs.h"
 #include "la3g_vp.cuh"
 
 using la3g_vp::Edge;

@@ -108,14 +108,14 @@ def test_load_errors_are_reported(native, tmp_path):
 
 
 def test_drivers_and_programs_are_built(native):
-    """The eight command-line drivers and the vertex-program library exist;
+    """The nine command-line drivers and the vertex-program library exist;
     a driver prints its usage without touching a GPU."""
     import la3_gb300.build as B
-    for d in ("pr", "bfs", "sssp", "cc", "tc", "bm25", "lm", "degree"):
+    for d in ("pr", "bfs", "sssp", "cc", "tc", "bm25", "lm", "degree", "graphsim"):
         assert (B.BIN / d).exists(), d
     r = subprocess.run([str(B.BIN / "tc")], capture_output=True, text=True)
     assert r.returncode == 1 and "Usage" in r.stdout
     out = subprocess.run(["nm", "-D", "--defined-only", str(B.PROGRAMS_LIB)], capture_output=True, text=True,
                          check=True).stdout
-    for s in ("la3gp_degree", "la3gp_pagerank", "la3gp_bfs", "la3gp_sssp", "la3gp_cc"):
+    for s in ("la3gp_degree", "la3gp_pagerank", "la3gp_bfs", "la3gp_sssp", "la3gp_cc", "la3gp_graphsim"):
         assert re.search(r"\bT " + s + r"\b", out), s

@@ -24,6 +24,7 @@ def progs(gpu):
     lib.la3gp_sssp.argtypes = [P, C.c_uint32, u32p, u32p]
     lib.la3gp_cc.argtypes = [P, u32p, u32p]
     lib.la3gp_degree.argtypes = [P, u32p]
+    lib.la3gp_graphsim.argtypes = [P, u32p, C.c_uint32, u32p, u32p, C.c_uint32, u8p, C.c_char_p, u32p, u32p]
     return lib
 
 
@@ -117,3 +118,75 @@ def test_programs_vs_oracle_rmat(gpu, progs, oracle, tmp_path):
     lab, it = _cc(L, progs, gu)
     olab, oit = ou.cc()
     assert np.array_equal(lab, olab) and it == oit
+
+
+def _graphsim(L, progs, c):
+    g = L.Graph.load_directed(DATA / c["file"], c["n"], reverse_edges=True)
+    vl = L.read_graphsim_labels(DATA / c["labels"], c["n"])
+    ql, qe = L.read_graphsim_query(DATA / c["qlabels"], DATA / c["qmtx"])
+    v, q = L.graphsim_label_ids(vl, ql, g.nslots)
+    e = np.ascontiguousarray(np.asarray(qe, np.uint32).reshape(-1))
+    matched = np.empty(g.nslots, np.uint8)
+    res = C.create_string_buffer(g.nslots * q.size)
+    nm, it = C.c_uint32(), C.c_uint32()
+    assert progs.la3gp_graphsim(g._h, _p(v, C.c_uint32), q.size, _p(q, C.c_uint32), _p(e, C.c_uint32), e.size // 2,
+                                _p(matched, C.c_uint8), res, C.byref(nm), C.byref(it)) == 0
+    return matched, np.frombuffer(res.raw, np.uint8).reshape(g.nslots, q.size), nm.value, it.value
+
+
+def test_graphsim_golden(gpu, progs, golden):
+    """Graph simulation (variable-size messages bounded at 32 query vertices)
+    against the reference's per-vertex results: its sample data graph and
+    queries and synthetic ones (incl. the empty query label a trailing
+    newline adds, a vertex 0 without a label)."""
+    for name in sorted(k for k, v in golden.items() if v["app"] == "graphsim"):
+        c = golden[name]
+        ref = np.load(GOLD / f"{name}.npz")
+        matched, res, nm, _ = _graphsim(gpu, progs, c)
+        assert nm == c["nmatches"], name
+        assert np.array_equal(matched, ref["matched"]), name
+        assert np.array_equal(res, ref["res"]), name
+
+
+def test_graphsim_vs_oracle(gpu, progs, oracle, tmp_path):
+    """A larger seeded case against the oracle: R-MAT s14, 6 labels, random
+    queries with cycles."""
+    L = gpu
+    n = 1 << 14
+    p = tmp_path / "g.bin"
+    L.EdgeList.rmat(14, 8, seed=23).write(p)
+    rng = np.random.default_rng(29)
+    labs = ["A", "B", "C", "D", "E", "F"]
+    (tmp_path / "g.labels").write_text("[\n" + "".join('{"x":"%s"},\n' % labs[int(rng.integers(0, 6))]
+                                                       for _ in range(n)) + "]\n")
+    og = oracle.OracleGraph(p, n, oracle.DIRECTED | oracle.REVERSE)
+    for qi in range(4):
+        qn = int(rng.integers(3, 8))
+        (tmp_path / "q.labels").write_text(" ".join(labs[int(rng.integers(0, 6))] for _ in range(qn)))
+        edges = {(int(rng.integers(0, qn)), int(rng.integers(0, qn))) for _ in range(2 * qn)}
+        (tmp_path / "q.mtx").write_text("".join(f"{a} {b}\n" for a, b in sorted(edges) if a != b))
+        c = {"file": p, "n": n, "labels": tmp_path / "g.labels", "qlabels": tmp_path / "q.labels",
+             "qmtx": tmp_path / "q.mtx"}
+        matched, res, nm, it = _graphsim(L, progs, c)
+        vl = L.read_graphsim_labels(c["labels"], n)
+        ql, qe = L.read_graphsim_query(c["qlabels"], c["qmtx"])
+        v, q = L.graphsim_label_ids(vl, ql, og.nslots)
+        om, ores, onm, oit = og.graphsim(v, q, qe)
+        assert nm == onm and it == oit, qi
+        assert np.array_equal(matched, om) and np.array_equal(res, ores), qi
+
+
+def test_graphsim_driver(gpu, golden):
+    import re
+    import subprocess
+    import la3_gb300.build as B
+    for name in sorted(k for k, v in golden.items() if v["app"] == "graphsim"):
+        c = golden[name]
+        out = subprocess.run([str(B.BIN / "graphsim"), str(DATA / c["labels"]), str(DATA / c["file"]), str(c["n"]),
+                              str(DATA / c["qlabels"]), str(DATA / c["qmtx"])], capture_output=True, text=True,
+                             check=True).stdout
+        assert int(re.search(r"Num matches = (\d+)", out).group(1)) == c["nmatches"], name
+        shown = {int(a): b for a, b in re.findall(r"^(\d+): (\d*)$", out, flags=re.M)}
+        ref = np.load(GOLD / f"{name}.npz")["matched"]
+        assert all((shown[v] == str(v)) == bool(ref[v]) for v in shown), name
+
