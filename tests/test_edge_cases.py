@@ -102,3 +102,23 @@ def test_header_format_matches_plain(gpu, tmp_path):
     au = L.Graph.load_undirected(ph, 0, weighted=True)
     bu = L.Graph.load_undirected(pp, n, weighted=True)
     assert np.array_equal(L.bfs(au, 3)[0], L.bfs(bu, 3)[0])
+
+
+def test_lm_degenerate_queries(gpu, oracle, tmp_path):
+    """LM on the queries BM25's edge cases use, in sequence (the first one
+    also ranks the term vertices the TL pass left active), against the
+    oracle."""
+    L = gpu
+    D, T = 300, 60
+    e = L.EdgeList.bipartite(D, T, 10, seed=6)
+    p = tmp_path / "c.bin"
+    e.write(p)
+    g = L.Graph.load_bipartite(p, D, T)
+    b = L.LM(g)
+    ob = oracle.OracleLM(oracle.OracleGraph(p, D, oracle.BIPARTITE | oracle.WEIGHTED, nright=T))
+    for q, k in (([], 10), ([0], 10), ([D + T + 5], 10), ([D + 1], 0), ([D + 1, D + 2], 64), ([1, D + 3], 10),
+                 ([D + 4, D + 4, D + 4], 5)):
+        ids, sc, (alls, act), _ = b.query(q, k, full=True)
+        oids, osc, oscores, oact = ob.query(q, k)
+        assert ids.tolist() == oids.tolist() and np.array_equal(sc, osc), (q, k)
+        assert np.array_equal(act, oact) and np.array_equal(alls.view(np.uint32), oscores.view(np.uint32)), (q, k)
