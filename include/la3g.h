@@ -19,7 +19,7 @@
  * Every entry point below names the reference interface it stands in for.
  * The reference has no C ABI of its own: it is a C++ template library whose
  * plugin API is the VertexProgram<W, M, A, S> class
- * (src/vprogram/vertex_program.h:21-383) driven by six app run() functions.
+ * (src/vprogram/vertex_program.h:21-383) driven by the apps' run() functions.
  */
 #ifndef LA3G_H
 #define LA3G_H
@@ -158,7 +158,7 @@ typedef struct la3g_device_graph
 
 int la3g_graph_device_view(la3g_graph* g, la3g_device_graph* out);
 
-/* ---- apps (replace the six app run() functions) ------------------------ */
+/* ---- apps (replace the apps' run() functions) ---------------------------- */
 
 /* PageRank, FP64, un-normalised, alpha = 0.15: the reference pr app
  * (src/apps/graph_analytics/pr.cpp:11-55, pr.h:12-46) on a graph loaded with

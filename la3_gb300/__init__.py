@@ -1,8 +1,10 @@
 """la3_gb300 — GB300-native LA3 vertex-program engine (host-side mirror).
 
 The reference's user-facing surface is the `Graph<W>::load_*` calls
-(src/matrix/graph.h:38-47) and the six apps' `run()` functions
-(src/apps/graph_analytics/*.cpp, src/apps/information_retrieval/bm25.cpp).
+(src/matrix/graph.h:38-47) and the apps' `run()` functions (pr, bfs, sssp,
+cc, tc, degree: src/apps/graph_analytics/*.cpp; bm25, lm:
+src/apps/information_retrieval/*.cpp; graph simulation's input readers:
+src/apps/graph_simulation/).
 This module exposes the same loads and apps over the native C ABI
 (include/la3g.h); every result is a numpy array indexed by vertex id with
 n + 1 slots, as the reference's per-vertex states are.

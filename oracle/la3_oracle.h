@@ -8,8 +8,9 @@
  * It restates, in plain C, the reference's ingest (Graph::load_binary,
  * SimpleBucketHasher, vertex classification, locators, per-tile dedup + CSC),
  * its BSP execution engine (VertexProgram::execute and its optimizable /
- * non-optimizable / single-iteration paths) and the six apps (pr, bfs, sssp,
- * cc, tc, bm25, lm).  Every result is indexed by ORIGINAL vertex id 0..nslots-1.
+ * non-optimizable / single-iteration paths) and the apps (pr, bfs, sssp,
+ * cc, tc, bm25, lm, graph simulation).  Every result is indexed by
+ * ORIGINAL vertex id 0..nslots-1.
  * Function comments cite the reference file:line each one follows.
  *
  * Parity is pinned against the reference itself: the same sources are built
