@@ -276,7 +276,8 @@ enum
 {
   LA3G_QUERY_BFS = 1,   /* hops from root (la3g_bfs) */
   LA3G_QUERY_SSSP = 2,  /* distances from root (la3g_sssp) */
-  LA3G_QUERY_BM25 = 3   /* top-k documents (la3g_bm25_query) */
+  LA3G_QUERY_BM25 = 3,  /* top-k documents (la3g_bm25_query) */
+  LA3G_QUERY_LM = 4     /* top-k documents by query likelihood (la3g_lm_query) */
 };
 
 typedef struct la3g_query
@@ -284,11 +285,11 @@ typedef struct la3g_query
   uint32_t kind;          /* LA3G_QUERY_* */
   uint32_t graph;         /* id returned by la3g_server_add_graph */
   uint32_t root;          /* BFS / SSSP root vertex id */
-  uint32_t k;             /* BM25: documents wanted */
-  const uint32_t* terms;  /* BM25: term vertex ids (copied at submit) */
+  uint32_t k;             /* BM25 / LM: documents wanted */
+  const uint32_t* terms;  /* BM25 / LM: term vertex ids (copied at submit) */
   uint32_t nterms;
-  void* out;              /* BFS: uint8 hops[nslots]; SSSP: uint32 dist[nslots]; BM25: uint32 ids[k]; may be NULL */
-  float* scores_out;      /* BM25: scores[k]; may be NULL */
+  void* out;              /* BFS: uint8 hops[nslots]; SSSP: uint32 dist[nslots]; BM25 / LM: uint32 ids[k]; may be NULL */
+  float* scores_out;      /* BM25 / LM: scores[k]; may be NULL */
 } la3g_query;
 
 typedef struct la3g_query_result
@@ -315,8 +316,9 @@ typedef struct la3g_server_stats
  * them into any free lane. */
 int la3g_server_create(uint64_t budget_bytes, uint32_t bfs_lanes, uint32_t sssp_lanes, la3g_server** out);
 /* Makes a loaded graph resident in the server: undirected graphs serve BFS,
- * DIRECTED|WEIGHTED graphs SSSP, BIPARTITE graphs BM25 (prepared here if
- * needed).  The graph's device bytes plus its engine's lane state must fit
+ * DIRECTED|WEIGHTED graphs SSSP, BIPARTITE graphs BM25 and LM (both
+ * prepared here if needed; LM's first-query leftover activity is taken here,
+ * so every served LM query sees the reference's steady state).  The graph's device bytes plus its engine's lane state must fit
  * in the budget left (the lane count is halved down to 64 first), else
  * LA3G_EBUDGET.  The caller keeps ownership but must not use the graph while
  * it is served; la3g_server_free releases it. */

@@ -374,7 +374,7 @@ def read_queries(labels_path: str, queries_path: str, ndocs: int) -> list[list[i
     return out
 
 
-QUERY_BFS, QUERY_SSSP, QUERY_BM25 = 1, 2, 3
+QUERY_BFS, QUERY_SSSP, QUERY_BM25, QUERY_LM = 1, 2, 3, 4
 
 
 class Server:
@@ -430,13 +430,19 @@ class Server:
         q = N.Query(kind=QUERY_SSSP, graph=gid, root=root, out=_addr(out))
         return self._submit(q, (out,))
 
-    def submit_bm25(self, gid: int, term_vids: Sequence[int], k: int = 10) -> int:
+    def submit_bm25(self, gid: int, term_vids: Sequence[int], k: int = 10, kind: int = QUERY_BM25) -> int:
         terms = np.ascontiguousarray(term_vids, dtype=np.uint32)
         ids = np.zeros(k, np.uint32)
         sc = np.zeros(k, np.float32)
-        q = N.Query(kind=QUERY_BM25, graph=gid, k=k, terms=_ptr(terms, C.c_uint32), nterms=terms.size,
+        q = N.Query(kind=kind, graph=gid, k=k, terms=_ptr(terms, C.c_uint32), nterms=terms.size,
                     out=_addr(ids), scores_out=_ptr(sc, C.c_float))
         return self._submit(q, (ids, sc))
+
+    def submit_lm(self, gid: int, term_vids: Sequence[int], k: int = 10) -> int:
+        """An LM query on a served corpus (the corpus's first-query leftover
+        activity is taken at add_graph, so every LM query sees the steady
+        state)."""
+        return self.submit_bm25(gid, term_vids, k, kind=QUERY_LM)
 
     def poll(self, ticket: int, timeout_ms: int = -1):
         """(result struct, outputs) when done, None while pending."""
@@ -446,7 +452,7 @@ class Server:
             return None
         N.check(st)
         bufs = self._live.pop(ticket)
-        if r.kind == QUERY_BM25:
+        if r.kind in (QUERY_BM25, QUERY_LM):
             bufs = (bufs[0][: r.nout], bufs[1][: r.nout])
         return r, bufs
 

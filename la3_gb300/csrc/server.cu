@@ -1,4 +1,4 @@
-// Serving loop: BFS / SSSP / BM25 queries against several device-resident
+// Serving loop: BFS / SSSP / BM25 / LM queries against several device-resident
 // graphs, admitted as they arrive.
 //
 // The reference answers one query per VertexProgram run (bfs.cpp:11-37,
@@ -23,7 +23,8 @@
 //    queries waiting answers them one at a time through the single-root
 //    entry point (faster per query at low load); lanes take over when the
 //    queue is deeper.
-//  * BM25 engines run their queries one after another on their corpus.
+//  * BM25 engines run their queries (BM25 and LM) one after another on their
+//    corpus.
 //
 // Admission by HBM budget: a graph joins only if its device bytes plus the
 // engine's lane state fit in what is left of the budget (the lane count is
@@ -965,8 +966,11 @@ int bm25_loop(Engine* E)
       t->start_ms = wall_ms();
       t->in_flight = 1;
       uint32_t nout = 0;
-      const int st = la3g_bm25_query(E->G, t->terms.data(), (uint32_t) t->terms.size(), t->q.k, (uint32_t*) t->q.out,
-                                     t->q.scores_out, &nout, nullptr, nullptr, nullptr);
+      const int st = t->q.kind == LA3G_QUERY_LM
+                         ? la3g_lm_query(E->G, t->terms.data(), (uint32_t) t->terms.size(), t->q.k,
+                                         (uint32_t*) t->q.out, t->q.scores_out, &nout, nullptr, nullptr, nullptr)
+                         : la3g_bm25_query(E->G, t->terms.data(), (uint32_t) t->terms.size(), t->q.k,
+                                           (uint32_t*) t->q.out, t->q.scores_out, &nout, nullptr, nullptr, nullptr);
       t->nout = nout;
       finish_ticket(E->S, t, st);
     }
@@ -1019,6 +1023,13 @@ extern "C" int la3g_server_add_graph(la3g_server* S, la3g_graph* G, uint32_t* gr
   }
   if (kind == kEngSssp) LA3G_TRY(build_push_csr(G));
   if (kind == kEngBm25 && !G->slot[kSlotBm25]) LA3G_TRY(la3g_bm25_prepare(G, nullptr, nullptr, nullptr));
+  if (kind == kEngBm25)
+  {
+    // LM too; one empty query takes the first query's leftover term activity
+    // (lm.cpp:46-86), so every served LM query sees the steady state
+    if (!G->slot[kSlotLm]) LA3G_TRY(la3g_lm_prepare(G, nullptr, nullptr));
+    LA3G_TRY(la3g_lm_query(G, nullptr, 0, 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr));
+  }
   const uint32_t N = g.nslots;
   uint32_t L = kind == kEngBfs ? S->bfs_lanes : (kind == kEngSssp ? S->sssp_lanes : 0);
   auto need = [&](uint32_t lanes) -> uint64_t {
@@ -1097,7 +1108,7 @@ extern "C" int la3g_server_submit(la3g_server* S, const la3g_query* q, uint64_t*
   }
   Engine* E = S->engines[q->graph];
   const int want = q->kind == LA3G_QUERY_BFS ? kEngBfs : q->kind == LA3G_QUERY_SSSP ? kEngSssp
-                                                    : q->kind == LA3G_QUERY_BM25 ? kEngBm25 : -1;
+                                                    : (q->kind == LA3G_QUERY_BM25 || q->kind == LA3G_QUERY_LM) ? kEngBm25 : -1;
   if (want != E->kind)
   {
     delete t;
@@ -1113,7 +1124,7 @@ extern "C" int la3g_server_submit(la3g_server* S, const la3g_query* q, uint64_t*
     if (!q->terms || q->nterms == 0 || q->k == 0)
     {
       delete t;
-      return set_error(LA3G_EINVAL, "bm25 queries need terms and k > 0");
+      return set_error(LA3G_EINVAL, "bm25 / lm queries need terms and k > 0");
     }
     t->terms.assign(q->terms, q->terms + q->nterms);
     t->q.terms = nullptr;

@@ -106,6 +106,9 @@ def test_mixed_graphs_and_threads(gpu, servers, tmp_path):
     rng = np.random.default_rng(7)
     queries = [sorted(set(int(x) for x in rng.integers(D + 1, D + T + 1, int(rng.integers(2, 9))))) for _ in range(40)]
     want_b = [b.query(q, 10)[:2] for q in queries]
+    lm = L.LM(gb)
+    lm.query([], 0)  # the first query's leftover activity, as the server takes it
+    want_l = [lm.query(q, 10)[:2] for q in queries]
     r1, r2, r3 = _roots(gu, 80, 3), _roots(gw, 60, 4), _roots(gu2, 80, 5)
     want1 = {r: L.bfs(gu, r, True, False)[0] for r in set(r1)}
     want2 = {r: L.sssp(gw, r)[0] for r in set(r2)}
@@ -126,6 +129,8 @@ def test_mixed_graphs_and_threads(gpu, servers, tmp_path):
                 mine.append(("b3", r3[i], S.submit_bfs(g3, r3[i])))
             if part == 1 and i < len(queries):
                 mine.append(("q", i, S.submit_bm25(g4, queries[i], 10)))
+            if part == 0 and i < len(queries):
+                mine.append(("l", i, S.submit_lm(g4, queries[i], 10)))
         for kind, key, t in mine:
             res, bufs = _wait(S, t)
             with lock:
@@ -136,7 +141,7 @@ def test_mixed_graphs_and_threads(gpu, servers, tmp_path):
         t.start()
     for t in th:
         t.join()
-    assert len(got) == len(r1) + len(r2) + len(r3) + len(queries)
+    assert len(got) == len(r1) + len(r2) + len(r3) + 2 * len(queries)
     for kind, key, bufs in got:
         if kind == "b1":
             assert np.array_equal(bufs[0], want1[key])
@@ -145,9 +150,10 @@ def test_mixed_graphs_and_threads(gpu, servers, tmp_path):
         elif kind == "s":
             assert np.array_equal(bufs[0], want2[key])
         else:
+            want = want_b if kind == "q" else want_l
             ids, sc = bufs
-            assert ids.tolist() == want_b[key][0].tolist()
-            assert np.array_equal(sc, want_b[key][1])
+            assert ids.tolist() == want[key][0].tolist()
+            assert np.array_equal(sc, want[key][1])
     info = S.info()
     assert info["ngraphs"] == 4 and info["pending"] == 0
     S.free()
