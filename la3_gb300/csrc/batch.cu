@@ -804,7 +804,7 @@ extern "C" int la3g_batch_autotune(la3g_graph* G, const uint32_t* roots, uint32_
   double best_ms = 1e300;
   const int modes[] = {0, 1};
   const int blocks[] = {128, 256, 512};
-  const double fracs[] = {0.0, 0.02, 0.05, 0.1, 0.2, 0.4};
+  const double fracs[] = {0.0, 0.001, 0.003, 0.01, 0.02, 0.05, 0.1, 0.2, 0.4};
   for (int mode : modes)
     for (int block : blocks)
       for (double frac : fracs)
