@@ -49,9 +49,10 @@ def parse_args(argv=None):
     ap.add_argument("--scale", type=int, default=SCALE)
     ap.add_argument("--tc-scale", type=int, default=TC_SCALE)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["plain", "batched", "precision", "serve"], default="plain",
+    ap.add_argument("--workload", choices=["plain", "batched", "precision", "serve", "next"], default="plain",
                     help="plain (default): the single-query BFS/SSSP/CC/TC step; batched: multi-source BFS/SSSP; "
-                         "precision: FP32 vs FP64 PageRank on s24; serve: Poisson query stream over resident graphs")
+                         "precision: FP32 vs FP64 PageRank on s24; serve: Poisson query stream over resident graphs; "
+                         "next: LM queries, the degree app and graph simulation")
     ap.add_argument("--serve-seconds", type=float, default=1.0, help="arrival window per offered rate")
     ap.add_argument("--serve-rates", default="1000,5000,20000,50000")
     return ap.parse_args(argv)
@@ -835,6 +836,121 @@ def serve_line(args, rank, world, local) -> dict | None:
     }
 
 
+def next_line(args, rank, world, local) -> dict | None:
+    """The widened apps: LM top-10 queries over the serve line's corpus (8M
+    docs x 1M terms, ~50 terms per doc, Zipf 1.1 queries of 2-8 terms), the
+    degree app on R-MAT s22 (directed), graph simulation on R-MAT s20 (data
+    graph reversed, 6 labels, a 5-vertex query with a cycle).  A step = 100
+    LM queries + one degree call + one graph simulation.  value = LM queries/s
+    from device time; e2e = the same calls timed on the host clock."""
+    import ctypes as C
+    import numpy as np
+    import torch
+    import la3_gb300 as L
+    import la3_gb300.build as B
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    small = args.scale != SCALE
+    D, T, tpd = (100_000, 20_000, 30) if small else (8_000_000, 1_000_000, 50)
+    t_setup = time.time()
+    eb = L.EdgeList.bipartite(D, T, tpd, seed=300)
+    postings = eb.m
+    gb = L.Graph.from_edges(eb, L.BIPARTITE | L.WEIGHTED, D, T)
+    del eb
+    gb.set_stream(stream.cuda_stream)
+    t0 = time.time()
+    lm = L.LM(gb)
+    lm_prepare_s = time.time() - t0
+    lm.query([], 0)  # the first query's leftover term activity
+    rng = np.random.default_rng(500 + rank)
+    zipf_w = 1.0 / np.arange(1, T + 1) ** 1.1
+    zipf_w /= zipf_w.sum()
+
+    def queries(n):
+        return [sorted(set(int(D + 1 + t) for t in rng.choice(T, int(rng.integers(2, 9)), p=zipf_w)))
+                for _ in range(n)]
+
+    gd = L.Graph.from_edges(L.EdgeList.rmat(args.scale, 16, seed=GRAPH_SEED), L.DIRECTED)
+    gd.set_stream(stream.cuda_stream)
+    gs_scale = args.tc_scale
+    gr = L.Graph.from_edges(L.EdgeList.rmat(gs_scale, 16, seed=GRAPH_SEED + 7), L.DIRECTED | L.REVERSE)
+    gr.set_stream(stream.cuda_stream)
+    vlab = np.zeros(gr.nslots, np.uint32)
+    vlab[: 1 << gs_scale] = rng.integers(1, 7, 1 << gs_scale)  # 6 labels, vertex n unlabelled
+    qlab = np.array([1, 2, 3, 2, 4], np.uint32)
+    qedges = np.array([[0, 1], [1, 2], [2, 3], [3, 1], [1, 4]], np.uint32).reshape(-1)
+    progs = C.CDLL(str(B.PROGRAMS_LIB))
+    u32p = C.POINTER(C.c_uint32)
+    progs.la3gp_graphsim.argtypes = [C.c_void_p, u32p, C.c_uint32, u32p, u32p, C.c_uint32, C.POINTER(C.c_uint8),
+                                     C.c_char_p, u32p, u32p]
+    matched = np.empty(gr.nslots, np.uint8)
+    setup_s = time.time() - t_setup
+
+    def graphsim():
+        nm, it = C.c_uint32(), C.c_uint32()
+        L.N.check(progs.la3gp_graphsim(gr._h, vlab.ctypes.data_as(u32p), qlab.size, qlab.ctypes.data_as(u32p),
+                                       qedges.ctypes.data_as(u32p), qedges.size // 2,
+                                       matched.ctypes.data_as(C.POINTER(C.c_uint8)), None, C.byref(nm), C.byref(it)))
+        return nm.value, it.value
+
+    def step(qs):
+        lm_dev, lm_post = [], 0
+        th = time.perf_counter()
+        for q in qs:
+            _, _, _, st = lm.query(q, 10)
+            lm_dev.append(st.device_ms)
+            lm_post += st.edges_examined
+        lm_host = time.perf_counter() - th
+        _, _, _, dst = L.degree(gd, 3)
+        th = time.perf_counter()
+        nm, it = graphsim()
+        gs_s = time.perf_counter() - th
+        return lm_dev, lm_post, lm_host, dst.device_ms, gs_s, nm, it
+
+    for _ in range(args.warmup):
+        step(queries(20))
+    torch.cuda.synchronize()
+    L.profile_reset()
+    L.profile(True)
+    res = []
+    with ClockSampler(local) as clocks:
+        clocks.start_timed()
+        for _ in range(args.steps):
+            res.append(step(queries(100)))
+    L.profile(False)
+    prof = L.profile_report().get("lm_term", {"ms": 0.0, "bytes": 0.0, "launches": 0})
+    peaks = measured_peaks()
+    lm_dev = [x for r in res for x in r[0]]
+    lm_host = sum(r[2] for r in res)
+    lm_gbs = prof["bytes"] / (prof["ms"] / 1e3) / 1e9 if prof["ms"] else None
+    deg_ms = statistics.median(r[3] for r in res)
+    gs_s = statistics.median(r[4] for r in res)
+    nq = len(lm_dev)
+    if rank != 0:
+        return None
+    return {
+        "metric": "LM queries/s on 1 GB300 (8M-doc corpus); degree and graph-simulation rates", "value": nq /
+        (sum(lm_dev) / 1e3), "unit": "queries/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": sum(lm_dev) / args.steps + deg_ms + gs_s * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 LM scores / u32 degrees / u32 masks", "data": "synthetic (seeded)",
+        "config": {"workload": f"LM top-10 over {D} docs x {T} terms ({postings} postings); degree on R-MAT "
+                               f"s{args.scale}; graph simulation on R-MAT s{gs_scale} (5-vertex query, 6 labels)",
+                   "lm": {"queries": nq, "device_ms_mean": statistics.mean(lm_dev),
+                          "device_ms_p50": _pct(lm_dev, 50), "device_ms_p99": _pct(lm_dev, 99),
+                          "postings_per_query": sum(r[1] for r in res) / nq, "term_kernel_gbs": lm_gbs,
+                          "term_kernel_frac": (lm_gbs / peaks["hbm_gbs"]) if lm_gbs else None,
+                          "prepare_s": round(lm_prepare_s, 2)},
+                   "degree": {"device_ms": deg_ms, "gteps": gd.info.nentries / (deg_ms / 1e3) / 1e9},
+                   "graphsim": {"ms": gs_s * 1e3, "iterations": res[-1][6], "matches": res[-1][5],
+                                "edge_passes_per_s": res[-1][6] * gr.info.nentries / gs_s},
+                   "setup_s": round(setup_s, 1), "peak_source": peaks.get("source", "measured")},
+        "e2e": {"value": nq / lm_host, "unit": "queries/s", "h2d_bytes_per_step": 4 * 5 * 100,
+                "d2h_bytes_per_step": 8 * 10 * 100},
+        "clocks": clocks.summary(),
+    }
+
+
 def main(argv=None) -> int:
     args = parse_args(argv)
     rank, world, local = dist_env()
@@ -850,7 +966,8 @@ def main(argv=None) -> int:
         import torch.distributed as dist
         torch.cuda.set_device(local)
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    fn = {"plain": gpu_line, "batched": batched_line, "precision": precision_line, "serve": serve_line}[args.workload]
+    fn = {"plain": gpu_line, "batched": batched_line, "precision": precision_line, "serve": serve_line,
+          "next": next_line}[args.workload]
     line = fn(args, rank, world, local)
     if line is not None:
         print(json.dumps(line), flush=True)
