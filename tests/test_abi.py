@@ -119,3 +119,22 @@ def test_drivers_and_programs_are_built(native):
                          check=True).stdout
     for s in ("la3gp_degree", "la3gp_pagerank", "la3gp_bfs", "la3gp_sssp", "la3gp_cc", "la3gp_graphsim"):
         assert re.search(r"\bT " + s + r"\b", out), s
+
+
+def test_new_entry_points_reject_bad_arguments(native):
+    """LM, degree, top-k and graph simulation refuse bad arguments with
+    LA3G_EINVAL and a message, before any device work."""
+    import ctypes as C
+    import la3_gb300.build as B
+    L = native._native.lib()
+    u32 = (C.c_uint32 * 8)()
+    assert L.la3g_lm_prepare(None, None, None) == 1 and L.la3g_last_error_string()
+    assert L.la3g_lm_query(None, None, 0, 10, None, None, None, None, None, None) == 1
+    assert L.la3g_degree(None, None, 3, None, None, None, None) == 1
+    assert L.la3g_topk_u32(None, 5, 3, None, None, None) == 1              # values missing
+    assert L.la3g_topk_u32(u32, 8, 65, None, None, None) == 1              # k above 64
+    assert b"64" in L.la3g_last_error_string()
+    progs = C.CDLL(str(B.PROGRAMS_LIB))
+    progs.la3gp_graphsim.argtypes = [C.c_void_p] + [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint32,
+                                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    assert progs.la3gp_graphsim(None, None, 4, None, None, 0, None, None, None, None) == 1
