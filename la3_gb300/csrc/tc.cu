@@ -3,201 +3,615 @@
 //
 // The reference orients every edge from the lower to the higher original id
 // (remove_cycles, graph.hpp:174-179), collects for each vertex v the list
-// N<(v) of its lower neighbours (GnVertex), and for every oriented edge
-// (u, v), u < v, adds |N<(u) ∩ N<(v)| to u, accumulating in uint32 (CtVertex).
-// Each triangle a < b < c is therefore counted once, at its middle vertex b.
+// N<(v) of its lower neighbours (GnVertex, pass 1), and for every oriented
+// edge (u, v), u < v, adds |N<(u) ∩ N<(v)| to u, accumulating in uint32
+// (CtVertex, pass 2).  Each triangle a < b < c is therefore counted once, at
+// its middle vertex b.  Both passes are inside the reference's timed window,
+// and both are inside every call here.
 //
-// Here the triangles are found once each by the usual degree ordering
-// instead: rank(x) = (degree, id), N+(x) = neighbours of higher rank (sorted
-// by id), and every triangle x < y < w in rank order is found while scanning
-// the edge (x, y) as w ∈ N+(x) ∩ N+(y).  The middle vertex BY ID is then the
-// median of the three ids; since y and w both lie in N+(x), the warp that
-// owns x keeps one shared-memory counter per element of N+(x) (plus one for
-// x) and adds every found triangle to the counter of its middle vertex,
-// flushing them to the global uint32 counts once per x.  The per-vertex
-// counts are those of the reference (sums are order-free); the lists stay
-// short (max |N+| is about sqrt(2m)), which is what makes this fast on
-// skewed graphs.
+// Here every triangle is found once by degree ordering instead, and counted
+// at the middle vertex BY ID (the median of its three ids), which gives the
+// reference's per-vertex counts (sums are order-free, uint32 wraps alike):
+//
+//   rank(v) = position of v after sorting by (undirected degree, position);
+//   N+(x)   = neighbours of higher rank, kept as ranks, each row ascending;
+//   a triangle x < y < w in rank order has y, w in N+(x) and w in N+(y),
+//   and w lies in the part of N+(x) ranked above y (a suffix of the row).
+//
+// Pass 1 (list building, every call): degrees, ranks (one radix sort of the
+// vertices), N+ rows by an edge-parallel count / scan / fill, a segmented
+// sort of the rows, and the transposed pair lists: for each y the pairs
+// (x, start of the suffix of N+(x) after y), i.e. every oriented edge once.
+//
+// Pass 2 (counting) is y-centric: a task is a vertex y and a slice of its
+// pairs; N+(y) goes into a shared-memory hash table (rank -> index) with
+// the ids of its elements, and the walk reads the suffixes of the slice's
+// pairs concatenated, 32 list elements per warp step, each probed in the
+// table.  A hit w closes {x, y, w}; its middle id takes the count: x in a
+// per-pair shared counter, y in a register, w in a shared counter per element
+// of N+(y); all are flushed once per pair batch or task.  On R-MAT this
+// walks the shorter side of almost every pair (the suffix), and the lists
+// stay L2-resident.  N+(y) up to kTcWarpCap: one warp per task; longer: one
+// block per task with a block-wide table; beyond kTcBlockCap (no such rows on
+// R-MAT up to scale 24): a binary search in the sorted row in global memory.
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
+#include <cub/device/device_segmented_sort.cuh>
 
 #include "la3g_internal.h"
 
 namespace la3g {
 
-static constexpr uint32_t kTcCap = 1024;     // N+(x) held in shared memory up to this length
-static constexpr uint32_t kTcSmall = 192;    // lists up to this length use the high-occupancy variant
-static constexpr uint32_t kTcWalkFactor = 16;  // heavy x: N+(y) is walked unless > 16 |N+(x)| (then searched)
-static constexpr uint32_t kTcHubMin = 32;    // N+(y) longer than this (and than N+(x)) is a hub list:
-static constexpr uint32_t kTcHubCap = 1024;  // ... small x's pairs with it go to the hub kernel, up to this length
-static constexpr int kTcHubLanes = 8;        // lanes per hub pair in k_tc_hub
-
-// A pair (x, y) of a list N+(x) (at most kTcCap long) with a longer list
-// N+(y) of moderate length: instead of walking N+(y) against N+(x), or
-// binary-searching N+(y) in global memory for every element of N+(x), the
-// pair is handled hub-centrically (k_tc_hub walks the shorter N+(x)).
-__device__ __forceinline__ bool tc_is_hub_pair(uint32_t d, uint32_t ylen)
-{
-  return ylen > d && ylen > kTcHubMin && ylen <= kTcHubCap;
-}
+static constexpr uint32_t kTcEdgesPerThread = 8;  // edge-parallel passes: contiguous edges per thread
+static constexpr uint32_t kTcWarpCap = 256;       // |N+(y)| up to this: a warp per task
+static constexpr uint32_t kTcWarpSlots = 512;     // hash slots of a warp table (>= 2 kTcWarpCap)
+static constexpr int kTcWarpBloomBits = 11;       // Bloom bits of a warp table: 2^11
+static constexpr uint32_t kTcWarpPairs = 256;     // pairs per warp task
+static constexpr uint32_t kTcBlockCap = 2048;     // |N+(y)| up to this: a block table; longer: global search
+static constexpr uint32_t kTcBlockSlots = 4096;   // hash slots of a block table (>= 2 kTcBlockCap)
+static constexpr int kTcBlockBloomBits = 16;      // Bloom bits of a block table: 2^16
+static constexpr uint32_t kTcBlockPairs = 2048;   // pairs per block task
+static constexpr int kTcWarpKernelWarps = 8;
+static constexpr int kTcBlockThreads = 512;
+static constexpr uint32_t kTcSortWarpCap = 1024;  // N+ rows up to this are sorted by one warp
+static constexpr uint32_t kTcSortBlockCap = 16384;  // ... up to this by one block; longer: library sort
+static constexpr uint32_t kEmpty = 0xFFFFFFFFu;
 
 struct TcScratch
 {
-  uint32_t* plus_ptr = nullptr;  // [nslots + 1] by original id
-  uint32_t* plus_col = nullptr;  // [nent] ids, each row ascending
-  uint32_t* plus_col_r = nullptr;  // [nent] the same rows ordered by rank (ids stored)
-  uint32_t* order = nullptr;     // ids with 0 < |N+| <= kTcSmall, heaviest first
-  uint32_t* order_mid = nullptr; // ids with kTcSmall < |N+| <= kTcCap, heaviest first
-  uint32_t* big = nullptr;       // ids with |N+| > kTcCap
-  uint32_t norder = 0, nmid = 0, nbig = 0;
-  uint32_t* ntri = nullptr;      // [nslots] by id
-  unsigned int* next = nullptr;  // dynamic work counter
-  unsigned long long* total = nullptr;
-  double work = 0;               // sum over x of |N+(x)| + sum_y |N+(y)| (list elements read)
-  double work_mid = 0, work_big = 0;  // the part of it in the block-per-x and the global-search classes
-  // hub-centric pairs: small x with y in N+(x), |N+(y)| > max(|N+(x)|, kTcHubMin)
-  uint32_t* hub_ptr = nullptr;   // [nslots + 1] by id of y
-  uint32_t* hub_x = nullptr;     // the x's of each hub y
-  uint32_t* hub_j = nullptr;     // ... and the index of y in x's rank-ordered row
-  uint32_t* hubs = nullptr;      // hub ids, heaviest first
-  uint32_t nhubs = 0;
-  uint32_t hub_pairs = 0;
-  double hub_items = 0;          // sum over hub pairs of the part of N+(x) ranked above y
-  double hub_lists = 0;          // sum over hubs of |N+(y)|
+  uint32_t N = 0;
+  uint64_t m = 0;
+  uint32_t* deg = nullptr;          // [N] undirected degree by position
+  uint32_t* iota = nullptr;         // [N] 0..N-1
+  uint32_t* deg_of_rank = nullptr;  // [N]
+  uint32_t* pos_of_rank = nullptr;  // [N]
+  uint32_t* rank_of_pos = nullptr;  // [N]
+  uint32_t* id_of_rank = nullptr;   // [N]
+  uint32_t* dplus = nullptr;        // [N + 1] |N+| by rank, then the row offsets' input
+  uint32_t* pptr = nullptr;         // [N + 1] N+ row offsets (rows = ranks)
+  uint32_t* fill = nullptr;         // [N] fill cursors
+  uint32_t* pcol_raw = nullptr;     // [m] N+ rows as filled (ranks)
+  uint32_t* pcol = nullptr;         // [m] N+ rows, each ascending
+  uint32_t* mcount = nullptr;       // [N + 1] pairs per y
+  uint32_t* mptr = nullptr;         // [N + 1] pair offsets per y
+  uint2* pairs = nullptr;           // [m] (suffix start in pcol, x) grouped by y
+  unsigned long long* tcount = nullptr;  // [N + 1] tasks per y: block << 32 | warp
+  unsigned long long* toff = nullptr;    // [N + 1] their exclusive sums
+  uint2* wtasks = nullptr;          // (y, first pair) of the warp tasks
+  uint2* btasks = nullptr;          // ... and of the block tasks
+  uint32_t* ntri = nullptr;         // [N] by id
+  uint32_t* big_rows = nullptr;     // [N] N+ rows too long for a warp's sort
+  // [0] warp-task cursor [1] block-task cursor [2] walked [3] table builds
+  // [4] triangles [5] self-check failures [6] big rows [7] rows too long
+  // for the block sort
+  unsigned long long* ctr = nullptr;
+  unsigned long long* hctr = nullptr;  // pinned mirror
+  void* temp = nullptr;
+  size_t temp_bytes = 0;
+  void* seg_temp = nullptr;         // the library segmented sort's storage (oversize rows only)
+  size_t seg_bytes = 0;
+  int end_bit = 32;
 };
 
-static void tc_scratch_free(void* p) { delete (TcScratch*) p; }
-
-// Undirected degree by id: lower + higher neighbours.
-__global__ void k_tc_deg(const uint32_t* __restrict__ iptr, const uint32_t* __restrict__ optr,
-                         const uint32_t* __restrict__ id_of_pos, uint32_t N, uint32_t* deg)
+static void tc_scratch_free(void* p)
 {
-  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x)
-    deg[id_of_pos[p]] = (iptr[p + 1] - iptr[p]) + (optr[p + 1] - optr[p]);
+  TcScratch* s = (TcScratch*) p;
+  if (s->hctr) cudaFreeHost(s->hctr);
+  delete s;
 }
 
-// Every undirected edge once (push CSR of the id-oriented graph), emitted as
-// (lower rank, higher rank) = id(x) << 32 | id(y).
-__global__ void k_tc_rank_edges(const uint32_t* __restrict__ optr, const uint32_t* __restrict__ orow, uint32_t N,
-                                const uint32_t* __restrict__ id_of_pos, const uint32_t* __restrict__ deg,
-                                uint64_t* keys)
+// ---------------------------------------------------------------- pass 1
+
+__global__ void k_tc_deg(const uint32_t* __restrict__ iptr, const uint32_t* __restrict__ optr, uint32_t N,
+                         uint32_t* deg, uint32_t* iota)
 {
   for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x)
   {
-    const uint32_t a = id_of_pos[p];
-    const uint32_t da = deg[a];
-    for (uint32_t e = optr[p]; e < optr[p + 1]; e++)
-    {
-      const uint32_t b = id_of_pos[orow[e]];
-      const uint32_t db = deg[b];
-      const bool a_low = da < db || (da == db && a < b);
-      keys[e] = a_low ? ((uint64_t) a << 32 | b) : ((uint64_t) b << 32 | a);
-    }
+    deg[p] = (iptr[p + 1] - iptr[p]) + (optr[p + 1] - optr[p]);
+    iota[p] = p;
   }
 }
 
-__global__ void k_tc_split_keys(const uint64_t* __restrict__ keys, uint64_t m, uint32_t* col)
-{
-  for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (uint64_t) gridDim.x * blockDim.x)
-    col[i] = (uint32_t) keys[i];
-}
-
-__global__ void k_tc_rows(const uint64_t* __restrict__ k, uint64_t m, uint32_t N, uint32_t* ptr)
-{
-  for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i <= m; i += (uint64_t) gridDim.x * blockDim.x)
-  {
-    int64_t r = i < m ? (int64_t) (k[i] >> 32) : (int64_t) N;
-    int64_t rp = i == 0 ? -1 : (int64_t) (k[i - 1] >> 32);
-    for (int64_t q = rp + 1; q <= r; q++) ptr[q] = (uint32_t) i;
-  }
-}
-
-// Vertex ranks for the rank-ordered rows: keys (degree, id) sorted give
-// rank -> id; rank_of_id is its inverse.
-__global__ void k_tc_vkeys(uint32_t N, const uint32_t* __restrict__ deg, uint64_t* keys)
-{
-  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < N; v += gridDim.x * blockDim.x)
-    keys[v] = (uint64_t) deg[v] << 32 | v;
-}
-
-__global__ void k_tc_ranks(uint32_t N, const uint64_t* __restrict__ sorted, uint32_t* rank_of_id, uint32_t* id_of_rank)
+__global__ void k_tc_ranks(uint32_t N, const uint32_t* __restrict__ pos_of_rank, const uint32_t* __restrict__ id_of_pos,
+                           uint32_t* rank_of_pos, uint32_t* id_of_rank)
 {
   for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < N; r += gridDim.x * blockDim.x)
   {
-    const uint32_t v = (uint32_t) sorted[r];
-    rank_of_id[v] = r;
-    id_of_rank[r] = v;
+    const uint32_t p = pos_of_rank[r];
+    rank_of_pos[p] = r;
+    id_of_rank[r] = id_of_pos[p];
   }
 }
 
-// (x, id) keys of the id-ordered rows -> (x, rank) keys, and back to ids
-// once sorted.
-__global__ void k_tc_rank_keys(const uint64_t* __restrict__ k, uint64_t m, const uint32_t* __restrict__ rank_of_id,
-                               uint64_t* out)
+// Row of entry e: the largest r < nrows with ptr[r] <= e (e < ptr[nrows]).
+__device__ __forceinline__ uint32_t tc_row_of(const uint32_t* __restrict__ ptr, uint32_t nrows, uint64_t e)
 {
-  for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (uint64_t) gridDim.x * blockDim.x)
-    out[i] = (k[i] & 0xFFFFFFFF00000000ull) | rank_of_id[(uint32_t) k[i]];
-}
-
-__global__ void k_tc_rank_ids(const uint64_t* __restrict__ k, uint64_t m, const uint32_t* __restrict__ id_of_rank,
-                              uint32_t* col)
-{
-  for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (uint64_t) gridDim.x * blockDim.x)
-    col[i] = id_of_rank[(uint32_t) k[i]];
-}
-
-// Work estimate per vertex and the lists of vertices to process.
-__global__ void k_tc_work(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, uint32_t N,
-                          uint32_t* wkey, uint32_t* wid, uint32_t* big, unsigned long long* counts)
-{
-  for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < N; x += gridDim.x * blockDim.x)
+  uint32_t lo = 0, hi = nrows;
+  while (hi - lo > 1)
   {
-    const uint32_t b = ptr[x], e = ptr[x + 1];
-    if (b == e) continue;
-    uint64_t w = e - b;
-    const uint32_t d = e - b;
-    for (uint32_t i = b; i < e; i++)
+    const uint32_t mid = (lo + hi) >> 1;
+    if (ptr[mid] <= e) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Every undirected edge once (the pull CSR of the id-oriented graph: row =
+// higher id, column = lower id); each thread takes kTcEdgesPerThread
+// consecutive entries, so a hub row spreads over many threads.  PLUS = false
+// counts |N+| per lower-rank end; PLUS = true writes the higher-rank end into
+// the lower end's row.
+template <bool FILL>
+__global__ void __launch_bounds__(256)
+k_tc_orient(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, uint32_t nrows, uint64_t m,
+            const uint32_t* __restrict__ rank_of_pos, uint32_t* count_or_fill, const uint32_t* __restrict__ pptr,
+            uint32_t* pcol)
+{
+  const uint64_t e0 = ((uint64_t) blockIdx.x * blockDim.x + threadIdx.x) * kTcEdgesPerThread;
+  if (e0 >= m) return;
+  const uint64_t e1 = min(e0 + kTcEdgesPerThread, m);
+  uint32_t r = tc_row_of(ptr, nrows, e0);
+  uint32_t rr = rank_of_pos[r];
+  uint64_t rend = ptr[r + 1];
+  for (uint64_t e = e0; e < e1; e++)
+  {
+    if (e >= rend)  // the next non-empty row (runs of empty rows are skipped by the search)
     {
-      const uint32_t ylen = ptr[col[i] + 1] - ptr[col[i]];
-      // a hub pair is walked by k_tc_hub (|N+(x)| elements, counted there)
-      if (d <= kTcCap && tc_is_hub_pair(d, ylen)) continue;
-      w += ylen;
+      r = tc_row_of(ptr, nrows, e);
+      rr = rank_of_pos[r];
+      rend = ptr[r + 1];
     }
-    if (e - b > kTcCap)
+    const uint32_t ru = rank_of_pos[col[e]];
+    const uint32_t lo = min(rr, ru), hi = max(rr, ru);
+    if (FILL) pcol[pptr[lo] + atomicAdd(&count_or_fill[lo], 1u)] = hi;
+    else atomicAdd(&count_or_fill[lo], 1u);
+  }
+}
+
+// Pairs per y (a y with an empty N+(y) closes no triangle as the middle
+// rank) and the tasks they form.
+__global__ void k_tc_pair_counts(uint32_t N, const uint32_t* __restrict__ pptr, const uint32_t* __restrict__ deg_of_rank,
+                                 uint32_t* mcount, unsigned long long* tcount)
+{
+  for (uint32_t y = blockIdx.x * blockDim.x + threadIdx.x; y <= N; y += gridDim.x * blockDim.x)
+  {
+    uint32_t c = 0;
+    unsigned long long t = 0;
+    if (y < N)
     {
-      big[atomicAdd(&counts[1], 1ull)] = x;
-      atomicAdd(&counts[5], (unsigned long long) w);
-    }
-    else
-    {
-      // keys: class bit on top (small lists first), then ~work (heaviest first)
-      const uint32_t cls = (e - b) > kTcSmall ? 1u : 0u;
-      const unsigned long long slot = atomicAdd(&counts[0], 1ull);
-      const uint32_t wq = (uint32_t) (w < 0x7FFFFFFFull ? w : 0x7FFFFFFFull);
-      wkey[slot] = (cls << 31) | (0x7FFFFFFFu - wq);
-      wid[slot] = x;
-      if (cls)
+      const uint32_t dp = pptr[y + 1] - pptr[y];
+      c = dp ? deg_of_rank[y] - dp : 0u;
+      if (c)
       {
-        atomicAdd(&counts[3], 1ull);
-        atomicAdd(&counts[4], (unsigned long long) w);
+        if (dp <= kTcWarpCap) t = (c + kTcWarpPairs - 1) / kTcWarpPairs;
+        else t = (unsigned long long) ((c + kTcBlockPairs - 1) / kTcBlockPairs) << 32;
       }
     }
-    atomicAdd(&counts[2], (unsigned long long) w);
+    mcount[y] = c;
+    tcount[y] = t;
   }
 }
 
-// Shared-memory set of N+(x) for O(1) membership: open addressing with
-// linear probing over a power-of-two table of at least 2 |N+(x)| slots;
-// each slot holds a vertex id and its index in N+(x).
-static constexpr uint32_t kEmpty = 0xFFFFFFFFu;
+// Index of rank y in the ascending row [b, e) (y is known to be there).
+__device__ __forceinline__ uint32_t tc_find_in_row(const uint32_t* __restrict__ pcol, uint32_t b, uint32_t e, uint32_t y)
+{
+  while (b < e)
+  {
+    const uint32_t mid = (b + e) >> 1;
+    if (pcol[mid] < y) b = mid + 1;
+    else e = mid;
+  }
+  return b;
+}
 
-__device__ __forceinline__ uint32_t tc_slot(uint32_t w, int lg) { return (w * 0x9E3779B1u) >> (32 - lg); }
+// Pair lists by y, built from each y's own adjacency (its in- and out-rows in
+// the id-oriented graph), so that a hub's many pairs come from consecutive
+// entries: the lanes of a warp that hold the same y reserve their slots with
+// one atomic.  A neighbour x of lower rank gives the pair (s, x), s the
+// index after y in the sorted row N+(x).  Thread chunks [0, m8) cover the
+// in-rows' m entries, [m8, m8 + m) the out-rows' (m8 = m rounded up to the
+// chunk size, so that no chunk straddles the two).
+__global__ void __launch_bounds__(256)
+k_tc_pairs(const uint32_t* __restrict__ iptr, const uint32_t* __restrict__ icol, const uint32_t* __restrict__ optr,
+           const uint32_t* __restrict__ orow, uint32_t nrows, uint32_t N, uint64_t m,
+           const uint32_t* __restrict__ rank_of_pos, const uint32_t* __restrict__ pptr,
+           const uint32_t* __restrict__ pcol, const uint32_t* __restrict__ mptr, uint32_t* fill, uint2* pairs)
+{
+  const int lane = threadIdx.x & 31;
+  const uint64_t m8 = (m + kTcEdgesPerThread - 1) / kTcEdgesPerThread * kTcEdgesPerThread;
+  const uint64_t e0 = ((uint64_t) blockIdx.x * blockDim.x + threadIdx.x) * kTcEdgesPerThread;
+  const bool in_part = e0 < m8;
+  const uint32_t* ptr = in_part ? iptr : optr;
+  const uint32_t* col = in_part ? icol : orow;
+  const uint64_t base = in_part ? 0 : m8;
+  const uint64_t lim = in_part ? m : m8 + m;
+  const bool live = e0 < lim;
+  uint32_t r = 0, ry = 0;
+  uint64_t rend = 0;
+  if (live)
+  {
+    r = tc_row_of(ptr, in_part ? nrows : N, e0 - base);
+    ry = rank_of_pos[r];
+    rend = ptr[r + 1] + base;
+  }
+  for (uint32_t u = 0; u < kTcEdgesPerThread; u++)
+  {
+    const uint64_t e = e0 + u;
+    bool emit = false;
+    uint32_t x = 0;
+    if (live && e < lim)
+    {
+      if (e >= rend)  // the next non-empty row (sinks' out-rows are empty, in runs)
+      {
+        r = tc_row_of(ptr, in_part ? nrows : N, e - base);
+        ry = rank_of_pos[r];
+        rend = ptr[r + 1] + base;
+      }
+      x = rank_of_pos[col[e - base]];
+      emit = x < ry && pptr[ry + 1] > pptr[ry];
+    }
+    const unsigned want = __ballot_sync(0xffffffffu, emit);
+    if (!want) continue;
+    const unsigned grp = __match_any_sync(0xffffffffu, emit ? ry : 0xFFFFFFFFu);
+    if (emit)
+    {
+      const int leader = __ffs(grp) - 1;
+      uint32_t slot = 0;
+      if (lane == leader) slot = atomicAdd(&fill[ry], (uint32_t) __popc(grp));
+      slot = __shfl_sync(grp, slot, leader) + __popc(grp & ((1u << lane) - 1));
+      const uint32_t sidx = tc_find_in_row(pcol, pptr[x], pptr[x + 1], ry);
+      pairs[mptr[ry] + slot] = make_uint2(sidx + 1, x);
+    }
+  }
+}
 
-__host__ __device__ constexpr uint32_t tc_pow2(uint32_t v) { return v <= 32 ? 32 : 2 * tc_pow2((v + 1) / 2); }
+__global__ void k_tc_tasks(uint32_t N, const unsigned long long* __restrict__ toff, const uint32_t* __restrict__ mptr,
+                           uint2* wtasks, uint2* btasks)
+{
+  for (uint32_t y = blockIdx.x * blockDim.x + threadIdx.x; y < N; y += gridDim.x * blockDim.x)
+  {
+    const unsigned long long c = toff[y + 1] - toff[y];
+    const uint32_t nw = (uint32_t) c, nb = (uint32_t) (c >> 32);
+    const uint32_t wo = (uint32_t) toff[y], bo = (uint32_t) (toff[y] >> 32);
+    for (uint32_t k = 0; k < nw; k++) wtasks[wo + k] = make_uint2(y, mptr[y] + k * kTcWarpPairs);
+    for (uint32_t k = 0; k < nb; k++) btasks[bo + k] = make_uint2(y, mptr[y] + k * kTcBlockPairs);
+  }
+}
+
+// ---------------------------------------------------------------- row sort
+
+// Sorts every N+ row ascending (pass 1 fills them in arbitrary order): up to
+// 32 elements in a warp's registers (a bitonic network over shuffles), up to
+// kTcSortWarpCap in a warp's shared buffer; longer rows are listed for
+// k_tc_sort_big.
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
+k_tc_sort_rows(const uint32_t* __restrict__ pptr, uint32_t N, const uint32_t* __restrict__ raw, uint32_t* out,
+               uint32_t* big_rows, unsigned long long* nbig)
+{
+  __shared__ uint32_t s_buf[WARPS][kTcSortWarpCap];
+  const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
+  uint32_t* buf = s_buf[wi];
+  const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t x = gw; x < N; x += nw)
+  {
+    const uint32_t b = pptr[x], d = pptr[x + 1] - b;
+    if (d <= 1)
+    {
+      if (d == 1 && lane == 0) out[b] = raw[b];
+      continue;
+    }
+    if (d <= 32)
+    {
+      uint32_t v = (uint32_t) lane < d ? raw[b + lane] : kEmpty;
+#pragma unroll
+      for (int k = 2; k <= 32; k <<= 1)
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1)
+        {
+          const uint32_t o = __shfl_xor_sync(0xffffffffu, v, j);
+          const bool asc = (lane & k) == 0, low = (lane & j) == 0;
+          v = (low == asc) ? min(v, o) : max(v, o);
+        }
+      if ((uint32_t) lane < d) out[b + lane] = v;
+      continue;
+    }
+    if (d > kTcSortWarpCap)
+    {
+      if (lane == 0) big_rows[atomicAdd(nbig, 1ull)] = x;
+      continue;
+    }
+    uint32_t n = 64;
+    while (n < d) n <<= 1;
+    for (uint32_t i = lane; i < n; i += 32) buf[i] = i < d ? raw[b + i] : kEmpty;
+    __syncwarp();
+    for (uint32_t k = 2; k <= n; k <<= 1)
+      for (uint32_t j = k >> 1; j > 0; j >>= 1)
+      {
+        for (uint32_t q = lane; q < n / 2; q += 32)
+        {
+          const uint32_t i = 2 * j * (q / j) + (q % j), l = i + j;
+          const uint32_t a = buf[i], c = buf[l];
+          if ((a > c) == ((i & k) == 0))
+          {
+            buf[i] = c;
+            buf[l] = a;
+          }
+        }
+        __syncwarp();
+      }
+    for (uint32_t i = lane; i < d; i += 32) out[b + i] = buf[i];
+    __syncwarp();
+  }
+}
+
+// Rows longer than kTcSortWarpCap, one block each, in dynamic shared memory
+// (up to kTcSortBlockCap elements); longer ones are counted in *over so that
+// the call sorts with the library's segmented sort instead.
+__global__ void __launch_bounds__(1024)
+k_tc_sort_big(const uint32_t* __restrict__ pptr, const uint32_t* __restrict__ raw, uint32_t* out,
+              const uint32_t* __restrict__ big_rows, const unsigned long long* __restrict__ nbig,
+              unsigned long long* over)
+{
+  extern __shared__ uint32_t sbig[];
+  const uint32_t nrows = (uint32_t) *nbig;
+  for (uint32_t r = blockIdx.x; r < nrows; r += gridDim.x)
+  {
+    const uint32_t x = big_rows[r];
+    const uint32_t b = pptr[x], d = pptr[x + 1] - b;
+    if (d > kTcSortBlockCap)
+    {
+      if (threadIdx.x == 0) atomicAdd(over, 1ull);
+      continue;
+    }
+    uint32_t n = 64;
+    while (n < d) n <<= 1;
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) sbig[i] = i < d ? raw[b + i] : kEmpty;
+    __syncthreads();
+    for (uint32_t k = 2; k <= n; k <<= 1)
+      for (uint32_t j = k >> 1; j > 0; j >>= 1)
+      {
+        for (uint32_t q = threadIdx.x; q < n / 2; q += blockDim.x)
+        {
+          const uint32_t i = 2 * j * (q / j) + (q % j), l = i + j;
+          const uint32_t a = sbig[i], c = sbig[l];
+          if ((a > c) == ((i & k) == 0))
+          {
+            sbig[i] = c;
+            sbig[l] = a;
+          }
+        }
+        __syncthreads();
+      }
+    for (uint32_t i = threadIdx.x; i < d; i += blockDim.x) out[b + i] = sbig[i];
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------- pass 2
+
+__device__ __forceinline__ uint32_t tc_mid3(uint32_t a, uint32_t b, uint32_t c)
+{
+  return max(min(a, b), min(max(a, b), c));
+}
+
+__device__ __forceinline__ uint32_t tc_hash(uint32_t w, int lg) { return (w * 0x9E3779B1u) >> (32 - lg); }
+__device__ __forceinline__ uint32_t tc_bloom_bit(uint32_t w, int bbits) { return (w * 0x85EBCA6Bu) >> (32 - bbits); }
+
+// Membership in N+(y): one-hash Bloom bits for a branch-free first test, a
+// shared-memory table (rank -> index in the row) for the candidates; rows
+// longer than the block table use a binary search in the sorted row in
+// global memory instead (no Bloom bits, every element is a candidate).
+template <class IDX>
+struct TcTable
+{
+  const uint32_t* key;
+  const IDX* idx;
+  const uint32_t* bloom;
+  uint32_t mask;
+  int lg, bbits;
+  const uint32_t* __restrict__ row;  // global row (search mode), else null
+  uint32_t d;
+  __device__ __forceinline__ bool maybe(uint32_t w) const
+  {
+    if (!bloom) return true;
+    const uint32_t h = tc_bloom_bit(w, bbits);
+    return (bloom[h >> 5] >> (h & 31)) & 1u;
+  }
+  __device__ __forceinline__ int find(uint32_t w) const
+  {
+    if (row)
+    {
+      uint32_t lo = 0, hi = d;
+      while (lo < hi)
+      {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (row[mid] < w) lo = mid + 1;
+        else hi = mid;
+      }
+      return (lo < d && row[lo] == w) ? (int) lo : -1;
+    }
+    uint32_t sl = tc_hash(w, lg);
+    for (;;)
+    {
+      const uint32_t k = key[sl];
+      if (k == w) return idx[sl];
+      if (k == kEmpty) return -1;
+      sl = (sl + 1) & mask;
+    }
+  }
+};
+
+// Per-warp batch state: up to 32 pairs with non-empty suffixes, compacted,
+// and the queue of candidate elements (those that pass the Bloom test),
+// resolved 32 at a time so that the table probes and the counting run with
+// all lanes.
+struct TcBatch
+{
+  uint32_t start[32];  // suffix start in pcol
+  uint32_t off[32];    // offset of the pair's first element in the batch's walk
+  uint32_t len[32];    // suffix length
+  uint32_t xid[32];
+  uint32_t cx[32];     // triangles counted at x
+  uint32_t qw[64];     // queued candidates (ring)
+  uint8_t qk[64];      // ... and their pair's index in the batch
+};
+
+// Resolves queue entries [qh, qh + cnt) (cnt <= 32, one per lane).
+template <class IDX>
+__device__ __forceinline__ void tc_drain(TcBatch& B, uint32_t qh, uint32_t cnt, const TcTable<IDX>& T, uint32_t yid,
+                                         const uint32_t* lid, uint32_t* cn, const uint32_t* __restrict__ id_of_rank,
+                                         uint32_t& cy, uint32_t* ntri, unsigned long long* err)
+{
+  const uint32_t lane = threadIdx.x & 31;
+  __syncwarp();
+  if (lane < cnt)
+  {
+    const uint32_t pos = (qh + lane) & 63;
+    const uint32_t w = B.qw[pos], k = B.qk[pos];
+    const int j = T.find(w);
+    if (j >= (int) T.d) atomicAdd(err, 1ull << 32);
+    else if (j >= 0)
+    {
+      const uint32_t xo = B.xid[k];
+      const uint32_t wid = lid ? lid[j] : id_of_rank[w];
+      const uint32_t mid = tc_mid3(xo, yid, wid);
+      if (mid == yid) cy++;
+      else if (mid == xo) atomicAdd(&B.cx[k], 1u);
+      else if (cn) atomicAdd(&cn[j], 1u);
+      else atomicAdd(&ntri[wid], 1u);
+    }
+  }
+  __syncwarp();
+}
+
+// One warp walks pairs [p0, p1) of y against table T, 32 pairs per round:
+// the suffixes of a round are concatenated and read 64 elements per step
+// (two 32-element windows, loads in flight together); element w0 + lane
+// belongs to the pair whose start offset is the last one at or below it,
+// found from the window's start bits and the count of pairs started
+// before it.  Hits whose middle id is y go to cy, at x to the pair's shared
+// counter, at an element of N+(y) to cn[index] (or straight to ntri in
+// search mode).
+template <class IDX>
+__device__ __forceinline__ void tc_walk_pairs(uint32_t p0, uint32_t p1, const uint2* __restrict__ pairs,
+                                              const uint32_t* __restrict__ pptr, const uint32_t* __restrict__ pcol,
+                                              const uint32_t* __restrict__ id_of_rank, uint32_t yid,
+                                              const TcTable<IDX>& T, const uint32_t* lid, uint32_t* cn, TcBatch& B,
+                                              uint32_t& cy, unsigned long long& walked, uint32_t* ntri,
+                                              unsigned long long* err)
+{
+  const uint32_t lane = threadIdx.x & 31;
+  const unsigned full = 0xffffffffu;
+  const unsigned lt = (1u << lane) - 1, le = lane == 31 ? full : ((2u << lane) - 1);
+  for (uint32_t pb = p0; pb < p1; pb += 32)
+  {
+    const uint32_t p = pb + lane;
+    uint32_t s = 0, L = 0, xid = 0;
+    if (p < p1)
+    {
+      const uint2 px = pairs[p];
+      s = px.x;
+      L = pptr[px.y + 1] - s;
+      xid = id_of_rank[px.y];
+    }
+    const unsigned nz = __ballot_sync(full, L > 0);
+    uint32_t incl = L;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+      const uint32_t v = __shfl_up_sync(full, incl, o);
+      if (lane >= (uint32_t) o) incl += v;
+    }
+    const uint32_t total = __shfl_sync(full, incl, 31);
+    if (L > 0)
+    {
+      const uint32_t k = __popc(nz & lt);
+      B.start[k] = s;
+      B.off[k] = incl - L;
+      B.len[k] = L;
+      B.xid[k] = xid;
+      B.cx[k] = 0;
+    }
+    __syncwarp();
+    const uint32_t npairs = __popc(nz);
+    // lane k holds the start offset of the k-th compacted pair
+    const uint32_t pk = lane < npairs ? B.off[lane] : kEmpty;
+    uint32_t qh = 0, qn = 0;
+    for (uint32_t w0 = 0; w0 < total; w0 += 64)
+    {
+      uint32_t wv[2], kv[2];
+      bool okv[2];
+#pragma unroll
+      for (int u = 0; u < 2; u++)
+      {
+        const uint32_t base = w0 + 32u * u;
+        const uint32_t bit = (pk >= base && pk < base + 32) ? (1u << (pk - base)) : 0u;
+        const unsigned starts = __reduce_or_sync(full, bit);
+        const uint32_t before = __popc(__ballot_sync(full, pk < base));
+        const uint32_t t = base + lane;
+        const uint32_t k = min(before + __popc(starts & le) - 1u, 31u);
+        // the owner lies in this round and t inside its suffix (by
+        // construction; checked so that a slip cannot turn into a fault)
+        const bool ok = t < total && k < npairs && t >= B.off[k] && t - B.off[k] < B.len[k];
+        if (t < total && !ok) atomicAdd(err, 1ull);
+        wv[u] = ok ? pcol[B.start[k] + (t - B.off[k])] : kEmpty;
+        kv[u] = k;
+        okv[u] = ok;
+      }
+#pragma unroll
+      for (int u = 0; u < 2; u++)
+      {
+        const bool cand = okv[u] && T.maybe(wv[u]);
+        const unsigned m = __ballot_sync(full, cand);
+        if (cand)
+        {
+          const uint32_t pos = (qh + qn + __popc(m & lt)) & 63;
+          B.qw[pos] = wv[u];
+          B.qk[pos] = (uint8_t) kv[u];
+        }
+        qn += __popc(m);
+        if (qn >= 32)
+        {
+          tc_drain(B, qh, 32, T, yid, lid, cn, id_of_rank, cy, ntri, err);
+          qh = (qh + 32) & 63;
+          qn -= 32;
+        }
+      }
+    }
+    if (qn) tc_drain(B, qh, qn, T, yid, lid, cn, id_of_rank, cy, ntri, err);
+    walked += total;
+    __syncwarp();
+    if (lane < npairs && B.cx[lane]) atomicAdd(&ntri[B.xid[lane]], B.cx[lane]);
+    __syncwarp();
+  }
+}
+
+// Builds the table and Bloom bits of N+(y) (d elements at row) with
+// `nthreads` threads starting at thread `tid`; the caller clears the table
+// and the bits and synchronises before and after.
+template <class IDX>
+__device__ __forceinline__ void tc_build(const uint32_t* __restrict__ row, uint32_t d, int lg, int bbits,
+                                         const uint32_t* __restrict__ id_of_rank, uint32_t* key, IDX* idx,
+                                         uint32_t* bloom, uint32_t* lid, uint32_t* cn, uint32_t tid, uint32_t nthreads)
+{
+  const uint32_t mask = (1u << lg) - 1;
+  for (uint32_t j = tid; j < d; j += nthreads)
+  {
+    const uint32_t w = row[j];
+    lid[j] = id_of_rank[w];
+    cn[j] = 0;
+    uint32_t sl = tc_hash(w, lg);
+    while (atomicCAS(&key[sl], kEmpty, w) != kEmpty) sl = (sl + 1) & mask;
+    idx[sl] = (IDX) j;
+    const uint32_t h = tc_bloom_bit(w, bbits);
+    atomicOr(&bloom[h >> 5], 1u << (h & 31));
+  }
+}
 
 __device__ __forceinline__ int tc_lg(uint32_t d)
 {
@@ -206,496 +620,138 @@ __device__ __forceinline__ int tc_lg(uint32_t d)
   return lg;
 }
 
-// Counts the triangle {x, y, w} (w found at index pw of N+(x), y at index
-// jy) at its middle id: x through cx, the others through their counters.
-__device__ __forceinline__ void tc_attribute(uint32_t x, uint32_t y, uint32_t w, uint32_t jy, uint32_t pw,
-                                             uint32_t* Cn, uint32_t& cx)
-{
-  // the middle id of {x, y, w}: w itself, or the larger / smaller of x, y;
-  // x's count stays in a register (one shared word would serialise lanes)
-  const uint32_t mn = min(x, y), mx = max(x, y);
-  const uint32_t mid = w < mn ? mn : (w > mx ? mx : w);
-  if (mid == x) cx++;
-  else atomicAdd(&Cn[mid == w ? pw : jy], 1u);
-}
-
-// x's walk with lane groups of G lanes: group g takes y = L[jy] for jy = g,
-// g + ngroups, ...; its lanes walk N+(y) (coalesced loads, each element
-// probed in the hash set of N+(x)) unless N+(y) is more than walk_factor
-// times longer than N+(x), in which case they walk N+(x) and binary-search
-// each element in N+(y).
-// Bloom bits of N+(x) (one hash, kBloomBits bits): most candidates that
-// are not in N+(x) are rejected by one shared load, before the probe loop.
-static constexpr uint32_t kBloomBits = 1u << 16;
-__device__ __forceinline__ uint32_t tc_bloom(uint32_t w) { return (w * 0x85EBCA6Bu) >> 16; }
-
-template <int G, class IDX>
-__device__ __forceinline__ void tc_walk(uint32_t x, uint32_t d, const uint32_t* L, uint32_t* Cn, const uint32_t* key,
-                                        const IDX* idx, int lg, uint32_t* cx, const uint32_t* __restrict__ ptr,
-                                        const uint32_t* __restrict__ col, uint32_t walk_factor, uint32_t g,
-                                        uint32_t ngroups, uint32_t glane, const uint32_t* bloom = nullptr)
-{
-  const uint32_t mask = (1u << lg) - 1;
-  uint32_t cxr = 0;  // triangles counted at x by this lane
-  for (uint32_t jy = g; jy < d; jy += ngroups)
-  {
-    const uint32_t y = L[jy];
-    const uint32_t yb = ptr[y], ylen = ptr[y + 1] - yb;
-    if (tc_is_hub_pair(d, ylen)) continue;  // k_tc_hub walks this pair
-    if (ylen <= walk_factor * d)
-    {
-      // four independent list loads in flight per lane, then the probes
-      for (uint32_t r0 = glane; r0 < ylen; r0 += 4 * G)
-      {
-        uint32_t wv[4];
-#pragma unroll
-        for (int u = 0; u < 4; u++) wv[u] = r0 + u * G < ylen ? col[yb + r0 + u * G] : kEmpty;
-#pragma unroll
-        for (int u = 0; u < 4; u++)
-        {
-          const uint32_t w = wv[u];
-          if (w == kEmpty) continue;
-          if (bloom)
-          {
-            const uint32_t bb = tc_bloom(w);
-            if (!((bloom[bb >> 5] >> (bb & 31)) & 1u)) continue;
-          }
-          uint32_t sl = tc_slot(w, lg);
-          for (;;)
-          {
-            const uint32_t kk = key[sl];
-            if (kk == w)
-            {
-              tc_attribute(x, y, w, jy, idx[sl], Cn, cxr);
-              break;
-            }
-            if (kk == kEmpty) break;
-            sl = (sl + 1) & mask;
-          }
-        }
-      }
-    }
-    else
-    {
-      for (uint32_t r = glane; r < d; r += G)
-      {
-        const uint32_t w = L[r];
-        uint32_t a = yb, c = yb + ylen;
-        while (a < c)
-        {
-          const uint32_t mid = (a + c) >> 1;
-          if (col[mid] < w) a = mid + 1;
-          else c = mid;
-        }
-        if (a < yb + ylen && col[a] == w) tc_attribute(x, y, w, jy, r, Cn, cxr);
-      }
-    }
-  }
-  for (int o = 16; o > 0; o >>= 1) cxr += __shfl_xor_sync(0xffffffffu, cxr, o);
-  if ((threadIdx.x & 31) == 0 && cxr) atomicAdd(cx, cxr);
-}
-
-template <class IDX>
-__device__ __forceinline__ void tc_insert_t(uint32_t* key, IDX* idx, int lg, uint32_t w, uint32_t j)
-{
-  const uint32_t mask = (1u << lg) - 1;
-  uint32_t sl = tc_slot(w, lg);
-  while (atomicCAS(&key[sl], kEmpty, w) != kEmpty) sl = (sl + 1) & mask;
-  idx[sl] = (IDX) j;
-}
-
-__device__ __forceinline__ uint32_t lower_bound_s(const uint32_t* s, uint32_t n, uint32_t key)
-{
-  uint32_t lo = 0, hi = n;
-  while (lo < hi)
-  {
-    uint32_t mid = (lo + hi) >> 1;
-    if (s[mid] < key) lo = mid + 1;
-    else hi = mid;
-  }
-  return lo;
-}
-
-// One warp per vertex x (fetched dynamically, heaviest first).  Shared
-// memory holds N+(x), the prefix offsets of the per-y work, and one counter
-// per element of N+(x).  For each y in N+(x) the shorter of N+(y) and N+(x)
-// is walked and its elements looked up in the other (a shared-memory binary
-// search into N+(x), or a global one into N+(y)); lanes share the
-// concatenated work of all y.  A hit w closes the triangle {x, y, w}, which
-// is counted at its middle id.
-// Counts, per hub y, the x's (|N+(x)| <= kTcCap) pointing at it and the
-// part of their rows a walk reads: only the elements ranked above y (after y
-// in the rank-ordered row) can lie in N+(y).
-__global__ void k_tc_hub_count(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ colr, uint32_t N,
-                               uint32_t* cnt, unsigned long long* work)
-{
-  for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < N; x += gridDim.x * blockDim.x)
-  {
-    const uint32_t b = ptr[x], d = ptr[x + 1] - b;
-    if (d == 0 || d > kTcCap) continue;
-    for (uint32_t i = b; i < b + d; i++)
-    {
-      const uint32_t y = colr[i];
-      if (tc_is_hub_pair(d, ptr[y + 1] - ptr[y]))
-      {
-        atomicAdd(&cnt[y], 1u);
-        atomicAdd(&work[y], (unsigned long long) (b + d - i - 1));
-      }
-    }
-  }
-}
-
-__global__ void k_tc_hub_fill(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ colr, uint32_t N,
-                              const uint32_t* __restrict__ hub_ptr, uint32_t* fill, uint32_t* hub_x, uint32_t* hub_j)
-{
-  for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < N; x += gridDim.x * blockDim.x)
-  {
-    const uint32_t b = ptr[x], d = ptr[x + 1] - b;
-    if (d == 0 || d > kTcCap) continue;
-    for (uint32_t i = b; i < b + d; i++)
-    {
-      const uint32_t y = colr[i];
-      if (tc_is_hub_pair(d, ptr[y + 1] - ptr[y]))
-      {
-        const uint32_t slot = hub_ptr[y] + atomicAdd(&fill[y], 1u);
-        hub_x[slot] = x;
-        hub_j[slot] = i - b;
-      }
-    }
-  }
-}
-
-// Totals for the algorithmic byte count: sum of |N+(x)| over hub pairs and
-// of |N+(y)| over hubs.
-__global__ void k_tc_hub_sums(const uint32_t* __restrict__ ptr, uint32_t N, const uint32_t* __restrict__ cnt,
-                              const unsigned long long* __restrict__ work, unsigned long long* out)
-{
-  unsigned long long a = 0, b = 0;
-  for (uint32_t y = blockIdx.x * blockDim.x + threadIdx.x; y < N; y += gridDim.x * blockDim.x)
-    if (cnt[y])
-    {
-      a += work[y];
-      b += ptr[y + 1] - ptr[y];
-    }
-  for (int o = 16; o > 0; o >>= 1)
-  {
-    a += __shfl_xor_sync(0xffffffffu, a, o);
-    b += __shfl_xor_sync(0xffffffffu, b, o);
-  }
-  if ((threadIdx.x & 31) == 0)
-  {
-    if (a) atomicAdd(&out[0], a);
-    if (b) atomicAdd(&out[1], b);
-  }
-}
-
-// Hub keys for sorting: ~work so that heavier hubs come first.
-__global__ void k_tc_hub_keys(uint32_t N, const uint32_t* __restrict__ cnt, const unsigned long long* __restrict__ work,
-                              uint32_t* keys, uint32_t* ids, unsigned long long* n)
-{
-  for (uint32_t y = blockIdx.x * blockDim.x + threadIdx.x; y < N; y += gridDim.x * blockDim.x)
-    if (cnt[y])
-    {
-      const unsigned long long k = atomicAdd(n, 1ull);
-      const unsigned long long w = work[y];
-      keys[k] = 0xFFFFFFFFu - (uint32_t) (w < 0xFFFFFFFFull ? w : 0xFFFFFFFFull);
-      ids[k] = y;
-    }
-}
-
-// One block per hub y (heaviest first): N+(y) is staged in shared memory
-// with a hash set and Bloom bits; warps take the x's pointing at y, their
-// lanes walk the part of x's rank-ordered row after y (coalesced; the rest
-// is ranked below y and cannot lie in N+(y)) and probe N+(y).  A hit w closes the
-// triangle {x, y, w}, counted at its middle id: y and w in shared counters
-// (flushed once per hub), x through a warp sum per x.  (A flattened walk
-// over chunks of x's, which fills the lanes better for short N+(x), measured
-// slower: its staging and barriers cost more than the idle lanes.)
-template <uint32_t CAP, int THREADS, int G>
-__global__ void __launch_bounds__(THREADS)
-k_tc_hub(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ colr, const uint32_t* __restrict__ hubs, uint32_t nhubs, const uint32_t* __restrict__ hub_ptr,
-         const uint32_t* __restrict__ hub_x, const uint32_t* __restrict__ hub_j, unsigned int* next, uint32_t* ntri)
-{
-  __shared__ uint32_t L[CAP], Cn[CAP], key[2 * CAP];
-  __shared__ uint16_t idx[2 * CAP];
-  __shared__ uint32_t bloom[kBloomBits / 32];
-  __shared__ uint32_t s_k, s_y;
-  const int lane = threadIdx.x & 31;
-  for (uint32_t i = threadIdx.x; i < kBloomBits / 32; i += THREADS) bloom[i] = 0;
-  for (;;)
-  {
-    if (threadIdx.x == 0) s_k = atomicAdd(next, 1u);
-    __syncthreads();
-    const uint32_t k = s_k;
-    if (k >= nhubs) break;
-    const uint32_t y = hubs[k];
-    const uint32_t yb = ptr[y], d = ptr[y + 1] - yb;
-    const int lg = tc_lg(d);
-    const uint32_t mask = (1u << lg) - 1;
-    for (uint32_t i = threadIdx.x; i < (1u << lg); i += THREADS) key[i] = kEmpty;
-    if (threadIdx.x == 0) s_y = 0;
-    __syncthreads();
-    for (uint32_t j = threadIdx.x; j < d; j += THREADS)
-    {
-      const uint32_t w = colr[yb + j];  // set order is free: read the rows the walks read
-      L[j] = w;
-      Cn[j] = 0;
-      tc_insert_t(key, idx, lg, w, j);
-      const uint32_t bb = tc_bloom(w);
-      atomicOr(&bloom[bb >> 5], 1u << (bb & 31));
-    }
-    __syncthreads();
-    const uint32_t h0 = hub_ptr[y], h1 = hub_ptr[y + 1];
-    // G lanes per pair (THREADS / G pairs at a time): the walked suffixes are
-    // short, so whole warps per pair left most lanes idle
-    const int gl = lane % G;
-    const unsigned gmask = (G == 32 ? 0xffffffffu : ((1u << G) - 1) << (lane - gl));
-    for (uint32_t h = h0 + threadIdx.x / G; h < h1; h += THREADS / G)
-    {
-      const uint32_t x = hub_x[h];
-      const uint32_t j1 = hub_j[h] + 1;
-      const uint32_t xb = ptr[x] + j1, xd = ptr[x + 1] - xb;
-      const uint32_t mn = min(x, y), mx = max(x, y);
-      uint32_t cnt_x = 0, cnt_y = 0;
-      for (uint32_t r0 = gl; r0 < xd; r0 += 4 * G)
-      {
-        uint32_t wv[4];
-#pragma unroll
-        for (int u = 0; u < 4; u++) wv[u] = r0 + u * G < xd ? colr[xb + r0 + u * G] : kEmpty;
-#pragma unroll
-        for (int u = 0; u < 4; u++)
-        {
-          const uint32_t w = wv[u];
-          if (w == kEmpty) continue;
-          const uint32_t bb = tc_bloom(w);
-          if (!((bloom[bb >> 5] >> (bb & 31)) & 1u)) continue;
-          uint32_t sl = tc_slot(w, lg);
-          for (;;)
-          {
-            const uint32_t kk = key[sl];
-            if (kk == w)
-            {
-              const uint32_t mid = w < mn ? mn : (w > mx ? mx : w);
-              if (mid == x) cnt_x++;
-              else if (mid == y) cnt_y++;
-              else atomicAdd(&Cn[idx[sl]], 1u);
-              break;
-            }
-            if (kk == kEmpty) break;
-            sl = (sl + 1) & mask;
-          }
-        }
-      }
-      for (int o = G / 2; o > 0; o >>= 1)
-      {
-        cnt_x += __shfl_xor_sync(gmask, cnt_x, o);
-        cnt_y += __shfl_xor_sync(gmask, cnt_y, o);
-      }
-      if (gl == 0)
-      {
-        if (cnt_x) atomicAdd(&ntri[x], cnt_x);
-        if (cnt_y) atomicAdd(&s_y, cnt_y);
-      }
-    }
-    __syncthreads();
-    for (uint32_t j = threadIdx.x; j < d; j += THREADS)
-    {
-      if (Cn[j]) atomicAdd(&ntri[L[j]], Cn[j]);
-      const uint32_t bb = tc_bloom(L[j]);
-      bloom[bb >> 5] = 0;
-    }
-    if (threadIdx.x == 0 && s_y) atomicAdd(&ntri[y], s_y);
-    __syncthreads();
-  }
-}
-
-template <uint32_t CAP, int WARPS>
+// Warp tasks: |N+(y)| <= kTcWarpCap, a table per warp in static shared
+// memory (indices fit a byte).
+template <int WARPS>
 __global__ void __launch_bounds__(WARPS * 32)
-k_tc_rank_flat(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ order,
-          uint32_t norder, unsigned int* next, uint32_t* ntri)
+k_tc_count_warp(const uint32_t* __restrict__ pptr, const uint32_t* __restrict__ pcol, const uint2* __restrict__ pairs,
+                const uint32_t* __restrict__ mptr, const uint2* __restrict__ tasks,
+                const unsigned long long* __restrict__ ntasks_packed, const uint32_t* __restrict__ id_of_rank,
+                uint32_t* ntri, unsigned long long* ctr)
 {
-  __shared__ uint32_t s_list[WARPS][CAP];
-  __shared__ uint32_t s_off[WARPS][CAP + 1];
-  __shared__ uint32_t s_cnt[WARPS][CAP];
-  __shared__ uint32_t s_x[WARPS];
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  uint32_t* L = s_list[wib];
-  uint32_t* O = s_off[wib];
-  uint32_t* Cn = s_cnt[wib];
+  constexpr int kBloomWords = (1 << kTcWarpBloomBits) / 32;
+  __shared__ uint32_t s_key[WARPS][kTcWarpSlots];
+  __shared__ uint8_t s_idx[WARPS][kTcWarpSlots];
+  __shared__ uint32_t s_lid[WARPS][kTcWarpCap];
+  __shared__ uint32_t s_cn[WARPS][kTcWarpCap];
+  __shared__ uint32_t s_bloom[WARPS][kBloomWords];
+  __shared__ TcBatch s_b[WARPS];
+  const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
+  uint32_t* key = s_key[wi];
+  uint8_t* idx = s_idx[wi];
+  uint32_t* lid = s_lid[wi];
+  uint32_t* cn = s_cn[wi];
+  uint32_t* bloom = s_bloom[wi];
+  const uint32_t ntasks = (uint32_t) *ntasks_packed;
+  unsigned long long walked = 0, built = 0;
   for (;;)
   {
-    uint32_t k = 0;
-    if (lane == 0) k = atomicAdd(next, 1u);
-    k = __shfl_sync(0xffffffffu, k, 0);
-    if (k >= norder) break;
-    const uint32_t x = order[k];
-    const uint32_t xb = ptr[x], d = ptr[x + 1] - xb;
-    // stage N+(x), the work offsets (min(|N+(y)|, d) per y) and zeroed counters
-    uint32_t base = 0;
-    for (uint32_t j0 = 0; j0 < d; j0 += 32)
-    {
-      const uint32_t j = j0 + lane;
-      uint32_t len = 0;
-      if (j < d)
-      {
-        const uint32_t y = col[xb + j];
-        const uint32_t ylen = ptr[y + 1] - ptr[y];
-        // pairs with a hub list are walked by k_tc_hub instead
-        len = tc_is_hub_pair(d, ylen) ? 0u : min(ylen, d);
-        L[j] = y;
-        Cn[j] = 0;
-      }
-      uint32_t incl = len;
-      for (int o = 1; o < 32; o <<= 1)
-      {
-        uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += t;
-      }
-      if (j < d) O[j] = base + incl - len;
-      base += __shfl_sync(0xffffffffu, incl, 31);
-    }
-    if (lane == 0)
-    {
-      O[d] = base;
-      s_x[wib] = 0;
-    }
+    uint32_t t = 0;
+    if (lane == 0) t = (uint32_t) atomicAdd(&ctr[0], 1ull);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= ntasks) break;
+    const uint2 tk = tasks[t];
+    const uint32_t y = tk.x, p0 = tk.y, p1 = min(p0 + kTcWarpPairs, mptr[y + 1]);
+    const uint32_t yb = pptr[y], d = pptr[y + 1] - yb;
+    if (d == 0 || d > kTcWarpCap) continue;  // not a warp task (never built so)
+    const int lg = tc_lg(d);
+    for (uint32_t i = lane; i < (1u << lg); i += 32) key[i] = kEmpty;
+    for (uint32_t i = lane; i < kBloomWords; i += 32) bloom[i] = 0;
     __syncwarp();
-    const uint32_t total = base;
-    for (uint32_t t0 = 0; t0 < total; t0 += 32)
-    {
-      const uint32_t t = t0 + lane;
-      if (t < total)
-      {
-        // y-index: the last j with O[j] <= t
-        uint32_t lo = 0, hi = d;
-        while (hi - lo > 1)
-        {
-          uint32_t mid = (lo + hi) >> 1;
-          if (O[mid] <= t) lo = mid;
-          else hi = mid;
-        }
-        const uint32_t jy = lo;
-        const uint32_t y = L[jy];
-        const uint32_t yb = ptr[y], ylen = ptr[y + 1] - yb;
-        const uint32_t r = t - O[jy];
-        uint32_t w, pw;
-        bool hit;
-        if (ylen <= d)
-        {
-          w = col[yb + r];
-          pw = lower_bound_s(L, d, w);
-          hit = pw < d && L[pw] == w;
-        }
-        else
-        {
-          pw = r;
-          w = L[r];
-          uint32_t a = yb, c = yb + ylen;
-          while (a < c)
-          {
-            uint32_t mid = (a + c) >> 1;
-            if (col[mid] < w) a = mid + 1;
-            else c = mid;
-          }
-          hit = a < yb + ylen && col[a] == w;
-        }
-        if (hit)
-        {
-          const uint32_t mn = min(x, y), mx = max(x, y);
-          if (w < mn) { if (mn == x) atomicAdd(&s_x[wib], 1u); else atomicAdd(&Cn[jy], 1u); }
-          else if (w > mx) { if (mx == x) atomicAdd(&s_x[wib], 1u); else atomicAdd(&Cn[jy], 1u); }
-          else atomicAdd(&Cn[pw], 1u);
-        }
-      }
-    }
+    tc_build<uint8_t>(pcol + yb, d, lg, kTcWarpBloomBits, id_of_rank, key, idx, bloom, lid, cn, lane, 32);
+    __syncwarp();
+    built += d;
+    const TcTable<uint8_t> T{key, idx, bloom, (1u << lg) - 1, lg, kTcWarpBloomBits, nullptr, d};
+    const uint32_t yid = id_of_rank[y];
+    uint32_t cy = 0;
+    tc_walk_pairs(p0, p1, pairs, pptr, pcol, id_of_rank, yid, T, lid, cn, s_b[wi], cy, walked, ntri, ctr + 5);
+    for (int o = 16; o > 0; o >>= 1) cy += __shfl_xor_sync(0xffffffffu, cy, o);
+    if (lane == 0 && cy) atomicAdd(&ntri[yid], cy);
     __syncwarp();
     for (uint32_t j = lane; j < d; j += 32)
-      if (Cn[j]) atomicAdd(&ntri[L[j]], Cn[j]);
-    if (lane == 0 && s_x[wib]) atomicAdd(&ntri[x], s_x[wib]);
+      if (cn[j]) atomicAdd(&ntri[lid[j]], cn[j]);
     __syncwarp();
   }
+  if (lane == 0)
+  {
+    atomicAdd(&ctr[2], walked);
+    atomicAdd(&ctr[3], built);
+  }
 }
 
-// Heavy vertices (kTcSmall < |N+(x)| <= kTcCap): a whole block per x, its
-// threads in groups of G lanes.
-template <uint32_t CAP, int THREADS, int G>
+// Block tasks: |N+(y)| > kTcWarpCap; one table per block in dynamic shared
+// memory, or a global binary search above kTcBlockCap.  The per-warp batch
+// state stays in static shared memory.
+template <int THREADS>
 __global__ void __launch_bounds__(THREADS)
-k_tc_rank_block(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ order,
-                uint32_t norder, unsigned int* next, uint32_t* ntri, uint32_t walk_factor)
+k_tc_count_block(const uint32_t* __restrict__ pptr, const uint32_t* __restrict__ pcol, const uint2* __restrict__ pairs,
+                 const uint32_t* __restrict__ mptr, const uint2* __restrict__ tasks,
+                 const unsigned long long* __restrict__ ntasks_packed, const uint32_t* __restrict__ id_of_rank,
+                 uint32_t* ntri, unsigned long long* ctr)
 {
-  __shared__ uint32_t L[CAP], Cn[CAP], key[2 * CAP];
-  __shared__ uint16_t idx[2 * CAP];
-  __shared__ uint32_t bloom[kBloomBits / 32];
-  __shared__ uint32_t s_k, s_x;
-  for (uint32_t i = threadIdx.x; i < kBloomBits / 32; i += THREADS) bloom[i] = 0;
+  constexpr int WARPS = THREADS / 32;
+  constexpr int kBloomWords = (1 << kTcBlockBloomBits) / 32;
+  extern __shared__ __align__(16) uint32_t tc_smem[];
+  uint32_t* key = tc_smem;                          // [kTcBlockSlots]
+  uint32_t* lid = key + kTcBlockSlots;              // [kTcBlockCap]
+  uint32_t* cn = lid + kTcBlockCap;                 // [kTcBlockCap]
+  uint32_t* bloom = cn + kTcBlockCap;               // [kBloomWords]
+  uint16_t* idx = (uint16_t*) (bloom + kBloomWords);  // [kTcBlockSlots]
+  __shared__ TcBatch s_b[WARPS];
+  __shared__ uint32_t s_t, s_cy;
+  const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
+  const uint32_t ntasks = (uint32_t) (*ntasks_packed >> 32);
+  unsigned long long walked = 0, built = 0;
   for (;;)
   {
-    if (threadIdx.x == 0) s_k = atomicAdd(next, 1u);
-    __syncthreads();
-    const uint32_t k = s_k;
-    if (k >= norder) break;
-    const uint32_t x = order[k];
-    const uint32_t xb = ptr[x], d = ptr[x + 1] - xb;
-    const int lg = tc_lg(d);
-    for (uint32_t i = threadIdx.x; i < (1u << lg); i += THREADS) key[i] = kEmpty;
-    if (threadIdx.x == 0) s_x = 0;
-    __syncthreads();
-    for (uint32_t j = threadIdx.x; j < d; j += THREADS)
+    if (threadIdx.x == 0)
     {
-      const uint32_t y = col[xb + j];
-      L[j] = y;
-      Cn[j] = 0;
-      tc_insert_t(key, idx, lg, y, j);
-      const uint32_t bb = tc_bloom(y);
-      atomicOr(&bloom[bb >> 5], 1u << (bb & 31));
+      s_t = (uint32_t) atomicAdd(&ctr[1], 1ull);
+      s_cy = 0;
     }
     __syncthreads();
-    tc_walk<G>(x, d, L, Cn, key, idx, lg, &s_x, ptr, col, walk_factor, threadIdx.x / G, THREADS / G, threadIdx.x % G,
-               bloom);
-    __syncthreads();
-    for (uint32_t j = threadIdx.x; j < d; j += THREADS)
+    const uint32_t t = s_t;
+    if (t >= ntasks) break;
+    const uint2 tk = tasks[t];
+    const uint32_t y = tk.x, p0 = tk.y, p1 = min(p0 + kTcBlockPairs, mptr[y + 1]);
+    const uint32_t yb = pptr[y], d = pptr[y + 1] - yb;
+    const bool search = d > kTcBlockCap;
+    const int lg = search ? 5 : tc_lg(d);
+    if (!search)
     {
-      if (Cn[j]) atomicAdd(&ntri[L[j]], Cn[j]);
-      const uint32_t bb = tc_bloom(L[j]);
-      bloom[bb >> 5] = 0;  // clears the words this x set (others are zero already)
+      for (uint32_t i = threadIdx.x; i < (1u << lg); i += THREADS) key[i] = kEmpty;
+      for (uint32_t i = threadIdx.x; i < kBloomWords; i += THREADS) bloom[i] = 0;
+      __syncthreads();
+      tc_build<uint16_t>(pcol + yb, d, lg, kTcBlockBloomBits, id_of_rank, key, idx, bloom, lid, cn, threadIdx.x,
+                         THREADS);
+      if (threadIdx.x == 0) built += d;
     }
-    if (threadIdx.x == 0 && s_x) atomicAdd(&ntri[x], s_x);
+    __syncthreads();
+    const TcTable<uint16_t> T{key, idx, search ? nullptr : bloom, (1u << lg) - 1, lg, kTcBlockBloomBits,
+                              search ? pcol + yb : nullptr, d};
+    const uint32_t yid = id_of_rank[y];
+    uint32_t cy = 0;
+    // the warps take 32-pair rounds of the slice in turn
+    for (uint32_t q = p0 + 32u * wi; q < p1; q += 32u * WARPS)
+      tc_walk_pairs(q, min(q + 32u, p1), pairs, pptr, pcol, id_of_rank, yid, T, search ? nullptr : lid,
+                    search ? nullptr : cn, s_b[wi], cy, walked, ntri, ctr + 5);
+    for (int o = 16; o > 0; o >>= 1) cy += __shfl_xor_sync(0xffffffffu, cy, o);
+    if (lane == 0 && cy) atomicAdd(&s_cy, cy);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_cy) atomicAdd(&ntri[yid], s_cy);
+    if (!search)
+      for (uint32_t j = threadIdx.x; j < d; j += THREADS)
+        if (cn[j]) atomicAdd(&ntri[lid[j]], cn[j]);
     __syncthreads();
   }
+  // every lane of a warp holds the warp's walked count
+  if (lane == 0 && walked) atomicAdd(&ctr[2], walked);
+  if (threadIdx.x == 0 && built) atomicAdd(&ctr[3], built);
 }
 
-// Vertices whose N+ exceeds kTcCap: one warp each, lists read from global
-// memory, every hit added with a global atomic.
-__global__ void __launch_bounds__(256)
-k_tc_rank_big(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ big,
-              uint32_t nbig, uint32_t* ntri)
-{
-  const int lane = threadIdx.x & 31;
-  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t k = warp; k < nbig; k += nwarps)
-  {
-    const uint32_t x = big[k];
-    const uint32_t xb = ptr[x], xe = ptr[x + 1];
-    for (uint32_t j = xb; j < xe; j++)
-    {
-      const uint32_t y = col[j];
-      const uint32_t mn = min(x, y), mx = max(x, y);
-      for (uint32_t i = ptr[y] + lane; i < ptr[y + 1]; i += 32)
-      {
-        const uint32_t w = col[i];
-        uint32_t lo = xb, hi = xe;
-        while (lo < hi)
-        {
-          uint32_t mid = (lo + hi) >> 1;
-          if (col[mid] < w) lo = mid + 1;
-          else hi = mid;
-        }
-        if (lo < xe && col[lo] == w) atomicAdd(&ntri[w < mn ? mn : (w > mx ? mx : w)], 1u);
-      }
-    }
-  }
-}
+static constexpr size_t kTcBlockSmem = (size_t) kTcBlockSlots * 4 + 2 * (size_t) kTcBlockCap * 4 +
+                                       (size_t) (1 << kTcBlockBloomBits) / 8 + (size_t) kTcBlockSlots * 2;
+static constexpr size_t kTcSortBigSmem = (size_t) kTcSortBlockCap * 4;
 
 __global__ void k_tc_sum(uint32_t N, const uint32_t* __restrict__ ntri, unsigned long long* total)
 {
@@ -705,159 +761,134 @@ __global__ void k_tc_sum(uint32_t N, const uint32_t* __restrict__ ntri, unsigned
   if ((threadIdx.x & 31) == 0 && s) atomicAdd(total, s);
 }
 
-static int tc_prepare(la3g_graph* G, TcScratch* ts)
+static int tc_scratch(la3g_graph* G, TcScratch** out)
+{
+  TcScratch* ts = (TcScratch*) G->slot[kSlotTc];
+  if (ts) { *out = ts; return LA3G_OK; }
+  ts = new (std::nothrow) TcScratch();
+  if (!ts) return set_error(LA3G_ENOMEM, "out of host memory");
+  G->slot[kSlotTc] = ts;
+  G->slot_free[kSlotTc] = tc_scratch_free;
+  const uint32_t N = G->g.nslots;
+  const uint64_t m = G->g.nent;
+  ts->N = N;
+  ts->m = m;
+  LA3G_TRY(galloc(G, &ts->deg, N));
+  LA3G_TRY(galloc(G, &ts->iota, N));
+  LA3G_TRY(galloc(G, &ts->deg_of_rank, N));
+  LA3G_TRY(galloc(G, &ts->pos_of_rank, N));
+  LA3G_TRY(galloc(G, &ts->rank_of_pos, N));
+  LA3G_TRY(galloc(G, &ts->id_of_rank, N));
+  LA3G_TRY(galloc(G, &ts->dplus, (size_t) N + 1));
+  LA3G_TRY(galloc(G, &ts->pptr, (size_t) N + 1));
+  LA3G_TRY(galloc(G, &ts->fill, N));
+  LA3G_TRY(galloc(G, &ts->pcol_raw, m + 1));
+  LA3G_TRY(galloc(G, &ts->pcol, m + 1));
+  LA3G_TRY(galloc(G, &ts->mcount, (size_t) N + 1));
+  LA3G_TRY(galloc(G, &ts->mptr, (size_t) N + 1));
+  LA3G_TRY(galloc(G, &ts->pairs, m + 1));
+  LA3G_TRY(galloc(G, &ts->tcount, (size_t) N + 1));
+  LA3G_TRY(galloc(G, &ts->toff, (size_t) N + 1));
+  LA3G_TRY(galloc(G, &ts->wtasks, m / kTcWarpPairs + N + 1));
+  LA3G_TRY(galloc(G, &ts->btasks, m / kTcBlockPairs + N + 1));
+  LA3G_TRY(galloc(G, &ts->ntri, N));
+  LA3G_TRY(galloc(G, &ts->big_rows, N));
+  LA3G_TRY(galloc(G, &ts->ctr, 8));
+  LA3G_CUDA(cudaHostAlloc(&ts->hctr, 8 * sizeof(unsigned long long), cudaHostAllocDefault));
+  // degrees are at most N - 1: the rank sort needs bit_width(N) key bits
+  ts->end_bit = 1;
+  while (ts->end_bit < 32 && ((uint64_t) N >> ts->end_bit) != 0) ts->end_bit++;
+  size_t a = 0, b = 0, c = 0;
+  LA3G_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, a, ts->deg, ts->deg_of_rank, ts->iota, ts->pos_of_rank, (int) N, 0,
+                                            ts->end_bit));
+  LA3G_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, b, ts->dplus, ts->pptr, (int) N + 1));
+  LA3G_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, c, ts->tcount, ts->toff, (int) N + 1));
+  ts->temp_bytes = std::max(a, std::max(b, c));
+  LA3G_TRY(galloc_bytes(G, &ts->temp, ts->temp_bytes));
+  *out = ts;
+  return LA3G_OK;
+}
+
+// Pass 1: the rank-ordered N+ rows and the per-y pair lists and tasks.
+// library_sort: sort the rows with the library's segmented sort (for rows
+// longer than kTcSortBlockCap, which this build's sort kernels leave).
+static int tc_lists(la3g_graph* G, TcScratch* ts, bool library_sort)
 {
   DevGraph& g = G->g;
   cudaStream_t s = G->stream;
-  const uint32_t N = g.nslots;
-  const uint64_t m = g.nent;
-  LA3G_TRY(galloc(G, &ts->plus_ptr, N + 1));
-  LA3G_TRY(galloc(G, &ts->plus_col, m + 1));
-  LA3G_TRY(galloc(G, &ts->ntri, N));
-  LA3G_TRY(galloc(G, &ts->total, 1));
-  LA3G_TRY(galloc(G, &ts->next, 4));
-  DevBuf deg, k1, k2, tmp, wkey, wid, wkey2, cnt;
-  LA3G_TRY(deg.alloc((size_t) N * 4));
-  LA3G_TRY(k1.alloc(m * 8 + 8));
-  LA3G_TRY(k2.alloc(m * 8 + 8));
-  k_tc_deg<<<grid_for(N, 256), 256, 0, s>>>(g.in_ptr, g.out_ptr, g.id_of_pos, N, deg.as<uint32_t>());
+  const uint32_t N = ts->N;
+  const uint64_t m = ts->m;
+  const unsigned eblocks = (unsigned) std::max<uint64_t>(1, (m + 256ull * kTcEdgesPerThread - 1) /
+                                                                (256ull * kTcEdgesPerThread));
+  size_t tb = ts->temp_bytes;
+  LA3G_CUDA(cudaMemsetAsync(ts->dplus, 0, ((size_t) N + 1) * 4, s));
+  LA3G_CUDA(cudaMemsetAsync(ts->fill, 0, (size_t) N * 4, s));
+  LA3G_CUDA(cudaMemsetAsync(ts->ctr, 0, 8 * sizeof(unsigned long long), s));
+  k_tc_deg<<<grid_for(N, 256), 256, 0, s>>>(g.in_ptr, g.out_ptr, N, ts->deg, ts->iota);
   LA3G_LAUNCHED();
+  LA3G_CUDA(cub::DeviceRadixSort::SortPairs(ts->temp, tb, ts->deg, ts->deg_of_rank, ts->iota, ts->pos_of_rank, (int) N,
+                                            0, ts->end_bit, s));
+  k_tc_ranks<<<grid_for(N, 256), 256, 0, s>>>(N, ts->pos_of_rank, g.id_of_pos, ts->rank_of_pos, ts->id_of_rank);
+  LA3G_LAUNCHED();
+  tls_launches += 2;
   if (m)
   {
-    k_tc_rank_edges<<<grid_for(N, 256), 256, 0, s>>>(g.out_ptr, g.out_row, N, g.id_of_pos, deg.as<uint32_t>(),
-                                                     k1.as<uint64_t>());
+    k_tc_orient<false><<<eblocks, 256, 0, s>>>(g.in_ptr, g.in_col, g.nrows(), m, ts->rank_of_pos, ts->dplus, nullptr,
+                                               nullptr);
     LA3G_LAUNCHED();
-    size_t tb = 0;
-    int end_bit = 33;
-    while (end_bit < 64 && ((uint64_t) N >> (end_bit - 32)) != 0) end_bit++;
-    LA3G_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, tb, k1.as<uint64_t>(), k2.as<uint64_t>(), m, 0, end_bit, s));
-    LA3G_TRY(tmp.alloc(tb));
-    LA3G_CUDA(cub::DeviceRadixSort::SortKeys(tmp.p, tb, k1.as<uint64_t>(), k2.as<uint64_t>(), m, 0, end_bit, s));
-    k_tc_split_keys<<<grid_for(m, 256), 256, 0, s>>>(k2.as<uint64_t>(), m, ts->plus_col);
-    LA3G_LAUNCHED();
-    // the same rows ordered by rank (degree, id), for the hub walks
-    DevBuf vk, vk2, rk, ir, k3, t3;
-    LA3G_TRY(vk.alloc((size_t) N * 8));
-    LA3G_TRY(vk2.alloc((size_t) N * 8));
-    LA3G_TRY(rk.alloc((size_t) N * 4));
-    LA3G_TRY(ir.alloc((size_t) N * 4));
-    LA3G_TRY(k3.alloc(m * 8 + 8));
-    k_tc_vkeys<<<grid_for(N, 256), 256, 0, s>>>(N, deg.as<uint32_t>(), vk.as<uint64_t>());
-    LA3G_LAUNCHED();
-    size_t tv = 0;
-    LA3G_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, tv, vk.as<uint64_t>(), vk2.as<uint64_t>(), N, 0, 64, s));
-    LA3G_TRY(t3.alloc(std::max(tv, tb)));
-    LA3G_CUDA(cub::DeviceRadixSort::SortKeys(t3.p, tv, vk.as<uint64_t>(), vk2.as<uint64_t>(), N, 0, 64, s));
-    k_tc_ranks<<<grid_for(N, 256), 256, 0, s>>>(N, vk2.as<uint64_t>(), rk.as<uint32_t>(), ir.as<uint32_t>());
-    LA3G_LAUNCHED();
-    k_tc_rank_keys<<<grid_for(m, 256), 256, 0, s>>>(k2.as<uint64_t>(), m, rk.as<uint32_t>(), k3.as<uint64_t>());
-    LA3G_LAUNCHED();
-    LA3G_CUDA(cub::DeviceRadixSort::SortKeys(t3.p, tb, k3.as<uint64_t>(), k1.as<uint64_t>(), m, 0, end_bit, s));
-    LA3G_TRY(galloc(G, &ts->plus_col_r, m + 1));
-    k_tc_rank_ids<<<grid_for(m, 256), 256, 0, s>>>(k1.as<uint64_t>(), m, ir.as<uint32_t>(), ts->plus_col_r);
-    LA3G_LAUNCHED();
-    LA3G_CUDA(cudaStreamSynchronize(s));
+    tls_launches++;
   }
-  else LA3G_TRY(galloc(G, &ts->plus_col_r, 1));
-  k_tc_rows<<<grid_for(m + 1, 256), 256, 0, s>>>(k2.as<uint64_t>(), m, N, ts->plus_ptr);
-  LA3G_LAUNCHED();
-  LA3G_TRY(wkey.alloc((size_t) N * 4));
-  LA3G_TRY(wid.alloc((size_t) N * 4));
-  LA3G_TRY(wkey2.alloc((size_t) N * 4));
-  LA3G_TRY(cnt.alloc(8 * 8));
-  LA3G_TRY(galloc(G, &ts->order, N));
-  LA3G_TRY(galloc(G, &ts->big, N));
-  LA3G_CUDA(cudaMemsetAsync(cnt.p, 0, 64, s));
-  k_tc_work<<<grid_for(N, 256), 256, 0, s>>>(ts->plus_ptr, ts->plus_col, N, wkey.as<uint32_t>(), wid.as<uint32_t>(),
-                                             ts->big, cnt.as<unsigned long long>());
-  LA3G_LAUNCHED();
-  unsigned long long hc[8];
-  LA3G_CUDA(cudaMemcpyAsync(hc, cnt.p, 64, cudaMemcpyDeviceToHost, s));
-  LA3G_CUDA(cudaStreamSynchronize(s));
-  ts->nmid = (uint32_t) hc[3];
-  ts->norder = (uint32_t) hc[0];  // small + mid, sorted: small first
-  ts->nbig = (uint32_t) hc[1];
-  ts->work = (double) hc[2];
-  ts->work_mid = (double) hc[4];
-  ts->work_big = (double) hc[5];
-  if (ts->norder)
+  tb = ts->temp_bytes;
+  LA3G_CUDA(cub::DeviceScan::ExclusiveSum(ts->temp, tb, ts->dplus, ts->pptr, (int) N + 1, s));
+  if (m)
   {
-    size_t tb = 0;
-    LA3G_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tb, wkey.as<uint32_t>(), wkey2.as<uint32_t>(), wid.as<uint32_t>(),
-                                              ts->order, ts->norder, 0, 32, s));
-    DevBuf t2;
-    LA3G_TRY(t2.alloc(tb));
-    LA3G_CUDA(cub::DeviceRadixSort::SortPairs(t2.p, tb, wkey.as<uint32_t>(), wkey2.as<uint32_t>(), wid.as<uint32_t>(),
-                                              ts->order, ts->norder, 0, 32, s));
+    k_tc_orient<true><<<eblocks, 256, 0, s>>>(g.in_ptr, g.in_col, g.nrows(), m, ts->rank_of_pos, ts->fill, ts->pptr,
+                                              ts->pcol_raw);
+    LA3G_LAUNCHED();
+    tls_launches++;
+    if (library_sort)
+    {
+      if (!ts->seg_temp)
+      {
+        LA3G_CUDA(cub::DeviceSegmentedSort::SortKeys(nullptr, ts->seg_bytes, ts->pcol_raw, ts->pcol, (int64_t) m,
+                                                     (int64_t) N, ts->pptr, ts->pptr + 1, s));
+        LA3G_TRY(galloc_bytes(G, &ts->seg_temp, ts->seg_bytes));
+      }
+      tb = ts->seg_bytes;
+      LA3G_CUDA(cub::DeviceSegmentedSort::SortKeys(ts->seg_temp, tb, ts->pcol_raw, ts->pcol, (int64_t) m, (int64_t) N,
+                                                   ts->pptr, ts->pptr + 1, s));
+    }
+    else
+    {
+      k_tc_sort_rows<8><<<kSMs * 8, 256, 0, s>>>(ts->pptr, N, ts->pcol_raw, ts->pcol, ts->big_rows, ts->ctr + 6);
+      LA3G_LAUNCHED();
+      k_tc_sort_big<<<kSMs, 1024, kTcSortBigSmem, s>>>(ts->pptr, ts->pcol_raw, ts->pcol, ts->big_rows, ts->ctr + 6,
+                                                       ts->ctr + 7);
+      LA3G_LAUNCHED();
+      tls_launches += 2;
+    }
   }
-  LA3G_CUDA(cudaStreamSynchronize(s));
-  ts->order_mid = ts->order + (ts->norder - ts->nmid);
-  ts->norder -= ts->nmid;
-
-  // hub-centric pairs (small x, moderate hub y): CSR by y, hubs heaviest first
-  DevBuf hcnt, hwork, hkeys, hkeys2, hids, hn;
-  LA3G_TRY(hcnt.alloc((size_t) (N + 1) * 4));
-  LA3G_TRY(hwork.alloc((size_t) N * 8));
-  LA3G_CUDA(cudaMemsetAsync(hcnt.p, 0, (size_t) (N + 1) * 4, s));
-  LA3G_CUDA(cudaMemsetAsync(hwork.p, 0, (size_t) N * 8, s));
-  k_tc_hub_count<<<grid_for(N, 256), 256, 0, s>>>(ts->plus_ptr, ts->plus_col_r, N, hcnt.as<uint32_t>(),
-                                                  hwork.as<unsigned long long>());
+  k_tc_pair_counts<<<grid_for((uint64_t) N + 1, 256), 256, 0, s>>>(N, ts->pptr, ts->deg_of_rank, ts->mcount,
+                                                                   ts->tcount);
   LA3G_LAUNCHED();
-  LA3G_TRY(galloc(G, &ts->hub_ptr, N + 1));
+  tls_launches++;
+  tb = ts->temp_bytes;
+  LA3G_CUDA(cub::DeviceScan::ExclusiveSum(ts->temp, tb, ts->mcount, ts->mptr, (int) N + 1, s));
+  tb = ts->temp_bytes;
+  LA3G_CUDA(cub::DeviceScan::ExclusiveSum(ts->temp, tb, ts->tcount, ts->toff, (int) N + 1, s));
+  if (m)
   {
-    size_t tb = 0;
-    LA3G_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tb, hcnt.as<uint32_t>(), ts->hub_ptr, N + 1, s));
-    DevBuf t;
-    LA3G_TRY(t.alloc(tb));
-    LA3G_CUDA(cub::DeviceScan::ExclusiveSum(t.p, tb, hcnt.as<uint32_t>(), ts->hub_ptr, N + 1, s));
+    LA3G_CUDA(cudaMemsetAsync(ts->fill, 0, (size_t) N * 4, s));
+    const uint64_t m8 = (m + kTcEdgesPerThread - 1) / kTcEdgesPerThread * kTcEdgesPerThread;
+    const unsigned pblocks = (unsigned) ((m8 + m + 256ull * kTcEdgesPerThread - 1) / (256ull * kTcEdgesPerThread));
+    k_tc_pairs<<<pblocks, 256, 0, s>>>(g.in_ptr, g.in_col, g.out_ptr, g.out_row, g.nrows(), N, m, ts->rank_of_pos,
+                                       ts->pptr, ts->pcol, ts->mptr, ts->fill, ts->pairs);
+    LA3G_LAUNCHED();
+    tls_launches++;
   }
-  uint32_t npairs = 0;
-  LA3G_CUDA(cudaMemcpyAsync(&npairs, ts->hub_ptr + N, 4, cudaMemcpyDeviceToHost, s));
-  LA3G_CUDA(cudaStreamSynchronize(s));
-  LA3G_TRY(galloc(G, &ts->hub_x, std::max<uint32_t>(npairs, 1)));
-  LA3G_TRY(galloc(G, &ts->hub_j, std::max<uint32_t>(npairs, 1)));
-  ts->hub_pairs = npairs;
-  LA3G_TRY(galloc(G, &ts->hubs, N));
-  if (npairs)
-  {
-    DevBuf fill;
-    LA3G_TRY(fill.alloc((size_t) N * 4));
-    LA3G_CUDA(cudaMemsetAsync(fill.p, 0, (size_t) N * 4, s));
-    k_tc_hub_fill<<<grid_for(N, 256), 256, 0, s>>>(ts->plus_ptr, ts->plus_col_r, N, ts->hub_ptr, fill.as<uint32_t>(),
-                                                   ts->hub_x, ts->hub_j);
-    LA3G_LAUNCHED();
-    LA3G_TRY(hkeys.alloc((size_t) N * 4));
-    LA3G_TRY(hkeys2.alloc((size_t) N * 4));
-    LA3G_TRY(hids.alloc((size_t) N * 4));
-    LA3G_TRY(hn.alloc(8));
-    LA3G_CUDA(cudaMemsetAsync(hn.p, 0, 8, s));
-    k_tc_hub_keys<<<grid_for(N, 256), 256, 0, s>>>(N, hcnt.as<uint32_t>(), hwork.as<unsigned long long>(),
-                                                   hkeys.as<uint32_t>(), hids.as<uint32_t>(),
-                                                   hn.as<unsigned long long>());
-    LA3G_LAUNCHED();
-    DevBuf hsum;
-    LA3G_TRY(hsum.alloc(16));
-    LA3G_CUDA(cudaMemsetAsync(hsum.p, 0, 16, s));
-    k_tc_hub_sums<<<grid_for(N, 256), 256, 0, s>>>(ts->plus_ptr, N, hcnt.as<uint32_t>(), hwork.as<unsigned long long>(),
-                                                   hsum.as<unsigned long long>());
-    LA3G_LAUNCHED();
-    unsigned long long hs[2] = {0, 0};
-    LA3G_CUDA(cudaMemcpyAsync(hs, hsum.p, 16, cudaMemcpyDeviceToHost, s));
-    unsigned long long nh = 0;
-    LA3G_CUDA(cudaMemcpyAsync(&nh, hn.p, 8, cudaMemcpyDeviceToHost, s));
-    LA3G_CUDA(cudaStreamSynchronize(s));
-    ts->nhubs = (uint32_t) nh;
-    ts->hub_items = (double) hs[0];
-    ts->hub_lists = (double) hs[1];
-    size_t tb = 0;
-    LA3G_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tb, hkeys.as<uint32_t>(), hkeys2.as<uint32_t>(),
-                                              hids.as<uint32_t>(), ts->hubs, ts->nhubs, 0, 32, s));
-    DevBuf t;
-    LA3G_TRY(t.alloc(tb));
-    LA3G_CUDA(cub::DeviceRadixSort::SortPairs(t.p, tb, hkeys.as<uint32_t>(), hkeys2.as<uint32_t>(),
-                                              hids.as<uint32_t>(), ts->hubs, ts->nhubs, 0, 32, s));
-  }
-  LA3G_CUDA(cudaStreamSynchronize(s));
+  k_tc_tasks<<<grid_for(N, 256), 256, 0, s>>>(N, ts->toff, ts->mptr, ts->wtasks, ts->btasks);
+  LA3G_LAUNCHED();
+  tls_launches++;
   return LA3G_OK;
 }
 
@@ -871,70 +902,71 @@ extern "C" int la3g_tc(la3g_graph* G, uint64_t* total_out, uint32_t* per_vertex_
   DevGraph& g = G->g;
   if ((g.flags & (LA3G_DIRECTED | LA3G_ACYCLIC | LA3G_REVERSE | LA3G_BIPARTITE)) != (LA3G_DIRECTED | LA3G_ACYCLIC))
     return set_error(LA3G_EINVAL, "tc needs a graph loaded with LA3G_DIRECTED | LA3G_ACYCLIC");
+  if (g.nent >= 0xFFFFFFFFull) return set_error(LA3G_EINVAL, "tc: more than 2^32 - 2 edges");
   CallTimer T(G, st);
   LA3G_TRY(build_push_csr(G));
-  TcScratch* ts = (TcScratch*) G->slot[kSlotTc];
-  if (!ts)
+  TcScratch* ts = nullptr;
+  LA3G_TRY(tc_scratch(G, &ts));
+  static bool smem_set = false;  // the opt-ins are per function and device; idempotent
+  if (!smem_set)
   {
-    ts = new (std::nothrow) TcScratch();
-    if (!ts) return set_error(LA3G_ENOMEM, "out of host memory");
-    G->slot[kSlotTc] = ts;
-    G->slot_free[kSlotTc] = tc_scratch_free;
-    LA3G_TRY(tc_prepare(G, ts));
+    LA3G_CUDA(cudaFuncSetAttribute(k_tc_count_block<kTcBlockThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int) kTcBlockSmem));
+    LA3G_CUDA(cudaFuncSetAttribute(k_tc_sort_big, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) kTcSortBigSmem));
+    smem_set = true;
   }
   cudaStream_t s = G->stream;
   const uint32_t N = g.nslots;
-  T.device_begin();
-  LA3G_CUDA(cudaMemsetAsync(ts->ntri, 0, (size_t) N * 4, s));
-  LA3G_CUDA(cudaMemsetAsync(ts->total, 0, 8, s));
-  LA3G_CUDA(cudaMemsetAsync(ts->next, 0, 16, s));
-  if (ts->nmid)
+  const double m = (double) g.nent;
+  // rows longer than the block sort's capacity (none on R-MAT up to scale
+  // 24): the whole call runs again with the library's segmented sort
+  for (int attempt = 0; attempt < 2; attempt++)
   {
-    // list reads (N+(x) once, N+(y) per oriented edge) + the x's two offsets
-    ProfileScope p("tc_rank_mid", s, 4.0 * ts->work_mid + 8.0 * ts->nmid);
-    k_tc_rank_block<kTcCap, 256, 32><<<kSMs * 8, 256, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->order_mid, ts->nmid,
-                                                              ts->next + 1, ts->ntri, kTcWalkFactor);
-    LA3G_LAUNCHED();
-  }
-  if (ts->norder)
-  {
-    ProfileScope p("tc_rank", s, 4.0 * (ts->work - ts->work_mid - ts->work_big) + 8.0 * ts->norder);
-    // short lists: the flattened walk keeps all 32 lanes busy across the y's
-    k_tc_rank_flat<kTcSmall, 8><<<kSMs * 8, 8 * 32, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->order, ts->norder, ts->next,
-                                                            ts->ntri);
-    LA3G_LAUNCHED();
-  }
-  if (ts->nhubs)
-  {
-    // the walked part of N+(x) of every hub pair + each hub's N+(y) once + the
-    // pair's x, index and two offsets
-    ProfileScope p("tc_hub", s, 4.0 * ts->hub_items + 4.0 * ts->hub_lists + 16.0 * (double) ts->hub_pairs);
-    k_tc_hub<kTcHubCap, 256, kTcHubLanes><<<kSMs * 6, 256, 0, s>>>(ts->plus_ptr, ts->plus_col_r, ts->hubs, ts->nhubs,
-                                                      ts->hub_ptr, ts->hub_x, ts->hub_j, ts->next + 2, ts->ntri);
-    LA3G_LAUNCHED();
-  }
-  if (ts->nbig)
-  {
-    k_tc_rank_big<<<grid_for((uint64_t) ts->nbig * 32, 256), 256, 0, s>>>(ts->plus_ptr, ts->plus_col, ts->big, ts->nbig,
-                                                                           ts->ntri);
+    T.device_begin();
+    {
+      // pass 1: degrees, ranks, N+ rows (count, fill, sort), pair lists,
+      // tasks; compulsory bytes: the edge list read by the count and fill
+      // passes, the rows written, sorted (read + write), the adjacency read
+      // once more for the pair lists (8 B per pair), plus the per-vertex
+      // arrays (about 48 B per vertex)
+      ProfileScope p("tc_lists", s, 4.0 * m + 8.0 * m + 8.0 * m + 8.0 * m + 8.0 * m + 48.0 * N);
+      LA3G_TRY(tc_lists(G, ts, attempt == 1));
+    }
+    LA3G_CUDA(cudaMemsetAsync(ts->ntri, 0, (size_t) N * 4, s));
+    {
+      // pass 2; its bytes (walked list elements, pairs, tables) are added below
+      ProfileScope p("tc_count", s, 0.0);
+      k_tc_count_warp<kTcWarpKernelWarps><<<kSMs * 4, kTcWarpKernelWarps * 32, 0, s>>>(
+          ts->pptr, ts->pcol, ts->pairs, ts->mptr, ts->wtasks, ts->toff + N, ts->id_of_rank, ts->ntri, ts->ctr);
+      LA3G_LAUNCHED();
+      k_tc_count_block<kTcBlockThreads><<<kSMs * 2, kTcBlockThreads, kTcBlockSmem, s>>>(
+          ts->pptr, ts->pcol, ts->pairs, ts->mptr, ts->btasks, ts->toff + N, ts->id_of_rank, ts->ntri, ts->ctr);
+      LA3G_LAUNCHED();
+      tls_launches++;
+    }
+    k_tc_sum<<<grid_for(N, 256), 256, 0, s>>>(N, ts->ntri, ts->ctr + 4);
     LA3G_LAUNCHED();
     tls_launches++;
+    T.device_end();
+    LA3G_CUDA(cudaMemcpyAsync(ts->hctr, ts->ctr, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    LA3G_CUDA(cudaStreamSynchronize(s));
+    if (ts->hctr[5]) return set_error(LA3G_ECUDA, "tc: %llu internal consistency checks failed",
+                                      (unsigned long long) ts->hctr[5]);
+    if (!ts->hctr[7]) break;
   }
-  k_tc_sum<<<grid_for(N, 256), 256, 0, s>>>(N, ts->ntri, ts->total);
-  LA3G_LAUNCHED();
-  tls_launches++;
-  T.device_end();
-  unsigned long long total = 0;
-  LA3G_CUDA(cudaMemcpyAsync(&total, ts->total, 8, cudaMemcpyDeviceToHost, s));
   if (per_vertex_out) LA3G_CUDA(cudaMemcpyAsync(per_vertex_out, ts->ntri, (size_t) N * 4, cudaMemcpyDeviceToHost, s));
   LA3G_TRY(T.finish());
-  if (total_out) *total_out = total;
+  const double walked = (double) ts->hctr[2], built = (double) ts->hctr[3];
+  // walked suffix elements (4 B), each pair's entry, row end and x id (16 B),
+  // each table's row and its ids (8 B per element)
+  profile_add_bytes("tc_count", 4.0 * walked + 16.0 * m + 8.0 * built);
+  if (total_out) *total_out = ts->hctr[4];
   if (st)
   {
     st->iterations = 2;
     st->teps_edges = g.nent;
-    st->edges_examined = (uint64_t) ts->work;
-    st->algo_bytes = (uint64_t) (4.0 * ts->work + 8.0 * N);
+    st->edges_examined = (uint64_t) walked;
+    st->algo_bytes = (uint64_t) (4.0 * walked + 16.0 * m + 8.0 * built + 36.0 * m + 48.0 * N);
   }
   return LA3G_OK;
 }
