@@ -56,6 +56,7 @@ struct BfsScratch
   FrontierCounters* ctr = nullptr;      // device
   FrontierCounters* hctr = nullptr;     // pinned host mirror
   unsigned long long* red = nullptr;  // reduction scratch
+  uint32_t* by_id = nullptr;          // [nslots] outputs reordered by id before they leave the device
   uint32_t words = 0;
 };
 
@@ -394,6 +395,7 @@ static int bfs_scratch(la3g_graph* G, BfsScratch** out)
   LA3G_TRY(galloc(G, &bs->bits[1], bs->words));
   LA3G_TRY(galloc(G, &bs->ctr, 1));
   LA3G_TRY(galloc(G, &bs->red, 1));
+  LA3G_TRY(galloc(G, &bs->by_id, N));
   LA3G_CUDA(cudaHostAlloc(&bs->hctr, sizeof(FrontierCounters), cudaHostAllocDefault));
   *out = bs;
   return LA3G_OK;
@@ -577,20 +579,19 @@ extern "C" int la3g_bfs(la3g_graph* G, uint32_t root, uint8_t* hops_out, uint32_
   }
   if (hops_out || parent_out)
   {
-    DevBuf tmp;
-    LA3G_TRY(tmp.alloc((size_t) N * 4));
+    // the graph's own reorder buffer: no allocation per call
     if (hops_out)
     {
-      k_by_id<uint8_t><<<grid_for(N, 256), 256, 0, s>>>(N, g.id_of_pos, bs->hops, tmp.as<uint8_t>());
+      k_by_id<uint8_t><<<grid_for(N, 256), 256, 0, s>>>(N, g.id_of_pos, bs->hops, (uint8_t*) bs->by_id);
       LA3G_LAUNCHED();
-      LA3G_CUDA(cudaMemcpyAsync(hops_out, tmp.p, N, cudaMemcpyDeviceToHost, s));
+      LA3G_CUDA(cudaMemcpyAsync(hops_out, bs->by_id, N, cudaMemcpyDeviceToHost, s));
       LA3G_CUDA(cudaStreamSynchronize(s));
     }
     if (parent_out)
     {
-      k_by_id<uint32_t><<<grid_for(N, 256), 256, 0, s>>>(N, g.id_of_pos, bs->parent, tmp.as<uint32_t>());
+      k_by_id<uint32_t><<<grid_for(N, 256), 256, 0, s>>>(N, g.id_of_pos, bs->parent, bs->by_id);
       LA3G_LAUNCHED();
-      LA3G_CUDA(cudaMemcpyAsync(parent_out, tmp.p, (size_t) N * 4, cudaMemcpyDeviceToHost, s));
+      LA3G_CUDA(cudaMemcpyAsync(parent_out, bs->by_id, (size_t) N * 4, cudaMemcpyDeviceToHost, s));
       LA3G_CUDA(cudaStreamSynchronize(s));
     }
   }

@@ -34,9 +34,16 @@ struct CcScratch
   uint32_t* msg = nullptr;
   uint8_t* active[2] = {nullptr, nullptr};
   int* flag = nullptr;
+  unsigned long long* walked = nullptr;  // [0] rows, [1] edges k_cc_rest walked
+  unsigned long long* hwalked = nullptr; // pinned mirror
 };
 
-static void cc_scratch_free(void* p) { delete (CcScratch*) p; }
+static void cc_scratch_free(void* p)
+{
+  CcScratch* s = (CcScratch*) p;
+  if (s->hwalked) cudaFreeHost(s->hwalked);
+  delete s;
+}
 
 __global__ void k_cc_init(uint32_t N, uint32_t* parent)
 {
@@ -89,18 +96,26 @@ __global__ void k_cc_sample(const uint32_t* __restrict__ ptr, const uint32_t* __
 // the giant component is seen from its other endpoint.  One warp per row.
 __global__ void __launch_bounds__(256)
 k_cc_rest(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ id_of_pos,
-          uint32_t nrows, uint32_t k, uint32_t giant, uint32_t* parent)
+          uint32_t nrows, uint32_t k, uint32_t giant, uint32_t* parent, unsigned long long* walked)
 {
   const int lane = threadIdx.x & 31;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  unsigned long long rows = 0, edges = 0;
   for (uint32_t u = warp; u < nrows; u += nwarps)
   {
     const uint32_t b = ptr[u] + k, e = ptr[u + 1];
     if (b >= e) continue;
     const uint32_t iu = id_of_pos[u];
     if (cc_find(parent, iu) == giant) continue;
+    rows++;
+    edges += e - b;
     for (uint32_t i = b + lane; i < e; i += 32) cc_union(parent, iu, id_of_pos[col[i]]);
+  }
+  if (lane == 0 && rows)
+  {
+    atomicAdd(&walked[0], rows);
+    atomicAdd(&walked[1], edges);
   }
 }
 
@@ -188,6 +203,8 @@ static int cc_scratch(la3g_graph* G, CcScratch** out)
   G->slot_free[kSlotCc] = cc_scratch_free;
   LA3G_TRY(galloc(G, &cs->label, G->g.nslots));
   LA3G_TRY(galloc(G, &cs->flag, 1));
+  LA3G_TRY(galloc(G, &cs->walked, 2));
+  LA3G_CUDA(cudaHostAlloc(&cs->hwalked, 2 * sizeof(unsigned long long), cudaHostAllocDefault));
   *out = cs;
   return LA3G_OK;
 }
@@ -211,6 +228,7 @@ extern "C" int la3g_cc(la3g_graph* G, uint32_t* label_out, la3g_stats* st)
   LA3G_CUDA(cudaStreamSynchronize(s));
   const bool zero_has_edges = p0 < nrows;
   uint32_t iters = 0;
+  bool rest_counted = false;
   T.device_begin();
   if (!zero_has_edges && nrows)
   {
@@ -246,12 +264,18 @@ extern "C" int la3g_cc(la3g_graph* G, uint32_t* label_out, la3g_stats* st)
       for (j = i; j < nsamples && h[j] == h[i]; j++) {}
       if (j - i > best) { best = j - i; giant = h[i]; }
     }
+    LA3G_CUDA(cudaMemsetAsync(cs->walked, 0, 16, s));
     {
-      ProfileScope p("cc_rest", s, 4.0 * g.nent + 4.0 * (nrows + 1) + 8.0 * N);
+      // every row: its offsets, id and root (16 B); the walked rows' edges:
+      // index, neighbour id and its root (12 B each), added once the walked
+      // counts are back on the host
+      ProfileScope p("cc_rest", s, 16.0 * nrows);
       k_cc_rest<<<grid_for((uint64_t) nrows * 32, 256, kSMs * 32), 256, 0, s>>>(g.in_ptr, g.in_col, g.id_of_pos, nrows,
-                                                                               k, giant, cs->label);
+                                                                               k, giant, cs->label, cs->walked);
       LA3G_LAUNCHED();
     }
+    LA3G_CUDA(cudaMemcpyAsync(cs->hwalked, cs->walked, 16, cudaMemcpyDeviceToHost, s));
+    rest_counted = true;
     {
       ProfileScope p("cc_flatten", s, 8.0 * N);
       k_cc_flatten<<<grid_for(N, 256), 256, 0, s>>>(N, cs->label);
@@ -308,5 +332,17 @@ extern "C" int la3g_cc(la3g_graph* G, uint32_t* label_out, la3g_stats* st)
     st->algo_bytes = (uint64_t) (4.0 * g.nent + 12.0 * N);
   }
   if (label_out) LA3G_CUDA(cudaMemcpyAsync(label_out, cs->label, (size_t) N * 4, cudaMemcpyDeviceToHost, s));
-  return T.finish();
+  LA3G_TRY(T.finish());
+  if (rest_counted)
+  {
+    profile_add_bytes("cc_rest", 12.0 * (double) cs->hwalked[1]);
+    if (st)
+    {
+      // two sampled neighbours per row (28 B), three compressions (8 B per
+      // vertex each), every row's root test (16 B), the walked edges (12 B)
+      st->edges_examined = 2ull * nrows + cs->hwalked[1];
+      st->algo_bytes = (uint64_t) (56.0 * nrows + 24.0 * N + 16.0 * nrows + 12.0 * (double) cs->hwalked[1]);
+    }
+  }
+  return LA3G_OK;
 }

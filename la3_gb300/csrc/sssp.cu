@@ -56,6 +56,7 @@ struct SsspScratch
   uint32_t* ymin = nullptr;       // [nlong] partial minima of the long rows (INF between steps)
   uint64_t reg_in = 0;            // in-edges of the regular rows
   uint32_t max_w = 0;             // largest weight: pull steps need INF + w to stay in uint32
+  uint32_t* by_id = nullptr;      // [nslots] distances reordered by id before they leave the device
 };
 
 static void sssp_scratch_free(void* p)
@@ -392,6 +393,7 @@ static int sssp_scratch(la3g_graph* G, SsspScratch** out)
   LA3G_TRY(galloc(G, &ss->big_task0[0], N));
   LA3G_TRY(galloc(G, &ss->big_task0[1], N));
   LA3G_TRY(galloc(G, &ss->ctr, 8));
+  LA3G_TRY(galloc(G, &ss->by_id, N));
   LA3G_CUDA(cudaHostAlloc(&ss->hctr, 8 * sizeof(unsigned long long), cudaHostAllocDefault));
   k_sssp_reg_end<<<grid_for(N, 256), 256, 0, G->stream>>>(G->g.out_ptr, G->g.out_row, N, G->g.nreg, ss->reg_end);
   LA3G_LAUNCHED();
@@ -554,7 +556,10 @@ static int sssp_run(la3g_graph* G, SsspScratch* ss, uint32_t root, la3g_stats* s
   }
   if (g.nsink)
   {
-    ProfileScope p("sssp_sinks", s, 8.0 * g.nent);
+    // the sink rows' in-edges only (index + weight, and the column's
+    // distance), their offsets and the distance read and written
+    const double sink_in = (double) (g.nent - ss->reg_in);
+    ProfileScope p("sssp_sinks", s, 12.0 * sink_in + 12.0 * g.nsink);
     k_sssp_sinks<<<grid_for(g.nsink, 256), 256, 0, s>>>(g.in_ptr, g.in_col, g.in_w, g.nreg, g.nsink, src_root, ss->dist);
     LA3G_LAUNCHED();
   }
@@ -597,11 +602,10 @@ extern "C" int la3g_sssp(la3g_graph* G, uint32_t root, uint32_t* dist_out, la3g_
   }
   if (dist_out)
   {
-    DevBuf tmp;
-    LA3G_TRY(tmp.alloc((size_t) N * 4));
-    k_u32_by_id<<<grid_for(N, 256), 256, 0, s>>>(N, g.id_of_pos, ss->dist, tmp.as<uint32_t>());
+    // the graph's own reorder buffer: no allocation per call
+    k_u32_by_id<<<grid_for(N, 256), 256, 0, s>>>(N, g.id_of_pos, ss->dist, ss->by_id);
     LA3G_LAUNCHED();
-    LA3G_CUDA(cudaMemcpyAsync(dist_out, tmp.p, (size_t) N * 4, cudaMemcpyDeviceToHost, s));
+    LA3G_CUDA(cudaMemcpyAsync(dist_out, ss->by_id, (size_t) N * 4, cudaMemcpyDeviceToHost, s));
     LA3G_CUDA(cudaStreamSynchronize(s));
   }
   return T.finish();
