@@ -7,7 +7,8 @@ Everything is compiled for sm_103a only (`-gencode arch=compute_103a,
 code=sm_103a`); translation units compile in parallel and link into
 `la3_gb300/_build/libla3g.so`; the vertex programs of `la3_gb300/programs/`
 (written against `include/la3g_vp.cuh`) link into `libla3g_programs.so`.  The drivers (`pr`, `bfs`, `sssp`, `cc`, `tc`,
-`bm25`, `la3g_tool`) go to `la3_gb300/bin/`.  Floating-point contraction is
+`bm25`, `la3g_tool`) go to `la3_gb300/bin/`, and so does the host-only input
+generator `la3g_gen` (`la3_gb300/tools/`, no CUDA and no libla3g).  Floating-point contraction is
 disabled library-wide (`--fmad=false`, `-ffp-contract=off`) because the apps
 reproduce the reference's arithmetic operation by operation.
 """
@@ -25,6 +26,7 @@ PKG = Path(__file__).resolve().parent
 ROOT = PKG.parent
 CSRC = PKG / "csrc"
 DRIVERS = PKG / "drivers"
+TOOLS = PKG / "tools"
 PROGRAMS = PKG / "programs"
 BUILD = PKG / "_build"
 BIN = PKG / "bin"
@@ -91,6 +93,7 @@ def build(verbose: bool = False) -> Path:
         _run([nvcc()] + ARCH + ["-shared", "-o", str(LIB)] + [str(o) for o in objs] + ["-lpthread"])
     build_programs()
     build_drivers()
+    build_tools()
     return LIB
 
 
@@ -127,6 +130,18 @@ def build_drivers() -> None:
     with cf.ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 2)) as ex:
         for f in [ex.submit(_run, c) for c in jobs]:
             f.result()
+
+
+def build_tools() -> None:
+    """Host-only tools: compiled from their own sources (and the generator's),
+    linked to neither CUDA nor libla3g."""
+    BIN.mkdir(exist_ok=True)
+    gen = CSRC / "gen.cpp"
+    for src in sorted(TOOLS.glob("*.cpp")):
+        out = BIN / src.stem
+        deps = [src, gen, INCLUDE / "la3g.h", CSRC / "la3g_internal.h"]
+        if _stale(out, deps):
+            _run(["g++"] + CXX_FLAGS + [str(src), str(gen), "-o", str(out)])
 
 
 def clean() -> None:

@@ -794,12 +794,16 @@ int og_tc(const og_graph* g, uint32_t* ntriangles, uint64_t* total)
       uint32_t hr = g->hash_of_pos[g->ent_row[e]];
       lst[lptr[hr] + fill[hr]++] = g->hash_of_pos[c];
     }
+  /* the rows and the per-u intersections below are independent: shared over
+   * the host's threads (the reference runs its row tiles under OpenMP too) */
+#pragma omp parallel for schedule(dynamic, 1024)
   for (uint32_t h = 0; h < N; h++) qsort(lst + lptr[h], lptr[h + 1] - lptr[h], sizeof(uint32_t), u32_cmp);
   /* P2, CtVertex on the reversed acyclic graph (rows = lower endpoint u,
    * columns = higher endpoint v): u accumulates |N<(u) ∩ N<(v)| over its
    * higher neighbours v by a sorted merge (tc.h:84-97), as uint32.  The
    * reversed graph holds the same oriented edges, so the walk goes over G's
    * entries: in G the column is the lower endpoint and the row the higher. */
+#pragma omp parallel for schedule(dynamic, 256)
   for (uint32_t c = 0; c < N; c++)
   {
     uint32_t hu = g->hash_of_pos[c];
