@@ -7,12 +7,29 @@ duplicates removed) loaded undirected for BFS and CC and directed with
 uint32 weights in [1, 128] for SSSP, and R-MAT scale 20 loaded as the
 reference's TC loads it (directed, cycles removed).  One step = BFS and SSSP
 from the step's root (drawn by seed from the non-isolated vertices), CC, and
-TC, each through the C ABI.  GTEPS numerators: BFS = undirected edges with
-both endpoints reached, SSSP = directed edges whose source is reachable,
-CC = stored symmetric entries, TC = undirected edges; `value` is the sum of
-the four numerators over the timed steps divided by the timed device time.
+TC (both of its passes: the list building and the counting), each through
+the C ABI.  GTEPS numerators: BFS = undirected edges with both endpoints
+reached, SSSP = directed edges whose source is reachable, CC = stored
+symmetric entries, TC = undirected edges; `value` is the sum of the four
+numerators over the timed steps divided by the timed device time.
+
+The same line carries, outside the timed region: the first timed step's
+results checked against the C oracle on the same inputs ("parity") and the
+oracle's own times as the CPU baseline; per-app fractions of the HBM
+roofline; and the systems forms on their configurations ("systems":
+batched BFS/SSSP with 64/256/1024 roots on R-MAT s22 and ER 2^22, the
+served stream's saturation rate and p50/p99, PageRank FP64 on R-MAT s16
+and FP32 vs FP64 on R-MAT s24).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl la3g|reference]
+
+The reference arm (--impl reference) runs the reference's own CPU build on
+the same workload (inputs written by the host-only generator tool, so no
+library of this project is loaded): every graph ingested once, untimed;
+warm-up BFS runs, one CC and one TC run, then steps alternating BFS and
+SSSP from the same roots as the GPU arm; `value` = sum over apps of the
+mean numerator / sum over apps of the mean execute() time, i.e. the GTEPS
+of one step of the same composition.
 
 Multi-GPU runs are replicas (one process per GPU, launched by torchrun):
 each rank runs the whole workload on its own copy of the graphs with its own
@@ -37,7 +54,6 @@ sys.path.insert(0, str(ROOT))
 METRIC = "GTEPS per app on 1 GB300 (plain vs batched/served); p50/p99 query latency"
 SCALE, TC_SCALE = 22, 20
 GRAPH_SEED, WEIGHT_SEED, TC_SEED = 22, 23, 20
-CPU_SAMPLE_SCALE, CPU_SAMPLE_TC_SCALE = 18, 16
 
 
 def parse_args(argv=None):
@@ -48,7 +64,8 @@ def parse_args(argv=None):
     ap.add_argument("--impl", choices=["la3g", "reference"], default="la3g")
     ap.add_argument("--scale", type=int, default=SCALE)
     ap.add_argument("--tc-scale", type=int, default=TC_SCALE)
-    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the oracle parity check and CPU baseline")
+    ap.add_argument("--no-systems", action="store_true", help="skip the batched / served / PageRank sub-results")
     ap.add_argument("--workload", choices=["plain", "batched", "precision", "serve", "next"], default="plain",
                     help="plain (default): the single-query BFS/SSSP/CC/TC step; batched: multi-source BFS/SSSP; "
                          "precision: FP32 vs FP64 PageRank on s24; serve: Poisson query stream over resident graphs; "
@@ -168,81 +185,108 @@ def ncu_traffic(kernel: str):
     return d.get(kernel)
 
 
-# ---------------------------------------------------------------- CPU baseline
+# ---------------------------------------------------------------- workload
+
+def workload_config(args) -> dict:
+    """The workload's description, identical in both arms' lines."""
+    return {"workload": f"plain BFS+SSSP+CC on R-MAT s{args.scale} (ef 16) + TC on R-MAT s{args.tc_scale}",
+            "graphs": {"bfs_cc": f"R-MAT s{args.scale} ef 16 seed {GRAPH_SEED}, undirected",
+                       "sssp": f"R-MAT s{args.scale} ef 16 seed {GRAPH_SEED}, directed, u32 weights in [1, 128] "
+                               f"seed {WEIGHT_SEED}",
+                       "tc": f"R-MAT s{args.tc_scale} ef 16 seed {TC_SEED}, directed acyclic (lower id -> higher id)"},
+            "roots": "seeded draws: BFS from the non-isolated vertices, SSSP from the vertices with out-edges"}
+
+
+def candidate_roots(pairs_path: Path, triples_path: Path, n: int):
+    """Root candidates from the edge files (sorted ids): vertices with an
+    edge (BFS) and vertices with an out-edge (SSSP) - the same sets the GPU
+    arm reads off the loaded graphs' vertex classes."""
+    import numpy as np
+    a = np.fromfile(pairs_path, np.uint32)
+    nonisolated = np.nonzero(np.bincount(a, minlength=n + 1))[0].astype(np.uint32)
+    del a
+    w = np.fromfile(triples_path, np.uint32).reshape(-1, 3)
+    with_out = np.nonzero(np.bincount(w[:, 0], minlength=n + 1))[0].astype(np.uint32)
+    return nonisolated, with_out
+
+
+# ---------------------------------------------------------------- reference arm
 
 def ref_bench_bin() -> Path:
     return ROOT / "oracle" / "_ref" / "bin" / "bench_ref"
 
 
-def run_reference_sample(steps: int, scale: int, tc_scale: int, nroots: int = 4, seed: int = 99,
-                         threads: int = 0) -> dict:
-    """Runs the reference's own CPU implementation (built from its sources with
-    the single-rank MPI stand-in; np = 1, OMP_NUM_THREADS = threads, all host
-    cores by default) on a seeded R-MAT sample, ingest untimed, execute()
-    windows timed."""
-    import numpy as np
-    import la3_gb300 as L
-    exe = ref_bench_bin()
-    if not exe.exists():
-        raise FileNotFoundError(str(exe))
-    with tempfile.TemporaryDirectory() as d:
-        d = Path(d)
-        n, ntc = 1 << scale, 1 << tc_scale
-        e = L.EdgeList.rmat(scale, 16, seed=GRAPH_SEED)
-        e.write(d / "g.bin")
-        ew = L.EdgeList.rmat(scale, 16, seed=GRAPH_SEED, weighted=True, wseed=WEIGHT_SEED)
-        ew.write(d / "g.w.bin")
-        L.EdgeList.rmat(tc_scale, 16, seed=TC_SEED).write(d / "t.bin")
-        src, dst, _ = e.arrays()
-        # roots with out-edges, so that the directed SSSP from them does work too
-        cand = np.unique(src[src != dst])
-        roots = rank_roots(cand, nroots, 0, seed)
-        env = dict(os.environ, OMP_NUM_THREADS=str(threads or os.cpu_count() or 1))
-        t0 = time.time()
-        r = subprocess.run([str(exe), str(d / "g.bin"), str(d / "g.w.bin"), str(n), str(d / "t.bin"), str(ntc),
-                            str(steps)] + [str(x) for x in roots], capture_output=True, text=True, env=env, check=True)
-        wall = time.time() - t0
-    out = [json.loads(l) for l in r.stdout.splitlines() if l.startswith("{")]
-    summ = [o for o in out if o.get("summary")][-1]
-    per_step = [o for o in out if "step" in o]
-    return {"summary": summ, "steps": per_step, "wall_s": wall, "roots": roots,
-            "threads": int(env["OMP_NUM_THREADS"])}
+def gen_tool() -> Path:
+    return ROOT / "la3_gb300" / "bin" / "la3g_gen"
 
 
 def cpu_threads_note() -> str:
-    try:
-        import platform
-        return f"{platform.machine()} x{os.cpu_count()}"
-    except Exception:
-        return "unknown"
+    import platform
+    return f"{platform.machine()} x{os.cpu_count()}"
 
 
 def reference_line(args) -> dict:
-    """--impl reference: the reference CPU path on a bounded sample."""
-    res = run_reference_sample(args.warmup + args.steps, CPU_SAMPLE_SCALE, CPU_SAMPLE_TC_SCALE)
-    steps = res["steps"][args.warmup:]
-    e = sum(s["bfs_e"] + s["sssp_e"] + s["cc_e"] + s["tc_e"] for s in steps)
-    t = sum(s["bfs_s"] + s["sssp_s"] + s["cc_s"] + s["tc_s"] for s in steps)
-    v = e / t / 1e9
-    apps = {a: sum(s[f"{a}_e"] for s in steps) / max(1e-12, sum(s[f"{a}_s"] for s in steps)) / 1e9
-            for a in ("bfs", "sssp", "cc", "tc")}
-    sample = (f"reference apps (np=1, OMP_NUM_THREADS={res['threads']}; one tile, so its SpMV runs on one thread) on R-MAT "
-              f"s{CPU_SAMPLE_SCALE} (BFS/SSSP/CC) + s{CPU_SAMPLE_TC_SCALE} (TC); execute() windows only; "
-              f"host {cpu_threads_note()}")
+    """--impl reference: the reference's own CPU build on the same workload
+    (inputs from the host-only generator tool; no library of this project
+    is loaded in this process or its children)."""
+    exe, gen = ref_bench_bin(), gen_tool()
+    for f in (exe, gen):
+        if not f.exists():
+            raise FileNotFoundError(f"{f} (run __graft_entry__.build() first)")
+    K, W = args.steps, args.warmup
+    threads = os.cpu_count() or 1
+    n, ntc = 1 << args.scale, 1 << args.tc_scale
+    with tempfile.TemporaryDirectory() as d:
+        d = Path(d)
+        g, gw, gt = d / "g.bin", d / "g.w.bin", d / "t.bin"
+        t0 = time.time()
+        subprocess.run([str(gen), "rmat", str(args.scale), "16", str(GRAPH_SEED), str(g)], check=True,
+                       capture_output=True)
+        subprocess.run([str(gen), "rmat", str(args.scale), "16", str(GRAPH_SEED), str(gw), str(WEIGHT_SEED)],
+                       check=True, capture_output=True)
+        subprocess.run([str(gen), "rmat", str(args.tc_scale), "16", str(TC_SEED), str(gt)], check=True,
+                       capture_output=True)
+        gen_s = time.time() - t0
+        nonisolated, with_out = candidate_roots(g, gw, n)
+        roots = rank_roots(nonisolated, K + W, 0)
+        sroots = rank_roots(with_out, K + W, 0, seed=98)
+        npairs = max(1, (K + 1) // 2)
+        pair_args = []
+        for i in range(npairs):
+            pair_args += [str(roots[W + i]), str(sroots[W + i])]
+        env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+        t0 = time.time()
+        r = subprocess.run([str(exe), str(g), str(gw), str(n), str(gt), str(ntc), str(W), str(K), "1", "1"] + pair_args,
+                           capture_output=True, text=True, env=env, check=True)
+        wall = time.time() - t0
+    out = [json.loads(l) for l in r.stdout.splitlines() if l.startswith("{")]
+    summ = [o for o in out if o.get("summary")][-1]
+    runs = summ["runs"]
+    mean_e = {a: summ[f"{a}_e"] / max(1, runs[a]) for a in ("bfs", "sssp", "cc", "tc")}
+    mean_s = {a: summ[f"{a}_s"] / max(1, runs[a]) for a in ("bfs", "sssp", "cc", "tc")}
+    v = sum(mean_e.values()) / sum(mean_s.values()) / 1e9
+    apps = {a: mean_e[a] / max(1e-12, mean_s[a]) / 1e9 for a in mean_e}
+    sample = (f"reference apps built from their sources (np=1, OMP_NUM_THREADS={threads}; one tile, so the SpMV runs on "
+              f"one thread) on the same inputs: {W} untimed BFS runs, then {runs['cc']} CC, {runs['tc']} TC (both "
+              f"passes), {runs['bfs']} BFS and {runs['sssp']} SSSP execute() windows; value = sum of per-app mean "
+              f"numerators / sum of per-app mean times (one step's composition); ingest {summ['ingest_s']:.0f} s "
+              f"untimed; host {cpu_threads_note()}")
+    cfg = workload_config(args)
+    cfg.update({"apps_gteps": apps, "apps_s_per_run": mean_s, "runs": runs, "ingest_s": summ["ingest_s"],
+                "generate_s": round(gen_s, 1), "wall_s": round(wall, 1)})
     return {"metric": METRIC, "value": v, "unit": "GTEPS", "impl": "reference", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / len(steps),
+            "steps": K, "warmup": W, "ms_per_step": 1e3 * sum(mean_s.values()),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
-            "data": "synthetic (seeded R-MAT)",
-            "config": {"workload": f"plain BFS+SSSP+CC R-MAT s{CPU_SAMPLE_SCALE} + TC s{CPU_SAMPLE_TC_SCALE} "
-                                   f"(bounded CPU sample of the s{SCALE}/s{TC_SCALE} workload)",
-                       "apps_gteps": apps},
-            "cpu_baseline": {"value": v, "unit": "GTEPS", "cores": res["threads"], "kind": "reference", "sample": sample},
+            "data": "synthetic (seeded R-MAT, written by the host-only generator tool)",
+            "config": cfg,
+            "cpu_baseline": {"value": v, "unit": "GTEPS", "cores": threads, "kind": "reference", "sample": sample},
             "e2e": {"value": v, "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
 # ---------------------------------------------------------------- GPU arm
 
 def gpu_line(args, rank: int, world: int, local: int) -> dict | None:
+    import ctypes as C
     import numpy as np
     import torch
     import la3_gb300 as L
@@ -257,6 +301,14 @@ def gpu_line(args, rank: int, world: int, local: int) -> dict | None:
     GU = L.Graph.from_edges(e, 0)
     GW = L.Graph.from_edges(ew, L.DIRECTED | L.WEIGHTED)
     GT = L.Graph.from_edges(et, L.DIRECTED | L.ACYCLIC)
+    check = rank == 0 and not args.no_cpu_baseline
+    tmpdir = tempfile.TemporaryDirectory() if check else None
+    if check:
+        # the same records for the oracle (written outside every timed region)
+        d = Path(tmpdir.name)
+        e.write(d / "g.bin")
+        ew.write(d / "g.w.bin")
+        et.write(d / "t.bin")
     pos, ids = GU.positions()
     nonisolated = ids[: GU.info.nregular + GU.info.nsink]
     # SSSP roots: vertices with out-edges in the directed graph (regular and
@@ -272,14 +324,14 @@ def gpu_line(args, rank: int, world: int, local: int) -> dict | None:
         g.set_stream(stream.cuda_stream)
     setup_s = time.time() - t_setup
 
-    # TEPS numerators per root (computed once, outside every timed region)
-    teps_b, teps_s = {}, {}
+    # TEPS numerators and algorithmic bytes per root (outside every timed region)
+    teps_b, teps_s, bytes_b, bytes_s = {}, {}, {}, {}
     for r in set(roots):
         _, _, sb = L.bfs(GU, r, False, False)
-        teps_b[r] = sb.teps_edges
+        teps_b[r], bytes_b[r] = sb.teps_edges, sb.algo_bytes
     for r in set(sroots):
         _, ss = L.sssp(GW, r, False)
-        teps_s[r] = ss.teps_edges
+        teps_s[r], bytes_s[r] = ss.teps_edges, ss.algo_bytes
     _, sc = L.cc(GU, False)
     _, _, stc = L.tc(GT, False)
     cc_e, tc_e = sc.teps_edges, stc.teps_edges
@@ -302,8 +354,8 @@ def gpu_line(args, rank: int, world: int, local: int) -> dict | None:
     torch.cuda.synchronize()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
     app_ev = [[torch.cuda.Event(enable_timing=True) for _ in range(5)] for _ in range(K)]
-    edges = 0.0
     app_edges = {"bfs": 0, "sssp": 0, "cc": 0, "tc": 0}
+    app_bytes = {"bfs": 0.0, "sssp": 0.0, "cc": 0.0, "tc": 0.0}
     lib = L.N.lib()
     with ClockSampler(local) as clocks:
         step(0)  # one more untimed step with the sampler running
@@ -330,6 +382,10 @@ def gpu_line(args, rank: int, world: int, local: int) -> dict | None:
                 app_edges["sssp"] += teps_s[rs]
                 app_edges["cc"] += cc_e
                 app_edges["tc"] += tc_e
+                app_bytes["bfs"] += bytes_b[r]
+                app_bytes["sssp"] += bytes_s[rs]
+                app_bytes["cc"] += sc.algo_bytes
+                app_bytes["tc"] += stc.algo_bytes
             ev[1].record(stream)
         torch.cuda.synchronize()
     if world > 1:
@@ -352,7 +408,6 @@ def gpu_line(args, rank: int, world: int, local: int) -> dict | None:
     roots_h = pin(2 * K, torch.int32).view(np.uint32)
     roots_h[:K] = roots[W:W + K]
     roots_h[K:] = sroots[W:W + K]
-    import ctypes as C
     u8p, u32p = C.POINTER(C.c_uint8), C.POINTER(C.c_uint32)
     tot = C.c_uint64()
     torch.cuda.synchronize()
@@ -366,7 +421,7 @@ def gpu_line(args, rank: int, world: int, local: int) -> dict | None:
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     e2e_edges, e2e_s = reduce_results(edges, e2e_s, device=dev)
-    e2e = {"value": e2e_edges / e2e_s / 1e9, "unit": "GTEPS", "h2d_bytes_per_step": 16,
+    e2e = {"value": e2e_edges / e2e_s / 1e9, "unit": "GTEPS", "h2d_bytes_per_step": 8,
            "d2h_bytes_per_step": N * (1 + 4 + 4 + 4) + NT * 4 + 8}
 
     # roofline of the dominant kernel: per-launch CUDA events inside the library
@@ -388,53 +443,140 @@ def gpu_line(args, rank: int, world: int, local: int) -> dict | None:
                 "ms_per_launch": dom[1]["ms"] / launches,
                 "kernels": {k: {"launches": v["launches"], "ms": round(v["ms"], 4),
                                 "gbs": (v["bytes"] / (v["ms"] / 1e3) / 1e9) if v["ms"] > 0 else None}
-                            for k, v in sorted(prof.items(), key=lambda kv: -kv[1]["ms"])}}
-    launches_per_step = None
+                            for k, v in sorted(prof.items(), key=lambda kv: -kv[1]["ms"])},
+                # each app's algorithmic bytes over the timed steps / its timed device time / peak
+                "apps": {a: {"gbs": app_bytes[a] / (app_ms[a] / 1e3) / 1e9,
+                             "frac": app_bytes[a] / (app_ms[a] / 1e3) / 1e9 / peaks["hbm_gbs"],
+                             "bytes_per_step": app_bytes[a] / K}
+                         for a in app_ms}}
 
-    if rank != 0:
-        return None
-    line = {
-        "metric": METRIC, "value": value, "unit": "GTEPS", "n_gpus": world, "steps": K, "warmup": W,
-        "ms_per_step": region_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "u32", "data": "synthetic (seeded R-MAT, generated in-process)",
-        "config": {"workload": f"plain BFS+SSSP+CC on R-MAT s{args.scale} (ef 16) + TC on R-MAT s{args.tc_scale}",
-                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                   "l2": "inputs larger than L2 (s22 CSR ~0.5 GB) and 256 MB L2 flush before every step",
-                   "apps_gteps": {a: app_edges[a] / (app_ms[a] / 1e3) / 1e9 for a in app_ms},
-                   "apps_ms_per_step": {a: app_ms[a] / K for a in app_ms},
-                   "nentries": {"undirected_s22": GU.info.nentries, "directed_s22": GW.info.nentries,
-                                "tc_s20": GT.info.nentries},
-                   "setup_s": round(setup_s, 2)},
-        "roofline": roofline,
-        "e2e": e2e,
-        "clocks": clocks.summary(),
-    }
-    # kernels of this library per step (counted by the library)
-    st = [L.Stats() for _ in range(4)]
-    lib.la3g_bfs(GU._h, roots[W], None, None, C.byref(st[0]))
-    lib.la3g_sssp(GW._h, sroots[W], None, C.byref(st[1]))
-    lib.la3g_cc(GU._h, None, C.byref(st[2]))
-    lib.la3g_tc(GT._h, None, None, C.byref(st[3]))
-    launches_per_step = sum(s.kernel_launches for s in st)
-    line["gpu_launches"] = launches_per_step * K
-    line["config"]["iterations"] = {"bfs": st[0].iterations, "bfs_bottom_up": st[0].pull_iterations,
-                                    "sssp": st[1].iterations}
-    if not args.no_cpu_baseline:
-        try:
-            res = run_reference_sample(2, CPU_SAMPLE_SCALE, CPU_SAMPLE_TC_SCALE)
-            s = res["summary"]
-            e_ = s["bfs_e"] + s["sssp_e"] + s["cc_e"] + s["tc_e"]
-            t_ = s["bfs_s"] + s["sssp_s"] + s["cc_s"] + s["tc_s"]
-            line["cpu_baseline"] = {
-                "value": e_ / t_ / 1e9, "unit": "GTEPS", "cores": res["threads"], "kind": "reference",
-                "sample": (f"2 steps of BFS+SSSP+CC on R-MAT s{CPU_SAMPLE_SCALE} + TC on s{CPU_SAMPLE_TC_SCALE}, "
-                           f"reference apps np=1 OMP_NUM_THREADS={res['threads']} (one tile: its SpMV runs on one "
-                           f"thread), execute() windows only, host {cpu_threads_note()}, {res['wall_s']:.1f} s wall "
-                           f"incl. ingest")}
-        except Exception as ex:  # the baseline is reported, never required
-            line["cpu_baseline"] = {"value": None, "unit": "GTEPS", "cores": 0, "kind": "reference",
-                                    "sample": f"unavailable: {type(ex).__name__}: {ex}"}
+    line = None
+    if rank == 0:
+        cfg = workload_config(args)
+        cfg.update({"parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                    "l2": "inputs larger than L2 (s22 CSR ~0.5 GB) and 256 MB L2 flush before every step",
+                    "apps_gteps": {a: app_edges[a] / (app_ms[a] / 1e3) / 1e9 for a in app_ms},
+                    "apps_ms_per_step": {a: app_ms[a] / K for a in app_ms},
+                    "nentries": {"undirected": GU.info.nentries, "directed": GW.info.nentries,
+                                 "tc": GT.info.nentries},
+                    "setup_s": round(setup_s, 2)})
+        line = {
+            "metric": METRIC, "value": value, "unit": "GTEPS", "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": region_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u32", "data": "synthetic (seeded R-MAT, generated in-process)",
+            "config": cfg, "roofline": roofline, "e2e": e2e, "clocks": clocks.summary(),
+        }
+        # kernels of this library per step (counted by the library)
+        st = [L.Stats() for _ in range(4)]
+        lib.la3g_bfs(GU._h, roots[W], None, None, C.byref(st[0]))
+        lib.la3g_sssp(GW._h, sroots[W], None, C.byref(st[1]))
+        lib.la3g_cc(GU._h, None, C.byref(st[2]))
+        lib.la3g_tc(GT._h, None, None, C.byref(st[3]))
+        line["gpu_launches"] = sum(x.kernel_launches for x in st) * K
+        cfg["iterations"] = {"bfs": st[0].iterations, "bfs_bottom_up": st[0].pull_iterations,
+                             "sssp": st[1].iterations}
+        if check:
+            try:
+                par_, cpu = oracle_check(Path(tmpdir.name), args, GU, GW, GT, roots[W], sroots[W])
+                line["parity"] = par_
+                line["cpu_baseline"] = cpu
+            except Exception as ex:  # reported, never required
+                line["parity"] = {"checked": False, "error": f"{type(ex).__name__}: {ex}"}
+            tmpdir.cleanup()
+        if not args.no_systems:
+            line["systems"] = systems_results(args, GU, GW, stream, dev)
     return line
+
+
+def oracle_check(d: Path, args, GU, GW, GT, root: int, sroot: int):
+    """The first timed step's results against the C oracle on the same
+    records, every vector compared in full (bit-exact); the oracle's own
+    execution times form the CPU baseline (kind "port")."""
+    import numpy as np
+    import la3_gb300 as L
+    from oracle import oracle as O
+    O.build()
+    n, ntc = 1 << args.scale, 1 << args.tc_scale
+    hops, parent, sb = L.bfs(GU, root)
+    dist, ss = L.sssp(GW, sroot)
+    lab, sc = L.cc(GU)
+    tot, ntri, stc = L.tc(GT)
+    res, times, edges = {}, {}, {}
+    og = O.OracleGraph(d / "g.bin", n, 0)
+    t0 = time.perf_counter()
+    oh, op, _ = og.bfs(root)
+    times["bfs"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ol, _ = og.cc()
+    times["cc"] = time.perf_counter() - t0
+    del og
+    res["bfs"] = bool(np.array_equal(hops, oh) and np.array_equal(parent, op))
+    res["cc"] = bool(np.array_equal(lab, ol))
+    ow = O.OracleGraph(d / "g.w.bin", n, O.DIRECTED | O.WEIGHTED)
+    t0 = time.perf_counter()
+    od, _ = ow.sssp(sroot)
+    times["sssp"] = time.perf_counter() - t0
+    del ow
+    res["sssp"] = bool(np.array_equal(dist, od))
+    ot = O.OracleGraph(d / "t.bin", ntc, O.DIRECTED | O.ACYCLIC)
+    t0 = time.perf_counter()
+    otot, oper = ot.tc()
+    times["tc"] = time.perf_counter() - t0
+    del ot
+    res["tc"] = bool(otot == tot and np.array_equal(ntri, oper))
+    edges = {"bfs": sb.teps_edges, "sssp": ss.teps_edges, "cc": sc.teps_edges, "tc": stc.teps_edges}
+    parity = {"checked": True, "bit_exact": all(res.values()), "apps": res,
+              "case": f"BFS root {root} (hops + parent), SSSP root {sroot} (distances), CC (labels), TC (total "
+                      f"{tot} and per-vertex counts): full vectors against the C oracle on the same records"}
+    omp = os.environ.get("OMP_NUM_THREADS")
+    threads = int(omp) if omp and omp.isdigit() else (os.cpu_count() or 1)
+    cpu = {"value": sum(edges.values()) / sum(times.values()) / 1e9, "unit": "GTEPS", "cores": threads,
+           "kind": "port",
+           "sample": (f"one step of the same workload (BFS root {root}, SSSP root {sroot}, CC, TC) through the C "
+                      f"restatement of the reference's path: BFS/SSSP/CC single-threaded, TC's intersections over "
+                      f"{threads} OpenMP threads; execute windows only (ingest untimed); host {cpu_threads_note()}; "
+                      f"per app s: " + ", ".join(f"{a} {t:.2f}" for a, t in times.items()))}
+    return parity, cpu
+
+
+def systems_results(args, GU, GW, stream, dev) -> dict:
+    """The systems forms on their configurations, for the default line:
+    batched BFS/SSSP (64/256/1024 roots) on the plain step's R-MAT graphs and
+    on ER 2^22, PageRank (FP64 s16 with oracle parity, FP32 vs FP64 on
+    R-MAT and ER 2^24), and the served stream at 1k/s offered and at
+    saturation (20k/s offered).  Each part carries its own clock record;
+    a part that fails reports its error instead."""
+    import torch
+    out = {}
+    idx = torch.cuda.current_device()
+
+    def batched():
+        graphs = batched_graphs(args, rmat=(GU, GW))
+        for gu, gw in graphs.values():
+            gu.set_stream(stream.cuda_stream)
+            gw.set_stream(stream.cuda_stream)
+        r = batched_measure(args, 0, graphs, stream, dev)
+        for gu, gw in (graphs["er"],):
+            gu.free()
+            gw.free()
+        return r
+
+    parts = (("batched", batched),
+             ("pagerank", lambda: pagerank_measure(args, stream, dev)),
+             ("served", lambda: serve_measure(args, [1000.0, 20000.0], 1.0)))
+    for name, fn in parts:
+        t0 = time.time()
+        try:
+            with ClockSampler(idx) as clocks:
+                clocks.start_timed()
+                r = fn()
+            r["clocks"] = clocks.summary()
+        except Exception as ex:  # reported, never required
+            r = {"error": f"{type(ex).__name__}: {ex}"}
+        r["wall_s"] = round(time.time() - t0, 1)
+        out[name] = r
+        torch.cuda.synchronize()
+    return out
 
 
 # ---------------------------------------------------------------- other workloads
@@ -466,36 +608,23 @@ def _flush_fn(dev):
     def flush():
         count[0] += 1
         buf.fill_(count[0] & 0xFF)
+        torch.cuda.synchronize()  # done before the next timed call starts on its own stream
 
     return flush
 
 
-def batched_line(args, rank, world, local) -> dict | None:
-    """Batched multi-source BFS / SSSP (64 roots per frontier word) on R-MAT
-    s22 and Erdos-Renyi 2^22 (average degree 16): GTEPS = sum over roots of
-    the single-root numerator / batch time.  A step = one BFS batch of 1024
-    roots + one SSSP batch of 256 roots on R-MAT s22."""
+def batched_measure(args, rank: int, graphs: dict, stream, dev, sizes_b=(64, 256, 1024), sizes_s=(64, 256, 1024),
+                    parity_roots: int = 8) -> dict:
+    """Batched multi-source BFS / SSSP (64 roots per frontier word): per
+    graph and batch size, batch time after an L2 flush, GTEPS = sum over
+    roots of the single-root numerator / batch time, and its ratio to the
+    plain per-root rate (single-root calls of the same roots, timed alike).
+    Parity: for the 64-root batches, `parity_roots` sampled roots' full hop /
+    distance vectors equal the single-root calls'."""
     import numpy as np
-    import torch
     import la3_gb300 as L
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    stream = torch.cuda.Stream(device=dev)
-    n = 1 << args.scale
-    graphs = {
-        "rmat": (L.Graph.from_edges(L.EdgeList.rmat(args.scale, 16, seed=GRAPH_SEED), 0),
-                 L.Graph.from_edges(L.EdgeList.rmat(args.scale, 16, seed=GRAPH_SEED, weighted=True, wseed=WEIGHT_SEED),
-                                    L.DIRECTED | L.WEIGHTED)),
-        "er": (L.Graph.from_edges(L.EdgeList.er(n, 8 * n, seed=GRAPH_SEED + 100), 0),
-               L.Graph.from_edges(L.EdgeList.er(n, 16 * n, seed=GRAPH_SEED + 101, weighted=True, wseed=WEIGHT_SEED),
-                                  L.DIRECTED | L.WEIGHTED)),
-    }
-    for gu, gw in graphs.values():
-        gu.set_stream(stream.cuda_stream)
-        gw.set_stream(stream.cuda_stream)
-    sizes_b, sizes_s = (64, 256, 1024), (64, 256)
-    sweep, depth_hist, tune = {}, {}, {}
-    roots_of = {}
+    flush = _flush_fn(dev)
+    sweep, depth_hist, tune, parity = {}, {}, {}, {}
     for name, (gu, gw) in graphs.items():
         _, ids = gu.positions()
         cand_b = np.sort(ids[: gu.info.nregular])
@@ -505,20 +634,22 @@ def batched_line(args, rank, world, local) -> dict | None:
                                          wids[iw.nregular + iw.nsink: iw.nregular + iw.nsink + iw.nsource]]))
         rb = rank_roots(cand_b, max(sizes_b), rank, seed=7)
         rs = rank_roots(cand_s, max(sizes_s), rank, seed=8)
-        roots_of[name] = (rb, rs)
         # the project autotuner picks level mode, block size and push threshold
-        # for this graph and each batch size (untimed setup, separate root draws)
-        tune[name] = {R: L.batch_autotune(gu, rank_roots(cand_b, R, rank, seed=17 + R)) for R in sizes_b}
+        # for this graph and each batch size (untimed, separate root draws)
+        tune[name] = {R: min(L.batch_autotune(gu, rank_roots(cand_b, R, rank, seed=17 + R)), key=lambda c: c["ms"])
+                      for R in sizes_b}
         # single-root numerators and times (outside every timed batch)
         tb, ts, eb, es, lv = [], [], {}, {}, []
         for r in rb:
             st = L.Stats()
+            flush()
             ms = _timed(stream, lambda: L.N.check(L.N.lib().la3g_bfs(gu._h, r, None, None, L.C.byref(st))))
             tb.append(ms)
             eb[r] = st.teps_edges
             lv.append(st.iterations)
         for r in rs:
             st = L.Stats()
+            flush()
             ms = _timed(stream, lambda: L.N.check(L.N.lib().la3g_sssp(gw._h, r, None, L.C.byref(st))))
             ts.append(ms)
             es[r] = st.teps_edges
@@ -530,21 +661,58 @@ def batched_line(args, rank, world, local) -> dict | None:
         for R in sizes_b:
             rr = rb[:R]
             L.bfs_batch(gu, rr, want_hops=False)  # warm (allocations, graph capture)
+            flush()
             ms = _timed(stream, lambda: L.bfs_batch(gu, rr, want_hops=False))
             g_ = sum(eb[r] for r in rr) / (ms / 1e3) / 1e9
-            ent["bfs"][R] = {"ms": round(ms, 3), "gteps": g_, "per_root_ms": ms / R, "x_plain": g_ / plain_b}
+            ent["bfs"][R] = {"ms": round(ms, 3), "gteps": g_, "x_plain": g_ / plain_b}
         for R in sizes_s:
             rr = rs[:R]
             L.sssp_batch(gw, rr, want_dist=False)
+            flush()
             ms = _timed(stream, lambda: L.sssp_batch(gw, rr, want_dist=False))
             g_ = sum(es[r] for r in rr) / (ms / 1e3) / 1e9
-            ent["sssp"][R] = {"ms": round(ms, 3), "gteps": g_, "per_root_ms": ms / R, "x_plain": g_ / plain_s}
+            ent["sssp"][R] = {"ms": round(ms, 3), "gteps": g_, "x_plain": g_ / plain_s}
         ent["plain"] = {"bfs_gteps": plain_b, "sssp_gteps": plain_s, "bfs_ms_per_root": statistics.mean(tb),
                         "sssp_ms_per_root": statistics.mean(ts)}
         sweep[name] = ent
-    # timed steps on R-MAT
+        if parity_roots:
+            R = min(sizes_b)
+            hb, _ = L.bfs_batch(gu, rb[:R], want_hops=True)
+            ds, _ = L.sssp_batch(gw, rs[:R], want_dist=True)
+            pick = np.linspace(0, R - 1, parity_roots).astype(int)
+            ok_b = all(np.array_equal(hb[i], L.bfs(gu, rb[i], True, False)[0]) for i in pick)
+            ok_s = all(np.array_equal(ds[i], L.sssp(gw, rs[i])[0]) for i in pick)
+            parity[name] = {"bfs": ok_b, "sssp": ok_s,
+                            "case": f"{parity_roots} of the {R} roots of each batch, full vectors vs single-root calls"}
+            del hb, ds
+    return {"sweep": sweep, "bfs_depth_histogram": depth_hist, "autotune_best": tune, "parity": parity,
+            "l2": "256 MB L2 flush before every batch and every single-root call"}
+
+
+def batched_line(args, rank, world, local) -> dict | None:
+    """Batched multi-source BFS / SSSP on R-MAT s22 and Erdos-Renyi 2^22
+    (BFS: 8 n undirected pairs, average degree 16; SSSP: 16 n directed
+    pairs): the sweep above, then timed steps of one BFS batch of 1024 roots
+    and one SSSP batch of 1024 roots on R-MAT."""
+    import numpy as np
+    import torch
+    import la3_gb300 as L
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    graphs = batched_graphs(args)
+    for gu, gw in graphs.values():
+        gu.set_stream(stream.cuda_stream)
+        gw.set_stream(stream.cuda_stream)
+    res = batched_measure(args, rank, graphs, stream, dev)
     gu, gw = graphs["rmat"]
-    rb, rs = roots_of["rmat"]
+    _, ids = gu.positions()
+    rb = rank_roots(np.sort(ids[: gu.info.nregular]), 1024, rank, seed=7)
+    _, wids = gw.positions()
+    iw = gw.info
+    rs = rank_roots(np.sort(np.concatenate([wids[: iw.nregular],
+                                            wids[iw.nregular + iw.nsink: iw.nregular + iw.nsink + iw.nsource]])),
+                    1024, rank, seed=8)
     eb = sum(L.bfs(gu, r, False, False)[2].teps_edges for r in rb)
     es = sum(L.sssp(gw, r, False)[1].teps_edges for r in rs)
     flush = _flush_fn(dev)
@@ -578,79 +746,128 @@ def batched_line(args, rank, world, local) -> dict | None:
     e2e_s = time.perf_counter() - t0
     if rank != 0:
         return None
+    res["parallelism"] = f"replicas x{world}" if world > 1 else "single GPU"
+    res["workload"] = (f"batched BFS (1024 roots) + SSSP (1024 roots) on R-MAT s{args.scale}; sweep on R-MAT and "
+                       f"ER 2^{args.scale}")
     return {
         "metric": METRIC, "value": e_all / t_all / 1e9, "unit": "GTEPS", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": tot / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u64 frontier words / u32 distances", "data": "synthetic (seeded R-MAT and ER)",
-        "config": {"workload": f"batched BFS (1024 roots) + SSSP (256 roots) on R-MAT s{args.scale}; sweep on R-MAT "
-                               f"and ER 2^{args.scale} (deg 16)", "l2": "256 MB L2 flush before every step",
-                   "sweep": sweep, "bfs_depth_histogram": depth_hist,
-                   "autotune_best": {g: {R: min(t, key=lambda c: c["ms"]) for R, t in tr.items()}
-                                     for g, tr in tune.items()},
-                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "config": res,
         "e2e": {"value": (eb + es) / e2e_s / 1e9, "unit": "GTEPS", "h2d_bytes_per_step": 4 * (len(rb) + len(rs)),
                 "d2h_bytes_per_step": int(hb.nbytes + ds.nbytes)},
         "clocks": clocks.summary(),
     }
 
 
-def precision_line(args, rank, world, local) -> dict | None:
-    """FP32 SpMV / FP32 accumulation PageRank vs the FP64 path (bit-identical
-    to the reference) on R-MAT s24 and ER 2^24 (16 n directed pairs): 50
-    iterations or FP64 L1 residual < 1e-9; L1 and max-abs error and GTEPS."""
-    import numpy as np
-    import torch
+def batched_graphs(args, rmat=None) -> dict:
     import la3_gb300 as L
+    n = 1 << args.scale
+    if rmat is None:
+        rmat = (L.Graph.from_edges(L.EdgeList.rmat(args.scale, 16, seed=GRAPH_SEED), 0),
+                L.Graph.from_edges(L.EdgeList.rmat(args.scale, 16, seed=GRAPH_SEED, weighted=True, wseed=WEIGHT_SEED),
+                                   L.DIRECTED | L.WEIGHTED))
+    return {"rmat": rmat,
+            "er": (L.Graph.from_edges(L.EdgeList.er(n, 8 * n, seed=GRAPH_SEED + 100), 0),
+                   L.Graph.from_edges(L.EdgeList.er(n, 16 * n, seed=GRAPH_SEED + 101, weighted=True, wseed=WEIGHT_SEED),
+                                      L.DIRECTED | L.WEIGHTED))}
+
+
+def pagerank_measure(args, stream, dev, include_er: bool = True) -> dict:
+    """PageRank: (1) the plain-method configuration - FP64, 20 iterations on
+    R-MAT s16 (edge factor 16), ranks compared bit for bit with the C
+    oracle on the same records; (2) the precision study - FP32 SpMV with FP32
+    accumulation vs the FP64 path on R-MAT s24 (and ER 2^24 x16 directed):
+    50 iterations or FP64 L1 residual < 1e-9, L1 and max-abs error, GTEPS."""
+    import numpy as np
+    import la3_gb300 as L
+    from oracle import oracle as O
+    out = {}
+    flush = _flush_fn(dev)
+    # (1) s16 FP64, 20 iterations
+    e = L.EdgeList.rmat(16, 16, seed=GRAPH_SEED + 1)
+    G = L.Graph.from_edges(e, L.DIRECTED)
+    G.set_stream(stream.cuda_stream)
+    L.pagerank(G, 20, False, False)
+    ts = []
+    for _ in range(5):
+        flush()
+        st = L.Stats()
+        ts.append(_timed(stream, lambda: L.N.check(L.N.lib().la3g_pr(G._h, 20, None, None, L.C.byref(st)))))
+    m16 = G.info.nentries
+    rank16, deg16, _ = L.pagerank(G, 20)
+    with tempfile.TemporaryDirectory() as d:
+        e.write(Path(d) / "p.bin")
+        O.build()
+        og = O.OracleGraph(Path(d) / "p.bin", 1 << 16, O.DIRECTED)
+        orank, odeg = og.pagerank(20)
+    G.free()
+    del e
+    out["s16_fp64"] = {"m": m16, "iterations": 20, "ms": statistics.median(ts),
+                       "gteps": 20 * m16 / statistics.median(ts) / 1e6,
+                       "bit_exact_vs_oracle": bool(np.array_equal(rank16.view(np.uint64), orank.view(np.uint64))
+                                                   and np.array_equal(deg16, odeg)),
+                       "max_abs_vs_oracle": float(np.abs(rank16 - orank).max())}
+    # (2) precision study
+    scale = 24 if args.scale == SCALE else args.scale + 2
+    n = 1 << scale
+    iters, tol = 50, 1e-9
+    for name in (("rmat", "er") if include_er else ("rmat",)):
+        if name == "rmat":
+            e = L.EdgeList.rmat(scale, 16, seed=GRAPH_SEED + 2)
+        else:
+            e = L.EdgeList.er(n, 16 * n, seed=GRAPH_SEED + 3)
+        G = L.Graph.from_edges(e, L.DIRECTED)
+        del e
+        G.set_stream(stream.cuda_stream)
+        m = G.info.nentries
+        L.pagerank(G, 2, False, False)
+        L.pagerank_f32(G, 2)
+        st64, st32 = L.Stats(), L.Stats()
+        res = L.C.c_double()
+        flush()
+        t64 = _timed(stream, lambda: L.N.check(L.N.lib().la3g_pr(G._h, iters, None, None, L.C.byref(st64))))
+        flush()
+        t32 = _timed(stream, lambda: L.N.check(L.N.lib().la3g_pr_f32(G._h, iters, tol, None, L.C.byref(res),
+                                                                     L.C.byref(st32))))
+        r64 = L.pagerank(G, iters, True, False)[0]
+        r32, res32, _ = L.pagerank_f32(G, iters, tol)
+        d_ = np.abs(r32 - r64)
+        out[f"s{scale}_{name}"] = {
+            "m": m, "n": n, "dangling_frac": G.info.nsink / max(1, G.info.nvertices),
+            "fp64": {"iterations": st64.iterations, "ms": t64, "gteps": st64.iterations * m / t64 / 1e6},
+            "fp32": {"iterations": st32.iterations, "ms": t32, "gteps": st32.iterations * m / t32 / 1e6,
+                     "l1_residual": res32},
+            "l1_abs": float(d_.sum()), "l1_rel": float(d_.sum() / r64.sum()), "max_abs": float(d_.max()),
+            "max_rel": float((d_ / np.maximum(1.0, r64)).max())}
+        G.free()
+    return out
+
+
+def precision_line(args, rank, world, local) -> dict | None:
+    """The PageRank configurations alone (see pagerank_measure)."""
+    import torch
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)
-    scale = 24 if args.scale == SCALE else args.scale
-    n = 1 << scale
-    out, value = {}, None
-    iters, tol = 50, 1e-9
     with ClockSampler(local) as clocks:
-        for name in ("rmat", "er"):
-            if name == "rmat":
-                e = L.EdgeList.rmat(scale, 16, seed=GRAPH_SEED + 2)
-            else:
-                e = L.EdgeList.er(n, 16 * n, seed=GRAPH_SEED + 3)
-            G = L.Graph.from_edges(e, L.DIRECTED)
-            del e
-            G.set_stream(stream.cuda_stream)
-            m = G.info.nentries
-            L.pagerank(G, 2, False, False)
-            L.pagerank_f32(G, 2)
-            st64, st32 = L.Stats(), L.Stats()
-            res = L.C.c_double()
-            t64 = _timed(stream, lambda: L.N.check(L.N.lib().la3g_pr(G._h, iters, None, None, L.C.byref(st64))))
-            t32 = _timed(stream, lambda: L.N.check(L.N.lib().la3g_pr_f32(G._h, iters, tol, None, L.C.byref(res),
-                                                                         L.C.byref(st32))))
-            r64 = L.pagerank(G, iters, True, False)[0]
-            r32, res32, _ = L.pagerank_f32(G, iters, tol)
-            d = np.abs(r32 - r64)
-            out[name] = {"m": m, "n": n, "dangling_frac": G.info.nsink / max(1, G.info.nvertices),
-                         "fp64": {"iterations": st64.iterations, "ms": t64, "gteps": st64.iterations * m / t64 / 1e6},
-                         "fp32": {"iterations": st32.iterations, "ms": t32, "gteps": st32.iterations * m / t32 / 1e6,
-                                  "l1_residual": res32},
-                         "l1_abs": float(d.sum()), "l1_rel": float(d.sum() / r64.sum()), "max_abs": float(d.max()),
-                         "max_rel": float((d / np.maximum(1.0, r64)).max())}
-            if name == "rmat":
-                value = st32.iterations * m / t32 / 1e6
-            G.free()
+        clocks.start_timed()
+        out = pagerank_measure(args, stream, dev)
     if rank != 0:
         return None
+    key = [k for k in out if k.endswith("_rmat")][0]
     return {
-        "metric": METRIC, "value": value, "unit": "GTEPS", "n_gpus": world, "steps": 1, "warmup": 1,
-        "ms_per_step": out["rmat"]["fp32"]["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 (SpMV and accumulation); f64 residual", "data": "synthetic (seeded R-MAT and ER)",
-        "config": {"workload": f"PageRank precision study, R-MAT s{scale} and ER 2^{scale} x16 directed, "
-                               f"{iters} iterations or L1 residual < {tol}", "results": out,
-                   "l2": "inputs larger than L2 (s24 CSR ~1.1 GB)"},
+        "metric": METRIC, "value": out[key]["fp32"]["gteps"], "unit": "GTEPS", "n_gpus": world, "steps": 1,
+        "warmup": 1, "ms_per_step": out[key]["fp32"]["ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (SpMV and accumulation); f64 residual", "data": "synthetic (seeded R-MAT and ER)",
+        "config": {"workload": "PageRank: FP64 20 iterations on R-MAT s16; FP32 vs FP64 on R-MAT and ER 2^24, "
+                               "50 iterations or L1 residual < 1e-9", "results": out,
+                   "l2": "256 MB L2 flush before every timed call"},
         "e2e": None, "clocks": clocks.summary(),
     }
 
 
-def serve_line(args, rank, world, local) -> dict | None:
+def serve_measure(args, rates, seconds: float) -> dict:
     """Served query stream: BFS / SSSP from random roots over R-MAT s18, s21
     and s23 (undirected for BFS, directed weighted for SSSP) and BM25 top-10
     over a bipartite corpus (8M docs, 1M terms, ~50 terms per doc, Zipf 1.1),
@@ -659,10 +876,7 @@ def serve_line(args, rank, world, local) -> dict | None:
     single-query entry points (same arrival times).  Both arms leave the
     BFS / SSSP vectors on the device and copy the BM25 top-10 out."""
     import numpy as np
-    import torch
     import la3_gb300 as L
-    torch.cuda.set_device(local)
-    rates = [float(x) for x in args.serve_rates.split(",")]
     small = args.scale != SCALE  # reduced sizes for quick runs
     scales = (12, 14, 16) if small else (18, 21, 23)
     D, T, tpd = (100_000, 20_000, 30) if small else (8_000_000, 1_000_000, 50)
@@ -809,30 +1023,40 @@ def serve_line(args, rank, world, local) -> dict | None:
     served(arr, qs)
     plain(arr, qs)
     results = []
-    with ClockSampler(local) as clocks:
-        for rate in rates:
-            nq = int(min(max(rate * args.serve_seconds, 200), 20_000))
-            arr, qs = make_stream(rate, nq)
-            sv, _ = served(arr, qs)
-            pl = plain(arr, qs)
-            results.append({"offered_rate": rate, "queries": nq, "served": sv, "plain": pl,
-                            "mix": {k: sum(1 for q in qs if q[0] == k) for k in ("bfs", "sssp", "bm25")}})
+    for rate in rates:
+        nq = int(min(max(rate * seconds, 200), 20_000))
+        arr, qs = make_stream(rate, nq)
+        sv, _ = served(arr, qs)
+        pl = plain(arr, qs)
+        results.append({"offered_rate": rate, "queries": nq, "served": sv, "plain": pl,
+                        "x_plain_qps": sv["qps"] / pl["qps"],
+                        "mix": {k: sum(1 for q in qs if q[0] == k) for k in ("bfs", "sssp", "bm25")}})
     info = S.info()
     S.free()
+    top = results[-1]
+    return {"workload": f"served stream: BFS/SSSP over R-MAT s{scales[0]}/s{scales[1]}/s{scales[2]} + BM25 top-10 "
+                        f"over {D} docs x {T} terms ({postings} postings); Poisson arrivals",
+            "rates": results, "lanes": lanes, "hbm_budget_bytes": budget, "hbm_used_bytes": info["used_bytes"],
+            "bm25_alone": bm25, "setup_s": round(setup_s, 1),
+            "qps_at_top_rate": top["served"]["qps"], "x_plain_at_top_rate": top["x_plain_qps"],
+            "p50_ms_at_top_rate": top["served"]["p50_ms"], "p99_ms_at_top_rate": top["served"]["p99_ms"]}
+
+
+def serve_line(args, rank, world, local) -> dict | None:
+    """The served stream alone at the offered rates of --serve-rates."""
+    import torch
+    torch.cuda.set_device(local)
+    rates = [float(x) for x in args.serve_rates.split(",")]
+    with ClockSampler(local) as clocks:
+        clocks.start_timed()
+        res = serve_measure(args, rates, args.serve_seconds)
     if rank != 0:
         return None
-    top = results[-1]
     return {
-        "metric": METRIC, "value": top["served"]["qps"], "unit": "queries/s", "n_gpus": world, "steps": len(rates),
-        "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "u64 frontier words / u32 distances / f32 BM25", "data": "synthetic (seeded R-MAT, Zipf corpus)",
-        "config": {"workload": f"served stream: BFS/SSSP over R-MAT s{scales[0]}/s{scales[1]}/s{scales[2]} + BM25 "
-                               f"top-10 over {D} docs x {T} terms ({postings} postings); Poisson arrivals",
-                   "rates": results, "lanes": lanes, "hbm_budget_bytes": budget, "hbm_used_bytes": info["used_bytes"],
-                   "bm25_alone": bm25,
-                   "setup_s": round(setup_s, 1),
-                   "p50_ms_at_top_rate": top["served"]["p50_ms"], "p99_ms_at_top_rate": top["served"]["p99_ms"]},
-        "e2e": None, "clocks": clocks.summary(),
+        "metric": METRIC, "value": res["qps_at_top_rate"], "unit": "queries/s", "n_gpus": world,
+        "steps": len(rates), "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64 frontier words / u32 distances / f32 BM25",
+        "data": "synthetic (seeded R-MAT, Zipf corpus)", "config": res, "e2e": None, "clocks": clocks.summary(),
     }
 
 
