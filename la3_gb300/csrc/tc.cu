@@ -24,16 +24,19 @@
 // (x, start of the suffix of N+(x) after y), i.e. every oriented edge once.
 //
 // Pass 2 (counting) is y-centric: a task is a vertex y and a slice of its
-// pairs; N+(y) goes into a shared-memory hash table (rank -> index) with
-// the ids of its elements, and the walk reads the suffixes of the slice's
-// pairs concatenated, 32 list elements per warp step, each probed in the
-// table.  A hit w closes {x, y, w}; its middle id takes the count: x in a
-// per-pair shared counter, y in a register, w in a shared counter per element
-// of N+(y); all are flushed once per pair batch or task.  On R-MAT this
+// pairs; N+(y) goes into a shared-memory hash table (rank -> index, at least
+// four slots per element) with the ids of its elements, and a warp walks the
+// suffixes of 32 pairs at a time concatenated, 64 list elements per step,
+// each probed in the table; an element's pair is found from the window's
+// pair-start bits (one OR-reduction) and its address by a shuffle from the
+// pair's lane.  A hit w closes {x, y, w}; its middle id takes the count: x
+// in a per-pair shared counter, y in a register, w in a shared counter per
+// element of N+(y); all are flushed once per round or task.  On R-MAT this
 // walks the shorter side of almost every pair (the suffix), and the lists
 // stay L2-resident.  N+(y) up to kTcWarpCap: one warp per task; longer: one
-// block per task with a block-wide table; beyond kTcBlockCap (no such rows on
-// R-MAT up to scale 24): a binary search in the sorted row in global memory.
+// block per task with a block-wide table, its warps taking the rounds from a
+// shared counter; beyond kTcBlockCap (no such rows on R-MAT up to scale 24):
+// a binary search in the sorted row in global memory.
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
@@ -47,14 +50,12 @@
 namespace la3g {
 
 static constexpr uint32_t kTcEdgesPerThread = 8;  // edge-parallel passes: contiguous edges per thread
-static constexpr uint32_t kTcWarpCap = 256;       // |N+(y)| up to this: a warp per task
-static constexpr uint32_t kTcWarpSlots = 512;     // hash slots of a warp table (>= 2 kTcWarpCap)
-static constexpr int kTcWarpBloomBits = 11;       // Bloom bits of a warp table: 2^11
+static constexpr uint32_t kTcWarpCap = 128;       // |N+(y)| up to this: a warp per task
+static constexpr uint32_t kTcWarpSlots = 512;     // hash slots of a warp table (>= 4 kTcWarpCap)
 static constexpr uint32_t kTcWarpPairs = 256;     // pairs per warp task
 static constexpr uint32_t kTcBlockCap = 2048;     // |N+(y)| up to this: a block table; longer: global search
-static constexpr uint32_t kTcBlockSlots = 4096;   // hash slots of a block table (>= 2 kTcBlockCap)
-static constexpr int kTcBlockBloomBits = 16;      // Bloom bits of a block table: 2^16
-static constexpr uint32_t kTcBlockPairs = 2048;   // pairs per block task
+static constexpr uint32_t kTcBlockSlots = 8192;   // hash slots of a block table (>= 4 kTcBlockCap)
+static constexpr uint32_t kTcBlockPairs = 4096;   // pairs per block task
 static constexpr int kTcWarpKernelWarps = 8;
 static constexpr int kTcBlockThreads = 512;
 static constexpr uint32_t kTcSortWarpCap = 1024;  // N+ rows up to this are sorted by one warp
@@ -400,204 +401,159 @@ __device__ __forceinline__ uint32_t tc_mid3(uint32_t a, uint32_t b, uint32_t c)
 }
 
 __device__ __forceinline__ uint32_t tc_hash(uint32_t w, int lg) { return (w * 0x9E3779B1u) >> (32 - lg); }
-__device__ __forceinline__ uint32_t tc_bloom_bit(uint32_t w, int bbits) { return (w * 0x85EBCA6Bu) >> (32 - bbits); }
 
-// Membership in N+(y): one-hash Bloom bits for a branch-free first test, a
-// shared-memory table (rank -> index in the row) for the candidates; rows
-// longer than the block table use a binary search in the sorted row in
-// global memory instead (no Bloom bits, every element is a candidate).
+// The table of one task's N+(y): open addressing (rank -> index in the row)
+// with at least 4 slots per element, so that nearly every probe ends at its
+// first slot; the ids of the row's elements (lid) and one counter per
+// element (cn).
 template <class IDX>
 struct TcTable
 {
   const uint32_t* key;
   const IDX* idx;
-  const uint32_t* bloom;
+  const uint32_t* lid;
+  uint32_t* cn;
   uint32_t mask;
-  int lg, bbits;
-  const uint32_t* __restrict__ row;  // global row (search mode), else null
-  uint32_t d;
-  __device__ __forceinline__ bool maybe(uint32_t w) const
-  {
-    if (!bloom) return true;
-    const uint32_t h = tc_bloom_bit(w, bbits);
-    return (bloom[h >> 5] >> (h & 31)) & 1u;
-  }
-  __device__ __forceinline__ int find(uint32_t w) const
-  {
-    if (row)
-    {
-      uint32_t lo = 0, hi = d;
-      while (lo < hi)
-      {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (row[mid] < w) lo = mid + 1;
-        else hi = mid;
-      }
-      return (lo < d && row[lo] == w) ? (int) lo : -1;
-    }
-    uint32_t sl = tc_hash(w, lg);
-    for (;;)
-    {
-      const uint32_t k = key[sl];
-      if (k == w) return idx[sl];
-      if (k == kEmpty) return -1;
-      sl = (sl + 1) & mask;
-    }
-  }
+  int lg;
 };
 
-// Per-warp batch state: up to 32 pairs with non-empty suffixes, compacted,
-// and the queue of candidate elements (those that pass the Bloom test),
-// resolved 32 at a time so that the table probes and the counting run with
-// all lanes.
-struct TcBatch
+// Per-warp round state (shared memory): the compacted pairs' (suffix start
+// minus walk offset), walk offset and x id, and the triangles counted at
+// each pair's x.
+struct TcRound
 {
-  uint32_t start[32];  // suffix start in pcol
-  uint32_t off[32];    // offset of the pair's first element in the batch's walk
-  uint32_t len[32];    // suffix length
+  uint32_t so[32];
+  uint32_t off[32];
   uint32_t xid[32];
-  uint32_t cx[32];     // triangles counted at x
-  uint32_t qw[64];     // queued candidates (ring)
-  uint8_t qk[64];      // ... and their pair's index in the batch
+  uint32_t cx[32];
 };
 
-// Resolves queue entries [qh, qh + cnt) (cnt <= 32, one per lane).
-template <class IDX>
-__device__ __forceinline__ void tc_drain(TcBatch& B, uint32_t qh, uint32_t cnt, const TcTable<IDX>& T, uint32_t yid,
-                                         const uint32_t* lid, uint32_t* cn, const uint32_t* __restrict__ id_of_rank,
-                                         uint32_t& cy, uint32_t* ntri, unsigned long long* err)
+// Counts the element w (of the suffix of the pair at lane k of this round)
+// against N+(y): a hit closes {x, y, w}; its middle id takes the count - x
+// in the round's cx[k], y in cy, w in cn[j].  SEARCH: N+(y) too long for a
+// table, binary search in the sorted global row, w's count straight to ntri.
+template <class IDX, bool SEARCH>
+__device__ __forceinline__ void tc_probe(uint32_t w, uint32_t k, uint32_t xo, uint32_t yid, const TcTable<IDX>& T,
+                                         const uint32_t* __restrict__ row, uint32_t d,
+                                         const uint32_t* __restrict__ id_of_rank, TcRound& R, uint32_t& cy,
+                                         uint32_t* ntri)
 {
-  const uint32_t lane = threadIdx.x & 31;
-  __syncwarp();
-  if (lane < cnt)
+  if (w == kEmpty) return;
+  int j = -1;
+  if (SEARCH)
   {
-    const uint32_t pos = (qh + lane) & 63;
-    const uint32_t w = B.qw[pos], k = B.qk[pos];
-    const int j = T.find(w);
-    if (j >= (int) T.d) atomicAdd(err, 1ull << 32);
-    else if (j >= 0)
+    uint32_t lo = 0, hi = d;
+    while (lo < hi)
     {
-      const uint32_t xo = B.xid[k];
-      const uint32_t wid = lid ? lid[j] : id_of_rank[w];
-      const uint32_t mid = tc_mid3(xo, yid, wid);
-      if (mid == yid) cy++;
-      else if (mid == xo) atomicAdd(&B.cx[k], 1u);
-      else if (cn) atomicAdd(&cn[j], 1u);
-      else atomicAdd(&ntri[wid], 1u);
+      const uint32_t mid = (lo + hi) >> 1;
+      if (row[mid] < w) lo = mid + 1;
+      else hi = mid;
     }
+    if (lo < d && row[lo] == w) j = (int) lo;
   }
-  __syncwarp();
+  else
+  {
+    uint32_t sl = tc_hash(w, T.lg), kk = T.key[sl];
+    while (kk != w && kk != kEmpty)
+    {
+      sl = (sl + 1) & T.mask;
+      kk = T.key[sl];
+    }
+    if (kk == w) j = T.idx[sl];
+  }
+  if (j < 0) return;
+  const uint32_t wid = SEARCH ? id_of_rank[w] : T.lid[j];
+  const uint32_t mid = tc_mid3(xo, yid, wid);
+  if (mid == yid) cy++;
+  else if (mid == xo) atomicAdd(&R.cx[k], 1u);
+  else if (SEARCH) atomicAdd(&ntri[wid], 1u);
+  else atomicAdd(&T.cn[j], 1u);
 }
 
-// One warp walks pairs [p0, p1) of y against table T, 32 pairs per round:
-// the suffixes of a round are concatenated and read 64 elements per step
-// (two 32-element windows, loads in flight together); element w0 + lane
-// belongs to the pair whose start offset is the last one at or below it,
-// found from the window's start bits and the count of pairs started
-// before it.  Hits whose middle id is y go to cy, at x to the pair's shared
-// counter, at an element of N+(y) to cn[index] (or straight to ntri in
-// search mode).
-template <class IDX>
-__device__ __forceinline__ void tc_walk_pairs(uint32_t p0, uint32_t p1, const uint2* __restrict__ pairs,
-                                              const uint32_t* __restrict__ pptr, const uint32_t* __restrict__ pcol,
-                                              const uint32_t* __restrict__ id_of_rank, uint32_t yid,
-                                              const TcTable<IDX>& T, const uint32_t* lid, uint32_t* cn, TcBatch& B,
-                                              uint32_t& cy, unsigned long long& walked, uint32_t* ntri,
-                                              unsigned long long* err)
+// One warp walks one round: pairs [p0, p1) (at most 32) of y.  The pairs'
+// suffixes are concatenated and read 64 elements per step (two 32-element
+// windows whose loads are in flight together).  Element t belongs to the
+// compacted pair k whose walk offset is the last at or below t: k = (pairs
+// started before the window) + (pairs starting in the window at or below
+// the lane) - 1, from one OR-reduction of the window's start bits; the
+// owner's (start - offset) and x id come from its lane by shuffle, so the
+// address of element t is so[k] + t.
+template <class IDX, bool SEARCH>
+__device__ __forceinline__ void tc_round(uint32_t p0, uint32_t p1, const uint2* __restrict__ pairs,
+                                         const uint32_t* __restrict__ pptr, const uint32_t* __restrict__ pcol,
+                                         const uint32_t* __restrict__ id_of_rank, uint32_t yid, const TcTable<IDX>& T,
+                                         const uint32_t* __restrict__ row, uint32_t d, TcRound& R, uint32_t& cy,
+                                         unsigned long long& walked, uint32_t* ntri, unsigned long long* err)
 {
   const uint32_t lane = threadIdx.x & 31;
   const unsigned full = 0xffffffffu;
   const unsigned lt = (1u << lane) - 1, le = lane == 31 ? full : ((2u << lane) - 1);
-  for (uint32_t pb = p0; pb < p1; pb += 32)
+  const uint32_t p = p0 + lane;
+  uint32_t s = 0, L = 0, xid = 0;
+  if (p < p1)
   {
-    const uint32_t p = pb + lane;
-    uint32_t s = 0, L = 0, xid = 0;
-    if (p < p1)
-    {
-      const uint2 px = pairs[p];
-      s = px.x;
-      L = pptr[px.y + 1] - s;
-      xid = id_of_rank[px.y];
-    }
-    const unsigned nz = __ballot_sync(full, L > 0);
-    uint32_t incl = L;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1)
-    {
-      const uint32_t v = __shfl_up_sync(full, incl, o);
-      if (lane >= (uint32_t) o) incl += v;
-    }
-    const uint32_t total = __shfl_sync(full, incl, 31);
-    if (L > 0)
-    {
-      const uint32_t k = __popc(nz & lt);
-      B.start[k] = s;
-      B.off[k] = incl - L;
-      B.len[k] = L;
-      B.xid[k] = xid;
-      B.cx[k] = 0;
-    }
-    __syncwarp();
-    const uint32_t npairs = __popc(nz);
-    // lane k holds the start offset of the k-th compacted pair
-    const uint32_t pk = lane < npairs ? B.off[lane] : kEmpty;
-    uint32_t qh = 0, qn = 0;
-    for (uint32_t w0 = 0; w0 < total; w0 += 64)
-    {
-      uint32_t wv[2], kv[2];
-      bool okv[2];
-#pragma unroll
-      for (int u = 0; u < 2; u++)
-      {
-        const uint32_t base = w0 + 32u * u;
-        const uint32_t bit = (pk >= base && pk < base + 32) ? (1u << (pk - base)) : 0u;
-        const unsigned starts = __reduce_or_sync(full, bit);
-        const uint32_t before = __popc(__ballot_sync(full, pk < base));
-        const uint32_t t = base + lane;
-        const uint32_t k = min(before + __popc(starts & le) - 1u, 31u);
-        // the owner lies in this round and t inside its suffix (by
-        // construction; checked so that a slip cannot turn into a fault)
-        const bool ok = t < total && k < npairs && t >= B.off[k] && t - B.off[k] < B.len[k];
-        if (t < total && !ok) atomicAdd(err, 1ull);
-        wv[u] = ok ? pcol[B.start[k] + (t - B.off[k])] : kEmpty;
-        kv[u] = k;
-        okv[u] = ok;
-      }
-#pragma unroll
-      for (int u = 0; u < 2; u++)
-      {
-        const bool cand = okv[u] && T.maybe(wv[u]);
-        const unsigned m = __ballot_sync(full, cand);
-        if (cand)
-        {
-          const uint32_t pos = (qh + qn + __popc(m & lt)) & 63;
-          B.qw[pos] = wv[u];
-          B.qk[pos] = (uint8_t) kv[u];
-        }
-        qn += __popc(m);
-        if (qn >= 32)
-        {
-          tc_drain(B, qh, 32, T, yid, lid, cn, id_of_rank, cy, ntri, err);
-          qh = (qh + 32) & 63;
-          qn -= 32;
-        }
-      }
-    }
-    if (qn) tc_drain(B, qh, qn, T, yid, lid, cn, id_of_rank, cy, ntri, err);
-    walked += total;
-    __syncwarp();
-    if (lane < npairs && B.cx[lane]) atomicAdd(&ntri[B.xid[lane]], B.cx[lane]);
-    __syncwarp();
+    const uint2 px = pairs[p];
+    s = px.x;
+    L = pptr[px.y + 1] - s;
+    xid = id_of_rank[px.y];
   }
+  const unsigned nz = __ballot_sync(full, L > 0);
+  uint32_t incl = L;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1)
+  {
+    const uint32_t v = __shfl_up_sync(full, incl, o);
+    if (lane >= (uint32_t) o) incl += v;
+  }
+  const uint32_t total = __shfl_sync(full, incl, 31);
+  if (L > 0)
+  {
+    const uint32_t k = __popc(nz & lt);
+    R.so[k] = s - (incl - L);
+    R.off[k] = incl - L;
+    R.xid[k] = xid;
+  }
+  __syncwarp();
+  const uint32_t np = __popc(nz);
+  // lane k holds the k-th compacted pair
+  const uint32_t pk = lane < np ? R.off[lane] : kEmpty;
+  const uint32_t my_so = lane < np ? R.so[lane] : 0u;
+  const uint32_t my_x = lane < np ? R.xid[lane] : 0u;
+  R.cx[lane] = 0;
+  __syncwarp();
+  uint32_t before = 0;
+  for (uint32_t w0 = 0; w0 < total; w0 += 64)
+  {
+    const uint32_t ra = pk - w0, rb = pk - (w0 + 32);
+    const unsigned sa = __reduce_or_sync(full, ra < 32 ? 1u << ra : 0u);
+    const unsigned sb = __reduce_or_sync(full, rb < 32 ? 1u << rb : 0u);
+    const uint32_t ka = (before + __popc(sa & le) - 1u) & 31u;
+    before += __popc(sa);
+    const uint32_t kb = (before + __popc(sb & le) - 1u) & 31u;
+    before += __popc(sb);
+    const uint32_t ta = w0 + lane, tb = ta + 32;
+    const uint32_t soa = __shfl_sync(full, my_so, ka), sob = __shfl_sync(full, my_so, kb);
+    const uint32_t xa = __shfl_sync(full, my_x, ka), xb = __shfl_sync(full, my_x, kb);
+    // by construction every element below total has an owner in this round
+    if ((ta < total && ka >= np) || (tb < total && kb >= np)) atomicAdd(err, 1ull);
+    const uint32_t wa = (ta < total && ka < np) ? pcol[soa + ta] : kEmpty;
+    const uint32_t wb = (tb < total && kb < np) ? pcol[sob + tb] : kEmpty;
+    tc_probe<IDX, SEARCH>(wa, ka, xa, yid, T, row, d, id_of_rank, R, cy, ntri);
+    tc_probe<IDX, SEARCH>(wb, kb, xb, yid, T, row, d, id_of_rank, R, cy, ntri);
+  }
+  walked += total;
+  __syncwarp();
+  if (lane < np && R.cx[lane]) atomicAdd(&ntri[my_x], R.cx[lane]);
+  __syncwarp();
 }
 
-// Builds the table and Bloom bits of N+(y) (d elements at row) with
-// `nthreads` threads starting at thread `tid`; the caller clears the table
-// and the bits and synchronises before and after.
+// Builds the table of N+(y) (d elements at row) with `nthreads` threads
+// starting at thread `tid`; the caller clears the keys and synchronises
+// before and after.
 template <class IDX>
-__device__ __forceinline__ void tc_build(const uint32_t* __restrict__ row, uint32_t d, int lg, int bbits,
+__device__ __forceinline__ void tc_build(const uint32_t* __restrict__ row, uint32_t d, int lg,
                                          const uint32_t* __restrict__ id_of_rank, uint32_t* key, IDX* idx,
-                                         uint32_t* bloom, uint32_t* lid, uint32_t* cn, uint32_t tid, uint32_t nthreads)
+                                         uint32_t* lid, uint32_t* cn, uint32_t tid, uint32_t nthreads)
 {
   const uint32_t mask = (1u << lg) - 1;
   for (uint32_t j = tid; j < d; j += nthreads)
@@ -608,40 +564,36 @@ __device__ __forceinline__ void tc_build(const uint32_t* __restrict__ row, uint3
     uint32_t sl = tc_hash(w, lg);
     while (atomicCAS(&key[sl], kEmpty, w) != kEmpty) sl = (sl + 1) & mask;
     idx[sl] = (IDX) j;
-    const uint32_t h = tc_bloom_bit(w, bbits);
-    atomicOr(&bloom[h >> 5], 1u << (h & 31));
   }
 }
 
+// log2 of the table size: at least 4 slots per element, at least 32 slots.
 __device__ __forceinline__ int tc_lg(uint32_t d)
 {
   int lg = 5;
-  while ((1u << lg) < 2 * d) lg++;
+  while ((1u << lg) < 4 * d) lg++;
   return lg;
 }
 
-// Warp tasks: |N+(y)| <= kTcWarpCap, a table per warp in static shared
-// memory (indices fit a byte).
+// Warp tasks: |N+(y)| <= kTcWarpCap, one table per warp in static shared
+// memory (indices fit a byte), rounds of 32 pairs in turn.
 template <int WARPS>
-__global__ void __launch_bounds__(WARPS * 32)
+__global__ void __launch_bounds__(WARPS * 32, 5)
 k_tc_count_warp(const uint32_t* __restrict__ pptr, const uint32_t* __restrict__ pcol, const uint2* __restrict__ pairs,
                 const uint32_t* __restrict__ mptr, const uint2* __restrict__ tasks,
                 const unsigned long long* __restrict__ ntasks_packed, const uint32_t* __restrict__ id_of_rank,
                 uint32_t* ntri, unsigned long long* ctr)
 {
-  constexpr int kBloomWords = (1 << kTcWarpBloomBits) / 32;
   __shared__ uint32_t s_key[WARPS][kTcWarpSlots];
   __shared__ uint8_t s_idx[WARPS][kTcWarpSlots];
   __shared__ uint32_t s_lid[WARPS][kTcWarpCap];
   __shared__ uint32_t s_cn[WARPS][kTcWarpCap];
-  __shared__ uint32_t s_bloom[WARPS][kBloomWords];
-  __shared__ TcBatch s_b[WARPS];
+  __shared__ TcRound s_r[WARPS];
   const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
   uint32_t* key = s_key[wi];
   uint8_t* idx = s_idx[wi];
   uint32_t* lid = s_lid[wi];
   uint32_t* cn = s_cn[wi];
-  uint32_t* bloom = s_bloom[wi];
   const uint32_t ntasks = (uint32_t) *ntasks_packed;
   unsigned long long walked = 0, built = 0;
   for (;;)
@@ -656,15 +608,16 @@ k_tc_count_warp(const uint32_t* __restrict__ pptr, const uint32_t* __restrict__ 
     if (d == 0 || d > kTcWarpCap) continue;  // not a warp task (never built so)
     const int lg = tc_lg(d);
     for (uint32_t i = lane; i < (1u << lg); i += 32) key[i] = kEmpty;
-    for (uint32_t i = lane; i < kBloomWords; i += 32) bloom[i] = 0;
     __syncwarp();
-    tc_build<uint8_t>(pcol + yb, d, lg, kTcWarpBloomBits, id_of_rank, key, idx, bloom, lid, cn, lane, 32);
+    tc_build<uint8_t>(pcol + yb, d, lg, id_of_rank, key, idx, lid, cn, lane, 32);
     __syncwarp();
     built += d;
-    const TcTable<uint8_t> T{key, idx, bloom, (1u << lg) - 1, lg, kTcWarpBloomBits, nullptr, d};
+    const TcTable<uint8_t> T{key, idx, lid, cn, (1u << lg) - 1, lg};
     const uint32_t yid = id_of_rank[y];
     uint32_t cy = 0;
-    tc_walk_pairs(p0, p1, pairs, pptr, pcol, id_of_rank, yid, T, lid, cn, s_b[wi], cy, walked, ntri, ctr + 5);
+    for (uint32_t q = p0; q < p1; q += 32)
+      tc_round<uint8_t, false>(q, min(q + 32u, p1), pairs, pptr, pcol, id_of_rank, yid, T, nullptr, d, s_r[wi], cy,
+                               walked, ntri, ctr + 5);
     for (int o = 16; o > 0; o >>= 1) cy += __shfl_xor_sync(0xffffffffu, cy, o);
     if (lane == 0 && cy) atomicAdd(&ntri[yid], cy);
     __syncwarp();
@@ -680,8 +633,9 @@ k_tc_count_warp(const uint32_t* __restrict__ pptr, const uint32_t* __restrict__ 
 }
 
 // Block tasks: |N+(y)| > kTcWarpCap; one table per block in dynamic shared
-// memory, or a global binary search above kTcBlockCap.  The per-warp batch
-// state stays in static shared memory.
+// memory (or a global binary search above kTcBlockCap); the warps take the
+// task's 32-pair rounds from a shared counter.  The per-warp round state
+// stays in static shared memory.
 template <int THREADS>
 __global__ void __launch_bounds__(THREADS)
 k_tc_count_block(const uint32_t* __restrict__ pptr, const uint32_t* __restrict__ pcol, const uint2* __restrict__ pairs,
@@ -690,15 +644,13 @@ k_tc_count_block(const uint32_t* __restrict__ pptr, const uint32_t* __restrict__
                  uint32_t* ntri, unsigned long long* ctr)
 {
   constexpr int WARPS = THREADS / 32;
-  constexpr int kBloomWords = (1 << kTcBlockBloomBits) / 32;
   extern __shared__ __align__(16) uint32_t tc_smem[];
   uint32_t* key = tc_smem;                          // [kTcBlockSlots]
   uint32_t* lid = key + kTcBlockSlots;              // [kTcBlockCap]
   uint32_t* cn = lid + kTcBlockCap;                 // [kTcBlockCap]
-  uint32_t* bloom = cn + kTcBlockCap;               // [kBloomWords]
-  uint16_t* idx = (uint16_t*) (bloom + kBloomWords);  // [kTcBlockSlots]
-  __shared__ TcBatch s_b[WARPS];
-  __shared__ uint32_t s_t, s_cy;
+  uint16_t* idx = (uint16_t*) (cn + kTcBlockCap);   // [kTcBlockSlots]
+  __shared__ TcRound s_r[WARPS];
+  __shared__ uint32_t s_t, s_cy, s_round;
   const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
   const uint32_t ntasks = (uint32_t) (*ntasks_packed >> 32);
   unsigned long long walked = 0, built = 0;
@@ -708,6 +660,7 @@ k_tc_count_block(const uint32_t* __restrict__ pptr, const uint32_t* __restrict__
     {
       s_t = (uint32_t) atomicAdd(&ctr[1], 1ull);
       s_cy = 0;
+      s_round = 0;
     }
     __syncthreads();
     const uint32_t t = s_t;
@@ -720,21 +673,28 @@ k_tc_count_block(const uint32_t* __restrict__ pptr, const uint32_t* __restrict__
     if (!search)
     {
       for (uint32_t i = threadIdx.x; i < (1u << lg); i += THREADS) key[i] = kEmpty;
-      for (uint32_t i = threadIdx.x; i < kBloomWords; i += THREADS) bloom[i] = 0;
       __syncthreads();
-      tc_build<uint16_t>(pcol + yb, d, lg, kTcBlockBloomBits, id_of_rank, key, idx, bloom, lid, cn, threadIdx.x,
-                         THREADS);
+      tc_build<uint16_t>(pcol + yb, d, lg, id_of_rank, key, idx, lid, cn, threadIdx.x, THREADS);
       if (threadIdx.x == 0) built += d;
     }
     __syncthreads();
-    const TcTable<uint16_t> T{key, idx, search ? nullptr : bloom, (1u << lg) - 1, lg, kTcBlockBloomBits,
-                              search ? pcol + yb : nullptr, d};
+    const TcTable<uint16_t> T{key, idx, lid, cn, (1u << lg) - 1, lg};
     const uint32_t yid = id_of_rank[y];
     uint32_t cy = 0;
-    // the warps take 32-pair rounds of the slice in turn
-    for (uint32_t q = p0 + 32u * wi; q < p1; q += 32u * WARPS)
-      tc_walk_pairs(q, min(q + 32u, p1), pairs, pptr, pcol, id_of_rank, yid, T, search ? nullptr : lid,
-                    search ? nullptr : cn, s_b[wi], cy, walked, ntri, ctr + 5);
+    for (;;)
+    {
+      uint32_t r = 0;
+      if (lane == 0) r = atomicAdd(&s_round, 1u);
+      r = __shfl_sync(0xffffffffu, r, 0);
+      const uint32_t q = p0 + 32u * r;
+      if (q >= p1) break;
+      if (search)
+        tc_round<uint16_t, true>(q, min(q + 32u, p1), pairs, pptr, pcol, id_of_rank, yid, T, pcol + yb, d, s_r[wi],
+                                 cy, walked, ntri, ctr + 5);
+      else
+        tc_round<uint16_t, false>(q, min(q + 32u, p1), pairs, pptr, pcol, id_of_rank, yid, T, nullptr, d, s_r[wi],
+                                  cy, walked, ntri, ctr + 5);
+    }
     for (int o = 16; o > 0; o >>= 1) cy += __shfl_xor_sync(0xffffffffu, cy, o);
     if (lane == 0 && cy) atomicAdd(&s_cy, cy);
     __syncthreads();
@@ -750,7 +710,7 @@ k_tc_count_block(const uint32_t* __restrict__ pptr, const uint32_t* __restrict__
 }
 
 static constexpr size_t kTcBlockSmem = (size_t) kTcBlockSlots * 4 + 2 * (size_t) kTcBlockCap * 4 +
-                                       (size_t) (1 << kTcBlockBloomBits) / 8 + (size_t) kTcBlockSlots * 2;
+                                       (size_t) kTcBlockSlots * 2;
 static constexpr size_t kTcSortBigSmem = (size_t) kTcSortBlockCap * 4;
 
 __global__ void k_tc_sum(uint32_t N, const uint32_t* __restrict__ ntri, unsigned long long* total)
@@ -936,10 +896,10 @@ extern "C" int la3g_tc(la3g_graph* G, uint64_t* total_out, uint32_t* per_vertex_
     {
       // pass 2; its bytes (walked list elements, pairs, tables) are added below
       ProfileScope p("tc_count", s, 0.0);
-      k_tc_count_warp<kTcWarpKernelWarps><<<kSMs * 4, kTcWarpKernelWarps * 32, 0, s>>>(
+      k_tc_count_warp<kTcWarpKernelWarps><<<kSMs * 5, kTcWarpKernelWarps * 32, 0, s>>>(
           ts->pptr, ts->pcol, ts->pairs, ts->mptr, ts->wtasks, ts->toff + N, ts->id_of_rank, ts->ntri, ts->ctr);
       LA3G_LAUNCHED();
-      k_tc_count_block<kTcBlockThreads><<<kSMs * 2, kTcBlockThreads, kTcBlockSmem, s>>>(
+      k_tc_count_block<kTcBlockThreads><<<kSMs * 3, kTcBlockThreads, kTcBlockSmem, s>>>(
           ts->pptr, ts->pcol, ts->pairs, ts->mptr, ts->btasks, ts->toff + N, ts->id_of_rank, ts->ntri, ts->ctr);
       LA3G_LAUNCHED();
       tls_launches++;
