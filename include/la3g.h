@@ -357,11 +357,15 @@ void la3g_server_free(la3g_server* s);
  * with the largest key (with key = the hashed id of the reference's bucket
  * hasher, hops and parent equal la3g_bfs's).  The library's temporaries sit in
  * one fixed device array of about 12.8 MB, so nvertices is limited to
- * 1048576 (2^20); larger graphs are rejected with LA3G_EINVAL.  The first
- * call on a device looks the array up and caches its address: make that call
- * before capturing a stream.  Calls share the array, so calls that overlap on
- * the GPU race; run them one at a time.  cuda_stream: a cudaStream_t as void*
- * (NULL = the default stream).  st may be NULL. */
+ * 1048576 (2^20); larger graphs are rejected with LA3G_EINVAL.  Each call
+ * looks up the array's address on the current device (no allocation).  The
+ * call waits for its stream at every BFS level, since it reads the frontier
+ * size back to the host, and again before it returns, also after an error.
+ * Calls share the array, so calls that overlap on the GPU race; run them one
+ * at a time.  row_ptr must be non-decreasing with row_ptr[nvertices] = the
+ * entry count; that is not checked, while neighbour ids >= nvertices are
+ * skipped.  cuda_stream: a cudaStream_t as void* (NULL = the default
+ * stream).  st may be NULL. */
 int la3g_bfs_noalloc(const uint32_t* row_ptr, const uint32_t* col, const uint32_t* key, uint32_t nvertices,
                      uint32_t root, uint8_t* hops, uint32_t* parent, void* cuda_stream, la3g_stats* st);
 

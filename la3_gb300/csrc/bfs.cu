@@ -80,8 +80,8 @@ __global__ void k_bfs_init(uint32_t N, uint8_t* hops, uint32_t* parent, uint32_t
 // Top-down: one warp per frontier vertex, lanes over its neighbours.
 __global__ void __launch_bounds__(256)
 k_bfs_td(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ hash_of_pos,
-         const uint32_t* __restrict__ front, uint32_t nfront, const uint8_t* __restrict__ hops, uint32_t* cand,
-         uint32_t* next, BfsCounters* ctr)
+         uint32_t N, const uint32_t* __restrict__ front, uint32_t nfront, const uint8_t* __restrict__ hops,
+         uint32_t* cand, uint32_t* next, BfsCounters* ctr)
 {
   const int lane = threadIdx.x & 31;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -99,7 +99,7 @@ k_bfs_td(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, con
       if (i < e)
       {
         v = col[i];
-        if (hops[v] == 255)
+        if (v < N && hops[v] == 255)  // a neighbour id outside the graph is skipped
         {
           uint32_t old = atomicMax(&cand[v], hu);
           add = old == 0;
@@ -149,7 +149,7 @@ k_bfs_bu(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, con
     for (uint32_t i = e; i > b; i--)
     {
       const uint32_t u = col[i - 1];
-      if (fbits[u >> 5] & (1u << (u & 31)))
+      if (u < nrows && (fbits[u >> 5] & (1u << (u & 31))))  // ids outside the graph are skipped
       {
         hops[v] = hop;
         parent[v] = hash_of_pos[u];
@@ -607,15 +607,17 @@ extern "C" int la3g_bfs(la3g_graph* G, uint32_t root, uint8_t* hops_out, uint32_
 // array: each GPU that loads this library holds it (kNoAllocScratchBytes,
 // about 12.8 MB) until the process exits.  Host code must not hand the
 // array's name to a kernel (on the host it only names a stand-in object);
-// its device address is looked up once per device with
-// cudaGetSymbolAddress, on the first call made while that device is
-// current, and cached.  That first call therefore does the set-up and should
-// come before any stream capture that includes this entry point.
+// every call looks up its device address on the current device with
+// cudaGetSymbolAddress (which allocates nothing), so the address stays right
+// for whichever device and context is current.
 //
 // All calls share the one array and it keeps whatever the last call left in
 // it; the call clears what has to start at zero.  Two calls whose work
 // overlaps on the GPU (different streams, or different host threads on one
-// device) race on the array: serialise them.
+// device) race on the array: serialise them.  The call waits for its stream
+// at every BFS level (it reads the frontier size back), and before it
+// returns, on success and on every error after its first launch, so no work
+// of a finished call is left running on the array.
 // ---------------------------------------------------------------------------
 
 namespace la3g {
@@ -635,32 +637,27 @@ static constexpr size_t kNoAllocScratchBytes = kNaRedOff + na_round(sizeof(unsig
 
 static __device__ __align__(256) unsigned char g_bfs_noalloc_scratch[kNoAllocScratchBytes];
 
-static std::mutex g_noalloc_mu;
-static void* g_noalloc_addr[256];
-
-// Device address of the scratch array for the current device (looked up
-// once per device).
+// Device address of the scratch array on the current device.
 static int noalloc_scratch(unsigned char** out)
 {
-  int dev = 0;
-  LA3G_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 256) return set_error(LA3G_EINVAL, "device ordinal %d out of range", dev);
-  std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_addr[dev])
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_bfs_noalloc_scratch);
+  if (e != cudaSuccess || !p)
   {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_bfs_noalloc_scratch);
-    if (e != cudaSuccess || !p)
-    {
-      cudaGetLastError();
-      return set_error(LA3G_ECUDA, "cudaGetSymbolAddress(scratch) failed on device %d: %s", dev,
-                       cudaGetErrorString(e));
-    }
-    g_noalloc_addr[dev] = p;
+    cudaGetLastError();
+    return set_error(LA3G_ECUDA, "cudaGetSymbolAddress(scratch) failed: %s", cudaGetErrorString(e));
   }
-  *out = (unsigned char*) g_noalloc_addr[dev];
+  *out = (unsigned char*) p;
   return LA3G_OK;
 }
+
+}  // namespace la3g
+
+namespace la3g {
+
+static int bfs_noalloc_run(const uint32_t* row_ptr, const uint32_t* col, const uint32_t* key, uint32_t nvertices,
+                           uint32_t root, uint8_t* hops, uint32_t* parent, cudaStream_t s, la3g_stats* st,
+                           bool* launched);
 
 }  // namespace la3g
 
@@ -676,9 +673,26 @@ extern "C" int la3g_bfs_noalloc(const uint32_t* row_ptr, const uint32_t* col, co
                      nvertices, kNoAllocMaxVertices);
   if (!row_ptr || !col || !key || !hops || !parent)
     return set_error(LA3G_EINVAL, "la3g_bfs_noalloc: row_ptr, col, key, hops and parent must be device pointers");
+  cudaStream_t s = (cudaStream_t) cuda_stream;
+  bool launched = false;
+  const int rc = bfs_noalloc_run(row_ptr, col, key, nvertices, root, hops, parent, s, st, &launched);
+  if (rc != LA3G_OK && launched)
+  {
+    // let the work already queued finish before the caller may reuse the array
+    cudaStreamSynchronize(s);
+    cudaGetLastError();
+  }
+  return rc;
+}
+
+namespace la3g {
+
+static int bfs_noalloc_run(const uint32_t* row_ptr, const uint32_t* col, const uint32_t* key, uint32_t nvertices,
+                           uint32_t root, uint8_t* hops, uint32_t* parent, cudaStream_t s, la3g_stats* st,
+                           bool* launched)
+{
   unsigned char* base = nullptr;
   LA3G_TRY(noalloc_scratch(&base));
-  cudaStream_t s = (cudaStream_t) cuda_stream;
   uint32_t* cand = (uint32_t*) (base + kNaCandOff);
   uint32_t* list[2] = {(uint32_t*) (base + kNaList0Off), (uint32_t*) (base + kNaList1Off)};
   uint32_t* bits[2] = {(uint32_t*) (base + kNaBits0Off), (uint32_t*) (base + kNaBits1Off)};
@@ -689,6 +703,7 @@ extern "C" int la3g_bfs_noalloc(const uint32_t* row_ptr, const uint32_t* col, co
   double t0 = now_ms();
 
   // hops = 255, parent = 0 and the candidates cleared (they must start at 0)
+  *launched = true;
   k_bfs_init<<<grid_for(N, 256), 256, 0, s>>>(N, hops, parent, cand);
   LA3G_LAUNCHED();
   uint32_t iter = 0, pull_iters = 0;
@@ -737,8 +752,8 @@ extern "C" int la3g_bfs_noalloc(const uint32_t* row_ptr, const uint32_t* col, co
           k_bits_to_list<<<grid_for(words, 256), 256, 0, s>>>(bits[cur], words, list[cur], red);
           LA3G_LAUNCHED();
         }
-        k_bfs_td<<<grid_for(nfront * 32, 256), 256, 0, s>>>(row_ptr, col, key, list[cur], (uint32_t) nfront, hops, cand,
-                                                            list[cur ^ 1], ctr);
+        k_bfs_td<<<grid_for(nfront * 32, 256), 256, 0, s>>>(row_ptr, col, key, N, list[cur], (uint32_t) nfront, hops,
+                                                            cand, list[cur ^ 1], ctr);
         LA3G_LAUNCHED();
         LA3G_CUDA(cudaMemcpyAsync(&h, ctr, sizeof h, cudaMemcpyDeviceToHost, s));
         LA3G_CUDA(cudaStreamSynchronize(s));
@@ -773,3 +788,5 @@ extern "C" int la3g_bfs_noalloc(const uint32_t* row_ptr, const uint32_t* col, co
   }
   return LA3G_OK;
 }
+
+}  // namespace la3g
