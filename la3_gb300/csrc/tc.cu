@@ -53,14 +53,18 @@ static constexpr uint32_t kTcEdgesPerThread = 8;  // edge-parallel passes: conti
 static constexpr uint32_t kTcWarpCap = 128;       // |N+(y)| up to this: a warp per task
 static constexpr uint32_t kTcWarpSlots = 512;     // hash slots of a warp table (>= 4 kTcWarpCap)
 static constexpr uint32_t kTcWarpPairs = 256;     // pairs per warp task
-static constexpr uint32_t kTcBlockCap = 2048;     // |N+(y)| up to this: a block table; longer: global search
-static constexpr uint32_t kTcBlockSlots = 8192;   // hash slots of a block table (>= 4 kTcBlockCap)
-static constexpr uint32_t kTcBlockPairs = 4096;   // pairs per block task
+static constexpr uint32_t kTcMidCap = 512;        // |N+(y)| up to this: a small block per task
+static constexpr uint32_t kTcMidSlots = 2048;     // hash slots of its table (>= 4 kTcMidCap)
+static constexpr uint32_t kTcBlockCap = 2048;     // |N+(y)| up to this: a large block table; longer: global search
+static constexpr uint32_t kTcBlockSlots = 8192;   // hash slots of a large block table (>= 4 kTcBlockCap)
+static constexpr uint32_t kTcBlockPairs = 4096;   // pairs per block task (both block sizes)
 static constexpr int kTcWarpKernelWarps = 8;
+static constexpr int kTcMidThreads = 256;
 static constexpr int kTcBlockThreads = 512;
 static constexpr uint32_t kTcSortWarpCap = 1024;  // N+ rows up to this are sorted by one warp
 static constexpr uint32_t kTcSortBlockCap = 16384;  // ... up to this by one block; longer: library sort
 static constexpr uint32_t kEmpty = 0xFFFFFFFFu;
+static constexpr int kTcCounters = 12;
 
 struct TcScratch
 {
@@ -80,15 +84,18 @@ struct TcScratch
   uint32_t* mcount = nullptr;       // [N + 1] pairs per y
   uint32_t* mptr = nullptr;         // [N + 1] pair offsets per y
   uint2* pairs = nullptr;           // [m] (suffix start in pcol, x) grouped by y
-  unsigned long long* tcount = nullptr;  // [N + 1] tasks per y: block << 32 | warp
+  unsigned long long* tcount = nullptr;  // [N + 1] tasks per y: small block << 32 | warp
   unsigned long long* toff = nullptr;    // [N + 1] their exclusive sums
+  uint32_t* tcount2 = nullptr;      // [N + 1] large-block tasks per y
+  uint32_t* toff2 = nullptr;        // [N + 1] their exclusive sums
   uint2* wtasks = nullptr;          // (y, first pair) of the warp tasks
-  uint2* btasks = nullptr;          // ... and of the block tasks
+  uint2* mtasks = nullptr;          // ... of the small-block tasks
+  uint2* btasks = nullptr;          // ... and of the large-block tasks
   uint32_t* ntri = nullptr;         // [N] by id
   uint32_t* big_rows = nullptr;     // [N] N+ rows too long for a warp's sort
-  // [0] warp-task cursor [1] block-task cursor [2] walked [3] table builds
-  // [4] triangles [5] self-check failures [6] big rows [7] rows too long
-  // for the block sort
+  // [0] warp-task cursor [1] large-block-task cursor [2] walked [3] table
+  // builds [4] triangles [5] self-check failures [6] big rows [7] rows too
+  // long for the block sort [8] small-block-task cursor
   unsigned long long* ctr = nullptr;
   unsigned long long* hctr = nullptr;  // pinned mirror
   void* temp = nullptr;
@@ -176,11 +183,11 @@ k_tc_orient(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, 
 // Pairs per y (a y with an empty N+(y) closes no triangle as the middle
 // rank) and the tasks they form.
 __global__ void k_tc_pair_counts(uint32_t N, const uint32_t* __restrict__ pptr, const uint32_t* __restrict__ deg_of_rank,
-                                 uint32_t* mcount, unsigned long long* tcount)
+                                 uint32_t* mcount, unsigned long long* tcount, uint32_t* tcount2)
 {
   for (uint32_t y = blockIdx.x * blockDim.x + threadIdx.x; y <= N; y += gridDim.x * blockDim.x)
   {
-    uint32_t c = 0;
+    uint32_t c = 0, t2 = 0;
     unsigned long long t = 0;
     if (y < N)
     {
@@ -189,11 +196,13 @@ __global__ void k_tc_pair_counts(uint32_t N, const uint32_t* __restrict__ pptr, 
       if (c)
       {
         if (dp <= kTcWarpCap) t = (c + kTcWarpPairs - 1) / kTcWarpPairs;
-        else t = (unsigned long long) ((c + kTcBlockPairs - 1) / kTcBlockPairs) << 32;
+        else if (dp <= kTcMidCap) t = (unsigned long long) ((c + kTcBlockPairs - 1) / kTcBlockPairs) << 32;
+        else t2 = (c + kTcBlockPairs - 1) / kTcBlockPairs;
       }
     }
     mcount[y] = c;
     tcount[y] = t;
+    tcount2[y] = t2;
   }
 }
 
@@ -270,15 +279,16 @@ k_tc_pairs(const uint32_t* __restrict__ iptr, const uint32_t* __restrict__ icol,
   }
 }
 
-__global__ void k_tc_tasks(uint32_t N, const unsigned long long* __restrict__ toff, const uint32_t* __restrict__ mptr,
-                           uint2* wtasks, uint2* btasks)
+__global__ void k_tc_tasks(uint32_t N, const unsigned long long* __restrict__ toff, const uint32_t* __restrict__ toff2,
+                           const uint32_t* __restrict__ mptr, uint2* wtasks, uint2* mtasks, uint2* btasks)
 {
   for (uint32_t y = blockIdx.x * blockDim.x + threadIdx.x; y < N; y += gridDim.x * blockDim.x)
   {
     const unsigned long long c = toff[y + 1] - toff[y];
-    const uint32_t nw = (uint32_t) c, nb = (uint32_t) (c >> 32);
-    const uint32_t wo = (uint32_t) toff[y], bo = (uint32_t) (toff[y] >> 32);
+    const uint32_t nw = (uint32_t) c, nm = (uint32_t) (c >> 32), nb = toff2[y + 1] - toff2[y];
+    const uint32_t wo = (uint32_t) toff[y], mo = (uint32_t) (toff[y] >> 32), bo = toff2[y];
     for (uint32_t k = 0; k < nw; k++) wtasks[wo + k] = make_uint2(y, mptr[y] + k * kTcWarpPairs);
+    for (uint32_t k = 0; k < nm; k++) mtasks[mo + k] = make_uint2(y, mptr[y] + k * kTcBlockPairs);
     for (uint32_t k = 0; k < nb; k++) btasks[bo + k] = make_uint2(y, mptr[y] + k * kTcBlockPairs);
   }
 }
@@ -464,10 +474,9 @@ __device__ __forceinline__ void tc_probe(uint32_t w, uint32_t k, uint32_t xo, ui
   if (j < 0) return;
   const uint32_t wid = SEARCH ? id_of_rank[w] : T.lid[j];
   const uint32_t mid = tc_mid3(xo, yid, wid);
-  if (mid == yid) cy++;
-  else if (mid == xo) atomicAdd(&R.cx[k], 1u);
-  else if (SEARCH) atomicAdd(&ntri[wid], 1u);
-  else atomicAdd(&T.cn[j], 1u);
+  cy += mid == yid;
+  uint32_t* const at_w = SEARCH ? &ntri[wid] : &T.cn[j];
+  if (mid != yid) atomicAdd(mid == xo ? &R.cx[k] : at_w, 1u);
 }
 
 // One warp walks one round: pairs [p0, p1) (at most 32) of y.  The pairs'
@@ -522,6 +531,7 @@ __device__ __forceinline__ void tc_round(uint32_t p0, uint32_t p1, const uint2* 
   R.cx[lane] = 0;
   __syncwarp();
   uint32_t before = 0;
+  bool slip = false;
   for (uint32_t w0 = 0; w0 < total; w0 += 64)
   {
     const uint32_t ra = pk - w0, rb = pk - (w0 + 32);
@@ -534,13 +544,16 @@ __device__ __forceinline__ void tc_round(uint32_t p0, uint32_t p1, const uint2* 
     const uint32_t ta = w0 + lane, tb = ta + 32;
     const uint32_t soa = __shfl_sync(full, my_so, ka), sob = __shfl_sync(full, my_so, kb);
     const uint32_t xa = __shfl_sync(full, my_x, ka), xb = __shfl_sync(full, my_x, kb);
-    // by construction every element below total has an owner in this round
-    if ((ta < total && ka >= np) || (tb < total && kb >= np)) atomicAdd(err, 1ull);
-    const uint32_t wa = (ta < total && ka < np) ? pcol[soa + ta] : kEmpty;
-    const uint32_t wb = (tb < total && kb < np) ? pcol[sob + tb] : kEmpty;
+    // by construction every element below total has an owner in this round;
+    // checked all the same, so that a slip reads nothing outside the lists
+    const bool va = ta < total, vb = tb < total;
+    slip |= (va && ka >= np) || (vb && kb >= np);
+    const uint32_t wa = (va && ka < np) ? pcol[soa + ta] : kEmpty;
+    const uint32_t wb = (vb && kb < np) ? pcol[sob + tb] : kEmpty;
     tc_probe<IDX, SEARCH>(wa, ka, xa, yid, T, row, d, id_of_rank, R, cy, ntri);
     tc_probe<IDX, SEARCH>(wb, kb, xb, yid, T, row, d, id_of_rank, R, cy, ntri);
   }
+  if (slip) atomicAdd(err, 1ull);
   walked += total;
   __syncwarp();
   if (lane < np && R.cx[lane]) atomicAdd(&ntri[my_x], R.cx[lane]);
@@ -581,7 +594,7 @@ template <int WARPS>
 __global__ void __launch_bounds__(WARPS * 32, 5)
 k_tc_count_warp(const uint32_t* __restrict__ pptr, const uint32_t* __restrict__ pcol, const uint2* __restrict__ pairs,
                 const uint32_t* __restrict__ mptr, const uint2* __restrict__ tasks,
-                const unsigned long long* __restrict__ ntasks_packed, const uint32_t* __restrict__ id_of_rank,
+                const uint32_t* __restrict__ ntasks_ptr, const uint32_t* __restrict__ id_of_rank,
                 uint32_t* ntri, unsigned long long* ctr)
 {
   __shared__ uint32_t s_key[WARPS][kTcWarpSlots];
@@ -594,7 +607,7 @@ k_tc_count_warp(const uint32_t* __restrict__ pptr, const uint32_t* __restrict__ 
   uint8_t* idx = s_idx[wi];
   uint32_t* lid = s_lid[wi];
   uint32_t* cn = s_cn[wi];
-  const uint32_t ntasks = (uint32_t) *ntasks_packed;
+  const uint32_t ntasks = *ntasks_ptr;
   unsigned long long walked = 0, built = 0;
   for (;;)
   {
@@ -633,32 +646,34 @@ k_tc_count_warp(const uint32_t* __restrict__ pptr, const uint32_t* __restrict__ 
 }
 
 // Block tasks: |N+(y)| > kTcWarpCap; one table per block in dynamic shared
-// memory (or a global binary search above kTcBlockCap); the warps take the
-// task's 32-pair rounds from a shared counter.  The per-warp round state
-// stays in static shared memory.
-template <int THREADS>
-__global__ void __launch_bounds__(THREADS)
+// memory (CAP elements, SLOTS slots; rows longer than CAP fall back to a
+// global binary search), the warps taking the task's 32-pair rounds from a
+// shared counter.  Two sizes: small blocks with small tables for rows up to
+// kTcMidCap, so that many tasks run on an SM at once, and large ones.  The
+// per-warp round state stays in static shared memory.
+template <int THREADS, uint32_t SLOTS, uint32_t CAP, int CURSOR>
+__global__ void __launch_bounds__(THREADS, 1536 / THREADS)
 k_tc_count_block(const uint32_t* __restrict__ pptr, const uint32_t* __restrict__ pcol, const uint2* __restrict__ pairs,
                  const uint32_t* __restrict__ mptr, const uint2* __restrict__ tasks,
-                 const unsigned long long* __restrict__ ntasks_packed, const uint32_t* __restrict__ id_of_rank,
+                 const uint32_t* __restrict__ ntasks_ptr, const uint32_t* __restrict__ id_of_rank,
                  uint32_t* ntri, unsigned long long* ctr)
 {
   constexpr int WARPS = THREADS / 32;
   extern __shared__ __align__(16) uint32_t tc_smem[];
-  uint32_t* key = tc_smem;                          // [kTcBlockSlots]
-  uint32_t* lid = key + kTcBlockSlots;              // [kTcBlockCap]
-  uint32_t* cn = lid + kTcBlockCap;                 // [kTcBlockCap]
-  uint16_t* idx = (uint16_t*) (cn + kTcBlockCap);   // [kTcBlockSlots]
+  uint32_t* key = tc_smem;                          // [SLOTS]
+  uint32_t* lid = key + SLOTS;                      // [CAP]
+  uint32_t* cn = lid + CAP;                         // [CAP]
+  uint16_t* idx = (uint16_t*) (cn + CAP);           // [SLOTS]
   __shared__ TcRound s_r[WARPS];
   __shared__ uint32_t s_t, s_cy, s_round;
   const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
-  const uint32_t ntasks = (uint32_t) (*ntasks_packed >> 32);
+  const uint32_t ntasks = *ntasks_ptr;
   unsigned long long walked = 0, built = 0;
   for (;;)
   {
     if (threadIdx.x == 0)
     {
-      s_t = (uint32_t) atomicAdd(&ctr[1], 1ull);
+      s_t = (uint32_t) atomicAdd(&ctr[CURSOR], 1ull);
       s_cy = 0;
       s_round = 0;
     }
@@ -668,7 +683,7 @@ k_tc_count_block(const uint32_t* __restrict__ pptr, const uint32_t* __restrict__
     const uint2 tk = tasks[t];
     const uint32_t y = tk.x, p0 = tk.y, p1 = min(p0 + kTcBlockPairs, mptr[y + 1]);
     const uint32_t yb = pptr[y], d = pptr[y + 1] - yb;
-    const bool search = d > kTcBlockCap;
+    const bool search = d > CAP;
     const int lg = search ? 5 : tc_lg(d);
     if (!search)
     {
@@ -711,6 +726,9 @@ k_tc_count_block(const uint32_t* __restrict__ pptr, const uint32_t* __restrict__
 
 static constexpr size_t kTcBlockSmem = (size_t) kTcBlockSlots * 4 + 2 * (size_t) kTcBlockCap * 4 +
                                        (size_t) kTcBlockSlots * 2;
+static constexpr size_t kTcMidSmem = (size_t) kTcMidSlots * 4 + 2 * (size_t) kTcMidCap * 4 + (size_t) kTcMidSlots * 2;
+#define TC_MID_KERNEL k_tc_count_block<kTcMidThreads, kTcMidSlots, kTcMidCap, 8>
+#define TC_BIG_KERNEL k_tc_count_block<kTcBlockThreads, kTcBlockSlots, kTcBlockCap, 1>
 static constexpr size_t kTcSortBigSmem = (size_t) kTcSortBlockCap * 4;
 
 __global__ void k_tc_sum(uint32_t N, const uint32_t* __restrict__ ntri, unsigned long long* total)
@@ -749,12 +767,15 @@ static int tc_scratch(la3g_graph* G, TcScratch** out)
   LA3G_TRY(galloc(G, &ts->pairs, m + 1));
   LA3G_TRY(galloc(G, &ts->tcount, (size_t) N + 1));
   LA3G_TRY(galloc(G, &ts->toff, (size_t) N + 1));
+  LA3G_TRY(galloc(G, &ts->tcount2, (size_t) N + 1));
+  LA3G_TRY(galloc(G, &ts->toff2, (size_t) N + 1));
   LA3G_TRY(galloc(G, &ts->wtasks, m / kTcWarpPairs + N + 1));
+  LA3G_TRY(galloc(G, &ts->mtasks, m / kTcBlockPairs + N + 1));
   LA3G_TRY(galloc(G, &ts->btasks, m / kTcBlockPairs + N + 1));
   LA3G_TRY(galloc(G, &ts->ntri, N));
   LA3G_TRY(galloc(G, &ts->big_rows, N));
-  LA3G_TRY(galloc(G, &ts->ctr, 8));
-  LA3G_CUDA(cudaHostAlloc(&ts->hctr, 8 * sizeof(unsigned long long), cudaHostAllocDefault));
+  LA3G_TRY(galloc(G, &ts->ctr, kTcCounters));
+  LA3G_CUDA(cudaHostAlloc(&ts->hctr, kTcCounters * sizeof(unsigned long long), cudaHostAllocDefault));
   // degrees are at most N - 1: the rank sort needs bit_width(N) key bits
   ts->end_bit = 1;
   while (ts->end_bit < 32 && ((uint64_t) N >> ts->end_bit) != 0) ts->end_bit++;
@@ -763,7 +784,9 @@ static int tc_scratch(la3g_graph* G, TcScratch** out)
                                             ts->end_bit));
   LA3G_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, b, ts->dplus, ts->pptr, (int) N + 1));
   LA3G_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, c, ts->tcount, ts->toff, (int) N + 1));
-  ts->temp_bytes = std::max(a, std::max(b, c));
+  size_t c2 = 0;
+  LA3G_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, c2, ts->tcount2, ts->toff2, (int) N + 1));
+  ts->temp_bytes = std::max(std::max(a, b), std::max(c, c2));
   LA3G_TRY(galloc_bytes(G, &ts->temp, ts->temp_bytes));
   *out = ts;
   return LA3G_OK;
@@ -783,7 +806,7 @@ static int tc_lists(la3g_graph* G, TcScratch* ts, bool library_sort)
   size_t tb = ts->temp_bytes;
   LA3G_CUDA(cudaMemsetAsync(ts->dplus, 0, ((size_t) N + 1) * 4, s));
   LA3G_CUDA(cudaMemsetAsync(ts->fill, 0, (size_t) N * 4, s));
-  LA3G_CUDA(cudaMemsetAsync(ts->ctr, 0, 8 * sizeof(unsigned long long), s));
+  LA3G_CUDA(cudaMemsetAsync(ts->ctr, 0, kTcCounters * sizeof(unsigned long long), s));
   k_tc_deg<<<grid_for(N, 256), 256, 0, s>>>(g.in_ptr, g.out_ptr, N, ts->deg, ts->iota);
   LA3G_LAUNCHED();
   LA3G_CUDA(cub::DeviceRadixSort::SortPairs(ts->temp, tb, ts->deg, ts->deg_of_rank, ts->iota, ts->pos_of_rank, (int) N,
@@ -829,13 +852,15 @@ static int tc_lists(la3g_graph* G, TcScratch* ts, bool library_sort)
     }
   }
   k_tc_pair_counts<<<grid_for((uint64_t) N + 1, 256), 256, 0, s>>>(N, ts->pptr, ts->deg_of_rank, ts->mcount,
-                                                                   ts->tcount);
+                                                                   ts->tcount, ts->tcount2);
   LA3G_LAUNCHED();
   tls_launches++;
   tb = ts->temp_bytes;
   LA3G_CUDA(cub::DeviceScan::ExclusiveSum(ts->temp, tb, ts->mcount, ts->mptr, (int) N + 1, s));
   tb = ts->temp_bytes;
   LA3G_CUDA(cub::DeviceScan::ExclusiveSum(ts->temp, tb, ts->tcount, ts->toff, (int) N + 1, s));
+  tb = ts->temp_bytes;
+  LA3G_CUDA(cub::DeviceScan::ExclusiveSum(ts->temp, tb, ts->tcount2, ts->toff2, (int) N + 1, s));
   if (m)
   {
     LA3G_CUDA(cudaMemsetAsync(ts->fill, 0, (size_t) N * 4, s));
@@ -846,7 +871,7 @@ static int tc_lists(la3g_graph* G, TcScratch* ts, bool library_sort)
     LA3G_LAUNCHED();
     tls_launches++;
   }
-  k_tc_tasks<<<grid_for(N, 256), 256, 0, s>>>(N, ts->toff, ts->mptr, ts->wtasks, ts->btasks);
+  k_tc_tasks<<<grid_for(N, 256), 256, 0, s>>>(N, ts->toff, ts->toff2, ts->mptr, ts->wtasks, ts->mtasks, ts->btasks);
   LA3G_LAUNCHED();
   tls_launches++;
   return LA3G_OK;
@@ -870,8 +895,8 @@ extern "C" int la3g_tc(la3g_graph* G, uint64_t* total_out, uint32_t* per_vertex_
   static bool smem_set = false;  // the opt-ins are per function and device; idempotent
   if (!smem_set)
   {
-    LA3G_CUDA(cudaFuncSetAttribute(k_tc_count_block<kTcBlockThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int) kTcBlockSmem));
+    LA3G_CUDA(cudaFuncSetAttribute(TC_BIG_KERNEL, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) kTcBlockSmem));
+    LA3G_CUDA(cudaFuncSetAttribute(TC_MID_KERNEL, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) kTcMidSmem));
     LA3G_CUDA(cudaFuncSetAttribute(k_tc_sort_big, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) kTcSortBigSmem));
     smem_set = true;
   }
@@ -896,19 +921,26 @@ extern "C" int la3g_tc(la3g_graph* G, uint64_t* total_out, uint32_t* per_vertex_
     {
       // pass 2; its bytes (walked list elements, pairs, tables) are added below
       ProfileScope p("tc_count", s, 0.0);
+      // task counts on the device: warp and small-block counts are the two
+      // halves of the packed total (little-endian), large-block the other
+      const uint32_t* nw = (const uint32_t*) (ts->toff + N);
       k_tc_count_warp<kTcWarpKernelWarps><<<kSMs * 5, kTcWarpKernelWarps * 32, 0, s>>>(
-          ts->pptr, ts->pcol, ts->pairs, ts->mptr, ts->wtasks, ts->toff + N, ts->id_of_rank, ts->ntri, ts->ctr);
+          ts->pptr, ts->pcol, ts->pairs, ts->mptr, ts->wtasks, nw, ts->id_of_rank, ts->ntri, ts->ctr);
       LA3G_LAUNCHED();
-      k_tc_count_block<kTcBlockThreads><<<kSMs * 3, kTcBlockThreads, kTcBlockSmem, s>>>(
-          ts->pptr, ts->pcol, ts->pairs, ts->mptr, ts->btasks, ts->toff + N, ts->id_of_rank, ts->ntri, ts->ctr);
+      TC_MID_KERNEL<<<kSMs * 8, kTcMidThreads, kTcMidSmem, s>>>(ts->pptr, ts->pcol, ts->pairs, ts->mptr, ts->mtasks,
+                                                                 nw + 1, ts->id_of_rank, ts->ntri, ts->ctr);
       LA3G_LAUNCHED();
-      tls_launches++;
+      TC_BIG_KERNEL<<<kSMs * 3, kTcBlockThreads, kTcBlockSmem, s>>>(ts->pptr, ts->pcol, ts->pairs, ts->mptr,
+                                                                     ts->btasks, ts->toff2 + N, ts->id_of_rank,
+                                                                     ts->ntri, ts->ctr);
+      LA3G_LAUNCHED();
+      tls_launches += 2;
     }
     k_tc_sum<<<grid_for(N, 256), 256, 0, s>>>(N, ts->ntri, ts->ctr + 4);
     LA3G_LAUNCHED();
     tls_launches++;
     T.device_end();
-    LA3G_CUDA(cudaMemcpyAsync(ts->hctr, ts->ctr, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    LA3G_CUDA(cudaMemcpyAsync(ts->hctr, ts->ctr, kTcCounters * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
     LA3G_CUDA(cudaStreamSynchronize(s));
     if (ts->hctr[5]) return set_error(LA3G_ECUDA, "tc: %llu internal consistency checks failed",
                                       (unsigned long long) ts->hctr[5]);
