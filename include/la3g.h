@@ -266,6 +266,14 @@ int la3g_batch_autotune(la3g_graph* g, const uint32_t* roots, uint32_t nroots, c
  * push_frac in [0, 1]. */
 int la3g_batch_config(la3g_graph* g, int mode, int block, double push_frac);
 
+/* The persistent batched-BFS kernel's grid barriers wait at most `polls`
+ * polls per block (default 2^26, restored by polls < 0); a block that runs
+ * out sets an error word, every block leaves its kernel, and the call returns
+ * LA3G_ETIMEOUT with the device left usable.  No counterpart in the
+ * reference (it has no device waits); polls = 0 makes any wait give up at
+ * once, which exercises that error path. */
+int la3g_batch_set_wait_limit(la3g_graph* g, long long polls);
+
 /* ---- serving loop (no reference counterpart; the reference answers one
  *      query per VertexProgram run, bfs.cpp:11-37, sssp.cpp:11-37,
  *      bm25.cpp:8-114) ------------------------------------------------------ */

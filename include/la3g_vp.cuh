@@ -176,10 +176,24 @@ __global__ void k_by_id(uint32_t n, const uint32_t* id_of_pos, const T* in, T* o
   for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) out[id_of_pos[p]] = in[p];
 }
 
+// Blocks of 256 threads for n items, at most 16 per streaming multiprocessor
+// of the current device.
 inline unsigned blocks_for(uint64_t n)
 {
+  static thread_local int sms = 0;
+  if (!sms)
+  {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        sms <= 0)
+    {
+      cudaGetLastError();
+      sms = 152;
+    }
+  }
+  const uint64_t cap = (uint64_t) sms * 16;
   uint64_t b = (n + 255) / 256;
-  return (unsigned) (b < 1 ? 1 : (b > 152 * 16 ? 152 * 16 : b));
+  return (unsigned) (b < 1 ? 1 : (b > cap ? cap : b));
 }
 
 }  // namespace detail

@@ -496,6 +496,11 @@ def batch_config(G: Graph, mode: int, block: int = 256, push_frac: float = 0.05)
     N.check(N.lib().la3g_batch_config(G._h, mode, block, push_frac))
 
 
+def batch_set_wait_limit(G: Graph, polls: int = -1) -> None:
+    """Grid-barrier poll limit of the persistent batched-BFS kernel (< 0: the default)."""
+    N.check(N.lib().la3g_batch_set_wait_limit(G._h, polls))
+
+
 def sssp_batch(G: Graph, roots: Sequence[int], want_dist: bool = True):
     r = np.ascontiguousarray(np.asarray(roots, dtype=np.uint32))
     st = Stats()

@@ -47,8 +47,14 @@ struct BatchConfig
   bool tuned = false;
 };
 
+// Polls a block of the persistent kernel makes at a grid barrier before it
+// gives up (sets the error word, every block leaves, the call returns
+// LA3G_ETIMEOUT); la3g_batch_set_wait_limit changes it per graph.
+static constexpr long long kDefaultWaitPolls = 1ll << 26;
+
 struct BatchScratch
 {
+  long long wait_polls = kDefaultWaitPolls;  // grid-barrier poll limit of the persistent kernel
   uint32_t cap_r = 0;        // roots the buffers were sized for
   uint64_t* vis = nullptr;   // [N][W]
   uint64_t* buf[2] = {nullptr, nullptr};  // frontier / next, [N][W]
@@ -242,9 +248,9 @@ __global__ void k_ms_clear(uint64_t n, BufPair buf, unsigned long long* ctr)
     next[i] = 0;
 }
 
-// Grid barrier for the persistent kernel: bounded spin; on timeout the
-// error word is set and every block leaves.
-__device__ bool grid_barrier(unsigned int* bar, int* err, unsigned int nblocks)
+// Grid barrier for the persistent kernel: bounded spin (at most `limit`
+// polls); on timeout the error word is set and every block leaves.
+__device__ bool grid_barrier(unsigned int* bar, int* err, unsigned int nblocks, long long limit)
 {
   __syncthreads();
   bool ok = true;
@@ -264,7 +270,7 @@ __device__ bool grid_barrier(unsigned int* bar, int* err, unsigned int nblocks)
       long long spins = 0;
       while (*vgen == gen)
       {
-        if (++spins > (1ll << 26) || *(volatile int*) err)
+        if (spins++ >= limit || *(volatile int*) err)
         {
           atomicExch(err, 1);
           ok = false;
@@ -284,16 +290,17 @@ __device__ bool grid_barrier(unsigned int* bar, int* err, unsigned int nblocks)
 // All pull levels in one cooperative launch.
 __global__ void k_ms_persistent(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, uint32_t nrows,
                                 uint32_t N, uint32_t W, uint64_t* vis, BufPair buf, BufPair alive, uint8_t* hops,
-                                unsigned long long* ctr, unsigned int* bar, int* err, uint32_t max_levels)
+                                unsigned long long* ctr, unsigned int* bar, int* err, uint32_t max_levels,
+                                long long wait_limit)
 {
   const uint64_t tid = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x;
   const uint64_t nth = (uint64_t) gridDim.x * blockDim.x;
   for (uint32_t it = 0; it < max_levels; it++)
   {
     ms_pull_body(ptr, col, nrows, N, W, vis, buf.p, alive.p, hops, ctr, tid, nth);
-    if (!grid_barrier(bar, err, gridDim.x)) return;
+    if (!grid_barrier(bar, err, gridDim.x, wait_limit)) return;
     const unsigned long long found = ctr[0];
-    if (!grid_barrier(bar, err, gridDim.x)) return;
+    if (!grid_barrier(bar, err, gridDim.x, wait_limit)) return;
     if (blockIdx.x == 0)
     {
       const uint32_t level = (uint32_t) ctr[3];
@@ -307,7 +314,7 @@ __global__ void k_ms_persistent(const uint32_t* __restrict__ ptr, const uint32_t
         ctr[0] = 0;
       }
     }
-    if (!grid_barrier(bar, err, gridDim.x)) return;
+    if (!grid_barrier(bar, err, gridDim.x, wait_limit)) return;
     if (!found) return;
   }
 }
@@ -415,7 +422,7 @@ static int ms_bfs_run(la3g_graph* G, BatchScratch* b, const uint32_t* roots_host
   LA3G_CUDA(cudaMemcpyAsync(b->active, roots_host, (size_t) R * 4, cudaMemcpyHostToDevice, s));
   k_root_pos<<<grid_for(R, 256), 256, 0, s>>>(b->active, R, N, g.pos_of_id, b->rpos);
   LA3G_LAUNCHED();
-  k_ms_init<<<kSMs * 8, 256, 0, s>>>(N, W, R, b->vis, b->buf[0], b->buf[1]);
+  k_ms_init<<<num_sms() * 8, 256, 0, s>>>(N, W, R, b->vis, b->buf[0], b->buf[1]);
   LA3G_LAUNCHED();
   LA3G_CUDA(cudaMemsetAsync(b->hops, 0xFF, (size_t) N * W * 64, s));
   LA3G_CUDA(cudaMemsetAsync(b->alive[0], 0, (size_t) W * 8, s));
@@ -426,13 +433,13 @@ static int ms_bfs_run(la3g_graph* G, BatchScratch* b, const uint32_t* roots_host
   tls_launches += 4;
   *wrap = false;
   *edges_words = 0;
-  const unsigned blocks = kSMs * (2048 / cfg.block);
+  const unsigned blocks = num_sms() * (2048 / cfg.block);
   if (cfg.mode == 1)
   {
     // persistent cooperative kernel (pull levels)
     int per_sm = 0;
     LA3G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ms_persistent, cfg.block, 0));
-    int dev = 0, sms = kSMs;
+    int dev = 0, sms = num_sms();
     LA3G_CUDA(cudaGetDevice(&dev));
     LA3G_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     unsigned grid = (unsigned) std::max(1, per_sm) * (unsigned) sms;
@@ -446,8 +453,10 @@ static int ms_bfs_run(la3g_graph* G, BatchScratch* b, const uint32_t* roots_host
     unsigned int* bar = b->bar;
     int* err = b->err;
     uint32_t maxl = 255;
+    long long wait_limit = b->wait_polls;
     void* args[] = {(void*) &ptr, (void*) &col, (void*) &nrows, (void*) &N, (void*) &W, (void*) &vis, (void*) &buf,
-                    (void*) &alive, (void*) &hops, (void*) &ctr, (void*) &bar, (void*) &err, (void*) &maxl};
+                    (void*) &alive, (void*) &hops, (void*) &ctr, (void*) &bar, (void*) &err, (void*) &maxl,
+                    (void*) &wait_limit};
     {
       ProfileScope p("msbfs_persistent", s, 0.0);
       LA3G_CUDA(cudaLaunchCooperativeKernel((void*) k_ms_persistent, grid, cfg.block, args, 0, s));
@@ -629,9 +638,9 @@ extern "C" int la3g_bfs_batch(la3g_graph* G, const uint32_t* roots, uint32_t nro
     // bytes), which the next batch re-initialises
     DevBuf tpos;
     LA3G_TRY(tpos.alloc((size_t) nroots * N));
-    k_ms_out_pos<<<kSMs * 8, 256, 0, s>>>(N, nroots, (nroots + 63) / 64, b->hops, tpos.as<uint8_t>());
+    k_ms_out_pos<<<num_sms() * 8, 256, 0, s>>>(N, nroots, (nroots + 63) / 64, b->hops, tpos.as<uint8_t>());
     LA3G_LAUNCHED();
-    k_ms_out_id<<<kSMs * 8, 256, 0, s>>>(N, nroots, g.pos_of_id, tpos.as<uint8_t>(), b->hops);
+    k_ms_out_id<<<num_sms() * 8, 256, 0, s>>>(N, nroots, g.pos_of_id, tpos.as<uint8_t>(), b->hops);
     LA3G_LAUNCHED();
     LA3G_CUDA(cudaMemcpyAsync(hops_out, b->hops, (size_t) nroots * N, cudaMemcpyDeviceToHost, s));
     LA3G_CUDA(cudaStreamSynchronize(s));
@@ -732,7 +741,7 @@ static int sssp_batch_chunk(la3g_graph* G, BatchScratch* b, const uint32_t* root
   LA3G_CUDA(cudaMemcpyAsync(b->active, roots, (size_t) R * 4, cudaMemcpyHostToDevice, s));
   k_root_pos<<<grid_for(R, 256), 256, 0, s>>>(b->active, R, N, g.pos_of_id, b->rpos);
   LA3G_LAUNCHED();
-  k_bs_init<<<kSMs * 8, 256, 0, s>>>((uint64_t) N * R, b->sdist, (uint64_t) N * W, b->sfront[0], b->sfront[1]);
+  k_bs_init<<<num_sms() * 8, 256, 0, s>>>((uint64_t) N * R, b->sdist, (uint64_t) N * W, b->sfront[0], b->sfront[1]);
   LA3G_LAUNCHED();
   k_bs_roots<<<grid_for(R, 256), 256, 0, s>>>(b->rpos, R, N, W, g.nreg, g.src_base(), g.iso_base(), b->sdist,
                                               b->sfront[0]);
@@ -745,7 +754,7 @@ static int sssp_batch_chunk(la3g_graph* G, BatchScratch* b, const uint32_t* root
   PairList L[2];
   for (int c = 0; c < 2; c++) L[c] = PairList{b->sact[c], b->shub[c], b->shub_t0[c], b->ctr + c, b->ctr + 2 + c};
   LA3G_CUDA(cudaMemsetAsync(b->ctr, 0, 4 * 8, s));
-  k_bs_list<<<kSMs * 8, 256, 0, s>>>((uint64_t) N * W, W, g.out_ptr, b->reg_end, b->sfront[0], L[0]);
+  k_bs_list<<<num_sms() * 8, 256, 0, s>>>((uint64_t) N * W, W, g.out_ptr, b->reg_end, b->sfront[0], L[0]);
   LA3G_LAUNCHED();
   tls_launches++;
   for (;;)
@@ -754,13 +763,13 @@ static int sssp_batch_chunk(la3g_graph* G, BatchScratch* b, const uint32_t* root
     iters++;
     {
       ProfileScope p("sssp_batch_relax", s, 0.0);
-      k_bs_relax<<<kSMs * 16, 256, 0, s>>>(g.out_ptr, b->reg_end, g.out_row, g.out_w, R, W, b->sfront[cur], L[cur],
+      k_bs_relax<<<num_sms() * 16, 256, 0, s>>>(g.out_ptr, b->reg_end, g.out_row, g.out_w, R, W, b->sfront[cur], L[cur],
                                            b->sfront[cur ^ 1], b->sdist);
       LA3G_LAUNCHED();
     }
     LA3G_CUDA(cudaMemsetAsync(b->ctr + (cur ^ 1), 0, 8, s));
     LA3G_CUDA(cudaMemsetAsync(b->ctr + 2 + (cur ^ 1), 0, 8, s));
-    k_bs_apply<<<kSMs * 8, 256, 0, s>>>(N, W, g.out_ptr, b->reg_end, b->sfront[cur ^ 1], L[cur ^ 1], b->sfront[cur],
+    k_bs_apply<<<num_sms() * 8, 256, 0, s>>>(N, W, g.out_ptr, b->reg_end, b->sfront[cur ^ 1], L[cur ^ 1], b->sfront[cur],
                                         L[cur]);
     LA3G_LAUNCHED();
     tls_launches += 2;
@@ -772,7 +781,7 @@ static int sssp_batch_chunk(la3g_graph* G, BatchScratch* b, const uint32_t* root
   }
   if (g.nsink)
   {
-    k_bs_sinks<<<kSMs * 8, 256, 0, s>>>(g.in_ptr, g.in_col, g.in_w, g.nreg, g.nsink, R, b->rpos, g.src_base(),
+    k_bs_sinks<<<num_sms() * 8, 256, 0, s>>>(g.in_ptr, g.in_col, g.in_w, g.nreg, g.nsink, R, b->rpos, g.src_base(),
                                         g.iso_base(), b->sdist);
     LA3G_LAUNCHED();
     tls_launches++;
@@ -781,7 +790,7 @@ static int sssp_batch_chunk(la3g_graph* G, BatchScratch* b, const uint32_t* root
   {
     DevBuf tmp;
     LA3G_TRY(tmp.alloc((size_t) N * R * 4));
-    k_bs_out<<<kSMs * 8, 256, 0, s>>>(N, R, g.id_of_pos, b->sdist, tmp.as<uint32_t>());
+    k_bs_out<<<num_sms() * 8, 256, 0, s>>>(N, R, g.id_of_pos, b->sdist, tmp.as<uint32_t>());
     LA3G_LAUNCHED();
     LA3G_CUDA(cudaMemcpyAsync(dist_out, tmp.p, (size_t) N * R * 4, cudaMemcpyDeviceToHost, s));
     LA3G_CUDA(cudaStreamSynchronize(s));
@@ -850,6 +859,15 @@ extern "C" int la3g_batch_autotune(la3g_graph* G, const uint32_t* roots, uint32_
     std::memcpy(report, rep.data(), n);
     report[n] = 0;
   }
+  return LA3G_OK;
+}
+
+extern "C" int la3g_batch_set_wait_limit(la3g_graph* G, long long polls)
+{
+  if (!G) return set_error(LA3G_EINVAL, "null graph");
+  BatchScratch* b = nullptr;
+  LA3G_TRY(batch_scratch(G, &b));
+  b->wait_polls = polls < 0 ? kDefaultWaitPolls : polls;
   return LA3G_OK;
 }
 

@@ -438,7 +438,7 @@ static int bfs_run(la3g_graph* G, BfsScratch* bs, uint32_t root, la3g_stats* st)
   int cur = 0;
   const double alpha = 14.0, beta = 24.0;
   uint64_t edges_examined = 0;
-  const unsigned td_blocks = kSMs * 8;
+  const unsigned td_blocks = num_sms() * 8;
   for (;;)
   {
     if (iter > 100000) return set_error(LA3G_ETIMEOUT, "bfs did not converge");
@@ -473,7 +473,7 @@ static int bfs_run(la3g_graph* G, BfsScratch* bs, uint32_t root, la3g_stats* st)
       LA3G_CUDA(cudaMemsetAsync(bs->bits[cur ^ 1], 0, (size_t) bs->words * 4, s));
       {
         ProfileScope p("bfs_bottom_up", s, 4.0 * unvisited_deg + 8.0 * nrows + N / 8.0);
-        k_bfs_bu_split<<<grid_for(nrows, 256, kSMs * 16), 256, 0, s>>>(g.in_ptr, g.in_col, g.hash_of_pos, nrows,
+        k_bfs_bu_split<<<grid_for(nrows, 256, num_sms() * 16), 256, 0, s>>>(g.in_ptr, g.in_col, g.hash_of_pos, nrows,
                                                                       bs->bits[cur], bs->bits[cur ^ 1], hop, bs->hops,
                                                                       bs->parent, bs->ctr);
         LA3G_LAUNCHED();
@@ -521,7 +521,7 @@ static int bfs_run(la3g_graph* G, BfsScratch* bs, uint32_t root, la3g_stats* st)
       edges_examined += front_deg;
       // the apply kernel reads the touched count on the device: one host
       // synchronisation per iteration
-      k_bfs_td_apply_split<<<kSMs * 4, 256, 0, s>>>(g.in_ptr, bs->raw, hop, bs->hops, bs->parent, bs->cand,
+      k_bfs_td_apply_split<<<num_sms() * 4, 256, 0, s>>>(g.in_ptr, bs->raw, hop, bs->hops, bs->parent, bs->cand,
                                                    bs->small[cur ^ 1], bs->big[cur ^ 1], bs->big_task0[cur ^ 1],
                                                    bs->ctr);
       LA3G_LAUNCHED();
@@ -738,7 +738,7 @@ static int bfs_noalloc_run(const uint32_t* row_ptr, const uint32_t* col, const u
           LA3G_LAUNCHED();
         }
         LA3G_CUDA(cudaMemsetAsync(bits[cur ^ 1], 0, (size_t) words * 4, s));
-        k_bfs_bu<<<grid_for(N, 256, kSMs * 16), 256, 0, s>>>(row_ptr, col, key, N, bits[cur], bits[cur ^ 1], hop, hops,
+        k_bfs_bu<<<grid_for(N, 256, num_sms() * 16), 256, 0, s>>>(row_ptr, col, key, N, bits[cur], bits[cur ^ 1], hop, hops,
                                                             parent, ctr);
         LA3G_LAUNCHED();
         front_is_list = false;

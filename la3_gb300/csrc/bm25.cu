@@ -32,7 +32,6 @@
 
 namespace la3g {
 
-static_assert(kTopBlocks == 2 * kSMs, "two partial top-k blocks per SM");
 static constexpr float kK1 = 1.2f;
 static constexpr float kB = 0.75f;
 
@@ -358,7 +357,7 @@ extern "C" int la3g_bm25_query(la3g_graph* G, const uint32_t* term_vids, uint32_
   for (uint32_t j = 0; j < nterms; j++)
   {
     ProfileScope p("bm25_term", s, 0.0);
-    k_bm25_term<<<kSMs * 4, 256, 0, s>>>(g.in_ptr, g.in_col, g.in_w, b->qpos, nterms, j, b->length, b->term_row0,
+    k_bm25_term<<<num_sms() * 4, 256, 0, s>>>(g.in_ptr, g.in_col, g.in_w, b->qpos, nterms, j, b->length, b->term_row0,
                                         b->score, b->stamp, b->query_id, b->touched, b->ctr);
     LA3G_LAUNCHED();
   }
@@ -382,7 +381,7 @@ extern "C" int la3g_bm25_query(la3g_graph* G, const uint32_t* term_vids, uint32_
     DevBuf a, c;
     if (all_scores_out) { LA3G_TRY(a.alloc((size_t) N * 4)); LA3G_CUDA(cudaMemsetAsync(a.p, 0, (size_t) N * 4, s)); }
     if (active_out) { LA3G_TRY(c.alloc(N)); LA3G_CUDA(cudaMemsetAsync(c.p, 0, N, s)); }
-    k_bm25_dump<<<kSMs * 4, 256, 0, s>>>(b->touched, b->ctr, b->score, g.id_of_pos, a.as<float>(), c.as<uint8_t>());
+    k_bm25_dump<<<num_sms() * 4, 256, 0, s>>>(b->touched, b->ctr, b->score, g.id_of_pos, a.as<float>(), c.as<uint8_t>());
     LA3G_LAUNCHED();
     if (all_scores_out) LA3G_CUDA(cudaMemcpyAsync(all_scores_out, a.p, (size_t) N * 4, cudaMemcpyDeviceToHost, s));
     if (active_out) LA3G_CUDA(cudaMemcpyAsync(active_out, c.p, N, cudaMemcpyDeviceToHost, s));

@@ -270,7 +270,7 @@ extern "C" int la3g_cc(la3g_graph* G, uint32_t* label_out, la3g_stats* st)
       // index, neighbour id and its root (12 B each), added once the walked
       // counts are back on the host
       ProfileScope p("cc_rest", s, 16.0 * nrows);
-      k_cc_rest<<<grid_for((uint64_t) nrows * 32, 256, kSMs * 32), 256, 0, s>>>(g.in_ptr, g.in_col, g.id_of_pos, nrows,
+      k_cc_rest<<<grid_for((uint64_t) nrows * 32, 256, num_sms() * 32), 256, 0, s>>>(g.in_ptr, g.in_col, g.id_of_pos, nrows,
                                                                                k, giant, cs->label, cs->walked);
       LA3G_LAUNCHED();
     }

@@ -24,6 +24,28 @@ int set_error(int code, const char* fmt, ...)
   return code;
 }
 
+int num_sms()
+{
+  static int cached[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+  {
+    cudaGetLastError();
+    return 152;
+  }
+  if (!cached[dev])
+  {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0)
+    {
+      cudaGetLastError();
+      v = 152;
+    }
+    cached[dev] = v;  // the same value from any thread: a benign race
+  }
+  return cached[dev];
+}
+
 double now_ms()
 {
   using namespace std::chrono;

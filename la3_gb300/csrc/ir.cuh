@@ -13,7 +13,7 @@ namespace la3g {
 
 constexpr int kTopKMax = 64;       // largest k of a top-k query
 constexpr int kTopThreads = 128;   // threads of the top-k blocks
-constexpr int kTopBlocks = 2 * 152;  // partial top-k blocks (two per SM)
+constexpr int kTopBlocks = 2 * 152;  // partial top-k blocks (two per SM of a GB300)
 
 // Block-level top-k of a key stream: each thread keeps its k best keys, the
 // block then extracts the k largest by repeated block-wide max.

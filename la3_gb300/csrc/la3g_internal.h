@@ -69,9 +69,11 @@ namespace la3g {
 // kernel itself is checked at the next synchronisation).
 #define LA3G_LAUNCHED() LA3G_CUDA(cudaGetLastError())
 
-constexpr int kSMs = 152;  // GB300: 2 dies x 76 SMs
+// Streaming multiprocessors of the current device (152 on a GB300: 2 dies
+// x 76), queried once per device; grid sizes are multiples of it.
+int num_sms();
 
-inline unsigned grid_for(uint64_t n, unsigned block, unsigned max_blocks = kSMs * 16)
+inline unsigned grid_for(uint64_t n, unsigned block, unsigned max_blocks = num_sms() * 16)
 {
   uint64_t g = (n + block - 1) / block;
   if (g < 1) g = 1;

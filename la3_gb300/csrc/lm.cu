@@ -264,12 +264,12 @@ extern "C" int la3g_lm_query(la3g_graph* G, const uint32_t* term_vids, uint32_t 
   for (uint32_t j = 0; j < nterms; j++)
   {
     ProfileScope p("lm_term", s, 0.0);
-    k_lm_term<<<kSMs * 4, 256, 0, s>>>(g.in_ptr, g.in_col, g.in_w, b->qpos, nterms, j, b->score, b->stamp,
+    k_lm_term<<<num_sms() * 4, 256, 0, s>>>(g.in_ptr, g.in_col, g.in_w, b->qpos, nterms, j, b->score, b->stamp,
                                       b->query_id, b->touched, b->ctr);
     LA3G_LAUNCHED();
   }
   // query_nterms = queries[q].size() (lm.cpp:66), as float in the apply
-  k_lm_apply<<<kSMs * 4, 256, 0, s>>>(b->touched, b->ctr, b->factor, (float) nterms, b->score);
+  k_lm_apply<<<num_sms() * 4, 256, 0, s>>>(b->touched, b->ctr, b->factor, (float) nterms, b->score);
   LA3G_LAUNCHED();
   tls_launches++;
   if (b->leftover)
@@ -303,7 +303,7 @@ extern "C" int la3g_lm_query(la3g_graph* G, const uint32_t* term_vids, uint32_t 
     DevBuf a, c;
     if (all_scores_out) { LA3G_TRY(a.alloc((size_t) N * 4)); LA3G_CUDA(cudaMemsetAsync(a.p, 0, (size_t) N * 4, s)); }
     if (active_out) { LA3G_TRY(c.alloc(N)); LA3G_CUDA(cudaMemsetAsync(c.p, 0, N, s)); }
-    k_bm25_dump<<<kSMs * 4, 256, 0, s>>>(b->touched, b->ctr, b->score, g.id_of_pos, a.as<float>(), c.as<uint8_t>());
+    k_bm25_dump<<<num_sms() * 4, 256, 0, s>>>(b->touched, b->ctr, b->score, g.id_of_pos, a.as<float>(), c.as<uint8_t>());
     LA3G_LAUNCHED();
     if (all_scores_out) LA3G_CUDA(cudaMemcpyAsync(all_scores_out, a.p, (size_t) N * 4, cudaMemcpyDeviceToHost, s));
     if (active_out) LA3G_CUDA(cudaMemcpyAsync(active_out, c.p, N, cudaMemcpyDeviceToHost, s));

@@ -279,9 +279,9 @@ static int pr_launch(la3g_graph* G, PrScratch* ps, const double* x, double* xnex
 {
   DevGraph& g = G->g;
   if (row_hi <= row_lo) return LA3G_OK;
-  const uint32_t long_blocks = ps->nlong ? std::min<uint32_t>((ps->nlong + kWarpsPerBlock - 1) / kWarpsPerBlock, kSMs) : 0;
+  const uint32_t long_blocks = ps->nlong ? std::min<uint32_t>((ps->nlong + kWarpsPerBlock - 1) / kWarpsPerBlock, num_sms()) : 0;
   const uint32_t ntiles = (row_hi - row_lo + 31) / 32;
-  const uint32_t tile_blocks = std::min<uint32_t>((ntiles + kWarpsPerBlock - 1) / kWarpsPerBlock, kSMs * 8);
+  const uint32_t tile_blocks = std::min<uint32_t>((ntiles + kWarpsPerBlock - 1) / kWarpsPerBlock, num_sms() * 8);
   uint64_t edges = 0;  // algorithmic bytes: 4 B index per edge + per-row ptr, x, rank, xnext
   (void) edges;
   double bytes = 4.0 * (double) g.nent + 4.0 * (row_hi - row_lo + 1) + 8.0 * (double) g.nslots +
@@ -508,8 +508,8 @@ extern "C" int la3g_pr_f32(la3g_graph* G, uint32_t iters, double tol, double* ra
   int cur = 0;
   uint32_t it = 0;
   double res = 0.0;
-  const uint32_t long_blocks = ps->nlong ? std::min<uint32_t>(ps->nlong, kSMs * 2) : 0;
-  const unsigned blocks = long_blocks + std::max<uint32_t>(grid_for((uint64_t) g.nreg * 4, 256, kSMs * 8), 1);
+  const uint32_t long_blocks = ps->nlong ? std::min<uint32_t>(ps->nlong, num_sms() * 2) : 0;
+  const unsigned blocks = long_blocks + std::max<uint32_t>(grid_for((uint64_t) g.nreg * 4, 256, num_sms() * 8), 1);
   // algorithmic bytes per iteration (FP32 form of the FP64 count): column
   // index per edge, row offsets, x read, rank read + write, next x write
   const double it_bytes = 4.0 * g.nent + 4.0 * (g.nreg + 1) + 4.0 * N + 8.0 * g.nreg + 8.0 * g.nreg + 4.0 * g.nreg;
@@ -535,7 +535,7 @@ extern "C" int la3g_pr_f32(la3g_graph* G, uint32_t iters, double tol, double* ra
   if (tol <= 0) LA3G_CUDA(cudaMemcpyAsync(&res, ps->resid, 8, cudaMemcpyDeviceToHost, s));
   if (g.nsink)
   {
-    const unsigned sb = long_blocks + std::max<uint32_t>(grid_for((uint64_t) g.nsink * 4, 256, kSMs * 8), 1);
+    const unsigned sb = long_blocks + std::max<uint32_t>(grid_for((uint64_t) g.nsink * 4, 256, num_sms() * 8), 1);
     LA3G_CUDA(cudaMemsetAsync(ps->resid, 0, 8, s));
     k_prf_pull<<<sb, 256, 0, s>>>(g.in_ptr, g.in_col, ps->xf[cur], ps->xf[cur ^ 1], ps->rankf, ps->rank, ps->deg,
                                   ps->long_rows, ps->nlong, long_blocks, g.nreg, g.nreg + g.nsink, ps->resid, 0);

@@ -529,7 +529,7 @@ int bfs_engine_init(Engine* E)
   LA3G_CUDA(cudaMemsetAsync(E->buf[1].p, 0, NW * 8, s));
   LA3G_CUDA(cudaMemsetAsync(E->alive[0].p, 0, W * 8, s));
   LA3G_CUDA(cudaMemsetAsync(E->alive[1].p, 0, W * 8, s));
-  k_lb_fill_u8<<<kSMs * 8, 256, 0, s>>>((uint64_t) L * N, E->hops.as<uint8_t>(), 255);
+  k_lb_fill_u8<<<num_sms() * 8, 256, 0, s>>>((uint64_t) L * N, E->hops.as<uint8_t>(), 255);
   LA3G_LAUNCHED();
   (void) g;
   return LA3G_OK;
@@ -559,7 +559,7 @@ int sssp_engine_init(Engine* E)
   LA3G_TRY(E->staging.alloc((uint64_t) kOutChunkS * N * 4));
   LA3G_TRY(E->outpos.alloc((uint64_t) kOutChunkS * N * 4));
   LA3G_CUDA(cudaMemsetAsync(E->ctr.p, 0, 64, s));
-  k_ls_fill_u32<<<kSMs * 8, 256, 0, s>>>((uint64_t) N * L, E->dist.as<uint32_t>(), kInfD);
+  k_ls_fill_u32<<<num_sms() * 8, 256, 0, s>>>((uint64_t) N * L, E->dist.as<uint32_t>(), kInfD);
   LA3G_LAUNCHED();
   k_reg_end<<<grid_for(N, 256), 256, 0, s>>>(g.out_ptr, g.out_row, N, g.nreg, E->reg_end.as<uint32_t>());
   LA3G_LAUNCHED();
@@ -605,10 +605,10 @@ int bfs_retire(Engine* E, const std::vector<uint32_t>& lanes_in, bool deliver, u
     LA3G_CUDA(cudaMemcpyAsync(E->ret.p, wm.data(), W * 8, cudaMemcpyHostToDevice, s));
     LA3G_CUDA(cudaMemcpyAsync(E->ret.as<uint8_t>() + W * 8, wb.data(), W * 4, cudaMemcpyHostToDevice, s));
     ProfileScope prof("serve_bfs_out", s, 0.0);
-    k_lb_out_pos<<<kSMs * 8, 256, 0, s>>>(E->ret.as<uint64_t>(), (const uint32_t*) (E->ret.as<uint8_t>() + W * 8), N, W,
+    k_lb_out_pos<<<num_sms() * 8, 256, 0, s>>>(E->ret.as<uint64_t>(), (const uint32_t*) (E->ret.as<uint8_t>() + W * 8), N, W,
                                           E->hops.as<uint8_t>(), E->outpos.as<uint8_t>());
     LA3G_LAUNCHED();
-    k_lb_out_id<<<kSMs * 8, 256, 0, s>>>(nl, N, g.pos_of_id, E->outpos.as<uint8_t>(), E->staging.as<uint8_t>());
+    k_lb_out_id<<<num_sms() * 8, 256, 0, s>>>(nl, N, g.pos_of_id, E->outpos.as<uint8_t>(), E->staging.as<uint8_t>());
     LA3G_LAUNCHED();
     tls_launches += 2;
     for (uint32_t j = 0; deliver && j < nl; j++)
@@ -622,7 +622,7 @@ int bfs_retire(Engine* E, const std::vector<uint32_t>& lanes_in, bool deliver, u
   std::vector<uint64_t> m(W, 0);
   for (uint32_t l : lanes) m[l / 64] |= 1ull << (l % 64);
   LA3G_CUDA(cudaMemcpyAsync(E->mask.p, m.data(), W * 8, cudaMemcpyHostToDevice, s));
-  k_lb_unset<<<kSMs * 8, 256, 0, s>>>((uint64_t) N * W, W, E->mask.as<uint64_t>(), E->vis.as<uint64_t>(), front);
+  k_lb_unset<<<num_sms() * 8, 256, 0, s>>>((uint64_t) N * W, W, E->mask.as<uint64_t>(), E->vis.as<uint64_t>(), front);
   LA3G_LAUNCHED();
   tls_launches++;
   if (alive)
@@ -798,11 +798,11 @@ int bfs_loop(Engine* E)
     if (pull_words)
     {
       ProfileScope prof("serve_bfs_pull", s, 0.0);
-      k_lb_pull<<<kSMs * 8, 256, 0, s>>>(g.in_ptr, g.in_col, nrows, N, W, E->vis.as<uint64_t>(), front, next,
+      k_lb_pull<<<num_sms() * 8, 256, 0, s>>>(g.in_ptr, g.in_col, nrows, N, W, E->vis.as<uint64_t>(), front, next,
                                          E->alive[cur].as<uint64_t>(), E->alive[cur ^ 1].as<uint64_t>(),
                                          E->hops.as<uint8_t>(), hop, pull_words, fdeg);
       LA3G_LAUNCHED();
-      k_lb_clear<<<kSMs * 8, 256, 0, s>>>(NW, W, front, pull_words);
+      k_lb_clear<<<num_sms() * 8, 256, 0, s>>>(NW, W, front, pull_words);
       LA3G_LAUNCHED();
       tls_launches += 2;
     }
@@ -811,11 +811,11 @@ int bfs_loop(Engine* E)
       ProfileScope prof("serve_bfs_push", s, 0.0);
       const PairList pl{E->active.as<uint32_t>(), E->hub[0].as<uint32_t>(), E->hub_t0[0].as<uint32_t>(), ctr + 2, ctr + 4};
       LA3G_CUDA(cudaMemsetAsync(ctr + 4, 0, 8, s));
-      k_lb_list<<<kSMs * 8, 256, 0, s>>>(NW, W, g.in_ptr, front, push_words, pl);
+      k_lb_list<<<num_sms() * 8, 256, 0, s>>>(NW, W, g.in_ptr, front, push_words, pl);
       LA3G_LAUNCHED();
-      k_lb_push<<<kSMs * 8, 256, 0, s>>>(g.in_ptr, g.in_col, W, front, E->vis.as<uint64_t>(), next, pl);
+      k_lb_push<<<num_sms() * 8, 256, 0, s>>>(g.in_ptr, g.in_col, W, front, E->vis.as<uint64_t>(), next, pl);
       LA3G_LAUNCHED();
-      k_lb_apply<<<kSMs * 8, 256, 0, s>>>(g.in_ptr, nrows, N, W, E->vis.as<uint64_t>(), front, next,
+      k_lb_apply<<<num_sms() * 8, 256, 0, s>>>(g.in_ptr, nrows, N, W, E->vis.as<uint64_t>(), front, next,
                                           E->alive[cur ^ 1].as<uint64_t>(), E->hops.as<uint8_t>(), hop, push_words,
                                           fdeg);
       LA3G_LAUNCHED();
@@ -858,15 +858,15 @@ int sssp_retire(Engine* E, const std::vector<uint32_t>& lanes)
     ProfileScope prof("serve_sssp_out", s, 0.0);
     if (g.nsink)
     {
-      k_ls_sinks<<<kSMs * 8, 256, 0, s>>>(g.in_ptr, g.in_col, g.in_w, g.nreg, g.nsink, L, E->ret.as<uint32_t>(), nl,
+      k_ls_sinks<<<num_sms() * 8, 256, 0, s>>>(g.in_ptr, g.in_col, g.in_w, g.nreg, g.nsink, L, E->ret.as<uint32_t>(), nl,
                                           E->rpos.as<uint32_t>(), g.src_base(), g.iso_base(), E->dist.as<uint32_t>());
       LA3G_LAUNCHED();
       tls_launches++;
     }
-    k_ls_out_pos<<<kSMs * 8, 256, 0, s>>>(E->ret.as<uint32_t>(), nl, N, L, E->dist.as<uint32_t>(),
+    k_ls_out_pos<<<num_sms() * 8, 256, 0, s>>>(E->ret.as<uint32_t>(), nl, N, L, E->dist.as<uint32_t>(),
                                           E->outpos.as<uint32_t>());
     LA3G_LAUNCHED();
-    k_ls_out_id<<<kSMs * 8, 256, 0, s>>>(nl, N, g.pos_of_id, E->outpos.as<uint32_t>(), E->staging.as<uint32_t>());
+    k_ls_out_id<<<num_sms() * 8, 256, 0, s>>>(nl, N, g.pos_of_id, E->outpos.as<uint32_t>(), E->staging.as<uint32_t>());
     LA3G_LAUNCHED();
     tls_launches += 2;
     for (uint32_t j = 0; j < nl; j++)
@@ -922,14 +922,14 @@ int sssp_loop(Engine* E)
     LA3G_CUDA(cudaMemsetAsync(E->alive[0].p, 0, W * 8, s));
     {
       ProfileScope p("serve_sssp_relax", s, 0.0);
-      k_bs_relax<<<kSMs * 16, 256, 0, s>>>(g.out_ptr, E->reg_end.as<uint32_t>(), g.out_row, g.out_w, L, W,
+      k_bs_relax<<<num_sms() * 16, 256, 0, s>>>(g.out_ptr, E->reg_end.as<uint32_t>(), g.out_row, g.out_w, L, W,
                                            E->sfront[cur].as<uint64_t>(), PL[cur], E->sfront[cur ^ 1].as<uint64_t>(),
                                            E->dist.as<uint32_t>());
       LA3G_LAUNCHED();
     }
     LA3G_CUDA(cudaMemsetAsync(ctr + (cur ^ 1), 0, 8, s));
     LA3G_CUDA(cudaMemsetAsync(ctr + 2 + (cur ^ 1), 0, 8, s));
-    k_bs_apply<<<kSMs * 8, 256, 0, s>>>(N, W, g.out_ptr, E->reg_end.as<uint32_t>(), E->sfront[cur ^ 1].as<uint64_t>(),
+    k_bs_apply<<<num_sms() * 8, 256, 0, s>>>(N, W, g.out_ptr, E->reg_end.as<uint32_t>(), E->sfront[cur ^ 1].as<uint64_t>(),
                                         PL[cur ^ 1], E->sfront[cur].as<uint64_t>(), PL[cur],
                                         E->alive[0].as<uint64_t>());
     LA3G_LAUNCHED();

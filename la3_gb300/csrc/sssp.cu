@@ -484,7 +484,7 @@ static int sssp_run(la3g_graph* G, SsspScratch* ss, uint32_t root, la3g_stats* s
   uint32_t iter = 0;
   int cur = 0;
   uint64_t examined = 0;
-  const unsigned blocks = kSMs * 8;
+  const unsigned blocks = num_sms() * 8;
   for (;;)
   {
     if (iter > 1000000) return set_error(LA3G_ETIMEOUT, "sssp did not converge");
@@ -497,7 +497,7 @@ static int sssp_run(la3g_graph* G, SsspScratch* ss, uint32_t root, la3g_stats* s
       // messages of their columns, one dist read per row
       ProfileScope p("sssp_pull", s, 8.0 * ss->reg_in + 8.0 * ss->reg_in + 8.0 * g.nreg);
       // warps split between long-row tasks and short rows in proportion to their in-edges
-      const uint32_t all_warps = kSMs * 8 * 8;
+      const uint32_t all_warps = num_sms() * 8 * 8;
       const uint32_t task_warps =
           ss->ntasks ? std::min<uint32_t>(ss->ntasks, std::max<uint32_t>(1, (uint32_t) ((double) all_warps *
                                                                                           ss->task_edges /
@@ -509,7 +509,7 @@ static int sssp_run(la3g_graph* G, SsspScratch* ss, uint32_t root, la3g_stats* s
                                                                (uint32_t) nbig, ss->msg, ss->fmsg);
       LA3G_LAUNCHED();
       tls_launches += 2;
-      k_sssp_pull<<<kSMs * 8, 256, 0, s>>>(g.in_ptr, g.in_col, g.in_w, g.nreg, ss->task_row, ss->task_begin,
+      k_sssp_pull<<<num_sms() * 8, 256, 0, s>>>(g.in_ptr, g.in_col, g.in_w, g.nreg, ss->task_row, ss->task_begin,
                                             ss->ntasks, task_warps, ss->ymin, ss->fmsg, ss->msg, ss->dist, ss->raw,
                                             ss->ctr);
       LA3G_LAUNCHED();
@@ -532,7 +532,7 @@ static int sssp_run(la3g_graph* G, SsspScratch* ss, uint32_t root, la3g_stats* s
       LA3G_LAUNCHED();
       examined += front_deg;
     }
-    k_sssp_apply<<<kSMs * 4, 256, 0, s>>>(g.out_ptr, ss->reg_end, ss->raw, ss->dist, ss->msg, ss->stamp, iter,
+    k_sssp_apply<<<num_sms() * 4, 256, 0, s>>>(g.out_ptr, ss->reg_end, ss->raw, ss->dist, ss->msg, ss->stamp, iter,
                                          ss->small[cur ^ 1], ss->big[cur ^ 1], ss->big_task0[cur ^ 1], ss->ctr);
     LA3G_LAUNCHED();
     tls_launches++;

@@ -843,9 +843,9 @@ static int tc_lists(la3g_graph* G, TcScratch* ts, bool library_sort)
     }
     else
     {
-      k_tc_sort_rows<8><<<kSMs * 8, 256, 0, s>>>(ts->pptr, N, ts->pcol_raw, ts->pcol, ts->big_rows, ts->ctr + 6);
+      k_tc_sort_rows<8><<<num_sms() * 8, 256, 0, s>>>(ts->pptr, N, ts->pcol_raw, ts->pcol, ts->big_rows, ts->ctr + 6);
       LA3G_LAUNCHED();
-      k_tc_sort_big<<<kSMs, 1024, kTcSortBigSmem, s>>>(ts->pptr, ts->pcol_raw, ts->pcol, ts->big_rows, ts->ctr + 6,
+      k_tc_sort_big<<<num_sms(), 1024, kTcSortBigSmem, s>>>(ts->pptr, ts->pcol_raw, ts->pcol, ts->big_rows, ts->ctr + 6,
                                                        ts->ctr + 7);
       LA3G_LAUNCHED();
       tls_launches += 2;
@@ -924,13 +924,13 @@ extern "C" int la3g_tc(la3g_graph* G, uint64_t* total_out, uint32_t* per_vertex_
       // task counts on the device: warp and small-block counts are the two
       // halves of the packed total (little-endian), large-block the other
       const uint32_t* nw = (const uint32_t*) (ts->toff + N);
-      k_tc_count_warp<kTcWarpKernelWarps><<<kSMs * 5, kTcWarpKernelWarps * 32, 0, s>>>(
+      k_tc_count_warp<kTcWarpKernelWarps><<<num_sms() * 5, kTcWarpKernelWarps * 32, 0, s>>>(
           ts->pptr, ts->pcol, ts->pairs, ts->mptr, ts->wtasks, nw, ts->id_of_rank, ts->ntri, ts->ctr);
       LA3G_LAUNCHED();
-      TC_MID_KERNEL<<<kSMs * 8, kTcMidThreads, kTcMidSmem, s>>>(ts->pptr, ts->pcol, ts->pairs, ts->mptr, ts->mtasks,
+      TC_MID_KERNEL<<<num_sms() * 8, kTcMidThreads, kTcMidSmem, s>>>(ts->pptr, ts->pcol, ts->pairs, ts->mptr, ts->mtasks,
                                                                  nw + 1, ts->id_of_rank, ts->ntri, ts->ctr);
       LA3G_LAUNCHED();
-      TC_BIG_KERNEL<<<kSMs * 3, kTcBlockThreads, kTcBlockSmem, s>>>(ts->pptr, ts->pcol, ts->pairs, ts->mptr,
+      TC_BIG_KERNEL<<<num_sms() * 3, kTcBlockThreads, kTcBlockSmem, s>>>(ts->pptr, ts->pcol, ts->pairs, ts->mptr,
                                                                      ts->btasks, ts->toff2 + N, ts->id_of_rank,
                                                                      ts->ntri, ts->ctr);
       LA3G_LAUNCHED();

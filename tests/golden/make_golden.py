@@ -19,6 +19,7 @@ Run it from the repository root:  python tests/golden/make_golden.py
 from __future__ import annotations
 
 import json
+import os
 import shutil
 import subprocess
 import sys
@@ -30,7 +31,8 @@ import numpy as np
 ROOT = Path(__file__).resolve().parents[2]
 GOLD = ROOT / "tests" / "golden"
 DATA = GOLD / "data"
-REFDATA = Path("/root/reference/data")
+# the reference checkout whose sample data are copied (LA3_REFERENCE overrides it)
+REFDATA = Path(os.environ.get("LA3_REFERENCE", "/root/reference")) / "data"
 REF_BIN = ROOT / "oracle" / "_ref" / "bin"
 
 sys.path.insert(0, str(ROOT))

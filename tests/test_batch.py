@@ -75,3 +75,23 @@ def test_sssp_batch_equals_single(gpu, graphs):
     for i in list(range(0, 300, 23)) + [0, 1, 2, 3, 299]:
         d1, _ = L.sssp(g, int(roots[i]))
         assert np.array_equal(dist[i], d1), (i, int(roots[i]))
+
+
+def test_persistent_barrier_wait_runs_out_cleanly(gpu, graphs):
+    """The persistent kernel's grid-barrier waits are bounded: with a limit
+    of zero polls the first block that has to wait gives up, every block
+    leaves, and the call returns LA3G_ETIMEOUT.  The device stays usable:
+    with the default limit back, the same batch equals the single-root
+    runs."""
+    L = gpu
+    g = graphs["rmat"]
+    roots = _roots(graphs["n"], 96, 41)
+    L.batch_config(g, 1, 256, 0.0)
+    L.batch_set_wait_limit(g, 0)
+    with pytest.raises(L._native.LA3GError) as ex:
+        L.bfs_batch(g, roots)
+    assert ex.value.status == 6  # LA3G_ETIMEOUT
+    L.batch_set_wait_limit(g, -1)
+    hops, _ = L.bfs_batch(g, roots)
+    for i in (0, 5, 50, 95):
+        assert np.array_equal(hops[i], L.bfs(g, int(roots[i]), True, False)[0]), i
