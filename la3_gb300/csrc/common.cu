@@ -110,6 +110,13 @@ ProfileScope::~ProfileScope()
   k.bytes += bytes;
 }
 
+bool profile_enabled() { return prof_on; }
+
+DeviceLoop::~DeviceLoop()
+{
+  if (exec) cudaGraphExecDestroy(exec);
+}
+
 void profile_add_bytes(const char* name, double bytes)
 {
   if (!prof_on) return;

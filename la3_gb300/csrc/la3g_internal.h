@@ -81,6 +81,40 @@ inline unsigned grid_for(uint64_t n, unsigned block, unsigned max_blocks = num_s
   return (unsigned) g;
 }
 
+// Block-wide reductions for kernels that add their partial counts into one
+// global counter: one atomic per block instead of one per warp (thousands of
+// same-address atomics serialise in L2).  Every thread of the block must
+// call them; the result is valid in thread 0.
+__device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long v)
+{
+  __shared__ unsigned long long s_part[32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __syncthreads();  // s_part may still be read from a previous call
+  if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32)
+  {
+    v = threadIdx.x < (blockDim.x + 31) / 32 ? s_part[threadIdx.x] : 0ull;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  }
+  return v;
+}
+
+__device__ __forceinline__ uint32_t block_min_u32(uint32_t v)
+{
+  __shared__ uint32_t s_part[32];
+  for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32)
+  {
+    v = threadIdx.x < (blockDim.x + 31) / 32 ? s_part[threadIdx.x] : 0xFFFFFFFFu;
+    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+  }
+  return v;
+}
+
 // Kernel-level profiling: when on, a launch is bracketed by events on its
 // stream and its time accumulated under `name` with `bytes` algorithmic
 // bytes.  Always counts the launch.
@@ -207,6 +241,109 @@ struct CallTimer
 };
 
 double now_ms();
+
+// True while kernel-level profiling is on (la3g_profile_enable).
+bool profile_enabled();
+
+// An iteration loop that runs on the device: one CUDA graph holding
+//   while (cont) { decide; switch (mode) { body[0] ... body[n-1] } }
+// The decide kernel reads the loop state the previous iteration left in
+// device memory, picks the next body (push or pull, top-down or bottom-up,
+// the ping-pong parity of the frontier buffers) and ends the loop, all with
+// `cudaGraphSetConditional`; the host launches the graph once per call and
+// synchronises once at the end.  The same decide kernel and bodies also run
+// host-stepped (one mode read back per iteration) when profiling is on,
+// since event-timed scopes cannot sit inside a conditional body.
+struct DeviceLoop
+{
+  cudaGraphExec_t exec = nullptr;
+  cudaGraphConditionalHandle cont = 0, mode = 0;
+  int nbodies = 0;
+  uint32_t body_launches[16] = {};  // kernels one pass through each body launches
+  ~DeviceLoop();
+};
+
+// Builds `L`: `decide(cap, cont, mode)` enqueues the decide kernel on the
+// capture stream, `body(cap, k)` enqueues body k's kernels and memsets.
+template <class Decide, class Body>
+int device_loop_build(DeviceLoop* L, int nbodies, Decide&& decide, Body&& body);
+
+// Kernels of the loop state call this to end or steer the loop; in the
+// host-stepped form (handles 0) nothing is set and the host reads the state.
+__device__ __forceinline__ void loop_set(cudaGraphConditionalHandle h, unsigned v)
+{
+  if (h) cudaGraphSetConditional(h, v);
+}
+
+template <class Decide, class Body>
+int device_loop_build(DeviceLoop* L, int nbodies, Decide&& decide, Body&& body)
+{
+  if (nbodies > 16) return set_error(LA3G_EINVAL, "device loop with %d bodies", nbodies);
+  cudaGraph_t graph = nullptr;
+  cudaStream_t cap = nullptr;
+  const uint32_t launches0 = tls_launches;
+  int rc = LA3G_OK;
+  auto fail = [&](cudaError_t e) {
+    if (e == cudaSuccess) return false;
+    cudaGetLastError();
+    rc = set_error(LA3G_ECUDA, "device loop graph: %s", cudaGetErrorString(e));
+    return true;
+  };
+  do
+  {
+    if (fail(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking))) break;
+    if (fail(cudaGraphCreate(&graph, 0))) break;
+    if (fail(cudaGraphConditionalHandleCreate(&L->cont, graph, 1, cudaGraphCondAssignDefault))) break;
+    if (fail(cudaGraphConditionalHandleCreate(&L->mode, graph, 0, cudaGraphCondAssignDefault))) break;
+    cudaGraphNodeParams wp = {};
+    wp.type = cudaGraphNodeTypeConditional;
+    wp.conditional.handle = L->cont;
+    wp.conditional.type = cudaGraphCondTypeWhile;
+    wp.conditional.size = 1;
+    cudaGraphNode_t wnode;
+    if (fail(cudaGraphAddNode(&wnode, graph, nullptr, nullptr, 0, &wp))) break;
+    cudaGraph_t wbody = wp.conditional.phGraph_out[0];
+    // the decide kernel, then the switch over the bodies
+    if (fail(cudaStreamBeginCaptureToGraph(cap, wbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal))) break;
+    rc = decide(cap, L->cont, L->mode);
+    cudaStreamCaptureStatus cs;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    if (rc == LA3G_OK && fail(cudaStreamGetCaptureInfo(cap, &cs, nullptr, nullptr, &deps, nullptr, &ndeps))) {}
+    cudaGraphNode_t dnode = ndeps ? deps[0] : nullptr;
+    cudaGraph_t dummy = nullptr;
+    if (fail(cudaStreamEndCapture(cap, &dummy)) || rc != LA3G_OK || ndeps != 1) 
+    {
+      if (rc == LA3G_OK) rc = set_error(LA3G_ECUDA, "device loop graph: decide step is not one node");
+      break;
+    }
+    cudaGraphNodeParams sp = {};
+    sp.type = cudaGraphNodeTypeConditional;
+    sp.conditional.handle = L->mode;
+    sp.conditional.type = cudaGraphCondTypeSwitch;
+    sp.conditional.size = (unsigned) nbodies;
+    cudaGraphNode_t snode;
+    if (fail(cudaGraphAddNode(&snode, wbody, &dnode, nullptr, 1, &sp))) break;
+    for (int k = 0; k < nbodies && rc == LA3G_OK; k++)
+    {
+      if (fail(cudaStreamBeginCaptureToGraph(cap, sp.conditional.phGraph_out[k], nullptr, nullptr, 0,
+                                             cudaStreamCaptureModeThreadLocal)))
+        break;
+      const uint32_t before = tls_launches;
+      rc = body(cap, k);
+      L->body_launches[k] = tls_launches - before;
+      cudaGraph_t out = nullptr;
+      if (fail(cudaStreamEndCapture(cap, &out))) break;
+    }
+    if (rc != LA3G_OK) break;
+    if (fail(cudaGraphInstantiate(&L->exec, graph, 0))) break;
+    L->nbodies = nbodies;
+  } while (0);
+  tls_launches = launches0;
+  if (graph) cudaGraphDestroy(graph);
+  if (cap) cudaStreamDestroy(cap);
+  return rc;
+}
 
 }  // namespace la3g
 

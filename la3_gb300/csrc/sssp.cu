@@ -13,8 +13,12 @@
 //     vertex's final distance (activated or not, INF included) and from the
 //     root's message if the root is a source (:131-148).
 // Push relaxation uses atomicMin on dist: the value a row holds after the
-// iteration is min(old, min over messages) exactly as apply computes it,
-// and a row is activated iff some relaxation lowered it.
+// iteration is min(old, min over messages) exactly as apply computes it.  A
+// row is activated iff some relaxation lowered it, i.e. iff its distance is
+// now below its message (the distance it scattered when it was last
+// activated; INF if never): one dense pass over the regular rows after each
+// iteration finds those rows, scatters their new distance and forms the next
+// frontier, so the relaxations themselves only do a non-returning atomicMin.
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
@@ -35,18 +39,18 @@ static constexpr uint32_t kPullLanes = 4;     // lanes per short row in a pull s
 struct SsspScratch
 {
   uint32_t* dist = nullptr;
-  uint32_t* msg = nullptr;
-  uint32_t* stamp = nullptr;
+  uint32_t* msg = nullptr;        // the distance each vertex scattered at its last activation (INF if never)
   uint32_t* reg_end = nullptr;   // [nslots] end of each vertex's out-edges into regular rows
-  uint32_t* raw = nullptr;       // vertices lowered in the current iteration
-  uint32_t* small[2] = {nullptr, nullptr};
-  uint32_t* big[2] = {nullptr, nullptr};
-  uint32_t* big_task0[2] = {nullptr, nullptr};
-  // [0] raw count, [1] next degree sum, [2] next small count, [3] hub slots and tasks (frontier.cuh),
-  // [4] scratch
+  uint32_t* small[1] = {nullptr};      // push steps: the frontier's split lists
+  uint32_t* big[1] = {nullptr};
+  uint32_t* big_task0[1] = {nullptr};
+  // [0] activated count, [1] their regular out-degree sum, [2] activated with regular out-edges,
+  // [3] scratch, [4] scratch, [5] the next frontier's smallest message
   unsigned long long* ctr = nullptr;
   unsigned long long* hctr = nullptr;
-  uint32_t* fmsg = nullptr;       // pull steps: msg of the frontier vertices, INF elsewhere
+  uint32_t* fbits = nullptr;      // [nslots / 32 + 1] the current frontier, one bit per vertex
+  unsigned long long* fctr = nullptr;  // push steps: [0] small-list length, [1] hub slots and tasks
+  uint32_t* fmsg = nullptr;       // pull steps: msg of the current frontier's vertices, INF elsewhere
   uint32_t* long_rows = nullptr;  // regular rows with more than kPullLong in-edges
   uint32_t nlong = 0;
   uint32_t* task_row = nullptr;   // pull tasks over the long rows: kPullChunk in-edges each
@@ -56,6 +60,7 @@ struct SsspScratch
   uint32_t* ymin = nullptr;       // [nlong] partial minima of the long rows (INF between steps)
   uint64_t reg_in = 0;            // in-edges of the regular rows
   uint32_t max_w = 0;             // largest weight: pull steps need INF + w to stay in uint32
+  uint32_t min_w = 0;             // smallest weight of a regular row's in-edge
   uint32_t* by_id = nullptr;      // [nslots] distances reordered by id before they leave the device
 };
 
@@ -66,20 +71,21 @@ static void sssp_scratch_free(void* p)
   delete s;
 }
 
-__global__ void k_sssp_init(uint32_t N, uint32_t* dist, uint32_t* stamp)
+__global__ void k_sssp_init(uint32_t N, uint32_t* dist, uint32_t* msg, uint32_t* fmsg)
 {
   for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x)
   {
     dist[p] = kInf;
-    stamp[p] = 0;
+    msg[p] = kInf;
+    fmsg[p] = kInf;
   }
 }
 
-__global__ void k_sssp_root(uint32_t rp, int push, uint32_t* dist, uint32_t* msg, uint32_t* list, uint32_t* task0)
+__global__ void k_sssp_root(uint32_t rp, int scatter, uint32_t* dist, uint32_t* msg, uint32_t* fbits)
 {
   dist[rp] = 0;
   msg[rp] = 0;
-  if (push) { list[0] = rp; task0[0] = 0; }
+  if (scatter) fbits[rp >> 5] = 1u << (rp & 31);
 }
 
 // End of the regular-row part of every out-edge list (rows ascend, so the
@@ -100,23 +106,9 @@ __global__ void k_sssp_reg_end(const uint32_t* __restrict__ ptr, const uint32_t*
   }
 }
 
-__device__ __forceinline__ void relax(uint32_t v, uint32_t cand, bool valid, uint32_t* dist, uint32_t* stamp,
-                                      uint32_t tag, uint32_t* raw, unsigned long long* ctr, int lane)
+__device__ __forceinline__ void relax(uint32_t v, uint32_t cand, bool valid, uint32_t* dist)
 {
-  bool add = false;
-  if (valid && cand < dist[v])
-  {
-    const uint32_t old = atomicMin(&dist[v], cand);
-    if (cand < old) add = atomicExch(&stamp[v], tag) != tag;
-  }
-  const unsigned mask = __ballot_sync(0xffffffffu, add);
-  if (mask)
-  {
-    uint32_t base = 0;
-    if (lane == 0) base = (uint32_t) atomicAdd(&ctr[0], (unsigned long long) __popc(mask));
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (add) raw[base + __popc(mask & ((1u << lane) - 1))] = v;
-  }
+  if (valid && cand < dist[v]) atomicMin(&dist[v], cand);  // result unused: a reduction in L2
 }
 
 // Relaxation over a split frontier: hubs first (all warps share each hub's
@@ -125,11 +117,12 @@ __device__ __forceinline__ void relax(uint32_t v, uint32_t cand, bool valid, uin
 // scatter values are.
 __global__ void __launch_bounds__(256)
 k_sssp_push(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ reg_end, const uint32_t* __restrict__ row,
-            const uint32_t* __restrict__ w, const uint32_t* __restrict__ small, uint32_t nsmall,
-            const uint32_t* __restrict__ big, const uint32_t* __restrict__ big_task0, uint32_t nbig, uint32_t ntasks,
-            const uint32_t* __restrict__ msg, uint32_t* dist, uint32_t* stamp, uint32_t tag, uint32_t* raw,
-            unsigned long long* ctr)
+            const uint32_t* __restrict__ w, const uint32_t* __restrict__ small, const uint32_t* __restrict__ big,
+            const uint32_t* __restrict__ big_task0, const unsigned long long* __restrict__ fctr,
+            const uint32_t* __restrict__ msg, uint32_t* dist)
 {
+  const uint32_t nsmall = (uint32_t) fctr[0];
+  const uint32_t nbig = hub_count(fctr[1]), ntasks = hub_tasks(fctr[1]);
   const int lane = threadIdx.x & 31;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -140,48 +133,107 @@ k_sssp_push(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ reg_e
     const uint32_t mu = msg[u];
     const uint32_t b = ptr[u] + (t - big_task0[slot]) * kHubTask;
     const uint32_t e = min(b + kHubTask, reg_end[u]);
-    for (uint32_t i0 = b; i0 < e; i0 += 32)
-    {
-      const uint32_t i = i0 + lane;
-      const bool ok = i < e;
-      relax(ok ? row[i] : 0, ok ? mu + w[i] : 0, ok, dist, stamp, tag, raw, ctr, lane);
-    }
+    for (uint32_t i = b + lane; i < e; i += 32) relax(row[i], mu + w[i], true, dist);
   }
   for (uint32_t f = warp; f < nsmall; f += nwarps)
   {
     const uint32_t u = small[f];
     const uint32_t mu = msg[u];
     const uint32_t b = ptr[u], e = reg_end[u];
-    for (uint32_t i0 = b; i0 < e; i0 += 32)
-    {
-      const uint32_t i = i0 + lane;
-      const bool ok = i < e;
-      relax(ok ? row[i] : 0, ok ? mu + w[i] : 0, ok, dist, stamp, tag, raw, ctr, lane);
-    }
+    for (uint32_t i = b + lane; i < e; i += 32) relax(row[i], mu + w[i], true, dist);
   }
 }
 
-// Activated vertices scatter their new distance and form the next frontier
-// (stamp = this iteration's tag: the pull step finds the frontier by it).
-__global__ void k_sssp_apply(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ reg_end,
-                             const uint32_t* __restrict__ raw, const uint32_t* __restrict__ dist, uint32_t* msg,
-                             uint32_t* stamp, uint32_t tag, uint32_t* small, uint32_t* big, uint32_t* big_task0,
-                             unsigned long long* ctr)
+// After an iteration: the regular rows whose distance fell below their
+// message were activated.  They scatter (msg = dist) and form the next
+// frontier: one bit per vertex (a warp writes a whole word, so every word of
+// the bitmap is rewritten) and the pull step's message array (fmsg: msg for
+// the frontier, INF elsewhere); the counters get the frontier's size, its
+// regular out-degree sum, how many of it have regular out-edges, and its
+// smallest message.
+__global__ void __launch_bounds__(256)
+k_sssp_dense_apply(uint32_t nreg, uint32_t words, const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ reg_end,
+                   const uint32_t* __restrict__ dist, uint32_t* msg, uint32_t* fmsg, uint32_t* fbits,
+                   unsigned long long* ctr)
 {
-  unsigned long long deg = 0;
-  const uint32_t n = (uint32_t) ctr[0];
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+  const uint32_t lane = threadIdx.x & 31;
+  unsigned long long deg = 0, cnt = 0, out = 0;
+  uint32_t fmin = 0xFFFFFFFFu;
+  const uint32_t nth = gridDim.x * blockDim.x;
+  for (uint32_t v0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); v0 < words * 32u; v0 += nth)
   {
-    uint32_t v = raw[i];
-    msg[v] = dist[v];
-    stamp[v] = tag;
-    uint32_t d = reg_end[v] - ptr[v];
-    deg += d;
-    if (d > kBigDeg) hub_append(v, d, big, big_task0, &ctr[3]);
-    else if (d) small[atomicAdd(&ctr[2], 1ull)] = v;
+    const uint32_t v = v0 + lane;
+    bool act = false;
+    if (v < nreg)
+    {
+      const uint32_t dv = dist[v];
+      act = dv < msg[v];
+      fmsg[v] = act ? dv : kInf;
+      if (act)
+      {
+        msg[v] = dv;
+        const uint32_t d = reg_end[v] - ptr[v];
+        deg += d;
+        cnt++;
+        out += d != 0;
+        fmin = min(fmin, dv);
+      }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, act);
+    if (lane == 0) fbits[v0 >> 5] = m;
   }
-  for (int o = 16; o > 0; o >>= 1) deg += __shfl_xor_sync(0xffffffffu, deg, o);
-  if ((threadIdx.x & 31) == 0 && deg) atomicAdd(&ctr[1], deg);
+  cnt = block_sum_u64(cnt);
+  deg = block_sum_u64(deg);
+  out = block_sum_u64(out);
+  fmin = block_min_u32(fmin);
+  if (threadIdx.x == 0)
+  {
+    if (cnt) atomicAdd(&ctr[0], cnt);
+    if (deg) atomicAdd(&ctr[1], deg);
+    if (out) atomicAdd(&ctr[2], out);
+    if (fmin != 0xFFFFFFFFu) atomicMin(&ctr[5], (unsigned long long) fmin);
+  }
+}
+
+// Push steps only: the frontier bitmap into the split lists (vertices with
+// up to kBigDeg regular out-edges, appended a warp at a time; hubs with their
+// edge tasks).
+__global__ void __launch_bounds__(256)
+k_sssp_split(const uint32_t* __restrict__ fbits, uint32_t words, const uint32_t* __restrict__ ptr,
+             const uint32_t* __restrict__ reg_end, uint32_t* small, uint32_t* big, uint32_t* big_task0,
+             unsigned long long* fctr)
+{
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t nth = gridDim.x * blockDim.x;
+  for (uint32_t w0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); w0 < words; w0 += nth)
+  {
+    const uint32_t w = w0 + lane;
+    uint32_t bits = w < words ? fbits[w] : 0u, c = 0;
+    for (uint32_t x = bits; x; x &= x - 1)
+    {
+      const uint32_t v = w * 32 + (__ffs(x) - 1);
+      const uint32_t d = reg_end[v] - ptr[v];
+      if (d > kBigDeg) hub_append(v, d, big, big_task0, &fctr[1]);
+      else c += d != 0;
+    }
+    uint32_t incl = c;
+    for (int o = 1; o < 32; o <<= 1)
+    {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= (uint32_t) o) incl += t;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    if (!total) continue;
+    uint32_t base = 0;
+    if (lane == 31) base = (uint32_t) atomicAdd(&fctr[0], (unsigned long long) total);
+    base = __shfl_sync(0xffffffffu, base, 31) + incl - c;
+    for (uint32_t x = bits; x; x &= x - 1)
+    {
+      const uint32_t v = w * 32 + (__ffs(x) - 1);
+      const uint32_t d = reg_end[v] - ptr[v];
+      if (d && d <= kBigDeg) small[base++] = v;
+    }
+  }
 }
 
 // Pull step (for large frontiers; the reference's own SpMV direction):
@@ -201,28 +253,17 @@ __device__ __forceinline__ void sssp_pull_edge(uint32_t e, const uint32_t* __res
   y = min(y, fmsg[col[e]] + w[e]);
 }
 
-// fmsg = msg for the frontier lists' vertices (small list, then hub slots).
-__global__ void k_fill_inf(uint32_t n, uint32_t* a)
-{
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a[i] = kInf;
-}
-
-__global__ void k_sssp_fmsg(const uint32_t* __restrict__ small, uint32_t nsmall, const uint32_t* __restrict__ big,
-                            uint32_t nbig, const uint32_t* __restrict__ msg, uint32_t* fmsg)
-{
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nsmall + nbig; i += gridDim.x * blockDim.x)
-  {
-    const uint32_t v = i < nsmall ? small[i] : big[i - nsmall];
-    fmsg[v] = msg[v];
-  }
-}
-
 __global__ void __launch_bounds__(256)
 k_sssp_pull(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ w,
             uint32_t nreg, const uint32_t* __restrict__ task_row, const uint32_t* __restrict__ task_begin,
             uint32_t ntasks, uint32_t task_warps, uint32_t* ymin, const uint32_t* __restrict__ fmsg,
-            const uint32_t* __restrict__ msg, uint32_t* dist, uint32_t* raw, unsigned long long* ctr)
+            uint32_t* dist, const uint32_t* __restrict__ long_rows, unsigned long long fmin, uint32_t min_w)
 {
+  // Every candidate of this step is a frontier message plus a weight, so at
+  // least fmin + min_w: a row already at or below that cannot be lowered and
+  // its in-edges are not read (the result is the same).
+  const uint32_t settled =
+      fmin == ~0ull ? 0u : (fmin + min_w < kInf ? (uint32_t) (fmin + min_w) : kInf);
   const int lane = threadIdx.x & 31;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (warp < task_warps)
@@ -231,6 +272,7 @@ k_sssp_pull(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, 
     for (uint32_t t = warp; t < ntasks; t += task_warps)
     {
       const uint32_t k = task_row[t];  // index into the long-row list
+      if (dist[long_rows[k]] <= settled) continue;
       const uint32_t b = task_begin[t], e = task_begin[ntasks + t];  // [begins | ends]
       uint32_t y = kInf;
       for (uint32_t i = b + lane; i < e; i += 32) sssp_pull_edge(i, col, w, fmsg, y);
@@ -250,12 +292,13 @@ k_sssp_pull(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, 
   for (uint32_t k = 0; k < rounds; k++)
   {
     const uint32_t v = group + k * ngroups;
-    uint32_t y = kInf;
+    uint32_t y = kInf, dv = 0;
     bool mine = false;
     if (v < nreg)
     {
       const uint32_t b = ptr[v], e = ptr[v + 1];
-      mine = e - b <= kPullLong;
+      dv = dist[v];
+      mine = e - b <= kPullLong && dv > settled;
       if (mine)
         for (uint32_t i = b + sub; i < e; i += 4 * G)
         {
@@ -275,22 +318,12 @@ k_sssp_pull(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, 
     }
 #pragma unroll
     for (int o = G / 2; o > 0; o >>= 1) y = min(y, __shfl_xor_sync(0xffffffffu, y, o));
-    const bool low = mine && sub == 0 && y < dist[v];
-    if (low) dist[v] = y;
-    const unsigned m = __ballot_sync(0xffffffffu, low);
-    if (m)
-    {
-      uint32_t base = 0;
-      if (lane == 0) base = (uint32_t) atomicAdd(&ctr[0], (unsigned long long) __popc(m));
-      base = __shfl_sync(0xffffffffu, base, 0);
-      if (low) raw[base + __popc(m & ((1u << lane) - 1))] = v;
-    }
+    if (mine && sub == 0 && y < dv) dist[v] = y;
   }
 }
 
 // Long rows after a pull step: apply the partial minimum, reset it.
-__global__ void k_sssp_pull_long(const uint32_t* __restrict__ long_rows, uint32_t nlong, uint32_t* ymin, uint32_t* dist,
-                                 uint32_t* raw, unsigned long long* ctr)
+__global__ void k_sssp_pull_long(const uint32_t* __restrict__ long_rows, uint32_t nlong, uint32_t* ymin, uint32_t* dist)
 {
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nlong; k += gridDim.x * blockDim.x)
   {
@@ -298,40 +331,44 @@ __global__ void k_sssp_pull_long(const uint32_t* __restrict__ long_rows, uint32_
     if (y == kInf) continue;
     ymin[k] = kInf;
     const uint32_t v = long_rows[k];
-    if (y < dist[v])
-    {
-      dist[v] = y;
-      raw[atomicAdd(&ctr[0], 1ull)] = v;
-    }
+    if (y < dist[v]) dist[v] = y;
   }
 }
 
 __global__ void k_sssp_long_rows(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ w, uint32_t nreg,
-                                 uint32_t* list, unsigned long long* n, unsigned long long* edges, unsigned int* maxw)
+                                 uint32_t* list, unsigned long long* n, unsigned long long* edges, unsigned int* maxw,
+                                 unsigned int* minw)
 {
   unsigned long long s = 0;
-  unsigned int mw = 0;
+  unsigned int mw = 0, lw = 0xFFFFFFFFu;
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nreg; v += gridDim.x * blockDim.x)
   {
     const uint32_t d = ptr[v + 1] - ptr[v];
     s += d;
-    for (uint32_t i = ptr[v]; i < ptr[v + 1]; i++) mw = max(mw, w[i]);
+    for (uint32_t i = ptr[v]; i < ptr[v + 1]; i++)
+    {
+      mw = max(mw, w[i]);
+      lw = min(lw, w[i]);
+    }
     if (d > kPullLong) list[atomicAdd(n, 1ull)] = v;
   }
   for (int o = 16; o > 0; o >>= 1)
   {
     s += __shfl_xor_sync(0xffffffffu, s, o);
     mw = max(mw, __shfl_xor_sync(0xffffffffu, mw, o));
+    lw = min(lw, __shfl_xor_sync(0xffffffffu, lw, o));
   }
   if ((threadIdx.x & 31) == 0)
   {
     if (s) atomicAdd(edges, s);
     if (mw) atomicMax(maxw, mw);
+    if (lw != 0xFFFFFFFFu) atomicMin(minw, lw);
   }
 }
 
 // A step pulls when its frontier's out-degree sum exceeds the regular rows'
-// in-edges / kPullDivisor (measured on R-MAT s22: 2 and 4 are best).
+// in-edges / kPullDivisor (measured on R-MAT s22: 2 and 4 give 1.90 ms per
+// call, 6 to 16 give 2.16-2.18 ms).
 static constexpr double kPullDivisor = 4.0;
 
 // Sink pass: y = min over in-neighbours (regular: final dist; the root if it
@@ -383,16 +420,13 @@ static int sssp_scratch(la3g_graph* G, SsspScratch** out)
   const uint32_t N = G->g.nslots;
   LA3G_TRY(galloc(G, &ss->dist, N));
   LA3G_TRY(galloc(G, &ss->msg, N));
-  LA3G_TRY(galloc(G, &ss->stamp, N));
   LA3G_TRY(galloc(G, &ss->reg_end, N));
-  LA3G_TRY(galloc(G, &ss->raw, N));
   LA3G_TRY(galloc(G, &ss->small[0], N));
-  LA3G_TRY(galloc(G, &ss->small[1], N));
   LA3G_TRY(galloc(G, &ss->big[0], N));
-  LA3G_TRY(galloc(G, &ss->big[1], N));
   LA3G_TRY(galloc(G, &ss->big_task0[0], N));
-  LA3G_TRY(galloc(G, &ss->big_task0[1], N));
   LA3G_TRY(galloc(G, &ss->ctr, 8));
+  LA3G_TRY(galloc(G, &ss->fctr, 2));
+  LA3G_TRY(galloc(G, &ss->fbits, (size_t) N / 32 + 2));
   LA3G_TRY(galloc(G, &ss->by_id, N));
   LA3G_CUDA(cudaHostAlloc(&ss->hctr, 8 * sizeof(unsigned long long), cudaHostAllocDefault));
   k_sssp_reg_end<<<grid_for(N, 256), 256, 0, G->stream>>>(G->g.out_ptr, G->g.out_row, N, G->g.nreg, ss->reg_end);
@@ -400,14 +434,17 @@ static int sssp_scratch(la3g_graph* G, SsspScratch** out)
   LA3G_TRY(galloc(G, &ss->long_rows, std::max<uint32_t>(G->g.nreg, 1)));
   LA3G_TRY(galloc(G, &ss->fmsg, N));
   LA3G_CUDA(cudaMemsetAsync(ss->ctr, 0, 8 * sizeof(unsigned long long), G->stream));
+  LA3G_CUDA(cudaMemsetAsync(ss->ctr + 3, 0xFF, sizeof(unsigned long long), G->stream));
   k_sssp_long_rows<<<grid_for(G->g.nreg, 256), 256, 0, G->stream>>>(G->g.in_ptr, G->g.in_w, G->g.nreg, ss->long_rows,
-                                                                     ss->ctr, ss->ctr + 1, (unsigned int*) (ss->ctr + 2));
+                                                                     ss->ctr, ss->ctr + 1, (unsigned int*) (ss->ctr + 2),
+                                                                     (unsigned int*) (ss->ctr + 3));
   LA3G_LAUNCHED();
-  LA3G_CUDA(cudaMemcpyAsync(ss->hctr, ss->ctr, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, G->stream));
+  LA3G_CUDA(cudaMemcpyAsync(ss->hctr, ss->ctr, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, G->stream));
   LA3G_CUDA(cudaStreamSynchronize(G->stream));
   ss->nlong = (uint32_t) ss->hctr[0];
   ss->reg_in = ss->hctr[1];
   ss->max_w = (uint32_t) ss->hctr[2];
+  ss->min_w = (uint32_t) ss->hctr[3];
   if (ss->nlong)
   {
     // cut the long rows into tasks of kPullChunk in-edges (host side: few rows)
@@ -453,11 +490,14 @@ static int sssp_run(la3g_graph* G, SsspScratch* ss, uint32_t root, la3g_stats* s
   DevGraph& g = G->g;
   cudaStream_t s = G->stream;
   const uint32_t N = g.nslots;
-  k_sssp_init<<<grid_for(N, 256), 256, 0, s>>>(N, ss->dist, ss->stamp);
+  const uint32_t words = N / 32 + 1;
+  k_sssp_init<<<grid_for(N, 256), 256, 0, s>>>(N, ss->dist, ss->msg, ss->fmsg);
   LA3G_LAUNCHED();
+  LA3G_CUDA(cudaMemsetAsync(ss->fbits, 0, (size_t) words * 4, s));
   tls_launches++;
   uint32_t rp = 0xFFFFFFFFu, src_root = 0xFFFFFFFFu;
-  uint64_t nsmall = 0, nbig = 0, ntasks = 0, front_deg = 0;
+  // the current frontier: vertices with regular out-edges, their out-degree sum
+  uint64_t nlist = 0, front_deg = 0;
   if (root < N)
   {
     LA3G_CUDA(cudaMemcpyAsync(&rp, g.pos_of_id + root, 4, cudaMemcpyDeviceToHost, s));
@@ -473,24 +513,21 @@ static int sssp_run(la3g_graph* G, SsspScratch* ss, uint32_t root, la3g_stats* s
       LA3G_CUDA(cudaStreamSynchronize(s));
       front_deg = re - hp[0];
     }
-    const bool hub = front_deg > kBigDeg;
-    k_sssp_root<<<1, 1, 0, s>>>(rp, scat ? 1 : 0, ss->dist, ss->msg, hub ? ss->big[0] : ss->small[0],
-                                ss->big_task0[0]);
+    k_sssp_root<<<1, 1, 0, s>>>(rp, scat ? 1 : 0, ss->dist, ss->msg, ss->fbits);
     LA3G_LAUNCHED();
     tls_launches++;
-    if (scat) (hub ? nbig : nsmall) = 1;
-    if (scat && hub) ntasks = (front_deg + kHubTask - 1) / kHubTask;
+    // a scattering root makes the first iteration run, even with no regular out-edge
+    if (scat) nlist = 1;
   }
   uint32_t iter = 0;
-  int cur = 0;
   uint64_t examined = 0;
+  unsigned long long front_min = 0;  // smallest message of the current frontier (the root's: 0)
   const unsigned blocks = num_sms() * 8;
   for (;;)
   {
     if (iter > 1000000) return set_error(LA3G_ETIMEOUT, "sssp did not converge");
     iter++;
-    if (nsmall + nbig == 0) break;
-    LA3G_CUDA(cudaMemsetAsync(ss->ctr, 0, 4 * sizeof(unsigned long long), s));
+    if (nlist == 0) break;
     if (iter > 1 && ss->max_w <= 0x80000000u && (double) front_deg * kPullDivisor > (double) ss->reg_in)
     {
       // in-edges of every regular row (index + weight), stamps and
@@ -503,21 +540,14 @@ static int sssp_run(la3g_graph* G, SsspScratch* ss, uint32_t root, la3g_stats* s
                                                                                           ss->task_edges /
                                                                                           std::max<uint64_t>(ss->reg_in, 1))))
                      : 0;
-      k_fill_inf<<<grid_for(N, 256), 256, 0, s>>>(N, ss->fmsg);
-      LA3G_LAUNCHED();
-      k_sssp_fmsg<<<grid_for(nsmall + nbig, 256), 256, 0, s>>>(ss->small[cur], (uint32_t) nsmall, ss->big[cur],
-                                                               (uint32_t) nbig, ss->msg, ss->fmsg);
-      LA3G_LAUNCHED();
-      tls_launches += 2;
       k_sssp_pull<<<num_sms() * 8, 256, 0, s>>>(g.in_ptr, g.in_col, g.in_w, g.nreg, ss->task_row, ss->task_begin,
-                                            ss->ntasks, task_warps, ss->ymin, ss->fmsg, ss->msg, ss->dist, ss->raw,
-                                            ss->ctr);
+                                                ss->ntasks, task_warps, ss->ymin, ss->fmsg, ss->dist, ss->long_rows,
+                                                front_min, ss->min_w);
       LA3G_LAUNCHED();
       tls_launches++;
       if (ss->nlong)
       {
-        k_sssp_pull_long<<<grid_for(ss->nlong, 256), 256, 0, s>>>(ss->long_rows, ss->nlong, ss->ymin, ss->dist,
-                                                                  ss->raw, ss->ctr);
+        k_sssp_pull_long<<<grid_for(ss->nlong, 256), 256, 0, s>>>(ss->long_rows, ss->nlong, ss->ymin, ss->dist);
         LA3G_LAUNCHED();
         tls_launches++;
       }
@@ -525,30 +555,35 @@ static int sssp_run(la3g_graph* G, SsspScratch* ss, uint32_t root, la3g_stats* s
     }
     else
     {
-      ProfileScope p("sssp_push", s, 8.0 * front_deg + 12.0 * (nsmall + nbig));
-      k_sssp_push<<<blocks, 256, 0, s>>>(g.out_ptr, ss->reg_end, g.out_row, g.out_w, ss->small[cur], (uint32_t) nsmall,
-                                         ss->big[cur], ss->big_task0[cur], (uint32_t) nbig, (uint32_t) ntasks, ss->msg,
-                                         ss->dist, ss->stamp, iter, ss->raw, ss->ctr);
+      LA3G_CUDA(cudaMemsetAsync(ss->fctr, 0, 2 * sizeof(unsigned long long), s));
+      k_sssp_split<<<grid_for(words, 256), 256, 0, s>>>(ss->fbits, words, g.out_ptr, ss->reg_end, ss->small[0],
+                                                        ss->big[0], ss->big_task0[0], ss->fctr);
+      LA3G_LAUNCHED();
+      tls_launches++;
+      ProfileScope p("sssp_push", s, 8.0 * front_deg + 12.0 * nlist);
+      k_sssp_push<<<blocks, 256, 0, s>>>(g.out_ptr, ss->reg_end, g.out_row, g.out_w, ss->small[0], ss->big[0],
+                                         ss->big_task0[0], ss->fctr, ss->msg, ss->dist);
       LA3G_LAUNCHED();
       examined += front_deg;
     }
-    k_sssp_apply<<<num_sms() * 4, 256, 0, s>>>(g.out_ptr, ss->reg_end, ss->raw, ss->dist, ss->msg, ss->stamp, iter,
-                                         ss->small[cur ^ 1], ss->big[cur ^ 1], ss->big_task0[cur ^ 1], ss->ctr);
+    LA3G_CUDA(cudaMemsetAsync(ss->ctr, 0, 3 * sizeof(unsigned long long), s));
+    LA3G_CUDA(cudaMemsetAsync(ss->ctr + 5, 0xFF, sizeof(unsigned long long), s));  // the next frontier's minimum
+    k_sssp_dense_apply<<<grid_for((uint64_t) words * 32, 256, num_sms() * 4), 256, 0, s>>>(g.nreg, words, g.out_ptr, ss->reg_end,
+                                                                            ss->dist, ss->msg, ss->fmsg, ss->fbits,
+                                                                            ss->ctr);
     LA3G_LAUNCHED();
     tls_launches++;
-    LA3G_CUDA(cudaMemcpyAsync(ss->hctr, ss->ctr, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    LA3G_CUDA(cudaMemcpyAsync(ss->hctr, ss->ctr, 6 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
     LA3G_CUDA(cudaStreamSynchronize(s));
     const uint64_t nn = ss->hctr[0];
-    nsmall = ss->hctr[2];
-    nbig = ss->hctr[3] >> kHubSlotShift;
-    ntasks = ss->hctr[3] & ((1ull << kHubSlotShift) - 1);
     front_deg = ss->hctr[1];
-    cur ^= 1;
+    nlist = ss->hctr[2];
+    front_min = ss->hctr[5];
     // A vertex lowered only into sink-free regular rows with no regular
     // out-edges is activated but has nothing to relax; the loop still runs
     // the next iteration only if something was activated.
     if (nn == 0) break;
-    if (nsmall + nbig == 0)
+    if (nlist == 0)
     {
       iter++;  // the next iteration runs with messages that reach no regular row
       break;
