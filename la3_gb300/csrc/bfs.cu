@@ -53,17 +53,44 @@ struct BfsScratch
   uint32_t* big[2] = {nullptr, nullptr};
   uint32_t* big_task0[2] = {nullptr, nullptr};
   uint32_t* bits[2] = {nullptr, nullptr};
-  FrontierCounters* ctr = nullptr;      // device
-  FrontierCounters* hctr = nullptr;     // pinned host mirror
+  // [2] device: ctr[c] holds the sizes of the frontier in small[c] / big[c]
+  // and, after a step from buffer c, ctr[c ^ 1] the touched count and the
+  // degree sum of the next frontier
+  FrontierCounters* ctr = nullptr;
+  unsigned long long* state = nullptr;   // the level loop's state (kB* slots), device side
+  unsigned long long* hstate = nullptr;  // pinned host mirror
   unsigned long long* red = nullptr;  // reduction scratch
   uint32_t* by_id = nullptr;          // [nslots] outputs reordered by id before they leave the device
   uint32_t words = 0;
+  DeviceLoop* loop = nullptr;         // the device-driven level loop (built on first use)
 };
+
+// Level-loop state slots (unsigned long long each).
+enum : int {
+  kBIter = 0,    // levels, counted as the reference counts iterations
+  kBPulls,       // bottom-up levels
+  kBExamined,    // edges examined
+  kBStatus,      // 1: the level limit was reached
+  kBFirst,       // 1 until the first decision (the root's frontier is in ctr[0])
+  kBMode,        // the body chosen last (kBDone: the loop has ended)
+  kBCur,         // which buffer pair holds the current frontier
+  kBBottomUp,    // direction of the last level
+  kBList,        // 1: the current frontier is in the split lists, 0: only in bits[cur]
+  kBUnvisited,   // degree sum of the vertices not yet visited
+  kBFrontDeg,    // degree sum of the current frontier
+  kBNfront,      // size of the current frontier
+  kBCount,       // [8] levels run per body
+  kBSlots = kBCount + 8
+};
+// Bodies: variant * 2 + the current buffer pair.
+enum : unsigned { kTdList = 0, kTdBits = 1, kBuList = 2, kBuBits = 3, kBDone = 8 };
+static constexpr double kAlpha = 14.0, kBeta = 24.0;
 
 static void bfs_scratch_free(void* p)
 {
   BfsScratch* s = (BfsScratch*) p;
-  if (s->hctr) cudaFreeHost(s->hctr);
+  if (s->hstate) cudaFreeHost(s->hstate);
+  delete s->loop;
   delete s;
 }
 
@@ -230,10 +257,12 @@ __device__ __forceinline__ void td_visit(uint32_t v, bool valid, uint32_t hu, co
 
 __global__ void __launch_bounds__(256)
 k_bfs_td_split(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ key,
-               const uint32_t* __restrict__ small, uint32_t nsmall, const uint32_t* __restrict__ big,
-               const uint32_t* __restrict__ big_task0, uint32_t nbig, uint32_t ntasks,
+               const uint32_t* __restrict__ small, const uint32_t* __restrict__ big,
+               const uint32_t* __restrict__ big_task0, const FrontierCounters* __restrict__ front,
                const uint8_t* __restrict__ hops, uint32_t* cand, uint32_t* raw, FrontierCounters* ctr)
 {
+  const uint32_t nsmall = (uint32_t) front->nsmall;
+  const uint32_t nbig = hub_count(front->packed), ntasks = hub_tasks(front->packed);
   const int lane = threadIdx.x & 31;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -272,10 +301,12 @@ __device__ __forceinline__ void push_split(uint32_t v, uint32_t deg, uint32_t* s
 
 // Top-down apply: touched vertices take hops and parent and form the next
 // frontier, split by degree.
-__global__ void k_bfs_td_apply_split(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ raw, uint8_t hop,
-                                     uint8_t* hops, uint32_t* parent, uint32_t* cand, uint32_t* small, uint32_t* big,
-                                     uint32_t* big_task0, FrontierCounters* ctr)
+__global__ void k_bfs_td_apply_split(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ raw,
+                                     const unsigned long long* __restrict__ state, uint8_t* hops, uint32_t* parent,
+                                     uint32_t* cand, uint32_t* small, uint32_t* big, uint32_t* big_task0,
+                                     FrontierCounters* ctr)
 {
+  const uint8_t hop = (uint8_t) (state[kBIter] + 1);
   unsigned long long deg = 0;
   const uint32_t n = (uint32_t) ctr->raw;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -288,16 +319,17 @@ __global__ void k_bfs_td_apply_split(const uint32_t* __restrict__ ptr, const uin
     deg += d;
     push_split(v, d, small, big, big_task0, ctr);
   }
-  for (int o = 16; o > 0; o >>= 1) deg += __shfl_xor_sync(0xffffffffu, deg, o);
-  if ((threadIdx.x & 31) == 0 && deg) atomicAdd(&ctr->degsum, deg);
+  deg = block_sum_u64(deg);
+  if (threadIdx.x == 0 && deg) atomicAdd(&ctr->degsum, deg);
 }
 
 // Bottom-up with the split counters (same scan as k_bfs_bu).
 __global__ void __launch_bounds__(256)
 k_bfs_bu_split(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ key,
-               uint32_t nrows, const uint32_t* __restrict__ fbits, uint32_t* nbits, uint8_t hop, uint8_t* hops,
-               uint32_t* parent, FrontierCounters* ctr)
+               uint32_t nrows, const uint32_t* __restrict__ fbits, uint32_t* nbits,
+               const unsigned long long* __restrict__ state, uint8_t* hops, uint32_t* parent, FrontierCounters* ctr)
 {
+  const uint8_t hop = (uint8_t) (state[kBIter] + 1);
   unsigned long long cnt = 0, deg = 0;
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nrows; v += gridDim.x * blockDim.x)
   {
@@ -317,15 +349,24 @@ k_bfs_bu_split(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ co
       }
     }
   }
-  for (int o = 16; o > 0; o >>= 1)
-  {
-    cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-    deg += __shfl_xor_sync(0xffffffffu, deg, o);
-  }
-  if ((threadIdx.x & 31) == 0 && cnt)
+  cnt = block_sum_u64(cnt);
+  deg = block_sum_u64(deg);
+  if (threadIdx.x == 0 && cnt)
   {
     atomicAdd(&ctr->raw, cnt);
     atomicAdd(&ctr->degsum, deg);
+  }
+}
+
+// Split-list frontier (sizes in `front`) -> bitmap.
+__global__ void k_front_to_bits(const uint32_t* __restrict__ small, const uint32_t* __restrict__ big,
+                                const FrontierCounters* __restrict__ front, uint32_t* bits)
+{
+  const uint32_t ns = (uint32_t) front->nsmall, n = ns + hub_count(front->packed);
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+  {
+    const uint32_t v = i < ns ? small[i] : big[i - ns];
+    atomicOr(&bits[v >> 5], 1u << (v & 31));
   }
 }
 
@@ -364,11 +405,110 @@ __global__ void k_by_id(uint32_t N, const uint32_t* __restrict__ id_of_pos, cons
 
 __global__ void k_bfs_root(uint32_t rp, uint8_t* hops, uint32_t* list) { hops[rp] = 0; list[0] = rp; }
 
-__global__ void k_bfs_root_split(uint32_t rp, uint8_t* hops, uint32_t* list, uint32_t* task0)
+// The root (an id below N): hops 0, and the first frontier in small[0] or
+// big[0] with its sizes in ctr[0] (empty if the root has no edges); the
+// loop state starts at level 0, top-down, from the lists.
+__global__ void k_bfs_root_state(uint32_t root, const uint32_t* __restrict__ pos_of_id,
+                                 const uint32_t* __restrict__ ptr, uint32_t nrows, uint64_t nent, uint8_t* hops,
+                                 uint32_t* small, uint32_t* big, uint32_t* big_task0, FrontierCounters* ctr,
+                                 unsigned long long* state)
 {
+  for (int k = 0; k < kBSlots; k++) state[k] = 0;
+  state[kBFirst] = 1;
+  state[kBList] = 1;
+  const uint32_t rp = pos_of_id[root];
   hops[rp] = 0;
-  list[0] = rp;
-  task0[0] = 0;
+  uint64_t deg = 0;
+  if (rp < nrows)
+  {
+    deg = ptr[rp + 1] - ptr[rp];
+    if (deg > kBigDeg)
+    {
+      big[0] = rp;
+      big_task0[0] = 0;
+      ctr->packed = hub_pack_inc((uint32_t) ((deg + kHubTask - 1) / kHubTask));
+    }
+    else
+    {
+      small[0] = rp;
+      ctr->nsmall = 1;
+    }
+    state[kBNfront] = 1;
+  }
+  state[kBFrontDeg] = deg;
+  state[kBUnvisited] = nent - deg;
+}
+
+// Start of every level (one thread).  First folds in what the last level
+// left in ctr[cur ^ 1] (as the reference's loop does after each SpMV: the
+// next frontier's size and degree sum, the unvisited degree sum), then
+// picks the direction (Beamer's alpha / beta test) and the body: top-down
+// from the lists, top-down after turning the bottom-up bitmap into lists,
+// bottom-up after turning the lists into a bitmap, or bottom-up from the
+// bitmap.  An empty frontier ends the loop.
+__global__ void k_bfs_decide(unsigned long long* S, const FrontierCounters* __restrict__ ctr, uint32_t N,
+                             uint64_t limit, cudaGraphConditionalHandle cont, cudaGraphConditionalHandle mode)
+{
+  unsigned long long it = S[kBIter];
+  bool done = false, convert = false;
+  if (S[kBFirst]) S[kBFirst] = 0;
+  else
+  {
+    const unsigned cur = (unsigned) S[kBCur];
+    const FrontierCounters c = ctr[cur ^ 1];
+    const unsigned long long nn = c.raw;
+    unsigned long long fdeg, nfront = nn;
+    bool list = true;
+    if (S[kBMode] / 2 >= kBuList)
+    {
+      fdeg = c.degsum;
+      const bool next_bu = !((double) nn < (double) N / kBeta);
+      if (nn && !next_bu) convert = true;  // the bitmap becomes lists before the top-down level
+      else list = false;
+    }
+    else
+    {
+      nfront = nn ? c.nsmall + hub_count(c.packed) : 0;
+      fdeg = nn ? c.degsum : 0;
+    }
+    S[kBUnvisited] -= min(S[kBUnvisited], fdeg);
+    S[kBCur] = cur ^ 1;
+    S[kBFrontDeg] = fdeg;
+    S[kBNfront] = nfront;
+    S[kBList] = list;
+    it++;
+    if (nfront == 0) done = true;
+  }
+  unsigned m = kBDone;
+  if (!done)
+  {
+    if (it > limit) S[kBStatus] = 1;
+    else
+    {
+      const unsigned long long nfront = S[kBNfront], fdeg = S[kBFrontDeg], unv = S[kBUnvisited];
+      bool bu = S[kBBottomUp] != 0;
+      if (!bu && (double) fdeg > (double) unv / kAlpha) bu = true;
+      else if (bu && (double) nfront < (double) N / kBeta) bu = false;
+      S[kBBottomUp] = bu;
+      if (nfront == 0) it++;  // nothing active: this level activates nothing
+      else
+      {
+        const unsigned variant = bu ? (S[kBList] && !convert ? kBuList : kBuBits) : (convert ? kTdBits : kTdList);
+        m = variant * 2 + (unsigned) S[kBCur];
+        if (bu)
+        {
+          S[kBExamined] += unv;
+          S[kBPulls]++;
+        }
+        else S[kBExamined] += fdeg;
+        S[kBCount + m]++;
+      }
+    }
+  }
+  S[kBIter] = it;
+  S[kBMode] = m;
+  loop_set(cont, m != kBDone);
+  loop_set(mode, m);
 }
 
 static int bfs_scratch(la3g_graph* G, BfsScratch** out)
@@ -393,158 +533,144 @@ static int bfs_scratch(la3g_graph* G, BfsScratch** out)
   LA3G_TRY(galloc(G, &bs->big_task0[1], N));
   LA3G_TRY(galloc(G, &bs->bits[0], bs->words));
   LA3G_TRY(galloc(G, &bs->bits[1], bs->words));
-  LA3G_TRY(galloc(G, &bs->ctr, 1));
+  LA3G_TRY(galloc(G, &bs->ctr, 2));
+  LA3G_TRY(galloc(G, &bs->state, kBSlots));
   LA3G_TRY(galloc(G, &bs->red, 1));
   LA3G_TRY(galloc(G, &bs->by_id, N));
-  LA3G_CUDA(cudaHostAlloc(&bs->hctr, sizeof(FrontierCounters), cudaHostAllocDefault));
+  LA3G_CUDA(cudaHostAlloc(&bs->hstate, kBSlots * sizeof(unsigned long long), cudaHostAllocDefault));
   *out = bs;
   return LA3G_OK;
 }
 
-// Runs BFS from `root` with results left on the device (positions).
+// One level's body m = variant * 2 + c (c: the buffer pair holding the
+// current frontier).  `fdeg`, `nfront` and `unv` (frontier degree sum and
+// size, unvisited degree sum) only size the profile entries' bytes; the
+// kernels read every count they need on the device.
+static int bfs_body(la3g_graph* G, BfsScratch* bs, cudaStream_t s, unsigned m, double fdeg, double nfront, double unv)
+{
+  DevGraph& g = G->g;
+  const uint32_t N = g.nslots, nrows = g.nrows();
+  const unsigned variant = m / 2, c = m & 1;
+  FrontierCounters* cur = bs->ctr + c;
+  FrontierCounters* next = bs->ctr + (c ^ 1);
+  LA3G_CUDA(cudaMemsetAsync(next, 0, sizeof(FrontierCounters), s));
+  if (variant == kTdBits)
+  {
+    // the bottom-up level's bitmap becomes split lists (sizes into ctr[c])
+    LA3G_CUDA(cudaMemsetAsync(&cur->nsmall, 0, 2 * sizeof(unsigned long long), s));
+    k_bits_to_split<<<grid_for(bs->words, 256), 256, 0, s>>>(bs->bits[c], bs->words, g.in_ptr, bs->small[c],
+                                                              bs->big[c], bs->big_task0[c], cur);
+    LA3G_LAUNCHED();
+    tls_launches++;
+  }
+  if (variant == kTdList || variant == kTdBits)
+  {
+    {
+      ProfileScope p("bfs_top_down", s, 4.0 * fdeg + 8.0 * nfront + 1.0 * fdeg);
+      k_bfs_td_split<<<num_sms() * 8, 256, 0, s>>>(g.in_ptr, g.in_col, g.hash_of_pos, bs->small[c], bs->big[c],
+                                                   bs->big_task0[c], cur, bs->hops, bs->cand, bs->raw, next);
+      LA3G_LAUNCHED();
+    }
+    k_bfs_td_apply_split<<<num_sms() * 4, 256, 0, s>>>(g.in_ptr, bs->raw, bs->state, bs->hops, bs->parent, bs->cand,
+                                                       bs->small[c ^ 1], bs->big[c ^ 1], bs->big_task0[c ^ 1], next);
+    LA3G_LAUNCHED();
+    tls_launches++;
+    return LA3G_OK;
+  }
+  if (variant == kBuList)
+  {
+    LA3G_CUDA(cudaMemsetAsync(bs->bits[c], 0, (size_t) bs->words * 4, s));
+    k_front_to_bits<<<num_sms() * 4, 256, 0, s>>>(bs->small[c], bs->big[c], cur, bs->bits[c]);
+    LA3G_LAUNCHED();
+    tls_launches++;
+  }
+  LA3G_CUDA(cudaMemsetAsync(bs->bits[c ^ 1], 0, (size_t) bs->words * 4, s));
+  ProfileScope p("bfs_bottom_up", s, 4.0 * unv + 8.0 * nrows + N / 8.0);
+  k_bfs_bu_split<<<grid_for(nrows, 256, num_sms() * 16), 256, 0, s>>>(g.in_ptr, g.in_col, g.hash_of_pos, nrows,
+                                                                      bs->bits[c], bs->bits[c ^ 1], bs->state,
+                                                                      bs->hops, bs->parent, next);
+  LA3G_LAUNCHED();
+  return LA3G_OK;
+}
+
+static int bfs_decide(la3g_graph* G, BfsScratch* bs, cudaStream_t s, cudaGraphConditionalHandle cont,
+                      cudaGraphConditionalHandle mode)
+{
+  // every level visits at least one new vertex: N + 2 levels is a fault
+  k_bfs_decide<<<1, 1, 0, s>>>(bs->state, bs->ctr, G->g.nslots, (uint64_t) G->g.nslots + 2, cont, mode);
+  LA3G_LAUNCHED();
+  tls_launches++;
+  return LA3G_OK;
+}
+
+// Runs BFS from `root` with results left on the device (positions).  The
+// levels run as one device-driven graph (no host round trip per level);
+// with profiling on they are stepped from the host instead, so that each
+// kernel is timed.
 static int bfs_run(la3g_graph* G, BfsScratch* bs, uint32_t root, la3g_stats* st)
 {
   DevGraph& g = G->g;
   cudaStream_t s = G->stream;
-  const uint32_t N = g.nslots, nrows = g.nrows();
+  const uint32_t N = g.nslots;
   k_bfs_init<<<grid_for(N, 256), 256, 0, s>>>(N, bs->hops, bs->parent, bs->cand);
   LA3G_LAUNCHED();
   tls_launches++;
-  uint32_t iter = 0, pull_iters = 0;
   if (root >= N)
   {
     if (st) st->iterations = 1;
     return LA3G_OK;  // no vertex matches the root: every hop stays 255
   }
-  uint32_t rp = 0;
-  LA3G_CUDA(cudaMemcpyAsync(&rp, g.pos_of_id + root, 4, cudaMemcpyDeviceToHost, s));
-  LA3G_CUDA(cudaStreamSynchronize(s));
-  uint32_t h_ptr[2] = {0, 0};
-  if (rp < nrows)
-  {
-    LA3G_CUDA(cudaMemcpyAsync(h_ptr, g.in_ptr + rp, 8, cudaMemcpyDeviceToHost, s));
-    LA3G_CUDA(cudaStreamSynchronize(s));
-  }
-  uint64_t front_deg = h_ptr[1] - h_ptr[0];
-  // An isolated root has no edges: iteration 0 activates nothing.
-  uint64_t nsmall = 0, nbig = 0, ntasks = 0;
-  if (rp < nrows) (front_deg > kBigDeg ? nbig : nsmall) = 1;
-  if (nbig) ntasks = (front_deg + kHubTask - 1) / kHubTask;
-  k_bfs_root_split<<<1, 1, 0, s>>>(rp, bs->hops, nbig ? bs->big[0] : bs->small[0], bs->big_task0[0]);
+  LA3G_CUDA(cudaMemsetAsync(bs->ctr, 0, 2 * sizeof(FrontierCounters), s));
+  k_bfs_root_state<<<1, 1, 0, s>>>(root, g.pos_of_id, g.in_ptr, g.nrows(), g.nent, bs->hops, bs->small[0], bs->big[0],
+                                   bs->big_task0[0], bs->ctr, bs->state);
   LA3G_LAUNCHED();
   tls_launches++;
-  uint64_t unvisited_deg = g.nent - front_deg;
-  bool bottom_up = false, front_is_list = true;
-  int cur = 0;
-  const double alpha = 14.0, beta = 24.0;
-  uint64_t edges_examined = 0;
-  const unsigned td_blocks = num_sms() * 8;
-  for (;;)
+  unsigned long long* H = bs->hstate;
+  if (!profile_enabled())
   {
-    if (iter > 100000) return set_error(LA3G_ETIMEOUT, "bfs did not converge");
-    const uint64_t nfront = nsmall + nbig;
-    if (!bottom_up && (double) front_deg > (double) unvisited_deg / alpha) bottom_up = true;
-    else if (bottom_up && (double) nfront < (double) N / beta) bottom_up = false;
-    const uint8_t hop = (uint8_t) (iter + 1);
-    if (nfront == 0)
+    if (!bs->loop)
     {
-      iter++;
-      break;  // nothing active: this iteration activates nothing
-    }
-    LA3G_CUDA(cudaMemsetAsync(bs->ctr, 0, sizeof(FrontierCounters), s));
-    if (bottom_up)
-    {
-      if (front_is_list)
+      bs->loop = new (std::nothrow) DeviceLoop();
+      if (!bs->loop) return set_error(LA3G_ENOMEM, "out of host memory");
+      const int rc = device_loop_build(
+          bs->loop, 8,
+          [&](cudaStream_t c, cudaGraphConditionalHandle cont, cudaGraphConditionalHandle mode) {
+            return bfs_decide(G, bs, c, cont, mode);
+          },
+          [&](cudaStream_t c, int k) { return bfs_body(G, bs, c, (unsigned) k, 0.0, 0.0, 0.0); });
+      if (rc != LA3G_OK)
       {
-        LA3G_CUDA(cudaMemsetAsync(bs->bits[cur], 0, (size_t) bs->words * 4, s));
-        if (nsmall)
-        {
-          k_list_to_bits<<<grid_for(nsmall, 256), 256, 0, s>>>(bs->small[cur], (uint32_t) nsmall, bs->bits[cur]);
-          LA3G_LAUNCHED();
-          tls_launches++;
-        }
-        if (nbig)
-        {
-          k_list_to_bits<<<grid_for(nbig, 256), 256, 0, s>>>(bs->big[cur], (uint32_t) nbig, bs->bits[cur]);
-          LA3G_LAUNCHED();
-          tls_launches++;
-        }
-      }
-      LA3G_CUDA(cudaMemsetAsync(bs->bits[cur ^ 1], 0, (size_t) bs->words * 4, s));
-      {
-        ProfileScope p("bfs_bottom_up", s, 4.0 * unvisited_deg + 8.0 * nrows + N / 8.0);
-        k_bfs_bu_split<<<grid_for(nrows, 256, num_sms() * 16), 256, 0, s>>>(g.in_ptr, g.in_col, g.hash_of_pos, nrows,
-                                                                      bs->bits[cur], bs->bits[cur ^ 1], hop, bs->hops,
-                                                                      bs->parent, bs->ctr);
-        LA3G_LAUNCHED();
-      }
-      edges_examined += unvisited_deg;
-      front_is_list = false;
-      pull_iters++;
-      LA3G_CUDA(cudaMemcpyAsync(bs->hctr, bs->ctr, sizeof(FrontierCounters), cudaMemcpyDeviceToHost, s));
-      LA3G_CUDA(cudaStreamSynchronize(s));
-      const uint64_t nn = bs->hctr->raw;
-      front_deg = bs->hctr->degsum;
-      bool next_bottom_up = !((double) nn < (double) N / beta);
-      if (nn && !next_bottom_up)
-      {
-        // leaving bottom-up: the next frontier becomes split lists
-        LA3G_CUDA(cudaMemsetAsync(&bs->ctr->nsmall, 0, 16, s));
-        k_bits_to_split<<<grid_for(bs->words, 256), 256, 0, s>>>(bs->bits[cur ^ 1], bs->words, g.in_ptr,
-                                                                  bs->small[cur ^ 1], bs->big[cur ^ 1],
-                                                                  bs->big_task0[cur ^ 1], bs->ctr);
-        LA3G_LAUNCHED();
-        tls_launches++;
-        LA3G_CUDA(cudaMemcpyAsync(bs->hctr, bs->ctr, sizeof(FrontierCounters), cudaMemcpyDeviceToHost, s));
-        LA3G_CUDA(cudaStreamSynchronize(s));
-        nsmall = bs->hctr->nsmall;
-        nbig = bs->hctr->packed >> kHubSlotShift;
-        ntasks = bs->hctr->packed & ((1ull << kHubSlotShift) - 1);
-        front_is_list = true;
-      }
-      else
-      {
-        nsmall = nn;  // count only; the frontier stays a bitmap
-        nbig = 0;
-        ntasks = 0;
+        delete bs->loop;
+        bs->loop = nullptr;
+        return rc;
       }
     }
-    else
-    {
-      {
-        ProfileScope p("bfs_top_down", s, 4.0 * front_deg + 8.0 * nfront + 1.0 * front_deg);
-        k_bfs_td_split<<<td_blocks, 256, 0, s>>>(g.in_ptr, g.in_col, g.hash_of_pos, bs->small[cur], (uint32_t) nsmall,
-                                                 bs->big[cur], bs->big_task0[cur], (uint32_t) nbig, (uint32_t) ntasks,
-                                                 bs->hops, bs->cand, bs->raw, bs->ctr);
-        LA3G_LAUNCHED();
-      }
-      edges_examined += front_deg;
-      // the apply kernel reads the touched count on the device: one host
-      // synchronisation per iteration
-      k_bfs_td_apply_split<<<num_sms() * 4, 256, 0, s>>>(g.in_ptr, bs->raw, hop, bs->hops, bs->parent, bs->cand,
-                                                   bs->small[cur ^ 1], bs->big[cur ^ 1], bs->big_task0[cur ^ 1],
-                                                   bs->ctr);
-      LA3G_LAUNCHED();
-      tls_launches++;
-      LA3G_CUDA(cudaMemcpyAsync(bs->hctr, bs->ctr, sizeof(FrontierCounters), cudaMemcpyDeviceToHost, s));
-      LA3G_CUDA(cudaStreamSynchronize(s));
-      const uint64_t nn = bs->hctr->raw;
-      nsmall = nn ? bs->hctr->nsmall : 0;
-      nbig = nn ? bs->hctr->packed >> kHubSlotShift : 0;
-      ntasks = nn ? bs->hctr->packed & ((1ull << kHubSlotShift) - 1) : 0;
-      front_deg = nn ? bs->hctr->degsum : 0;
-      front_is_list = true;
-    }
-    unvisited_deg -= std::min<uint64_t>(unvisited_deg, front_deg);
-    cur ^= 1;
-    iter++;
-    if (nsmall + nbig == 0) break;
+    LA3G_CUDA(cudaGraphLaunch(bs->loop->exec, s));
+    LA3G_CUDA(cudaMemcpyAsync(H, bs->state, kBSlots * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    LA3G_CUDA(cudaStreamSynchronize(s));
+    // the graph's launches: one decide per pass, each body's kernels per level
+    uint64_t n = 1;
+    for (int k = 0; k < 8; k++) n += H[kBCount + k] * (1 + bs->loop->body_launches[k]);
+    tls_launches += (uint32_t) n;
   }
+  else
+  {
+    for (;;)
+    {
+      LA3G_TRY(bfs_decide(G, bs, s, 0, 0));
+      LA3G_CUDA(cudaMemcpyAsync(H, bs->state, kBSlots * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+      LA3G_CUDA(cudaStreamSynchronize(s));
+      const unsigned m = (unsigned) H[kBMode];
+      if (m == kBDone) break;
+      LA3G_TRY(bfs_body(G, bs, s, m, (double) H[kBFrontDeg], (double) H[kBNfront], (double) H[kBUnvisited]));
+    }
+  }
+  if (H[kBStatus]) return set_error(LA3G_ETIMEOUT, "bfs did not converge");
   if (st)
   {
-    st->iterations = iter;
-    st->pull_iterations = pull_iters;
-    st->edges_examined = edges_examined;
+    st->iterations = (uint32_t) H[kBIter];
+    st->pull_iterations = (uint32_t) H[kBPulls];
+    st->edges_examined = H[kBExamined];
   }
   return LA3G_OK;
 }

@@ -62,12 +62,33 @@ struct SsspScratch
   uint32_t max_w = 0;             // largest weight: pull steps need INF + w to stay in uint32
   uint32_t min_w = 0;             // smallest weight of a regular row's in-edge
   uint32_t* by_id = nullptr;      // [nslots] distances reordered by id before they leave the device
+  unsigned long long* state = nullptr;  // the iteration loop's state (kSt* slots), device side
+  DeviceLoop* loop = nullptr;     // the device-driven loop graph (built on first use)
 };
+
+// Loop state slots (unsigned long long each).
+enum : int {
+  kStIter = 0,      // iterations, counted as the reference counts them
+  kStExamined,      // edges relaxed or gathered
+  kStStatus,        // 1: the iteration limit was reached
+  kStFirst,         // 1 until the first decision (the root's frontier is in kStNlist0 / kStDeg0)
+  kStNlist0,        // the root's frontier: 1 if it scatters
+  kStDeg0,          // the root's regular out-degree
+  kStMode,          // the body chosen last: kPull, kPush or kDone
+  kStSrcRoot,       // the root's position if it is a source (the sink pass reads it), else ~0
+  kStFrontDeg,      // the chosen step's frontier out-degree sum
+  kStNlist,         // the chosen step's frontier: vertices with regular out-edges
+  kStPulls,         // pull steps run
+  kStPushes,        // push steps run
+  kStSlots = 16
+};
+enum : unsigned { kPull = 0, kPush = 1, kDone = 2 };
 
 static void sssp_scratch_free(void* p)
 {
   SsspScratch* s = (SsspScratch*) p;
   if (s->hctr) cudaFreeHost(s->hctr);
+  delete s->loop;
   delete s;
 }
 
@@ -81,11 +102,88 @@ __global__ void k_sssp_init(uint32_t N, uint32_t* dist, uint32_t* msg, uint32_t*
   }
 }
 
-__global__ void k_sssp_root(uint32_t rp, int scatter, uint32_t* dist, uint32_t* msg, uint32_t* fbits)
+// The root (an id; none if it is outside the graph): distance 0, scattered
+// (msg 0); regular and source vertices scatter, so they form the first
+// frontier (even with no regular out-edge: the first iteration runs).
+__global__ void k_sssp_root(uint32_t root, uint32_t N, const uint32_t* __restrict__ pos_of_id,
+                            const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ reg_end, uint32_t nreg,
+                            uint32_t src_base, uint32_t iso_base, uint32_t* dist, uint32_t* msg, uint32_t* fbits,
+                            unsigned long long* state)
 {
+  for (int k = 0; k < kStSlots; k++) state[k] = 0;
+  state[kStFirst] = 1;
+  state[kStSrcRoot] = ~0ull;
+  if (root >= N) return;
+  const uint32_t rp = pos_of_id[root];
+  const bool src = rp >= src_base && rp < iso_base;
   dist[rp] = 0;
   msg[rp] = 0;
-  if (scatter) fbits[rp >> 5] = 1u << (rp & 31);
+  if (src) state[kStSrcRoot] = rp;
+  if (rp < nreg || src)
+  {
+    fbits[rp >> 5] = 1u << (rp & 31);
+    state[kStNlist0] = 1;
+    state[kStDeg0] = reg_end[rp] - ptr[rp];
+  }
+}
+
+// Start of every iteration (one thread): reads the counters the last dense
+// apply left (or the root's frontier), ends the loop as the reference's
+// execute loop does (nothing activated; or activated vertices with no
+// regular out-edge, which take one more, empty iteration), and otherwise
+// counts the iteration and picks pull (frontier out-degree sum above the
+// regular rows' in-edges / divisor, after the first iteration, with weights
+// that keep INF + w in uint32) or push.
+__global__ void k_sssp_decide(unsigned long long* state, const unsigned long long* __restrict__ ctr, uint64_t reg_in,
+                              uint32_t max_w, double divisor, uint64_t limit, cudaGraphConditionalHandle cont,
+                              cudaGraphConditionalHandle mode)
+{
+  unsigned long long it = state[kStIter], nlist, deg;
+  bool done = false;
+  if (state[kStFirst])
+  {
+    state[kStFirst] = 0;
+    nlist = state[kStNlist0];
+    deg = state[kStDeg0];
+  }
+  else
+  {
+    deg = ctr[1];
+    nlist = ctr[2];
+    if (ctr[0] == 0) done = true;
+    else if (nlist == 0)
+    {
+      it++;  // the next iteration runs with messages that reach no regular row
+      done = true;
+    }
+  }
+  unsigned m = kDone;
+  if (!done)
+  {
+    if (it > limit) state[kStStatus] = 1;
+    else
+    {
+      it++;
+      if (nlist)
+        m = it > 1 && max_w <= 0x80000000u && (double) deg * divisor > (double) reg_in ? kPull : kPush;
+    }
+  }
+  state[kStIter] = it;
+  state[kStMode] = m;
+  state[kStFrontDeg] = deg;
+  state[kStNlist] = nlist;
+  if (m == kPull)
+  {
+    state[kStExamined] += reg_in;
+    state[kStPulls]++;
+  }
+  else if (m == kPush)
+  {
+    state[kStExamined] += deg;
+    state[kStPushes]++;
+  }
+  loop_set(cont, m != kDone);
+  loop_set(mode, m);
 }
 
 // End of the regular-row part of every out-edge list (rows ascend, so the
@@ -257,8 +355,10 @@ __global__ void __launch_bounds__(256)
 k_sssp_pull(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ w,
             uint32_t nreg, const uint32_t* __restrict__ task_row, const uint32_t* __restrict__ task_begin,
             uint32_t ntasks, uint32_t task_warps, uint32_t* ymin, const uint32_t* __restrict__ fmsg,
-            uint32_t* dist, const uint32_t* __restrict__ long_rows, unsigned long long fmin, uint32_t min_w)
+            uint32_t* dist, const uint32_t* __restrict__ long_rows, const unsigned long long* __restrict__ ctr,
+            uint32_t min_w)
 {
+  const unsigned long long fmin = ctr[5];  // the frontier's smallest message
   // Every candidate of this step is a frontier message plus a weight, so at
   // least fmin + min_w: a row already at or below that cannot be lowered and
   // its in-edges are not read (the result is the same).
@@ -374,9 +474,10 @@ static constexpr double kPullDivisor = 4.0;
 // Sink pass: y = min over in-neighbours (regular: final dist; the root if it
 // is a source: its message 0) of msg + w; dist = min(dist, y).
 __global__ void k_sssp_sinks(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col,
-                             const uint32_t* __restrict__ w, uint32_t nreg, uint32_t nsink, uint32_t src_root,
-                             uint32_t* dist)
+                             const uint32_t* __restrict__ w, uint32_t nreg, uint32_t nsink,
+                             const unsigned long long* __restrict__ state, uint32_t* dist)
 {
+  const uint32_t src_root = (uint32_t) state[kStSrcRoot];
   for (uint32_t v = nreg + blockIdx.x * blockDim.x + threadIdx.x; v < nreg + nsink; v += gridDim.x * blockDim.x)
   {
     uint32_t y = kInf;
@@ -428,7 +529,8 @@ static int sssp_scratch(la3g_graph* G, SsspScratch** out)
   LA3G_TRY(galloc(G, &ss->fctr, 2));
   LA3G_TRY(galloc(G, &ss->fbits, (size_t) N / 32 + 2));
   LA3G_TRY(galloc(G, &ss->by_id, N));
-  LA3G_CUDA(cudaHostAlloc(&ss->hctr, 8 * sizeof(unsigned long long), cudaHostAllocDefault));
+  LA3G_TRY(galloc(G, &ss->state, kStSlots));
+  LA3G_CUDA(cudaHostAlloc(&ss->hctr, kStSlots * sizeof(unsigned long long), cudaHostAllocDefault));
   k_sssp_reg_end<<<grid_for(N, 256), 256, 0, G->stream>>>(G->g.out_ptr, G->g.out_row, N, G->g.nreg, ss->reg_end);
   LA3G_LAUNCHED();
   LA3G_TRY(galloc(G, &ss->long_rows, std::max<uint32_t>(G->g.nreg, 1)));
@@ -485,6 +587,75 @@ static int sssp_scratch(la3g_graph* G, SsspScratch** out)
   return LA3G_OK;
 }
 
+// One iteration's body, k = kPull or kPush: the relaxation step, then the
+// dense apply that forms the next frontier and its counters.  `deg` and
+// `nlist` (the frontier's out-degree sum and size) only size the profile
+// entries' bytes; the kernels read every count they need on the device.
+static int sssp_body(la3g_graph* G, SsspScratch* ss, cudaStream_t s, unsigned k, double deg, double nlist)
+{
+  DevGraph& g = G->g;
+  const uint32_t words = g.nslots / 32 + 1;
+  if (k == kPull)
+  {
+    // in-edges of every regular row (index + weight), the frontier
+    // messages of their columns, one dist read per row
+    ProfileScope p("sssp_pull", s, 8.0 * ss->reg_in + 8.0 * ss->reg_in + 8.0 * g.nreg);
+    // warps split between long-row tasks and short rows in proportion to their in-edges
+    const uint32_t all_warps = num_sms() * 8 * 8;
+    const uint32_t task_warps =
+        ss->ntasks ? std::min<uint32_t>(ss->ntasks, std::max<uint32_t>(1, (uint32_t) ((double) all_warps *
+                                                                                        ss->task_edges /
+                                                                                        std::max<uint64_t>(ss->reg_in, 1))))
+                   : 0;
+    k_sssp_pull<<<num_sms() * 8, 256, 0, s>>>(g.in_ptr, g.in_col, g.in_w, g.nreg, ss->task_row, ss->task_begin,
+                                              ss->ntasks, task_warps, ss->ymin, ss->fmsg, ss->dist, ss->long_rows,
+                                              ss->ctr, ss->min_w);
+    LA3G_LAUNCHED();
+    if (ss->nlong)
+    {
+      k_sssp_pull_long<<<grid_for(ss->nlong, 256), 256, 0, s>>>(ss->long_rows, ss->nlong, ss->ymin, ss->dist);
+      LA3G_LAUNCHED();
+      tls_launches++;
+    }
+  }
+  else
+  {
+    LA3G_CUDA(cudaMemsetAsync(ss->fctr, 0, 2 * sizeof(unsigned long long), s));
+    k_sssp_split<<<grid_for(words, 256), 256, 0, s>>>(ss->fbits, words, g.out_ptr, ss->reg_end, ss->small[0],
+                                                      ss->big[0], ss->big_task0[0], ss->fctr);
+    LA3G_LAUNCHED();
+    tls_launches++;
+    ProfileScope p("sssp_push", s, 8.0 * deg + 12.0 * nlist);
+    k_sssp_push<<<num_sms() * 8, 256, 0, s>>>(g.out_ptr, ss->reg_end, g.out_row, g.out_w, ss->small[0], ss->big[0],
+                                              ss->big_task0[0], ss->fctr, ss->msg, ss->dist);
+    LA3G_LAUNCHED();
+  }
+  LA3G_CUDA(cudaMemsetAsync(ss->ctr, 0, 3 * sizeof(unsigned long long), s));
+  LA3G_CUDA(cudaMemsetAsync(ss->ctr + 5, 0xFF, sizeof(unsigned long long), s));  // the next frontier's minimum
+  k_sssp_dense_apply<<<grid_for((uint64_t) words * 32, 256, num_sms() * 4), 256, 0, s>>>(
+      g.nreg, words, g.out_ptr, ss->reg_end, ss->dist, ss->msg, ss->fmsg, ss->fbits, ss->ctr);
+  LA3G_LAUNCHED();
+  tls_launches++;
+  return LA3G_OK;
+}
+
+// Iteration limit: with non-negative weights every distance is final after
+// at most N + 1 iterations (Bellman-Ford), so a loop past N + 2 is a fault.
+static uint64_t sssp_limit(const DevGraph& g) { return (uint64_t) g.nslots + 2; }
+
+static int sssp_decide(la3g_graph* G, SsspScratch* ss, cudaStream_t s, cudaGraphConditionalHandle cont,
+                       cudaGraphConditionalHandle mode)
+{
+  k_sssp_decide<<<1, 1, 0, s>>>(ss->state, ss->ctr, ss->reg_in, ss->max_w, kPullDivisor, sssp_limit(G->g), cont, mode);
+  LA3G_LAUNCHED();
+  tls_launches++;
+  return LA3G_OK;
+}
+
+// Runs SSSP from `root` with the distances left on the device (positions).
+// The iterations run as one device-driven graph (no host round trip per
+// iteration); with profiling on they are stepped from the host instead, so
+// that each kernel is timed.
 static int sssp_run(la3g_graph* G, SsspScratch* ss, uint32_t root, la3g_stats* st)
 {
   DevGraph& g = G->g;
@@ -494,99 +665,41 @@ static int sssp_run(la3g_graph* G, SsspScratch* ss, uint32_t root, la3g_stats* s
   k_sssp_init<<<grid_for(N, 256), 256, 0, s>>>(N, ss->dist, ss->msg, ss->fmsg);
   LA3G_LAUNCHED();
   LA3G_CUDA(cudaMemsetAsync(ss->fbits, 0, (size_t) words * 4, s));
-  tls_launches++;
-  uint32_t rp = 0xFFFFFFFFu, src_root = 0xFFFFFFFFu;
-  // the current frontier: vertices with regular out-edges, their out-degree sum
-  uint64_t nlist = 0, front_deg = 0;
-  if (root < N)
+  k_sssp_root<<<1, 1, 0, s>>>(root, N, g.pos_of_id, g.out_ptr, ss->reg_end, g.nreg, g.src_base(), g.iso_base(),
+                              ss->dist, ss->msg, ss->fbits, ss->state);
+  LA3G_LAUNCHED();
+  tls_launches += 2;
+  if (!profile_enabled())
   {
-    LA3G_CUDA(cudaMemcpyAsync(&rp, g.pos_of_id + root, 4, cudaMemcpyDeviceToHost, s));
-    LA3G_CUDA(cudaStreamSynchronize(s));
-    // init returns true for the root; regular and source vertices scatter.
-    const bool scat = rp < g.nreg || (rp >= g.src_base() && rp < g.iso_base());
-    if (rp >= g.src_base() && rp < g.iso_base()) src_root = rp;
-    uint32_t re = 0, hp[2] = {0, 0};
-    if (scat)
+    if (!ss->loop)
     {
-      LA3G_CUDA(cudaMemcpyAsync(hp, g.out_ptr + rp, 8, cudaMemcpyDeviceToHost, s));
-      LA3G_CUDA(cudaMemcpyAsync(&re, ss->reg_end + rp, 4, cudaMemcpyDeviceToHost, s));
-      LA3G_CUDA(cudaStreamSynchronize(s));
-      front_deg = re - hp[0];
-    }
-    k_sssp_root<<<1, 1, 0, s>>>(rp, scat ? 1 : 0, ss->dist, ss->msg, ss->fbits);
-    LA3G_LAUNCHED();
-    tls_launches++;
-    // a scattering root makes the first iteration run, even with no regular out-edge
-    if (scat) nlist = 1;
-  }
-  uint32_t iter = 0;
-  uint64_t examined = 0;
-  unsigned long long front_min = 0;  // smallest message of the current frontier (the root's: 0)
-  const unsigned blocks = num_sms() * 8;
-  for (;;)
-  {
-    if (iter > 1000000) return set_error(LA3G_ETIMEOUT, "sssp did not converge");
-    iter++;
-    if (nlist == 0) break;
-    if (iter > 1 && ss->max_w <= 0x80000000u && (double) front_deg * kPullDivisor > (double) ss->reg_in)
-    {
-      // in-edges of every regular row (index + weight), stamps and
-      // messages of their columns, one dist read per row
-      ProfileScope p("sssp_pull", s, 8.0 * ss->reg_in + 8.0 * ss->reg_in + 8.0 * g.nreg);
-      // warps split between long-row tasks and short rows in proportion to their in-edges
-      const uint32_t all_warps = num_sms() * 8 * 8;
-      const uint32_t task_warps =
-          ss->ntasks ? std::min<uint32_t>(ss->ntasks, std::max<uint32_t>(1, (uint32_t) ((double) all_warps *
-                                                                                          ss->task_edges /
-                                                                                          std::max<uint64_t>(ss->reg_in, 1))))
-                     : 0;
-      k_sssp_pull<<<num_sms() * 8, 256, 0, s>>>(g.in_ptr, g.in_col, g.in_w, g.nreg, ss->task_row, ss->task_begin,
-                                                ss->ntasks, task_warps, ss->ymin, ss->fmsg, ss->dist, ss->long_rows,
-                                                front_min, ss->min_w);
-      LA3G_LAUNCHED();
-      tls_launches++;
-      if (ss->nlong)
+      ss->loop = new (std::nothrow) DeviceLoop();
+      if (!ss->loop) return set_error(LA3G_ENOMEM, "out of host memory");
+      const int rc = device_loop_build(
+          ss->loop, 2,
+          [&](cudaStream_t c, cudaGraphConditionalHandle cont, cudaGraphConditionalHandle mode) {
+            return sssp_decide(G, ss, c, cont, mode);
+          },
+          [&](cudaStream_t c, int k) { return sssp_body(G, ss, c, (unsigned) k, 0.0, 0.0); });
+      if (rc != LA3G_OK)
       {
-        k_sssp_pull_long<<<grid_for(ss->nlong, 256), 256, 0, s>>>(ss->long_rows, ss->nlong, ss->ymin, ss->dist);
-        LA3G_LAUNCHED();
-        tls_launches++;
+        delete ss->loop;
+        ss->loop = nullptr;
+        return rc;
       }
-      examined += ss->reg_in;
     }
-    else
+    LA3G_CUDA(cudaGraphLaunch(ss->loop->exec, s));
+  }
+  else
+  {
+    for (;;)
     {
-      LA3G_CUDA(cudaMemsetAsync(ss->fctr, 0, 2 * sizeof(unsigned long long), s));
-      k_sssp_split<<<grid_for(words, 256), 256, 0, s>>>(ss->fbits, words, g.out_ptr, ss->reg_end, ss->small[0],
-                                                        ss->big[0], ss->big_task0[0], ss->fctr);
-      LA3G_LAUNCHED();
-      tls_launches++;
-      ProfileScope p("sssp_push", s, 8.0 * front_deg + 12.0 * nlist);
-      k_sssp_push<<<blocks, 256, 0, s>>>(g.out_ptr, ss->reg_end, g.out_row, g.out_w, ss->small[0], ss->big[0],
-                                         ss->big_task0[0], ss->fctr, ss->msg, ss->dist);
-      LA3G_LAUNCHED();
-      examined += front_deg;
-    }
-    LA3G_CUDA(cudaMemsetAsync(ss->ctr, 0, 3 * sizeof(unsigned long long), s));
-    LA3G_CUDA(cudaMemsetAsync(ss->ctr + 5, 0xFF, sizeof(unsigned long long), s));  // the next frontier's minimum
-    k_sssp_dense_apply<<<grid_for((uint64_t) words * 32, 256, num_sms() * 4), 256, 0, s>>>(g.nreg, words, g.out_ptr, ss->reg_end,
-                                                                            ss->dist, ss->msg, ss->fmsg, ss->fbits,
-                                                                            ss->ctr);
-    LA3G_LAUNCHED();
-    tls_launches++;
-    LA3G_CUDA(cudaMemcpyAsync(ss->hctr, ss->ctr, 6 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
-    LA3G_CUDA(cudaStreamSynchronize(s));
-    const uint64_t nn = ss->hctr[0];
-    front_deg = ss->hctr[1];
-    nlist = ss->hctr[2];
-    front_min = ss->hctr[5];
-    // A vertex lowered only into sink-free regular rows with no regular
-    // out-edges is activated but has nothing to relax; the loop still runs
-    // the next iteration only if something was activated.
-    if (nn == 0) break;
-    if (nlist == 0)
-    {
-      iter++;  // the next iteration runs with messages that reach no regular row
-      break;
+      LA3G_TRY(sssp_decide(G, ss, s, 0, 0));
+      LA3G_CUDA(cudaMemcpyAsync(ss->hctr, ss->state, kStSlots * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+      LA3G_CUDA(cudaStreamSynchronize(s));
+      const unsigned m = (unsigned) ss->hctr[kStMode];
+      if (m == kDone) break;
+      LA3G_TRY(sssp_body(G, ss, s, m, (double) ss->hctr[kStFrontDeg], (double) ss->hctr[kStNlist]));
     }
   }
   if (g.nsink)
@@ -595,13 +708,24 @@ static int sssp_run(la3g_graph* G, SsspScratch* ss, uint32_t root, la3g_stats* s
     // distance), their offsets and the distance read and written
     const double sink_in = (double) (g.nent - ss->reg_in);
     ProfileScope p("sssp_sinks", s, 12.0 * sink_in + 12.0 * g.nsink);
-    k_sssp_sinks<<<grid_for(g.nsink, 256), 256, 0, s>>>(g.in_ptr, g.in_col, g.in_w, g.nreg, g.nsink, src_root, ss->dist);
+    k_sssp_sinks<<<grid_for(g.nsink, 256), 256, 0, s>>>(g.in_ptr, g.in_col, g.in_w, g.nreg, g.nsink, ss->state,
+                                                         ss->dist);
     LA3G_LAUNCHED();
+  }
+  LA3G_CUDA(cudaMemcpyAsync(ss->hctr, ss->state, kStSlots * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+  LA3G_CUDA(cudaStreamSynchronize(s));
+  if (ss->hctr[kStStatus]) return set_error(LA3G_ETIMEOUT, "sssp did not converge");
+  if (ss->loop && !profile_enabled())
+  {
+    // the graph's launches: one decide per pass, each body's kernels per step
+    const uint64_t passes = ss->hctr[kStPulls] + ss->hctr[kStPushes] + 1;
+    tls_launches += (uint32_t) (passes + ss->hctr[kStPulls] * ss->loop->body_launches[kPull] +
+                                ss->hctr[kStPushes] * ss->loop->body_launches[kPush]);
   }
   if (st)
   {
-    st->iterations = iter;
-    st->edges_examined = examined;
+    st->iterations = (uint32_t) ss->hctr[kStIter];
+    st->edges_examined = ss->hctr[kStExamined];
   }
   return LA3G_OK;
 }

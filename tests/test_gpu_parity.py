@@ -140,6 +140,31 @@ def test_repeated_calls_are_identical(gpu, rmat16):
     assert np.array_equal(r1.view(np.uint64), r2.view(np.uint64))
 
 
+def test_device_loop_matches_host_stepped(gpu, rmat16):
+    """BFS and SSSP levels run as one device-driven graph; with profiling on
+    the same decide kernel and bodies are stepped from the host.  Both forms
+    give the same results, iteration counts, examined edges and launches."""
+    p, pw, n = rmat16
+    gu = gpu.Graph.load_undirected(p, n)
+    gw = gpu.Graph.load_directed(pw, n, weighted=True)
+    hub = int(np.bincount(np.fromfile(p, np.uint32), minlength=n + 1).argmax())
+    fields = ("iterations", "pull_iterations", "edges_examined", "kernel_launches")
+    try:
+        for r in _roots(n, 3, 5) + [hub]:
+            runs = []
+            for prof in (False, True):
+                gpu.profile(prof)
+                h, par, st = gpu.bfs(gu, r)
+                d, sst = gpu.sssp(gw, r)
+                runs.append((h, par, d, [getattr(st, f) for f in fields], [getattr(sst, f) for f in fields]))
+            (h0, p0, d0, s0, t0), (h1, p1, d1, s1, t1) = runs
+            assert np.array_equal(h0, h1) and np.array_equal(p0, p1) and np.array_equal(d0, d1), r
+            assert s0 == s1 and t0 == t1, (r, s0, s1, t0, t1)
+    finally:
+        gpu.profile(False)
+        gpu.profile_reset()
+
+
 def test_wrong_graph_kind_is_rejected(gpu, rmat16):
     p, pw, n = rmat16
     g = gpu.Graph.load_undirected(p, n)
