@@ -118,7 +118,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -363,6 +363,8 @@ def gpu_line(args, rank: int, world: int, local: int) -> dict | None:
             torch.distributed.barrier()
         torch.cuda.synchronize()
         clocks.start_timed()
+        # an NVTX range around the timed steps lets a profiler capture exactly them
+        torch.cuda.nvtx.range_push("bench_timed_steps")
         with torch.cuda.stream(stream):
             ev[0].record(stream)
             for k in range(K):
@@ -388,6 +390,7 @@ def gpu_line(args, rank: int, world: int, local: int) -> dict | None:
                 app_bytes["tc"] += stc.algo_bytes
             ev[1].record(stream)
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
     if world > 1:
         torch.distributed.barrier()
     region_ms = ev[0].elapsed_time(ev[1])
@@ -830,14 +833,28 @@ def pagerank_measure(args, stream, dev, include_er: bool = True) -> dict:
         flush()
         t32 = _timed(stream, lambda: L.N.check(L.N.lib().la3g_pr_f32(G._h, iters, tol, None, L.C.byref(res),
                                                                      L.C.byref(st32))))
+        # the FP32 study over the tiled DCSC layout (built by the first call, untimed)
+        t0 = time.time()
+        L.pagerank_f32(G, 2, tiled=True)
+        tile_build_s = time.time() - t0
+        stt = L.Stats()
+        flush()
+        tt = _timed(stream, lambda: L.N.check(L.N.lib().la3g_pr_f32_tiled(G._h, iters, tol, None, L.C.byref(res),
+                                                                          L.C.byref(stt))))
         r64 = L.pagerank(G, iters, True, False)[0]
         r32, res32, _ = L.pagerank_f32(G, iters, tol)
+        rt, rest, _ = L.pagerank_f32(G, iters, tol, tiled=True)
         d_ = np.abs(r32 - r64)
+        dt = np.abs(rt - r64)
         out[f"s{scale}_{name}"] = {
             "m": m, "n": n, "dangling_frac": G.info.nsink / max(1, G.info.nvertices),
             "fp64": {"iterations": st64.iterations, "ms": t64, "gteps": st64.iterations * m / t64 / 1e6},
             "fp32": {"iterations": st32.iterations, "ms": t32, "gteps": st32.iterations * m / t32 / 1e6,
                      "l1_residual": res32},
+            "fp32_tiled": {"iterations": stt.iterations, "ms": tt, "gteps": stt.iterations * m / tt / 1e6,
+                           "x_flat": t32 / tt if tt else None, "l1_residual": rest,
+                           "l1_rel_vs_fp64": float(dt.sum() / r64.sum()), "max_abs_vs_fp64": float(dt.max()),
+                           "layout_build_s": round(tile_build_s, 2)},
             "l1_abs": float(d_.sum()), "l1_rel": float(d_.sum() / r64.sum()), "max_abs": float(d_.max()),
             "max_rel": float((d_ / np.maximum(1.0, r64)).max())}
         G.free()

@@ -158,6 +158,14 @@ typedef struct la3g_device_graph
 
 int la3g_graph_device_view(la3g_graph* g, la3g_device_graph* out);
 
+/* The push (out-edge) CSR over column positions, for engines that expand a
+ * frontier of active columns: out_ptr[nslots + 1], out_row[nentries] (row
+ * positions, ascending per column).  Built on the device on first use for
+ * directed graphs; an undirected graph's CSR is symmetric and is returned
+ * as is.  No counterpart in the reference, whose SpMV walks its per-tile
+ * CSC by active column (src/vprogram/vertex_program_execute.hpp:564-603). */
+int la3g_graph_push_view(la3g_graph* g, const uint32_t** out_ptr, const uint32_t** out_row);
+
 /* ---- apps (replace the apps' run() functions) ---------------------------- */
 
 /* PageRank, FP64, un-normalised, alpha = 0.15: the reference pr app
@@ -172,6 +180,16 @@ int la3g_pr(la3g_graph* g, uint32_t iters, double* rank_out, uint32_t* degree_ou
  * fixed iterations).  residual_out: last L1 residual. */
 int la3g_pr_f32(la3g_graph* g, uint32_t iters, double tol, double* rank_out, double* residual_out,
                 la3g_stats* st);
+
+/* The same FP32 study over a tiled copy of the matrix: the regular rows in
+ * tiles of 16384 rows, each tile doubly compressed by column as the
+ * reference's per-tile DCSC (src/utils/csc.h:60-130, tiles of
+ * src/matrix/matrix2d.hpp:6-25): non-empty columns with offsets and a 16-bit
+ * row per entry; the tile's row accumulators live in shared memory.  Built
+ * on the device on the first call (about 10 B per entry).  Results agree
+ * with la3g_pr_f32 to FP32 rounding (addition order inside a row differs). */
+int la3g_pr_f32_tiled(la3g_graph* g, uint32_t iters, double tol, double* rank_out, double* residual_out,
+                      la3g_stats* st);
 
 /* BFS (src/apps/graph_analytics/bfs.cpp:11-37, bfs.h:11-49) on an undirected
  * graph: hops (uint8, 255 = unreached) and parent (the hashed id of the

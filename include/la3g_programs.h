@@ -21,6 +21,26 @@ int la3gp_bfs(la3g_graph* g, uint32_t root, uint8_t* hops, uint32_t* parent, uin
 int la3gp_sssp(la3g_graph* g, uint32_t root, uint32_t* dist, uint32_t* iters);
 int la3gp_cc(la3g_graph* g, uint32_t* label, uint32_t* iters);
 
+/* The degree app's tail (degree.cpp:34-43) through the engine's topk and
+ * reduce: DegVertex execute(1) on g, then topk<vid, vid>(k) by degree,
+ * largest first (ids[k], degrees[k]), and reduce(sum of degrees).  With
+ * btopk set, also btopk<2>(k) over (degree, ~degree): the k largest and the
+ * k smallest degrees (bids[2k], bvals[2k]).  k <= 512. */
+int la3gp_degree_topk(la3g_graph* g, uint32_t k, uint32_t* ids, uint32_t* degrees, uint64_t* degree_sum,
+                      uint32_t* bids, uint32_t* bvals);
+
+/* TC (tc.cpp:11-52) through the engine: g loaded LA3G_DIRECTED |
+ * LA3G_ACYCLIC, gr the same file LA3G_DIRECTED | LA3G_ACYCLIC |
+ * LA3G_REVERSE.  CtVertex's neighbour lists travel as variable-size
+ * messages.  total: sum of the per-vertex counts (reduce); ntri: nslots
+ * counts by vertex id (nullable). */
+int la3gp_tc(la3g_graph* g, la3g_graph* gr, uint64_t* total, uint32_t* ntri);
+
+/* BFS (bfs.h) from root, then topk over the ACTIVE vertices (those apply
+ * reached; not the root, which init activates without marking) by hops,
+ * largest first: ids[k], hops[k]. */
+int la3gp_bfs_topk(la3g_graph* g, uint32_t root, uint32_t k, uint32_t* ids, uint32_t* hops);
+
 /* Graph simulation (src/apps/graph_simulation/graphsim.cpp:45-90,
  * graphsim.h:60-184) on the data graph loaded LA3G_DIRECTED | LA3G_REVERSE,
  * as the reference loads it.  vlabel: nslots label ids by vertex id (0 = the

@@ -161,12 +161,14 @@ def pagerank(G: Graph, iters: int, want_rank: bool = True, want_degree: bool = T
     return rank, deg, st
 
 
-def pagerank_f32(G: Graph, iters: int, tol: float = 0.0):
-    """FP32 SpMV / FP32 accumulation variant; returns (rank as f64, L1 residual, stats)."""
+def pagerank_f32(G: Graph, iters: int, tol: float = 0.0, tiled: bool = False):
+    """FP32 SpMV / FP32 accumulation variant; returns (rank as f64, L1 residual, stats).
+    tiled: run over the tiled DCSC copy of the matrix (la3g_pr_f32_tiled)."""
     st = Stats()
     rank = np.empty(G.nslots, np.float64)
     res = C.c_double(0.0)
-    N.check(N.lib().la3g_pr_f32(G._h, iters, tol, _ptr(rank, C.c_double), C.byref(res), C.byref(st)))
+    f = N.lib().la3g_pr_f32_tiled if tiled else N.lib().la3g_pr_f32
+    N.check(f(G._h, iters, tol, _ptr(rank, C.c_double), C.byref(res), C.byref(st)))
     return rank, res.value, st
 
 

@@ -139,8 +139,10 @@ SIGNATURES = {
     "la3g_graph_set_stream": (C.c_int, [_P, _P]),
     "la3g_graph_positions": (C.c_int, [_P, _u32p, _u32p]),
     "la3g_graph_device_view": (C.c_int, [_P, C.POINTER(DeviceGraph)]),
+    "la3g_graph_push_view": (C.c_int, [_P, C.POINTER(_P), C.POINTER(_P)]),
     "la3g_pr": (C.c_int, [_P, C.c_uint32, _f64p, _u32p, _statp]),
     "la3g_pr_f32": (C.c_int, [_P, C.c_uint32, C.c_double, _f64p, _f64p, _statp]),
+    "la3g_pr_f32_tiled": (C.c_int, [_P, C.c_uint32, C.c_double, _f64p, _f64p, _statp]),
     "la3g_bfs": (C.c_int, [_P, C.c_uint32, _u8p, _u32p, _statp]),
     "la3g_sssp": (C.c_int, [_P, C.c_uint32, _u32p, _statp]),
     "la3g_cc": (C.c_int, [_P, _u32p, _statp]),

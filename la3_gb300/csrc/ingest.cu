@@ -586,3 +586,13 @@ extern "C" int la3g_graph_device_view(la3g_graph* G, la3g_device_graph* out)
   out->stream = (void*) G->stream;
   return LA3G_OK;
 }
+
+extern "C" int la3g_graph_push_view(la3g_graph* G, const uint32_t** out_ptr, const uint32_t** out_row)
+{
+  if (!G || !out_ptr || !out_row) return set_error(LA3G_EINVAL, "null graph or output");
+  const DevGraph& g = G->g;
+  if (g.directed()) LA3G_TRY(build_push_csr(G));
+  *out_ptr = g.directed() ? g.out_ptr : g.in_ptr;
+  *out_row = g.directed() ? g.out_row : g.in_col;
+  return LA3G_OK;
+}

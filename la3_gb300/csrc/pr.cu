@@ -29,6 +29,7 @@
 #include <vector>
 
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
 
 #include "la3g_internal.h"
 
@@ -52,6 +53,14 @@ struct PrScratch
   float* rankf = nullptr;
   double* resid = nullptr;
   bool ready = false;
+  // tiled layout of the regular rows (la3g_pr_f32_tiled), built on first use
+  uint32_t tile_rows = 0, ntiles = 0;
+  uint64_t tile_ncols = 0, tile_nent = 0;
+  uint32_t* tile_col = nullptr;  // [ntiles + 1] first non-empty-column slot of each tile
+  uint32_t* tcol = nullptr;      // [ncols] column positions, ascending within a tile
+  uint32_t* tptr = nullptr;      // [ncols + 1] first entry of each non-empty column
+  uint16_t* trow = nullptr;      // [nent] row of each entry, local to its tile
+  int tile_blocks = 0;           // resident blocks per SM of the tiled kernel
 };
 
 static void pr_scratch_free(void* p) { delete (PrScratch*) p; }
@@ -409,6 +418,238 @@ k_prf_pull(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, c
   }
 }
 
+// ------------------------------------------------------------- tiled layout
+//
+// The regular rows are cut into tiles of kTileRows consecutive rows.  Each
+// tile keeps its entries doubly compressed by column (the reference's
+// per-tile DCSC, src/utils/csc.h:60-130: only the non-empty columns are
+// listed, with their offsets): tcol / tptr over the tile's non-empty columns
+// in ascending position, and a 16-bit row inside the tile per entry.  One
+// CTA takes a tile at a time with its rows' accumulators in shared memory
+// (64 KB), walks the tile's columns (one thread per column, four columns'
+// messages loaded at once; columns with many entries in the tile go to whole
+// warps) and adds each column's message into its rows with shared-memory
+// atomics, so every message is read once per tile and no row needs a
+// reduction across lanes.  Addition order inside a row is free in the FP32
+// study (the FP64 path keeps the reference's order on the flat CSR).
+static constexpr uint32_t kTileRows = 16384;   // rows per tile: 64 KB of FP32 accumulators
+static constexpr uint32_t kTileThreads = 512;
+static constexpr uint32_t kTileBig = 32;       // columns with more entries in a tile go to a warp
+static constexpr uint32_t kTileBigCap = 1024;  // such columns queued per tile (the rest run serially)
+
+__global__ void k_tile_colof(const uint32_t* __restrict__ ptr, uint32_t ncol, uint32_t* colof)
+{
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < ncol; c += gridDim.x * blockDim.x)
+    for (uint32_t i = ptr[c]; i < ptr[c + 1]; i++) colof[i] = c;
+}
+
+__global__ void k_tile_keys(const uint32_t* __restrict__ row, uint64_t m, uint32_t nreg, uint32_t* key, uint32_t* idx)
+{
+  for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < m; i += (uint64_t) gridDim.x * blockDim.x)
+  {
+    const uint32_t r = row[i];
+    key[i] = r < nreg ? r / kTileRows : 0xFFFFFFFFu;  // sink rows sort last and are dropped
+    idx[i] = (uint32_t) i;
+  }
+}
+
+// Entries in (tile, column, row) order: local rows, and a flag where a new
+// (tile, column) pair starts.
+__global__ void k_tile_flags(const uint32_t* __restrict__ order, uint64_t n, const uint32_t* __restrict__ colof,
+                             const uint32_t* __restrict__ row, uint16_t* trow, uint32_t* flag)
+{
+  for (uint64_t e = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; e < n; e += (uint64_t) gridDim.x * blockDim.x)
+  {
+    const uint32_t i = order[e];
+    const uint32_t r = row[i], t = r / kTileRows;
+    trow[e] = (uint16_t) (r - t * kTileRows);
+    bool start = e == 0;
+    if (!start)
+    {
+      const uint32_t j = order[e - 1];
+      start = colof[j] != colof[i] || row[j] / kTileRows != t;
+    }
+    flag[e] = start ? 1u : 0u;
+  }
+}
+
+__global__ void k_tile_cols(const uint32_t* __restrict__ order, uint64_t n, const uint32_t* __restrict__ colof,
+                            const uint32_t* __restrict__ row, const uint32_t* __restrict__ flag,
+                            const uint32_t* __restrict__ slot, uint32_t* tcol, uint32_t* tptr, uint32_t* tile_col)
+{
+  for (uint64_t e = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; e < n; e += (uint64_t) gridDim.x * blockDim.x)
+  {
+    if (!flag[e]) continue;
+    const uint32_t i = order[e], k = slot[e];
+    tcol[k] = colof[i];
+    tptr[k] = (uint32_t) e;
+    const uint32_t t = row[i] / kTileRows;
+    if (e == 0 || row[order[e - 1]] / kTileRows != t) tile_col[t] = k;
+  }
+}
+
+static int pr_build_tiles(la3g_graph* G, PrScratch* ps)
+{
+  if (ps->tile_col) return LA3G_OK;
+  DevGraph& g = G->g;
+  cudaStream_t s = G->stream;
+  LA3G_TRY(build_push_csr(G));
+  const uint64_t m = g.nent;
+  const uint32_t ntiles = (g.nreg + kTileRows - 1) / kTileRows;
+  DevBuf colof, key, key2, idx, idx2, flag, slot, tmp;
+  LA3G_TRY(colof.alloc(m * 4 + 4));
+  LA3G_TRY(key.alloc(m * 4 + 4));
+  LA3G_TRY(key2.alloc(m * 4 + 4));
+  LA3G_TRY(idx.alloc(m * 4 + 4));
+  LA3G_TRY(idx2.alloc(m * 4 + 4));
+  if (m)
+  {
+    k_tile_colof<<<grid_for(g.nslots, 256), 256, 0, s>>>(g.out_ptr, g.nslots, colof.as<uint32_t>());
+    LA3G_LAUNCHED();
+    k_tile_keys<<<grid_for(m, 256), 256, 0, s>>>(g.out_row, m, g.nreg, key.as<uint32_t>(), idx.as<uint32_t>());
+    LA3G_LAUNCHED();
+    // stable by tile: the push CSR's (column, row) order is kept inside each tile
+    size_t tb = 0;
+    LA3G_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tb, key.as<uint32_t>(), key2.as<uint32_t>(), idx.as<uint32_t>(),
+                                              idx2.as<uint32_t>(), (int64_t) m, 0, 32, s));
+    LA3G_TRY(tmp.alloc(tb));
+    LA3G_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tb, key.as<uint32_t>(), key2.as<uint32_t>(), idx.as<uint32_t>(),
+                                              idx2.as<uint32_t>(), (int64_t) m, 0, 32, s));
+  }
+  // entries of regular rows (they sort first): the pull CSR's regular-row entries
+  uint32_t nreg_ent = 0;
+  LA3G_CUDA(cudaMemcpyAsync(&nreg_ent, g.in_ptr + g.nreg, 4, cudaMemcpyDeviceToHost, s));
+  LA3G_CUDA(cudaStreamSynchronize(s));
+  const uint64_t n = nreg_ent;
+  LA3G_TRY(flag.alloc(n * 4 + 4));
+  LA3G_TRY(slot.alloc(n * 4 + 4));
+  LA3G_TRY(galloc(G, &ps->trow, n + 8));
+  uint32_t ncols = 0;
+  if (n)
+  {
+    k_tile_flags<<<grid_for(n, 256), 256, 0, s>>>(idx2.as<uint32_t>(), n, colof.as<uint32_t>(), g.out_row, ps->trow,
+                                                  flag.as<uint32_t>());
+    LA3G_LAUNCHED();
+    size_t tb = 0;
+    LA3G_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tb, flag.as<uint32_t>(), slot.as<uint32_t>(), (int64_t) n, s));
+    LA3G_TRY(tmp.alloc(tb));
+    LA3G_CUDA(cub::DeviceScan::ExclusiveSum(tmp.p, tb, flag.as<uint32_t>(), slot.as<uint32_t>(), (int64_t) n, s));
+    uint32_t last[2];
+    LA3G_CUDA(cudaMemcpyAsync(&last[0], slot.as<uint32_t>() + n - 1, 4, cudaMemcpyDeviceToHost, s));
+    LA3G_CUDA(cudaMemcpyAsync(&last[1], flag.as<uint32_t>() + n - 1, 4, cudaMemcpyDeviceToHost, s));
+    LA3G_CUDA(cudaStreamSynchronize(s));
+    ncols = last[0] + last[1];
+  }
+  LA3G_TRY(galloc(G, &ps->tcol, (size_t) ncols + 1));
+  LA3G_TRY(galloc(G, &ps->tptr, (size_t) ncols + 1));
+  LA3G_TRY(galloc(G, &ps->tile_col, (size_t) ntiles + 1));
+  std::vector<uint32_t> tc(ntiles + 1, ncols);
+  LA3G_CUDA(cudaMemcpyAsync(ps->tile_col, tc.data(), tc.size() * 4, cudaMemcpyHostToDevice, s));
+  if (n)
+  {
+    k_tile_cols<<<grid_for(n, 256), 256, 0, s>>>(idx2.as<uint32_t>(), n, colof.as<uint32_t>(), g.out_row,
+                                                 flag.as<uint32_t>(), slot.as<uint32_t>(), ps->tcol, ps->tptr,
+                                                 ps->tile_col);
+    LA3G_LAUNCHED();
+  }
+  const uint32_t end = (uint32_t) n;
+  LA3G_CUDA(cudaMemcpyAsync(ps->tptr + ncols, &end, 4, cudaMemcpyHostToDevice, s));
+  // empty tiles start where the next tile starts
+  LA3G_CUDA(cudaMemcpyAsync(tc.data(), ps->tile_col, tc.size() * 4, cudaMemcpyDeviceToHost, s));
+  LA3G_CUDA(cudaStreamSynchronize(s));
+  for (int64_t t = (int64_t) ntiles - 1; t >= 0; t--) tc[t] = std::min(tc[t], tc[t + 1]);
+  LA3G_CUDA(cudaMemcpyAsync(ps->tile_col, tc.data(), tc.size() * 4, cudaMemcpyHostToDevice, s));
+  LA3G_CUDA(cudaStreamSynchronize(s));
+  ps->tile_rows = kTileRows;
+  ps->ntiles = ntiles;
+  ps->tile_ncols = ncols;
+  ps->tile_nent = n;
+  return LA3G_OK;
+}
+
+__global__ void __launch_bounds__(kTileThreads)
+k_prf_tiles(const uint32_t* __restrict__ tile_col, const uint32_t* __restrict__ tcol,
+            const uint32_t* __restrict__ tptr, const uint16_t* __restrict__ trow, uint32_t ntiles, uint32_t nreg,
+            const float* __restrict__ x, float* __restrict__ xnext, float* __restrict__ rankf,
+            double* __restrict__ rank, const uint32_t* __restrict__ deg, double* resid)
+{
+  extern __shared__ float ys[];  // kTileRows accumulators
+  __shared__ uint32_t s_big[kTileBigCap];
+  __shared__ uint32_t s_nbig;
+  __shared__ double s_part[kTileThreads / 32];
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  double local = 0.0;
+  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x)
+  {
+    const uint32_t r0 = t * kTileRows, nr = min(kTileRows, nreg - r0);
+    for (uint32_t i = tid; i < nr; i += kTileThreads) ys[i] = 0.0f;
+    if (tid == 0) s_nbig = 0;
+    __syncthreads();
+    const uint32_t k0 = tile_col[t], k1 = tile_col[t + 1];
+    // a thread per column, four columns' messages in flight
+    for (uint32_t kb = k0; kb < k1; kb += 4 * kTileThreads)
+    {
+      uint32_t b[4], e[4];
+      float xv[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+      {
+        const uint32_t k = kb + u * kTileThreads + tid;
+        b[u] = e[u] = 0;
+        if (k < k1)
+        {
+          b[u] = tptr[k];
+          e[u] = tptr[k + 1];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+      {
+        const uint32_t k = kb + u * kTileThreads + tid;
+        xv[u] = (k < k1 && e[u] - b[u] <= kTileBig) ? x[tcol[k]] : 0.0f;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+      {
+        const uint32_t k = kb + u * kTileThreads + tid;
+        if (k >= k1) continue;
+        if (e[u] - b[u] > kTileBig)
+        {
+          const uint32_t q = atomicAdd(&s_nbig, 1u);
+          if (q < kTileBigCap)
+          {
+            s_big[q] = k;
+            continue;
+          }
+          xv[u] = x[tcol[k]];  // queue full: this thread adds the column itself
+        }
+        for (uint32_t j = b[u]; j < e[u]; j++) atomicAdd(&ys[trow[j]], xv[u]);
+      }
+    }
+    __syncthreads();
+    const uint32_t nb = min(s_nbig, kTileBigCap);
+    for (uint32_t q = warp; q < nb; q += kTileThreads / 32)
+    {
+      const uint32_t k = s_big[q];
+      const float v = x[tcol[k]];
+      for (uint32_t j = tptr[k] + lane; j < tptr[k + 1]; j += 32) atomicAdd(&ys[trow[j]], v);
+    }
+    __syncthreads();
+    for (uint32_t i = tid; i < nr; i += kTileThreads) local += prf_finish(r0 + i, ys[i], xnext, rankf, rank, deg, 1);
+    __syncthreads();
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
+  if (lane == 0) s_part[warp] = local;
+  __syncthreads();
+  if (tid == 0)
+  {
+    double sum = 0.0;
+    for (uint32_t w = 0; w < kTileThreads / 32; w++) sum += s_part[w];
+    if (sum != 0.0) atomicAdd(resid, sum);
+  }
+}
+
 }  // namespace la3g
 
 using namespace la3g;
@@ -480,8 +721,8 @@ extern "C" int la3g_pr(la3g_graph* G, uint32_t iters, double* rank_out, uint32_t
   return T.finish();
 }
 
-extern "C" int la3g_pr_f32(la3g_graph* G, uint32_t iters, double tol, double* rank_out, double* residual_out,
-                           la3g_stats* st)
+static int pr_f32_run(la3g_graph* G, uint32_t iters, double tol, double* rank_out, double* residual_out,
+                      la3g_stats* st, bool tiled)
 {
   if (!G) return set_error(LA3G_EINVAL, "null graph");
   DevGraph& g = G->g;
@@ -500,6 +741,13 @@ extern "C" int la3g_pr_f32(la3g_graph* G, uint32_t iters, double tol, double* ra
     LA3G_TRY(galloc(G, &ps->xf[1], N));
     LA3G_TRY(galloc(G, &ps->resid, 1));
   }
+  if (tiled && !ps->tile_col)
+  {
+    LA3G_TRY(pr_build_tiles(G, ps));
+    LA3G_CUDA(cudaFuncSetAttribute(k_prf_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) (kTileRows * 4)));
+    LA3G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ps->tile_blocks, k_prf_tiles, kTileThreads,
+                                                            kTileRows * 4));
+  }
   T.device_begin();
   k_prf_init<<<grid_for(N, 256), 256, 0, s>>>(N, g.nreg, g.src_base(), g.iso_base(), ps->deg, ps->rankf, ps->rank,
                                               ps->xf[0], ps->xf[1]);
@@ -516,6 +764,20 @@ extern "C" int la3g_pr_f32(la3g_graph* G, uint32_t iters, double tol, double* ra
   for (; it < iters;)
   {
     LA3G_CUDA(cudaMemsetAsync(ps->resid, 0, 8, s));
+    if (tiled)
+    {
+      // per tile: its non-empty columns (index, offset, message) and 2 B per
+      // entry, then the rows' rank read + write and next message write
+      ProfileScope p("pr_tiles_f32", s, 12.0 * ps->tile_ncols + 2.0 * ps->tile_nent + 4.0 * (g.nreg + 1) + 8.0 * g.nreg +
+                                            8.0 * g.nreg + 4.0 * g.nreg);
+      const unsigned tgrid = std::min<unsigned>(ps->ntiles, num_sms() * std::max(ps->tile_blocks, 1));
+      if (ps->ntiles)
+        k_prf_tiles<<<tgrid, kTileThreads, kTileRows * 4, s>>>(ps->tile_col, ps->tcol, ps->tptr, ps->trow, ps->ntiles,
+                                                               g.nreg, ps->xf[cur], ps->xf[cur ^ 1], ps->rankf,
+                                                               ps->rank, ps->deg, ps->resid);
+      LA3G_LAUNCHED();
+    }
+    else
     {
       ProfileScope p("pr_pull_f32", s, it_bytes);
       k_prf_pull<<<blocks, 256, 0, s>>>(g.in_ptr, g.in_col, ps->xf[cur], ps->xf[cur ^ 1], ps->rankf, ps->rank, ps->deg,
@@ -560,4 +822,16 @@ extern "C" int la3g_pr_f32(la3g_graph* G, uint32_t iters, double tol, double* ra
   LA3G_TRY(T.finish());
   if (residual_out) *residual_out = res;
   return LA3G_OK;
+}
+
+extern "C" int la3g_pr_f32(la3g_graph* G, uint32_t iters, double tol, double* rank_out, double* residual_out,
+                           la3g_stats* st)
+{
+  return pr_f32_run(G, iters, tol, rank_out, residual_out, st, false);
+}
+
+extern "C" int la3g_pr_f32_tiled(la3g_graph* G, uint32_t iters, double tol, double* rank_out, double* residual_out,
+                                 la3g_stats* st)
+{
+  return pr_f32_run(G, iters, tol, rank_out, residual_out, st, true);
 }

@@ -56,6 +56,7 @@ struct GsProgram
   static constexpr bool stationary = false;
   static constexpr bool gather_with_state = false;
   static constexpr bool apply_with_iteration = true;
+  static constexpr bool associative = true;  // counters add up in any grouping
   const GsQuery* q;          // device
   const uint32_t* vlabel;    // device, by vertex id
   const uint32_t* degree;    // device, by vertex id
@@ -143,6 +144,30 @@ struct GsProgram
   }
 };
 
+// is_matched (graphsim.h:50-57) and the per-query-vertex results of every
+// vertex, by original id, computed where the states are (a state is ~180
+// bytes; the outputs are 1 + qsize bytes per vertex).
+__global__ void k_gs_results(uint32_t N, const uint32_t* __restrict__ id_of_pos, const GsState* __restrict__ S,
+                             uint32_t qsize, uint8_t* matched, char* res, unsigned long long* nmatches)
+{
+  unsigned long long cnt = 0;
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x)
+  {
+    const uint32_t v = id_of_pos[p];
+    bool m = false;
+    for (uint32_t i = 0; i < qsize; i++)
+    {
+      const uint8_t r = S[p].res[i];
+      m |= r != '0';
+      if (res) res[(size_t) v * qsize + i] = (char) r;
+    }
+    matched[v] = m;
+    cnt += m;
+  }
+  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(nmatches, cnt);
+}
+
 }  // namespace
 
 extern "C" int la3gp_graphsim(la3g_graph* gr, const uint32_t* vlabel, uint32_t qsize, const uint32_t* qlabel,
@@ -175,39 +200,51 @@ extern "C" int la3gp_graphsim(la3g_graph* gr, const uint32_t* vlabel, uint32_t q
   if (st != LA3G_OK) return st;
   GsQuery* dq = nullptr;
   uint32_t *dl = nullptr, *dd = nullptr;
-  if (cudaMalloc(&dq, sizeof(GsQuery)) != cudaSuccess || cudaMalloc(&dl, (size_t) N * 4) != cudaSuccess ||
-      cudaMalloc(&dd, (size_t) N * 4) != cudaSuccess)
-  {
-    cudaGetLastError();
+  uint8_t* dm = nullptr;
+  char* dr = nullptr;
+  unsigned long long* dn = nullptr;
+  auto release = [&]() {
     cudaFree(dq);
     cudaFree(dl);
     cudaFree(dd);
+    cudaFree(dm);
+    cudaFree(dr);
+    cudaFree(dn);
+  };
+  if (cudaMalloc(&dq, sizeof(GsQuery)) != cudaSuccess || cudaMalloc(&dl, (size_t) N * 4) != cudaSuccess ||
+      cudaMalloc(&dd, (size_t) N * 4) != cudaSuccess || cudaMalloc(&dm, N) != cudaSuccess ||
+      cudaMalloc(&dn, 8) != cudaSuccess || (res && cudaMalloc(&dr, (size_t) N * qsize) != cudaSuccess))
+  {
+    cudaGetLastError();
+    release();
     return LA3G_ENOMEM;
   }
   cudaMemcpy(dq, &hq, sizeof(GsQuery), cudaMemcpyHostToDevice);
   cudaMemcpy(dl, vlabel, (size_t) N * 4, cudaMemcpyHostToDevice);
   cudaMemcpy(dd, deg.data(), (size_t) N * 4, cudaMemcpyHostToDevice);
-  std::vector<GsState> out(N);
+  cudaMemset(dn, 0, 8);
+  unsigned long long nm = 0;
   {
     la3g_vp::Engine<GsProgram> e(gr, GsProgram{dq, dl, dd});
     st = e.initialize();
     if (st == LA3G_OK) st = e.execute(0, iters);  // until convergence (graphsim.cpp:72)
-    if (st == LA3G_OK) st = e.states(out.data());
+    if (st == LA3G_OK)
+    {
+      cudaStream_t s = (cudaStream_t) e.view().stream;
+      k_gs_results<<<(N + 255) / 256, 256, 0, s>>>(N, e.view().id_of_pos, e.device_states(), qsize, dm, dr, dn);
+      if (cudaGetLastError() != cudaSuccess) st = LA3G_ECUDA;
+      if (st == LA3G_OK && cudaStreamSynchronize(s) != cudaSuccess) st = LA3G_ECUDA;
+    }
   }
-  cudaFree(dq);
-  cudaFree(dl);
-  cudaFree(dd);
-  if (st != LA3G_OK) return st;
-  uint32_t nm = 0;
-  for (uint32_t v = 0; v < N; v++)
+  if (st == LA3G_OK)
   {
-    bool m = false;  // is_matched (graphsim.h:50-57)
-    for (uint32_t i = 0; i < qsize; i++) m |= out[v].res[i] != '0';
-    nm += m;
-    if (matched) matched[v] = m;
-    if (res)
-      for (uint32_t i = 0; i < qsize; i++) res[(size_t) v * qsize + i] = (char) out[v].res[i];
+    if (cudaMemcpy(&nm, dn, 8, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        (matched && cudaMemcpy(matched, dm, N, cudaMemcpyDeviceToHost) != cudaSuccess) ||
+        (res && cudaMemcpy(res, dr, (size_t) N * qsize, cudaMemcpyDeviceToHost) != cudaSuccess))
+      st = LA3G_ECUDA;
   }
-  if (nmatches) *nmatches = nm;
+  release();
+  if (st != LA3G_OK) return st;
+  if (nmatches) *nmatches = (uint32_t) nm;
   return LA3G_OK;
 }

@@ -60,3 +60,38 @@ def test_f32_residual_and_tolerance_stop(gpu):
     a = L.pagerank_f32(g, 10)[0]
     b = L.pagerank_f32(g, 10)[0]
     assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("kind", ["rmat", "er"])
+def test_f32_tiled_vs_oracle(gpu, oracle, tmp_path, kind):
+    """The FP32 study over the tiled DCSC layout (la3g_pr_f32_tiled): the
+    same tolerances against the FP64 oracle, and within FP32 rounding of the
+    flat-CSR FP32 path (only the order of additions inside a row differs).
+    2^17 vertices: eight row tiles, R-MAT hub columns above the warp
+    threshold in every tile."""
+    L = gpu
+    if kind == "rmat":
+        e = L.EdgeList.rmat(17, 16, seed=35)
+    else:
+        e = L.EdgeList.er(1 << 17, 16 << 17, seed=36)
+    n = e.n
+    p = tmp_path / "g.bin"
+    e.write(p)
+    g = L.Graph.load_directed(p, n)
+    rt, rest, st = L.pagerank_f32(g, 20, tiled=True)
+    rf, resf, _ = L.pagerank_f32(g, 20)
+    assert st.iterations == 20
+    orank, _ = oracle.OracleGraph(p, n, oracle.DIRECTED).pagerank(20)
+    l1, mx, _ = _errors(rt, orank)
+    assert l1 < L1_REL_TOL and mx < MAX_REL_TOL, (l1, mx)
+    l1f, mxf, _ = _errors(rt, rf)
+    assert l1f < 1e-6 and mxf < 1e-5, (l1f, mxf)
+    assert abs(rest - resf) <= 1e-2 * resf
+    # sinks and sources as in the flat path
+    pos, ids = g.positions()
+    i = g.info
+    src = ids[i.nregular + i.nsink: i.nregular + i.nsink + i.nsource]
+    assert np.all(rt[src] == 0.15)
+    # repeated calls reuse the layout and give the same ranks up to FP32 rounding
+    rt2 = L.pagerank_f32(g, 20, tiled=True)[0]
+    assert np.abs(rt2 - rt).max() <= 1e-5 * max(1.0, np.abs(rt).max())

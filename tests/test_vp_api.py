@@ -190,3 +190,130 @@ def test_graphsim_driver(gpu, golden):
         ref = np.load(GOLD / f"{name}.npz")["matched"]
         assert all((shown[v] == str(v)) == bool(ref[v]) for v in shown), name
 
+
+
+def test_programs_hub_rows_vs_oracle(gpu, progs, oracle, tmp_path):
+    """R-MAT s17: rows with more in-edges than the engine's hub threshold
+    (4096), so associative programs (BFS, SSSP, degree) cut them into tasks
+    and combine the partials; PageRank (floating-point sums, not declared
+    associative) keeps the edge-by-edge order.  Every result against the
+    oracle."""
+    L = gpu
+    n = 1 << 17
+    e = L.EdgeList.rmat(17, 16, seed=43)
+    ew = L.EdgeList.rmat(17, 16, seed=43, weighted=True, wseed=44)
+    p, pw = tmp_path / "g.bin", tmp_path / "g.w.bin"
+    e.write(p)
+    ew.write(pw)
+    a = np.fromfile(p, np.uint32)
+    assert np.bincount(a, minlength=n + 1).max() > 2 * 4096  # hubs in both directions
+    rank, deg = _pr(L, progs, p, n, 5)
+    orank, odeg = oracle.OracleGraph(p, n, oracle.DIRECTED).pagerank(5)
+    assert np.array_equal(deg, odeg)
+    assert np.array_equal(rank.view(np.uint64), orank.view(np.uint64))
+    gu = L.Graph.load_undirected(p, n)
+    ou = oracle.OracleGraph(p, n, 0)
+    hub = int(np.bincount(a, minlength=n + 1).argmax())
+    for r in (1, hub):
+        hops, par, it = _bfs(L, progs, gu, r)
+        oh, opar, oit = ou.bfs(r)
+        assert np.array_equal(hops, oh) and np.array_equal(par, opar) and it == oit, r
+    gw = L.Graph.load_directed(pw, n, weighted=True)
+    ow = oracle.OracleGraph(pw, n, oracle.DIRECTED | oracle.WEIGHTED)
+    for r in (1, hub):
+        d, it = _sssp(L, progs, gw, r)
+        od, oit = ow.sssp(r)
+        assert np.array_equal(d, od) and it == oit, r
+
+
+def _order(values, ids, pos_ids, desc=True):
+    """Expected top-k order: value (largest first), ties by position."""
+    keyed = sorted(range(len(pos_ids)), key=lambda p: (-int(values[p]) if desc else int(values[p]), p))
+    return [int(pos_ids[p]) for p in keyed], [int(values[p]) for p in keyed]
+
+
+def test_engine_topk_btopk_reduce(gpu, progs, tmp_path):
+    """topk / btopk / reduce of the engine (vertex_program.hpp:558-767) on the
+    degree app's states: the k largest in-degrees (ties in position order),
+    btopk<2> over (degree, ~degree), and the degree sum."""
+    L = gpu
+    n = 1 << 14
+    p = tmp_path / "g.bin"
+    L.EdgeList.rmat(14, 8, seed=47).write(p)
+    g = L.Graph.load_directed(p, n)
+    deg = np.empty(g.nslots, np.uint32)
+    assert progs.la3gp_degree(g._h, _p(deg, C.c_uint32)) == 0
+    _, pos_ids = g.positions()
+    dpos = deg[pos_ids]  # degree at each position
+    u32p, u64p = C.POINTER(C.c_uint32), C.POINTER(C.c_uint64)
+    progs.la3gp_degree_topk.argtypes = [C.c_void_p, C.c_uint32, u32p, u32p, u64p, u32p, u32p]
+    for k in (1, 3, 10, 100, 512):
+        ids = np.empty(k, np.uint32)
+        vals = np.empty(k, np.uint32)
+        bids = np.empty(2 * k, np.uint32)
+        bvals = np.empty(2 * k, np.uint32)
+        tot = C.c_uint64()
+        assert progs.la3gp_degree_topk(g._h, k, _p(ids, C.c_uint32), _p(vals, C.c_uint32), C.byref(tot),
+                                       _p(bids, C.c_uint32), _p(bvals, C.c_uint32)) == 0
+        eids, evals = _order(dpos, None, pos_ids)
+        assert list(vals) == evals[:k] and list(ids) == eids[:k], k
+        assert tot.value == int(deg.sum()) == g.info.nentries
+        assert list(bids[:k]) == eids[:k] and list(bvals[:k]) == evals[:k], k
+        cids, cvals = _order(~dpos, None, pos_ids)
+        assert list(bids[k:]) == cids[:k] and list(bvals[k:]) == cvals[:k], k
+
+
+def test_engine_topk_active_only_pads(gpu, progs, tmp_path):
+    """topk(active_only) after a BFS: the vertices apply reached (not the
+    root, which init activates without marking), farthest first; with fewer
+    active vertices than k the list is padded with (0, 0) pairs, as one rank
+    of the reference pads."""
+    L = gpu
+    n = 1 << 12
+    p = tmp_path / "g.bin"
+    e = L.EdgeList.rmat(12, 4, seed=53)
+    e.write(p)
+    # plus a path 4097 - 4098 - 4099 - 4100 away from the rest: a root there
+    # reaches three vertices, fewer than k
+    np.concatenate([np.fromfile(p, np.uint32), np.array([4097, 4098, 4098, 4099, 4099, 4100], np.uint32)]).tofile(p)
+    n += 4
+    g = L.Graph.load_undirected(p, n)
+    _, pos_ids = g.positions()
+    u32p = C.POINTER(C.c_uint32)
+    progs.la3gp_bfs_topk.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, u32p, u32p]
+    for root in (1, 100, 4097):
+        hops, _, _ = _bfs(L, progs, g, root)
+        hpos = hops[pos_ids].astype(np.int64)
+        act = (hpos != 255) & (pos_ids != root)
+        cand = np.nonzero(act)[0]
+        ids_e, vals_e = _order(hpos[cand], None, pos_ids[cand])
+        for k in (5, 512):
+            ids = np.empty(k, np.uint32)
+            vals = np.empty(k, np.uint32)
+            assert progs.la3gp_bfs_topk(g._h, root, k, _p(ids, C.c_uint32), _p(vals, C.c_uint32)) == 0
+            m = min(k, len(cand))
+            assert list(vals[:m]) == vals_e[:m] and list(ids[:m]) == ids_e[:m], (root, k)
+            # padding: value-initialised pairs sorted in (value 0 sorts after every reached vertex)
+            assert all(v == 0 and i == 0 for i, v in zip(ids[m:], vals[m:])), (root, k)
+
+
+def test_tc_through_engine_vs_oracle(gpu, progs, oracle, tmp_path):
+    """TC written as the reference writes it (tc.cpp:11-52): CtVertex's
+    neighbour lists are variable-size messages of any length (R-MAT hubs
+    scatter lists of thousands of ids), gathered with the row's own list
+    (gather_with_state); per-vertex counts and the reduce() total against
+    the oracle."""
+    L = gpu
+    n = 1 << 15
+    p = tmp_path / "t.bin"
+    L.EdgeList.rmat(15, 16, seed=61).write(p)
+    g = L.Graph.load_directed(p, n, remove_cycles=True)
+    gr = L.Graph.load(p, n, L.DIRECTED | L.ACYCLIC | L.REVERSE)
+    progs.la3gp_tc.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32)]
+    tot = C.c_uint64()
+    ntri = np.empty(g.nslots, np.uint32)
+    assert progs.la3gp_tc(g._h, gr._h, C.byref(tot), _p(ntri, C.c_uint32)) == 0
+    otot, oper = oracle.OracleGraph(p, n, oracle.DIRECTED | oracle.ACYCLIC).tc()
+    assert tot.value == otot
+    assert np.array_equal(ntri, oper)
+    assert np.bincount(np.fromfile(p, np.uint32), minlength=n + 1).max() > 1000  # long messages
