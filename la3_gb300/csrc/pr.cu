@@ -425,14 +425,17 @@ k_prf_pull(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, c
 // per-tile DCSC, src/utils/csc.h:60-130: only the non-empty columns are
 // listed, with their offsets): tcol / tptr over the tile's non-empty columns
 // in ascending position, and a 16-bit row inside the tile per entry.  One
-// CTA takes a tile at a time with its rows' accumulators in shared memory
-// (64 KB), walks the tile's columns (one thread per column, four columns'
-// messages loaded at once; columns with many entries in the tile go to whole
-// warps) and adds each column's message into its rows with shared-memory
-// atomics, so every message is read once per tile and no row needs a
-// reduction across lanes.  Addition order inside a row is free in the FP32
-// study (the FP64 path keeps the reference's order on the flat CSR).
-static constexpr uint32_t kTileRows = 16384;   // rows per tile: 64 KB of FP32 accumulators
+// CTA takes a tile at a time with its rows' accumulators in shared memory,
+// walks the tile's columns (one thread per column, four columns' messages
+// loaded at once; columns with many entries in the tile go to whole warps)
+// and adds each column's message into its rows with shared-memory atomics,
+// so every message is read once per tile and no row needs a reduction across
+// lanes.  Rows with more than kLongRow in-edges stay out of the tiles (their
+// thousands of additions would serialise on one shared-memory word) and are
+// summed a block each by the first blocks of the same launch.
+// Addition order inside a row is free in the FP32 study (the FP64 path keeps
+// the reference's order on the flat CSR).
+static constexpr uint32_t kTileRows = 2048;    // rows per tile: 8 KB of FP32 accumulators
 static constexpr uint32_t kTileThreads = 512;
 static constexpr uint32_t kTileBig = 32;       // columns with more entries in a tile go to a warp
 static constexpr uint32_t kTileBigCap = 1024;  // such columns queued per tile (the rest run serially)
@@ -443,14 +446,25 @@ __global__ void k_tile_colof(const uint32_t* __restrict__ ptr, uint32_t ncol, ui
     for (uint32_t i = ptr[c]; i < ptr[c + 1]; i++) colof[i] = c;
 }
 
-__global__ void k_tile_keys(const uint32_t* __restrict__ row, uint64_t m, uint32_t nreg, uint32_t* key, uint32_t* idx)
+// Tile of each push entry; entries of sink rows and of long regular rows
+// (more than kLongRow in-edges: summed by the flat kernel's block-per-row
+// path, since thousands of additions into one shared-memory word would
+// serialise) sort last and are dropped.
+__global__ void k_tile_keys(const uint32_t* __restrict__ row, uint64_t m, uint32_t nreg,
+                            const uint32_t* __restrict__ in_ptr, uint32_t* key, uint32_t* idx,
+                            unsigned long long* kept)
 {
+  unsigned long long c = 0;
   for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < m; i += (uint64_t) gridDim.x * blockDim.x)
   {
     const uint32_t r = row[i];
-    key[i] = r < nreg ? r / kTileRows : 0xFFFFFFFFu;  // sink rows sort last and are dropped
+    const bool keep = r < nreg && in_ptr[r + 1] - in_ptr[r] <= kLongRow;
+    key[i] = keep ? r / kTileRows : 0xFFFFFFFFu;
     idx[i] = (uint32_t) i;
+    c += keep;
   }
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(kept, c);
 }
 
 // Entries in (tile, column, row) order: local rows, and a flag where a new
@@ -496,7 +510,9 @@ static int pr_build_tiles(la3g_graph* G, PrScratch* ps)
   LA3G_TRY(build_push_csr(G));
   const uint64_t m = g.nent;
   const uint32_t ntiles = (g.nreg + kTileRows - 1) / kTileRows;
-  DevBuf colof, key, key2, idx, idx2, flag, slot, tmp;
+  DevBuf colof, key, key2, idx, idx2, flag, slot, tmp, kept;
+  LA3G_TRY(kept.alloc(8));
+  LA3G_CUDA(cudaMemsetAsync(kept.p, 0, 8, s));
   LA3G_TRY(colof.alloc(m * 4 + 4));
   LA3G_TRY(key.alloc(m * 4 + 4));
   LA3G_TRY(key2.alloc(m * 4 + 4));
@@ -506,7 +522,8 @@ static int pr_build_tiles(la3g_graph* G, PrScratch* ps)
   {
     k_tile_colof<<<grid_for(g.nslots, 256), 256, 0, s>>>(g.out_ptr, g.nslots, colof.as<uint32_t>());
     LA3G_LAUNCHED();
-    k_tile_keys<<<grid_for(m, 256), 256, 0, s>>>(g.out_row, m, g.nreg, key.as<uint32_t>(), idx.as<uint32_t>());
+    k_tile_keys<<<grid_for(m, 256), 256, 0, s>>>(g.out_row, m, g.nreg, g.in_ptr, key.as<uint32_t>(), idx.as<uint32_t>(),
+                                                 kept.as<unsigned long long>());
     LA3G_LAUNCHED();
     // stable by tile: the push CSR's (column, row) order is kept inside each tile
     size_t tb = 0;
@@ -516,11 +533,11 @@ static int pr_build_tiles(la3g_graph* G, PrScratch* ps)
     LA3G_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tb, key.as<uint32_t>(), key2.as<uint32_t>(), idx.as<uint32_t>(),
                                               idx2.as<uint32_t>(), (int64_t) m, 0, 32, s));
   }
-  // entries of regular rows (they sort first): the pull CSR's regular-row entries
-  uint32_t nreg_ent = 0;
-  LA3G_CUDA(cudaMemcpyAsync(&nreg_ent, g.in_ptr + g.nreg, 4, cudaMemcpyDeviceToHost, s));
+  // the kept entries sort first
+  unsigned long long nkept = 0;
+  LA3G_CUDA(cudaMemcpyAsync(&nkept, kept.p, 8, cudaMemcpyDeviceToHost, s));
   LA3G_CUDA(cudaStreamSynchronize(s));
-  const uint64_t n = nreg_ent;
+  const uint64_t n = nkept;
   LA3G_TRY(flag.alloc(n * 4 + 4));
   LA3G_TRY(slot.alloc(n * 4 + 4));
   LA3G_TRY(galloc(G, &ps->trow, n + 8));
@@ -570,6 +587,8 @@ static int pr_build_tiles(la3g_graph* G, PrScratch* ps)
 __global__ void __launch_bounds__(kTileThreads)
 k_prf_tiles(const uint32_t* __restrict__ tile_col, const uint32_t* __restrict__ tcol,
             const uint32_t* __restrict__ tptr, const uint16_t* __restrict__ trow, uint32_t ntiles, uint32_t nreg,
+            const uint32_t* __restrict__ in_ptr, const uint32_t* __restrict__ in_col,
+            const uint32_t* __restrict__ long_rows, uint32_t nlong, uint32_t long_blocks,
             const float* __restrict__ x, float* __restrict__ xnext, float* __restrict__ rankf,
             double* __restrict__ rank, const uint32_t* __restrict__ deg, double* resid)
 {
@@ -577,9 +596,30 @@ k_prf_tiles(const uint32_t* __restrict__ tile_col, const uint32_t* __restrict__ 
   __shared__ uint32_t s_big[kTileBigCap];
   __shared__ uint32_t s_nbig;
   __shared__ double s_part[kTileThreads / 32];
+  __shared__ float s_lpart[kTileThreads / 32];
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   double local = 0.0;
-  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x)
+  // the first long_blocks blocks: the long rows, a block each, from the flat CSR
+  for (uint32_t k = blockIdx.x; blockIdx.x < long_blocks && k < nlong; k += long_blocks)
+  {
+    const uint32_t r = long_rows[k];
+    if (r >= nreg) continue;  // a sink row (uniform per block)
+    float acc = 0.0f;
+    for (uint32_t i = in_ptr[r] + tid; i < in_ptr[r + 1]; i += kTileThreads) acc += x[in_col[i]];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) s_lpart[warp] = acc;
+    __syncthreads();
+    if (tid == 0)
+    {
+      float t = 0.0f;
+      for (uint32_t w = 0; w < kTileThreads / 32; w++) t += s_lpart[w];
+      local += prf_finish(r, t, xnext, rankf, rank, deg, 1);
+    }
+    __syncthreads();
+  }
+  const uint32_t tblocks = gridDim.x - long_blocks;
+  for (uint32_t t = blockIdx.x - long_blocks; blockIdx.x >= long_blocks && t < ntiles; t += tblocks)
   {
     const uint32_t r0 = t * kTileRows, nr = min(kTileRows, nreg - r0);
     for (uint32_t i = tid; i < nr; i += kTileThreads) ys[i] = 0.0f;
@@ -635,7 +675,9 @@ k_prf_tiles(const uint32_t* __restrict__ tile_col, const uint32_t* __restrict__ 
       for (uint32_t j = tptr[k] + lane; j < tptr[k + 1]; j += 32) atomicAdd(&ys[trow[j]], v);
     }
     __syncthreads();
-    for (uint32_t i = tid; i < nr; i += kTileThreads) local += prf_finish(r0 + i, ys[i], xnext, rankf, rank, deg, 1);
+    for (uint32_t i = tid; i < nr; i += kTileThreads)
+      if (in_ptr[r0 + i + 1] - in_ptr[r0 + i] <= kLongRow)  // long rows are finished by the flat kernel
+        local += prf_finish(r0 + i, ys[i], xnext, rankf, rank, deg, 1);
     __syncthreads();
   }
 #pragma unroll
@@ -770,11 +812,12 @@ static int pr_f32_run(la3g_graph* G, uint32_t iters, double tol, double* rank_ou
       // entry, then the rows' rank read + write and next message write
       ProfileScope p("pr_tiles_f32", s, 12.0 * ps->tile_ncols + 2.0 * ps->tile_nent + 4.0 * (g.nreg + 1) + 8.0 * g.nreg +
                                             8.0 * g.nreg + 4.0 * g.nreg);
-      const unsigned tgrid = std::min<unsigned>(ps->ntiles, num_sms() * std::max(ps->tile_blocks, 1));
-      if (ps->ntiles)
-        k_prf_tiles<<<tgrid, kTileThreads, kTileRows * 4, s>>>(ps->tile_col, ps->tcol, ps->tptr, ps->trow, ps->ntiles,
-                                                               g.nreg, ps->xf[cur], ps->xf[cur ^ 1], ps->rankf,
-                                                               ps->rank, ps->deg, ps->resid);
+      // long rows first (a block each), then the tiles
+      const uint32_t lblocks = ps->nlong ? std::min<uint32_t>(ps->nlong, num_sms()) : 0;
+      const unsigned tgrid = std::min<unsigned>(std::max<uint32_t>(ps->ntiles, 1), num_sms() * std::max(ps->tile_blocks, 1));
+      k_prf_tiles<<<lblocks + tgrid, kTileThreads, kTileRows * 4, s>>>(
+          ps->tile_col, ps->tcol, ps->tptr, ps->trow, ps->ntiles, g.nreg, g.in_ptr, g.in_col, ps->long_rows, ps->nlong,
+          lblocks, ps->xf[cur], ps->xf[cur ^ 1], ps->rankf, ps->rank, ps->deg, ps->resid);
       LA3G_LAUNCHED();
     }
     else
