@@ -391,6 +391,10 @@ struct Engine
   // SSSP
   DevBuf dist, sfront[2], small[2], hub[2], hub_t0[2], reg_end, rpos;
   unsigned long long* hctr = nullptr;  // pinned: counters + alive words
+  // BM25 / LM: a stream of the device's greatest priority, so that a query's
+  // few small kernels get SMs ahead of the waiting blocks of the BFS / SSSP
+  // lane kernels on the other engines' streams
+  cudaStream_t prio = nullptr;
 };
 
 }  // namespace
@@ -966,11 +970,15 @@ int bm25_loop(Engine* E)
       t->start_ms = wall_ms();
       t->in_flight = 1;
       uint32_t nout = 0;
+      // the engine's priority stream for this call (only this worker uses the graph while it is served)
+      const cudaStream_t saved = E->G->stream;
+      if (E->prio) E->G->stream = E->prio;
       const int st = t->q.kind == LA3G_QUERY_LM
                          ? la3g_lm_query(E->G, t->terms.data(), (uint32_t) t->terms.size(), t->q.k,
                                          (uint32_t*) t->q.out, t->q.scores_out, &nout, nullptr, nullptr, nullptr)
                          : la3g_bm25_query(E->G, t->terms.data(), (uint32_t) t->terms.size(), t->q.k,
                                            (uint32_t*) t->q.out, t->q.scores_out, &nout, nullptr, nullptr, nullptr);
+      E->G->stream = saved;
       t->nout = nout;
       finish_ticket(E->S, t, st);
     }
@@ -1065,6 +1073,16 @@ extern "C" int la3g_server_add_graph(la3g_server* S, la3g_graph* G, uint32_t* gr
   E->wlevel.assign(E->W, 0);
   E->wbusy.assign(E->W, 0);
   int st = LA3G_OK;
+  if (kind == kEngBm25)
+  {
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&E->prio, cudaStreamNonBlocking, greatest) != cudaSuccess)
+    {
+      cudaGetLastError();
+      E->prio = nullptr;  // served on the graph's own stream
+    }
+  }
   if (kind != kEngBm25)
   {
     E->pos_of_id.resize(N);
@@ -1078,6 +1096,7 @@ extern "C" int la3g_server_add_graph(la3g_server* S, la3g_graph* G, uint32_t* gr
   if (st != LA3G_OK)
   {
     if (E->hctr) cudaFreeHost(E->hctr);
+    if (E->prio) cudaStreamDestroy(E->prio);
     delete E;
     std::lock_guard<std::mutex> lk(S->mu);
     S->used -= G->device_bytes + eng_bytes;
@@ -1218,6 +1237,7 @@ extern "C" void la3g_server_free(la3g_server* S)
   for (Engine* e : S->engines)
   {
     if (e->hctr) cudaFreeHost(e->hctr);
+    if (e->prio) cudaStreamDestroy(e->prio);
     delete e;
   }
   for (auto& kv : S->tickets) delete kv.second;
