@@ -1126,7 +1126,22 @@ def next_line(args, rank, world, local) -> dict | None:
     progs.la3gp_graphsim.argtypes = [C.c_void_p, u32p, C.c_uint32, u32p, u32p, C.c_uint32, C.POINTER(C.c_uint8),
                                      C.c_char_p, u32p, u32p]
     matched = np.empty(gr.nslots, np.uint8)
+    # TC as the reference writes it, through the generic engine (neighbour
+    # lists as variable-size messages), on the plain bench's TC graph
+    et = L.EdgeList.rmat(args.tc_scale, 16, seed=TC_SEED)
+    gt = L.Graph.from_edges(et, L.DIRECTED | L.ACYCLIC)
+    gtr = L.Graph.from_edges(et, L.DIRECTED | L.ACYCLIC | L.REVERSE)
+    del et
+    gt.set_stream(stream.cuda_stream)
+    gtr.set_stream(stream.cuda_stream)
+    progs.la3gp_tc.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32)]
     setup_s = time.time() - t_setup
+
+    def tc_engine():
+        tot = C.c_uint64()
+        th = time.perf_counter()
+        L.N.check(progs.la3gp_tc(gt._h, gtr._h, C.byref(tot), None))
+        return tot.value, time.perf_counter() - th
 
     def graphsim():
         nm, it = C.c_uint32(), C.c_uint32()
@@ -1151,6 +1166,9 @@ def next_line(args, rank, world, local) -> dict | None:
 
     for _ in range(args.warmup):
         step(queries(20))
+    tc_engine()
+    tc_runs = [tc_engine() for _ in range(3)]
+    tc_lib, _, _ = L.tc(gt, False)
     torch.cuda.synchronize()
     L.profile_reset()
     L.profile(True)
@@ -1185,6 +1203,9 @@ def next_line(args, rank, world, local) -> dict | None:
                    "degree": {"device_ms": deg_ms, "gteps": gd.info.nentries / (deg_ms / 1e3) / 1e9},
                    "graphsim": {"ms": gs_s * 1e3, "iterations": res[-1][6], "matches": res[-1][5],
                                 "edge_passes_per_s": res[-1][6] * gr.info.nentries / gs_s},
+                   "tc_engine": {"ms": statistics.median(t for _, t in tc_runs) * 1e3,
+                                 "triangles": tc_runs[-1][0], "equals_la3g_tc": tc_runs[-1][0] == tc_lib,
+                                 "graph": f"R-MAT s{args.tc_scale}, host clock incl. the Gn list build"},
                    "setup_s": round(setup_s, 1), "peak_source": peaks.get("source", "measured")},
         "e2e": {"value": nq / lm_host, "unit": "queries/s", "h2d_bytes_per_step": 4 * 5 * 100,
                 "d2h_bytes_per_step": 8 * 10 * 100},
