@@ -446,8 +446,8 @@ __global__ void k_bfs_root_state(uint32_t root, const uint32_t* __restrict__ pos
 // from the lists, top-down after turning the bottom-up bitmap into lists,
 // bottom-up after turning the lists into a bitmap, or bottom-up from the
 // bitmap.  An empty frontier ends the loop.
-__global__ void k_bfs_decide(unsigned long long* S, const FrontierCounters* __restrict__ ctr, uint32_t N,
-                             uint64_t limit, cudaGraphConditionalHandle cont, cudaGraphConditionalHandle mode)
+__global__ void k_bfs_decide(unsigned long long* S, FrontierCounters* ctr, uint32_t N, uint64_t limit,
+                             cudaGraphConditionalHandle cont, cudaGraphConditionalHandle mode)
 {
   unsigned long long it = S[kBIter];
   bool done = false, convert = false;
@@ -502,6 +502,16 @@ __global__ void k_bfs_decide(unsigned long long* S, const FrontierCounters* __re
         }
         else S[kBExamined] += fdeg;
         S[kBCount + m]++;
+        // the counters the body accumulates into start at zero (no memset
+        // node between the levels): the next frontier's, and the list sizes
+        // of a bitmap turned into lists
+        const unsigned c = m & 1;
+        ctr[c ^ 1] = FrontierCounters{0, 0, 0, 0};
+        if (variant == kTdBits)
+        {
+          ctr[c].nsmall = 0;
+          ctr[c].packed = 0;
+        }
       }
     }
   }
@@ -552,12 +562,10 @@ static int bfs_body(la3g_graph* G, BfsScratch* bs, cudaStream_t s, unsigned m, d
   const uint32_t N = g.nslots, nrows = g.nrows();
   const unsigned variant = m / 2, c = m & 1;
   FrontierCounters* cur = bs->ctr + c;
-  FrontierCounters* next = bs->ctr + (c ^ 1);
-  LA3G_CUDA(cudaMemsetAsync(next, 0, sizeof(FrontierCounters), s));
+  FrontierCounters* next = bs->ctr + (c ^ 1);  // zeroed by the decide kernel, as are cur's list sizes for kTdBits
   if (variant == kTdBits)
   {
     // the bottom-up level's bitmap becomes split lists (sizes into ctr[c])
-    LA3G_CUDA(cudaMemsetAsync(&cur->nsmall, 0, 2 * sizeof(unsigned long long), s));
     k_bits_to_split<<<grid_for(bs->words, 256), 256, 0, s>>>(bs->bits[c], bs->words, g.in_ptr, bs->small[c],
                                                               bs->big[c], bs->big_task0[c], cur);
     LA3G_LAUNCHED();

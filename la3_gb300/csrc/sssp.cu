@@ -80,6 +80,7 @@ enum : int {
   kStNlist,         // the chosen step's frontier: vertices with regular out-edges
   kStPulls,         // pull steps run
   kStPushes,        // push steps run
+  kStFmin,          // the chosen step's frontier minimum (what the pull's settled test reads)
   kStSlots = 16
 };
 enum : unsigned { kPull = 0, kPush = 1, kDone = 2 };
@@ -134,9 +135,12 @@ __global__ void k_sssp_root(uint32_t root, uint32_t N, const uint32_t* __restric
 // counts the iteration and picks pull (frontier out-degree sum above the
 // regular rows' in-edges / divisor, after the first iteration, with weights
 // that keep INF + w in uint32) or push.
-__global__ void k_sssp_decide(unsigned long long* state, const unsigned long long* __restrict__ ctr, uint64_t reg_in,
-                              uint32_t max_w, double divisor, uint64_t limit, cudaGraphConditionalHandle cont,
-                              cudaGraphConditionalHandle mode)
+// It also clears the counters the step's kernels accumulate into (the dense
+// apply's, keeping the frontier minimum for the pull in the state; the push
+// split's), so that no memset node sits between the iterations.
+__global__ void k_sssp_decide(unsigned long long* state, unsigned long long* ctr, unsigned long long* fctr,
+                              uint64_t reg_in, uint32_t max_w, double divisor, uint64_t limit,
+                              cudaGraphConditionalHandle cont, cudaGraphConditionalHandle mode)
 {
   unsigned long long it = state[kStIter], nlist, deg;
   bool done = false;
@@ -172,6 +176,10 @@ __global__ void k_sssp_decide(unsigned long long* state, const unsigned long lon
   state[kStMode] = m;
   state[kStFrontDeg] = deg;
   state[kStNlist] = nlist;
+  state[kStFmin] = ctr[5];
+  ctr[0] = ctr[1] = ctr[2] = 0;
+  ctr[5] = ~0ull;  // the next frontier's minimum
+  fctr[0] = fctr[1] = 0;
   if (m == kPull)
   {
     state[kStExamined] += reg_in;
@@ -355,10 +363,10 @@ __global__ void __launch_bounds__(256)
 k_sssp_pull(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ w,
             uint32_t nreg, const uint32_t* __restrict__ task_row, const uint32_t* __restrict__ task_begin,
             uint32_t ntasks, uint32_t task_warps, uint32_t* ymin, const uint32_t* __restrict__ fmsg,
-            uint32_t* dist, const uint32_t* __restrict__ long_rows, const unsigned long long* __restrict__ ctr,
+            uint32_t* dist, const uint32_t* __restrict__ long_rows, const unsigned long long* __restrict__ fmin_ptr,
             uint32_t min_w)
 {
-  const unsigned long long fmin = ctr[5];  // the frontier's smallest message
+  const unsigned long long fmin = *fmin_ptr;  // the frontier's smallest message
   // Every candidate of this step is a frontier message plus a weight, so at
   // least fmin + min_w: a row already at or below that cannot be lowered and
   // its in-edges are not read (the result is the same).
@@ -609,7 +617,7 @@ static int sssp_body(la3g_graph* G, SsspScratch* ss, cudaStream_t s, unsigned k,
                    : 0;
     k_sssp_pull<<<num_sms() * 8, 256, 0, s>>>(g.in_ptr, g.in_col, g.in_w, g.nreg, ss->task_row, ss->task_begin,
                                               ss->ntasks, task_warps, ss->ymin, ss->fmsg, ss->dist, ss->long_rows,
-                                              ss->ctr, ss->min_w);
+                                              ss->state + kStFmin, ss->min_w);
     LA3G_LAUNCHED();
     if (ss->nlong)
     {
@@ -620,7 +628,6 @@ static int sssp_body(la3g_graph* G, SsspScratch* ss, cudaStream_t s, unsigned k,
   }
   else
   {
-    LA3G_CUDA(cudaMemsetAsync(ss->fctr, 0, 2 * sizeof(unsigned long long), s));
     k_sssp_split<<<grid_for(words, 256), 256, 0, s>>>(ss->fbits, words, g.out_ptr, ss->reg_end, ss->small[0],
                                                       ss->big[0], ss->big_task0[0], ss->fctr);
     LA3G_LAUNCHED();
@@ -630,8 +637,6 @@ static int sssp_body(la3g_graph* G, SsspScratch* ss, cudaStream_t s, unsigned k,
                                               ss->big_task0[0], ss->fctr, ss->msg, ss->dist);
     LA3G_LAUNCHED();
   }
-  LA3G_CUDA(cudaMemsetAsync(ss->ctr, 0, 3 * sizeof(unsigned long long), s));
-  LA3G_CUDA(cudaMemsetAsync(ss->ctr + 5, 0xFF, sizeof(unsigned long long), s));  // the next frontier's minimum
   k_sssp_dense_apply<<<grid_for((uint64_t) words * 32, 256, num_sms() * 4), 256, 0, s>>>(
       g.nreg, words, g.out_ptr, ss->reg_end, ss->dist, ss->msg, ss->fmsg, ss->fbits, ss->ctr);
   LA3G_LAUNCHED();
@@ -646,7 +651,8 @@ static uint64_t sssp_limit(const DevGraph& g) { return (uint64_t) g.nslots + 2; 
 static int sssp_decide(la3g_graph* G, SsspScratch* ss, cudaStream_t s, cudaGraphConditionalHandle cont,
                        cudaGraphConditionalHandle mode)
 {
-  k_sssp_decide<<<1, 1, 0, s>>>(ss->state, ss->ctr, ss->reg_in, ss->max_w, kPullDivisor, sssp_limit(G->g), cont, mode);
+  k_sssp_decide<<<1, 1, 0, s>>>(ss->state, ss->ctr, ss->fctr, ss->reg_in, ss->max_w, kPullDivisor, sssp_limit(G->g),
+                                cont, mode);
   LA3G_LAUNCHED();
   tls_launches++;
   return LA3G_OK;
