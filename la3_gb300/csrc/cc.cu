@@ -36,6 +36,8 @@ struct CcScratch
   int* flag = nullptr;
   unsigned long long* walked = nullptr;  // [0] rows, [1] edges k_cc_rest walked
   unsigned long long* hwalked = nullptr; // pinned mirror
+  uint32_t* giant = nullptr;   // the sampled giant component's root
+  int zero_has_edges = -1;     // whether vertex 0 has edges (-1: not looked up yet)
 };
 
 static void cc_scratch_free(void* p)
@@ -96,8 +98,10 @@ __global__ void k_cc_sample(const uint32_t* __restrict__ ptr, const uint32_t* __
 // the giant component is seen from its other endpoint.  One warp per row.
 __global__ void __launch_bounds__(256)
 k_cc_rest(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ col, const uint32_t* __restrict__ id_of_pos,
-          uint32_t nrows, uint32_t k, uint32_t giant, uint32_t* parent, unsigned long long* walked)
+          uint32_t nrows, uint32_t k, const uint32_t* __restrict__ giant_ptr, uint32_t* parent,
+          unsigned long long* walked)
 {
+  const uint32_t giant = *giant_ptr;
   const int lane = threadIdx.x & 31;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -130,6 +134,57 @@ __global__ void k_cc_probe(const uint32_t* __restrict__ id_of_pos, uint32_t nrow
     x ^= x >> 31;
     out[i] = cc_find(parent, id_of_pos[(uint32_t) (x % nrows)]);
   }
+}
+
+// The most frequent root among the samples (ties: the smallest), on the
+// device: one block sorts them in shared memory and counts runs.
+template <uint32_t NS>
+__global__ void __launch_bounds__(NS) k_cc_giant(const uint32_t* __restrict__ probe, uint32_t* giant)
+{
+  __shared__ uint32_t v[NS];
+  __shared__ uint32_t best_len, best_val;
+  const uint32_t t = threadIdx.x;
+  v[t] = probe[t];
+  if (t == 0)
+  {
+    best_len = 0;
+    best_val = 0xFFFFFFFFu;
+  }
+  __syncthreads();
+  for (uint32_t size = 2; size <= NS; size <<= 1)
+    for (uint32_t stride = size >> 1; stride > 0; stride >>= 1)
+    {
+      const uint32_t j = t ^ stride;
+      if (j > t)
+      {
+        const bool up = (t & size) == 0;
+        const uint32_t a = v[t], b = v[j];
+        if ((a > b) == up)
+        {
+          v[t] = b;
+          v[j] = a;
+        }
+      }
+      __syncthreads();
+    }
+  // run starts: thread t owns the run beginning at t
+  if (t == 0 || v[t] != v[t - 1])
+  {
+    uint32_t e = t + 1;
+    while (e < NS && v[e] == v[t]) e++;
+    const uint32_t len = e - t;
+    // longest run, the smallest root among equal lengths: pack (len, ~val) into one word
+    atomicMax(&best_len, len);
+  }
+  __syncthreads();
+  if ((t == 0 || v[t] != v[t - 1]))
+  {
+    uint32_t e = t + 1;
+    while (e < NS && v[e] == v[t]) e++;
+    if (e - t == best_len) atomicMin(&best_val, v[t]);
+  }
+  __syncthreads();
+  if (t == 0) *giant = best_val;
 }
 
 __global__ void k_cc_flatten(uint32_t N, uint32_t* parent)
@@ -223,10 +278,14 @@ extern "C" int la3g_cc(la3g_graph* G, uint32_t* label_out, la3g_stats* st)
   LA3G_TRY(cc_scratch(G, &cs));
   cudaStream_t s = G->stream;
   const uint32_t N = g.nslots, nrows = g.nrows();
-  uint32_t p0 = 0;
-  LA3G_CUDA(cudaMemcpyAsync(&p0, g.pos_of_id, 4, cudaMemcpyDeviceToHost, s));
-  LA3G_CUDA(cudaStreamSynchronize(s));
-  const bool zero_has_edges = p0 < nrows;
+  if (cs->zero_has_edges < 0)
+  {
+    uint32_t p0 = 0;  // a property of the graph: looked up once
+    LA3G_CUDA(cudaMemcpyAsync(&p0, g.pos_of_id, 4, cudaMemcpyDeviceToHost, s));
+    LA3G_CUDA(cudaStreamSynchronize(s));
+    cs->zero_has_edges = p0 < nrows ? 1 : 0;
+  }
+  const bool zero_has_edges = cs->zero_has_edges == 1;
   uint32_t iters = 0;
   bool rest_counted = false;
   T.device_begin();
@@ -254,16 +313,10 @@ extern "C" int la3g_cc(la3g_graph* G, uint32_t* label_out, la3g_stats* st)
     k_cc_probe<<<4, 256, 0, s>>>(g.id_of_pos, nrows, nsamples, 0x5A3Dull, cs->label, cs->probe);
     LA3G_LAUNCHED();
     tls_launches++;
-    std::vector<uint32_t> h(nsamples);
-    LA3G_CUDA(cudaMemcpyAsync(h.data(), cs->probe, nsamples * 4, cudaMemcpyDeviceToHost, s));
-    LA3G_CUDA(cudaStreamSynchronize(s));
-    std::sort(h.begin(), h.end());
-    uint32_t giant = h[0], best = 0;
-    for (uint32_t i = 0, j; i < nsamples; i = j)
-    {
-      for (j = i; j < nsamples && h[j] == h[i]; j++) {}
-      if (j - i > best) { best = j - i; giant = h[i]; }
-    }
+    if (!cs->giant) LA3G_TRY(galloc(G, &cs->giant, 1));
+    k_cc_giant<1024><<<1, 1024, 0, s>>>(cs->probe, cs->giant);
+    LA3G_LAUNCHED();
+    tls_launches++;
     LA3G_CUDA(cudaMemsetAsync(cs->walked, 0, 16, s));
     {
       // every row: its offsets, id and root (16 B); the walked rows' edges:
@@ -271,7 +324,7 @@ extern "C" int la3g_cc(la3g_graph* G, uint32_t* label_out, la3g_stats* st)
       // counts are back on the host
       ProfileScope p("cc_rest", s, 16.0 * nrows);
       k_cc_rest<<<grid_for((uint64_t) nrows * 32, 256, num_sms() * 32), 256, 0, s>>>(g.in_ptr, g.in_col, g.id_of_pos, nrows,
-                                                                               k, giant, cs->label, cs->walked);
+                                                                               k, cs->giant, cs->label, cs->walked);
       LA3G_LAUNCHED();
     }
     LA3G_CUDA(cudaMemcpyAsync(cs->hwalked, cs->walked, 16, cudaMemcpyDeviceToHost, s));
