@@ -709,8 +709,8 @@ __device__ __forceinline__ bool top_before(const Cmp& cmp, const TopItem<I, V>& 
 }
 
 // Sorts kTopkTile items in shared memory (bitonic) and writes the first k
-// of each tile.  Round 0 maps the vertices of the tile's positions (all, or
-// the active ones); later rounds read the previous round's items.  With
+// of each tile.  The first pass maps the vertices of the tile's positions (all, or
+// the active ones); later passes read the previous pass's items.  With
 // batches, blockIdx.y is the batch b and map(id, state) returns an indexable
 // array of values.
 template <class P, class I, class V, class Map, class Cmp, bool BATCH>
@@ -1196,7 +1196,7 @@ class Engine
       cudaFree(bufs[0]);
       return fail(LA3G_ENOMEM, "topk");
     }
-    // round 0 maps the vertices; each round keeps k items per tile
+    // the first pass maps the vertices; every pass keeps k items per tile
     detail::k_topk_round<P, I, V, Map, Cmp, BATCH><<<dim3(tiles, nb), T / 2, 0, s_>>>(
         map, cmp, k, n, (const State*) S_, dv_.id_of_pos, (const uint8_t*) vact_, active_only, nullptr, (Item*) bufs[0]);
     ck(cudaGetLastError());
