@@ -60,6 +60,7 @@ struct PrScratch
   uint32_t* tcol = nullptr;      // [ncols] column positions, ascending within a tile
   uint32_t* tptr = nullptr;      // [ncols + 1] first entry of each non-empty column
   uint16_t* trow = nullptr;      // [nent] row of each entry, local to its tile
+  uint32_t* tecol = nullptr;     // [nent] column of each entry (the hypersparse tiles' form)
   int tile_blocks = 0;           // resident blocks per SM of the tiled kernel
 };
 
@@ -439,6 +440,7 @@ static constexpr uint32_t kTileRows = 2048;    // rows per tile: 8 KB of FP32 ac
 static constexpr uint32_t kTileThreads = 512;
 static constexpr uint32_t kTileBig = 32;       // columns with more entries in a tile go to a warp
 static constexpr uint32_t kTileBigCap = 1024;  // such columns queued per tile (the rest run serially)
+static constexpr uint32_t kTileDense = 2;      // entries per non-empty column at which a tile walks its DCSC columns
 
 __global__ void k_tile_colof(const uint32_t* __restrict__ ptr, uint32_t ncol, uint32_t* colof)
 {
@@ -470,13 +472,14 @@ __global__ void k_tile_keys(const uint32_t* __restrict__ row, uint64_t m, uint32
 // Entries in (tile, column, row) order: local rows, and a flag where a new
 // (tile, column) pair starts.
 __global__ void k_tile_flags(const uint32_t* __restrict__ order, uint64_t n, const uint32_t* __restrict__ colof,
-                             const uint32_t* __restrict__ row, uint16_t* trow, uint32_t* flag)
+                             const uint32_t* __restrict__ row, uint16_t* trow, uint32_t* tecol, uint32_t* flag)
 {
   for (uint64_t e = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; e < n; e += (uint64_t) gridDim.x * blockDim.x)
   {
     const uint32_t i = order[e];
     const uint32_t r = row[i], t = r / kTileRows;
     trow[e] = (uint16_t) (r - t * kTileRows);
+    tecol[e] = colof[i];
     bool start = e == 0;
     if (!start)
     {
@@ -541,11 +544,12 @@ static int pr_build_tiles(la3g_graph* G, PrScratch* ps)
   LA3G_TRY(flag.alloc(n * 4 + 4));
   LA3G_TRY(slot.alloc(n * 4 + 4));
   LA3G_TRY(galloc(G, &ps->trow, n + 8));
+  LA3G_TRY(galloc(G, &ps->tecol, n + 8));
   uint32_t ncols = 0;
   if (n)
   {
     k_tile_flags<<<grid_for(n, 256), 256, 0, s>>>(idx2.as<uint32_t>(), n, colof.as<uint32_t>(), g.out_row, ps->trow,
-                                                  flag.as<uint32_t>());
+                                                  ps->tecol, flag.as<uint32_t>());
     LA3G_LAUNCHED();
     size_t tb = 0;
     LA3G_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tb, flag.as<uint32_t>(), slot.as<uint32_t>(), (int64_t) n, s));
@@ -586,7 +590,8 @@ static int pr_build_tiles(la3g_graph* G, PrScratch* ps)
 
 __global__ void __launch_bounds__(kTileThreads)
 k_prf_tiles(const uint32_t* __restrict__ tile_col, const uint32_t* __restrict__ tcol,
-            const uint32_t* __restrict__ tptr, const uint16_t* __restrict__ trow, uint32_t ntiles, uint32_t nreg,
+            const uint32_t* __restrict__ tptr, const uint16_t* __restrict__ trow,
+            const uint32_t* __restrict__ tecol, uint32_t ntiles, uint32_t nreg,
             const uint32_t* __restrict__ in_ptr, const uint32_t* __restrict__ in_col,
             const uint32_t* __restrict__ long_rows, uint32_t nlong, uint32_t long_blocks,
             const float* __restrict__ x, float* __restrict__ xnext, float* __restrict__ rankf,
@@ -626,8 +631,28 @@ k_prf_tiles(const uint32_t* __restrict__ tile_col, const uint32_t* __restrict__ 
     if (tid == 0) s_nbig = 0;
     __syncthreads();
     const uint32_t k0 = tile_col[t], k1 = tile_col[t + 1];
+    const uint32_t e0 = tptr[k0], e1 = tptr[k1];
+    // hypersparse tile (fewer than kTileDense entries per non-empty column):
+    // a thread per entry, its column from the per-entry form, four entries in
+    // flight; denser tiles walk their DCSC columns, each message read once
+    const bool by_entry = (uint64_t) (e1 - e0) < (uint64_t) kTileDense * (k1 - k0);
+    for (uint32_t eb = e0; by_entry && eb < e1; eb += 4 * kTileThreads)
+    {
+      float xv[4];
+      uint32_t rr[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+      {
+        const uint32_t e = eb + u * kTileThreads + tid;
+        rr[u] = e < e1 ? trow[e] : 0xFFFFFFFFu;
+        xv[u] = e < e1 ? x[tecol[e]] : 0.0f;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+        if (rr[u] != 0xFFFFFFFFu) atomicAdd(&ys[rr[u]], xv[u]);
+    }
     // a thread per column, four columns' messages in flight
-    for (uint32_t kb = k0; kb < k1; kb += 4 * kTileThreads)
+    for (uint32_t kb = k0; !by_entry && kb < k1; kb += 4 * kTileThreads)
     {
       uint32_t b[4], e[4];
       float xv[4];
@@ -816,7 +841,8 @@ static int pr_f32_run(la3g_graph* G, uint32_t iters, double tol, double* rank_ou
       const uint32_t lblocks = ps->nlong ? std::min<uint32_t>(ps->nlong, num_sms()) : 0;
       const unsigned tgrid = std::min<unsigned>(std::max<uint32_t>(ps->ntiles, 1), num_sms() * std::max(ps->tile_blocks, 1));
       k_prf_tiles<<<lblocks + tgrid, kTileThreads, kTileRows * 4, s>>>(
-          ps->tile_col, ps->tcol, ps->tptr, ps->trow, ps->ntiles, g.nreg, g.in_ptr, g.in_col, ps->long_rows, ps->nlong,
+          ps->tile_col, ps->tcol, ps->tptr, ps->trow, ps->tecol, ps->ntiles, g.nreg, g.in_ptr, g.in_col, ps->long_rows,
+          ps->nlong,
           lblocks, ps->xf[cur], ps->xf[cur ^ 1], ps->rankf, ps->rank, ps->deg, ps->resid);
       LA3G_LAUNCHED();
     }
