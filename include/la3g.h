@@ -185,9 +185,10 @@ int la3g_pr_f32(la3g_graph* g, uint32_t iters, double tol, double* rank_out, dou
  * tiles of 2048 rows, each tile doubly compressed by column as the
  * reference's per-tile DCSC (src/utils/csc.h:60-130, tiles of
  * src/matrix/matrix2d.hpp:6-25): non-empty columns with offsets and a 16-bit
- * row per entry; the tile's row accumulators live in shared memory; rows
+ * row per entry (hypersparse tiles also keep each entry's column and are
+ * walked by entry); the tile's row accumulators live in shared memory; rows
  * with more than 1024 in-edges are summed from the flat CSR, a block each.  Built on the device
- * on the first call (about 10 B per entry).  Results agree with
+ * on the first call (about 14 B per entry).  Results agree with
  * la3g_pr_f32 to FP32 rounding (addition order inside a row differs). */
 int la3g_pr_f32_tiled(la3g_graph* g, uint32_t iters, double tol, double* rank_out, double* residual_out,
                       la3g_stats* st);
