@@ -505,9 +505,12 @@ static __global__ void k_mark(const uint32_t* __restrict__ optr, const uint32_t*
 }
 
 // Rows of a list, G lanes each; every lane walks the same number of edge
-// steps (the warp's longest row), so the shuffles see all 32 lanes.
+// steps (the warp's longest row), so the shuffles see all 32 lanes.  At
+// least two blocks per SM: wide accumulators (graph simulation's 32
+// counters, held three times in the tree) would otherwise take ~150
+// registers and leave one block per SM (R-MAT s20: 8.1 -> 7.4 ms).
 template <class P, int G>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 2)
 k_pull_rows(P prog, View g, const uint32_t* __restrict__ rows, const unsigned long long* __restrict__ count, Step<P> st)
 {
   using Acc = typename P::Acc;
