@@ -57,7 +57,7 @@ static constexpr uint32_t kTcMidCap = 512;        // |N+(y)| up to this: a small
 static constexpr uint32_t kTcMidSlots = 2048;     // hash slots of its table (>= 4 kTcMidCap)
 static constexpr uint32_t kTcBlockCap = 2048;     // |N+(y)| up to this: a large block table; longer: global search
 static constexpr uint32_t kTcBlockSlots = 8192;   // hash slots of a large block table (>= 4 kTcBlockCap)
-static constexpr uint32_t kTcBlockPairs = 4096;   // pairs per block task (both block sizes)
+static constexpr uint32_t kTcBlockPairs = 1024;   // pairs per block task (both block sizes; R-MAT s20 call: 4096 4.96 ms, 2048 4.83, 1024 4.73, 512 4.74, 256 5.01)
 static constexpr int kTcWarpKernelWarps = 8;
 static constexpr int kTcMidThreads = 256;
 static constexpr int kTcBlockThreads = 512;
