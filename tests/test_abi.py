@@ -117,7 +117,12 @@ def test_drivers_and_programs_are_built(native):
     assert r.returncode == 1 and "Usage" in r.stdout
     out = subprocess.run(["nm", "-D", "--defined-only", str(B.PROGRAMS_LIB)], capture_output=True, text=True,
                          check=True).stdout
-    for s in ("la3gp_degree", "la3gp_pagerank", "la3gp_bfs", "la3gp_sssp", "la3gp_cc", "la3gp_graphsim"):
+    # every entry point include/la3g_programs.h declares
+    hdr = (B.INCLUDE / "la3g_programs.h").read_text()
+    declared = re.findall(r"^int (la3gp_\w+)\(", hdr, flags=re.M)
+    assert {"la3gp_degree", "la3gp_pagerank", "la3gp_bfs", "la3gp_sssp", "la3gp_cc", "la3gp_graphsim", "la3gp_tc",
+            "la3gp_degree_topk", "la3gp_bfs_topk"} <= set(declared)
+    for s in declared:
         assert re.search(r"\bT " + s + r"\b", out), s
 
 
@@ -138,3 +143,12 @@ def test_new_entry_points_reject_bad_arguments(native):
     progs.la3gp_graphsim.argtypes = [C.c_void_p] + [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint32,
                                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     assert progs.la3gp_graphsim(None, None, 4, None, None, 0, None, None, None, None) == 1
+    # the engine-program entry points refuse a null graph before any device work
+    assert progs.la3gp_tc(None, None, None, None) == 1
+    progs.la3gp_degree_topk.argtypes = [C.c_void_p, C.c_uint32] + [C.c_void_p] * 5
+    assert progs.la3gp_degree_topk(None, 3, None, None, None, None, None) == 1
+    progs.la3gp_bfs_topk.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p]
+    assert progs.la3gp_bfs_topk(None, 1, 3, None, None) == 1
+    # the tiled PageRank and the push view refuse a null graph
+    assert L.la3g_pr_f32_tiled(None, 5, 0.0, None, None, None) == 1
+    assert L.la3g_graph_push_view(None, None, None) == 1
