@@ -546,8 +546,9 @@ def systems_results(args, GU, GW, stream, dev) -> dict:
     """The systems forms on their configurations, for the default line:
     batched BFS/SSSP (64/256/1024 roots) on the plain step's R-MAT graphs and
     on ER 2^22, PageRank (FP64 s16 with oracle parity, FP32 vs FP64 on
-    R-MAT and ER 2^24), and the served stream at 1k/s offered and at
-    saturation (20k/s offered).  Each part carries its own clock record;
+    R-MAT and ER 2^24), the served stream at 1k/s offered and at
+    saturation (20k/s offered), and the generic engine (graph simulation and
+    TC on the TC graph's size).  Each part carries its own clock record;
     a part that fails reports its error instead."""
     import torch
     out = {}
@@ -566,7 +567,8 @@ def systems_results(args, GU, GW, stream, dev) -> dict:
 
     parts = (("batched", batched),
              ("pagerank", lambda: pagerank_measure(args, stream, dev)),
-             ("served", lambda: serve_measure(args, [1000.0, 20000.0], 1.0)))
+             ("served", lambda: serve_measure(args, [1000.0, 20000.0], 1.0)),
+             ("engine", lambda: engine_measure(args, stream)))
     for name, fn in parts:
         t0 = time.time()
         try:
@@ -580,6 +582,69 @@ def systems_results(args, GU, GW, stream, dev) -> dict:
         out[name] = r
         torch.cuda.synchronize()
     return out
+
+
+def engine_measure(args, stream) -> dict:
+    """The generic vertex-program engine (include/la3g_vp.cuh) on the plain
+    bench's TC graph size: graph simulation (graphsim.cpp:45-90; a 5-vertex
+    query with a cycle, 6 labels, the data graph reversed) and TC written as
+    the reference writes it (tc.cpp:11-52; neighbour lists as variable-size
+    messages), each call timed on the host clock (median of three), results
+    checked: TC's total against la3g_tc."""
+    import ctypes as C
+    import numpy as np
+    import la3_gb300 as L
+    import la3_gb300.build as B
+    progs = C.CDLL(str(B.PROGRAMS_LIB))
+    u32p = C.POINTER(C.c_uint32)
+    progs.la3gp_graphsim.argtypes = [C.c_void_p, u32p, C.c_uint32, u32p, u32p, C.c_uint32, C.POINTER(C.c_uint8),
+                                     C.c_char_p, u32p, u32p]
+    progs.la3gp_tc.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint64), u32p]
+    sc = args.tc_scale
+    rng = np.random.default_rng(501)
+    gr = L.Graph.from_edges(L.EdgeList.rmat(sc, 16, seed=GRAPH_SEED + 7), L.DIRECTED | L.REVERSE)
+    gr.set_stream(stream.cuda_stream)
+    vlab = np.zeros(gr.nslots, np.uint32)
+    vlab[: 1 << sc] = rng.integers(1, 7, 1 << sc)
+    qlab = np.array([1, 2, 3, 2, 4], np.uint32)
+    qedges = np.array([[0, 1], [1, 2], [2, 3], [3, 1], [1, 4]], np.uint32).reshape(-1)
+    matched = np.empty(gr.nslots, np.uint8)
+
+    def gs():
+        nm, it = C.c_uint32(), C.c_uint32()
+        t0 = time.perf_counter()
+        L.N.check(progs.la3gp_graphsim(gr._h, vlab.ctypes.data_as(u32p), qlab.size, qlab.ctypes.data_as(u32p),
+                                       qedges.ctypes.data_as(u32p), qedges.size // 2,
+                                       matched.ctypes.data_as(C.POINTER(C.c_uint8)), None, C.byref(nm), C.byref(it)))
+        return time.perf_counter() - t0, nm.value, it.value
+
+    gs()
+    g_runs = [gs() for _ in range(3)]
+    gr.free()
+    et = L.EdgeList.rmat(sc, 16, seed=TC_SEED)
+    gt = L.Graph.from_edges(et, L.DIRECTED | L.ACYCLIC)
+    gtr = L.Graph.from_edges(et, L.DIRECTED | L.ACYCLIC | L.REVERSE)
+    del et
+    gt.set_stream(stream.cuda_stream)
+    gtr.set_stream(stream.cuda_stream)
+
+    def tce():
+        tot = C.c_uint64()
+        t0 = time.perf_counter()
+        L.N.check(progs.la3gp_tc(gt._h, gtr._h, C.byref(tot), None))
+        return time.perf_counter() - t0, tot.value
+
+    tce()
+    t_runs = [tce() for _ in range(3)]
+    lib_total = L.tc(gt, False)[0]
+    gt.free()
+    gtr.free()
+    return {"graph": f"R-MAT s{sc} (edge factor 16)",
+            "graphsim": {"ms": statistics.median(r[0] for r in g_runs) * 1e3, "matches": g_runs[-1][1],
+                         "iterations": g_runs[-1][2], "query": "5 vertices, a cycle, 6 labels"},
+            "tc_through_engine": {"ms": statistics.median(r[0] for r in t_runs) * 1e3, "triangles": t_runs[-1][1],
+                                  "equals_la3g_tc": t_runs[-1][1] == lib_total},
+            "timing": "host clock around each call (engine set-up and result copy included), median of 3"}
 
 
 # ---------------------------------------------------------------- other workloads
