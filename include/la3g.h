@@ -294,6 +294,14 @@ int la3g_batch_config(la3g_graph* g, int mode, int block, double push_frac);
  * once, which exercises that error path. */
 int la3g_batch_set_wait_limit(la3g_graph* g, long long polls);
 
+/* The batched SSSP's distance window: an iteration relaxes only the roots
+ * whose distance is at most (smallest distance in the frontier) + delta and
+ * keeps the others active for a later iteration (delta-stepping's buckets,
+ * one window over all roots of a 256-root chunk).  delta = 0 picks the width
+ * from the graph's largest weight; 0xFFFFFFFF relaxes every active root each
+ * iteration.  The distances are the same for every delta. */
+int la3g_batch_sssp_window(la3g_graph* g, uint32_t delta);
+
 /* ---- serving loop (no reference counterpart; the reference answers one
  *      query per VertexProgram run, bfs.cpp:11-37, sssp.cpp:11-37,
  *      bm25.cpp:8-114) ------------------------------------------------------ */

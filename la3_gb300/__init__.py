@@ -503,6 +503,12 @@ def batch_set_wait_limit(G: Graph, polls: int = -1) -> None:
     N.check(N.lib().la3g_batch_set_wait_limit(G._h, polls))
 
 
+def batch_sssp_window(G: Graph, delta: int = 0) -> None:
+    """Distance window of the batched SSSP (0: from the largest weight;
+    0xFFFFFFFF: none).  Results do not depend on it."""
+    N.check(N.lib().la3g_batch_sssp_window(G._h, delta))
+
+
 def sssp_batch(G: Graph, roots: Sequence[int], want_dist: bool = True):
     r = np.ascontiguousarray(np.asarray(roots, dtype=np.uint32))
     st = Stats()
@@ -591,5 +597,5 @@ def profile_report() -> dict:
 
 
 __all__ = ["Graph", "EdgeList", "BM25", "LA3GError", "Stats", "pagerank", "pagerank_f32", "bfs", "sssp", "cc", "tc",
-           "LM", "degree", "topk_u32", "read_graphsim_labels", "read_graphsim_query", "graphsim_label_ids", "bfs_batch", "sssp_batch", "batch_autotune", "batch_config", "read_queries", "profile", "profile_reset", "profile_report", "DIRECTED", "REVERSE", "ACYCLIC",
+           "LM", "degree", "topk_u32", "read_graphsim_labels", "read_graphsim_query", "graphsim_label_ids", "bfs_batch", "sssp_batch", "batch_autotune", "batch_config", "batch_set_wait_limit", "batch_sssp_window", "read_queries", "profile", "profile_reset", "profile_report", "DIRECTED", "REVERSE", "ACYCLIC",
            "BIPARTITE", "WEIGHTED", "SSSP_INF", "BFS_INF"]

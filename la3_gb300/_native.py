@@ -159,6 +159,7 @@ SIGNATURES = {
     "la3g_batch_autotune": (C.c_int, [_P, _u32p, C.c_uint32, C.c_char_p, C.c_size_t]),
     "la3g_batch_config": (C.c_int, [_P, C.c_int, C.c_int, C.c_double]),
     "la3g_batch_set_wait_limit": (C.c_int, [_P, C.c_longlong]),
+    "la3g_batch_sssp_window": (C.c_int, [_P, C.c_uint32]),
     "la3g_gen_rmat": (C.c_int, [C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double, C.c_uint64, C.c_int,
                                 C.c_uint64, C.POINTER(Edges)]),
     "la3g_gen_er": (C.c_int, [C.c_uint32, C.c_uint64, C.c_uint64, C.c_int, C.c_uint64, C.POINTER(Edges)]),

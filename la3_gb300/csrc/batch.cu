@@ -83,7 +83,9 @@ struct BatchScratch
   uint32_t* shub_t0[2] = {nullptr, nullptr}; // their first task numbers
   uint32_t* reg_end = nullptr;
   uint32_t max_w = 0;
+  uint32_t max_reg_deg = 0;    // most regular out-edges of one vertex
   bool max_w_known = false;
+  uint32_t sssp_delta = 0;     // distance window width; 0 = automatic, kNoWindow = none
 };
 
 static void batch_scratch_free(void* p)
@@ -662,6 +664,27 @@ extern "C" int la3g_bfs_batch(la3g_graph* G, const uint32_t* roots, uint32_t nro
 
 static constexpr uint32_t kSsspChunk = 256;  // roots per device pass (bounds the [N][R] state)
 
+// Default window width of the batched SSSP.  The window pays where degrees
+// are even (ER 2^22 x16, weights 1-128, 256 roots: 248 ms with a window of
+// 128 against 272 ms without; 64 and 256 give 257 / 282 ms) and costs where
+// hubs already make the frontier converge in few iterations (R-MAT s22: 88
+// against 75 ms), so it is on only when no vertex is a hub (more than kBigDeg
+// regular out-edges), with the largest weight as its width.
+static uint32_t sssp_auto_delta(uint32_t max_w, uint32_t max_reg_deg)
+{
+  return max_reg_deg <= kBigDeg ? std::max(max_w, 1u) : kNoWindow;
+}
+
+__global__ void k_max_reg_deg(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ reg_end, uint32_t N,
+                              unsigned int* out)
+{
+  unsigned int m = 0;
+  for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < N; u += gridDim.x * blockDim.x)
+    m = max(m, reg_end[u] - ptr[u]);
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
 static int sssp_batch_chunk(la3g_graph* G, BatchScratch* b, const uint32_t* roots, uint32_t R, uint32_t* dist_out,
                             uint32_t* iters_out);
 
@@ -702,19 +725,24 @@ static int sssp_batch_chunk(la3g_graph* G, BatchScratch* b, const uint32_t* root
   if (!b->max_w_known)
   {
     DevBuf m;
-    LA3G_TRY(m.alloc(4));
-    LA3G_CUDA(cudaMemsetAsync(m.p, 0, 4, s));
+    LA3G_TRY(m.alloc(8));
+    LA3G_CUDA(cudaMemsetAsync(m.p, 0, 8, s));
     if (g.nent)
     {
       k_max_u32<<<grid_for(g.nent, 256), 256, 0, s>>>(g.out_w, g.nent, m.as<unsigned int>());
       LA3G_LAUNCHED();
     }
-    LA3G_CUDA(cudaMemcpyAsync(&b->max_w, m.p, 4, cudaMemcpyDeviceToHost, s));
-    LA3G_CUDA(cudaStreamSynchronize(s));
-    b->max_w_known = true;
     LA3G_TRY(galloc(G, &b->reg_end, N));
     k_reg_end<<<grid_for(N, 256), 256, 0, s>>>(g.out_ptr, g.out_row, N, g.nreg, b->reg_end);
     LA3G_LAUNCHED();
+    k_max_reg_deg<<<grid_for(N, 256), 256, 0, s>>>(g.out_ptr, b->reg_end, N, m.as<unsigned int>() + 1);
+    LA3G_LAUNCHED();
+    uint32_t hm[2] = {0, 0};
+    LA3G_CUDA(cudaMemcpyAsync(hm, m.p, 8, cudaMemcpyDeviceToHost, s));
+    LA3G_CUDA(cudaStreamSynchronize(s));
+    b->max_w = hm[0];
+    b->max_reg_deg = hm[1];
+    b->max_w_known = true;
   }
   // Exact regardless of relaxation order only if no distance can reach INF.
   if ((uint64_t) b->max_w * (uint64_t) N >= (uint64_t) kInfD)
@@ -749,6 +777,12 @@ static int sssp_batch_chunk(la3g_graph* G, BatchScratch* b, const uint32_t* root
   tls_launches += 3;
   int cur = 0;
   uint32_t iters = 0;
+  // the distance window: roots at distance <= limit relax, the rest wait;
+  // after each iteration limit = (smallest distance left in the frontier) +
+  // delta, which ctr[6] collects (atomicMin over the relax kernel's warps)
+  const uint32_t delta = b->sssp_delta ? b->sssp_delta : sssp_auto_delta(b->max_w, b->max_reg_deg);
+  uint32_t limit = delta;
+  unsigned int* pend = (unsigned int*) (b->ctr + 6);
   // two alternating pair lists; ctr[c] / ctr[2 + c] count list c's small
   // pairs and its packed hub slots / tasks
   PairList L[2];
@@ -761,10 +795,12 @@ static int sssp_batch_chunk(la3g_graph* G, BatchScratch* b, const uint32_t* root
   {
     if (iters > 1000000) return set_error(LA3G_ETIMEOUT, "batched sssp did not converge");
     iters++;
+    if (delta != kNoWindow) LA3G_CUDA(cudaMemsetAsync(pend, 0xFF, 4, s));
     {
       ProfileScope p("sssp_batch_relax", s, 0.0);
       k_bs_relax<<<num_sms() * 16, 256, 0, s>>>(g.out_ptr, b->reg_end, g.out_row, g.out_w, R, W, b->sfront[cur], L[cur],
-                                           b->sfront[cur ^ 1], b->sdist);
+                                           b->sfront[cur ^ 1], b->sdist, delta == kNoWindow ? kNoWindow : limit,
+                                           delta == kNoWindow ? nullptr : pend);
       LA3G_LAUNCHED();
     }
     LA3G_CUDA(cudaMemsetAsync(b->ctr + (cur ^ 1), 0, 8, s));
@@ -773,11 +809,17 @@ static int sssp_batch_chunk(la3g_graph* G, BatchScratch* b, const uint32_t* root
                                         L[cur]);
     LA3G_LAUNCHED();
     tls_launches += 2;
-    unsigned long long act[4] = {0, 0, 0, 0};
-    LA3G_CUDA(cudaMemcpyAsync(act, b->ctr, 4 * 8, cudaMemcpyDeviceToHost, s));
+    unsigned long long act[7] = {0, 0, 0, 0, 0, 0, 0};
+    LA3G_CUDA(cudaMemcpyAsync(act, b->ctr, 7 * 8, cudaMemcpyDeviceToHost, s));
     LA3G_CUDA(cudaStreamSynchronize(s));
     cur ^= 1;
     if (!act[cur] && !act[2 + cur]) break;
+    if (delta != kNoWindow)
+    {
+      uint32_t lo;
+      std::memcpy(&lo, &act[6], 4);
+      limit = lo > kNoWindow - 1 - delta ? kNoWindow - 1 : lo + delta;
+    }
   }
   if (g.nsink)
   {
@@ -868,6 +910,15 @@ extern "C" int la3g_batch_set_wait_limit(la3g_graph* G, long long polls)
   BatchScratch* b = nullptr;
   LA3G_TRY(batch_scratch(G, &b));
   b->wait_polls = polls < 0 ? kDefaultWaitPolls : polls;
+  return LA3G_OK;
+}
+
+extern "C" int la3g_batch_sssp_window(la3g_graph* G, uint32_t delta)
+{
+  if (!G) return set_error(LA3G_EINVAL, "null graph");
+  BatchScratch* b = nullptr;
+  LA3G_TRY(batch_scratch(G, &b));
+  b->sssp_delta = delta;
   return LA3G_OK;
 }
 

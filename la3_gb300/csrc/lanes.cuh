@@ -14,6 +14,7 @@
 namespace la3g {
 
 static constexpr uint32_t kInfD = 0x7FFFFFFFu;
+static constexpr uint32_t kNoWindow = 0xFFFFFFFFu;  // relax every active root
 
 // Active (vertex, word) pairs of the batched SSSP are kept as a split
 // frontier: pairs whose vertex has at most kBigDeg regular out-edges are
@@ -64,7 +65,8 @@ static __device__ __forceinline__ int nth_set_bit(uint64_t f, int s)
 // lowered root ORs its own bit into the target's next word.
 static __device__ __forceinline__ void bs_relax_sparse(uint32_t k0, uint32_t k1, int lane, uint32_t R, uint32_t W,
                                                 const uint32_t* __restrict__ row, const uint32_t* __restrict__ wgt,
-                                                uint32_t u, uint32_t w, uint64_t f, int k, uint64_t* next, uint32_t* dist)
+                                                uint32_t u, uint32_t w, uint64_t f, int k, uint64_t* next, uint32_t* dist,
+                                                uint32_t& lmin)
 {
   const int S = k <= 1 ? 1 : 1 << (32 - __clz(k - 1));
   const uint32_t E = 32 / S;
@@ -97,6 +99,7 @@ static __device__ __forceinline__ void bs_relax_sparse(uint32_t k0, uint32_t k1,
       {
         atomicMin(&dist[(uint64_t) v[q] * R + r], c);
         atomicOr((unsigned long long*) &next[(uint64_t) v[q] * W + w], bit);
+        lmin = min(lmin, c);
       }
     }
   }
@@ -109,7 +112,8 @@ static __device__ __forceinline__ void bs_relax_sparse(uint32_t k0, uint32_t k1,
 // broadcast) so that up to 16 target reads per lane are in flight.
 static __device__ __forceinline__ void bs_relax_dense(uint32_t k0, uint32_t k1, int lane, uint32_t R, uint32_t W,
                                                const uint32_t* __restrict__ row, const uint32_t* __restrict__ wgt,
-                                               uint32_t u, uint32_t w, uint64_t f, uint64_t* next, uint32_t* dist)
+                                               uint32_t u, uint32_t w, uint64_t f, uint64_t* next, uint32_t* dist,
+                                               uint32_t& lmin)
 {
   constexpr int G = 8;
   const uint32_t r0 = w * 64 + lane, r1 = r0 + 32;
@@ -143,8 +147,16 @@ static __device__ __forceinline__ void bs_relax_dense(uint32_t k0, uint32_t k1, 
       if ((uint32_t) j >= cnt) break;
       const uint32_t wt = __shfl_sync(0xffffffffu, lw, j), c0 = m0 + wt, c1 = m1 + wt;
       const bool i0 = h0 && c0 < d0[j], i1 = h1 && c1 < d1[j];
-      if (i0) atomicMin(&dist[(uint64_t) v[j] * R + r0], c0);
-      if (i1) atomicMin(&dist[(uint64_t) v[j] * R + r1], c1);
+      if (i0)
+      {
+        atomicMin(&dist[(uint64_t) v[j] * R + r0], c0);
+        lmin = min(lmin, c0);
+      }
+      if (i1)
+      {
+        atomicMin(&dist[(uint64_t) v[j] * R + r1], c1);
+        lmin = min(lmin, c1);
+      }
       const uint64_t mask = (uint64_t) __ballot_sync(0xffffffffu, i0) | ((uint64_t) __ballot_sync(0xffffffffu, i1) << 32);
       if (lane == j) mine = mask;
     }
@@ -162,21 +174,46 @@ static __device__ __forceinline__ void bs_relax_dense(uint32_t k0, uint32_t k1, 
 // started with and the bit means "lowered in this iteration", exactly as an
 // atomic's returned old value would; the minimum itself is therefore a
 // reduction whose result nobody waits for.
+//
+// With a window (limit != kNoWindow) only roots whose distance at u is at most
+// limit relax; the others keep their bit, carried into the next frontier, as
+// delta-stepping keeps a vertex in a later bucket.  lmin collects the smallest
+// distance the next frontier will hold (carried distances and lowered
+// candidates), from which the host sets the next window.  Every active bit is
+// either relaxed or carried, so the shortest distances are the same.
 static __device__ __forceinline__ void bs_relax_range(uint32_t i, uint32_t k0, uint32_t k1, int lane, uint32_t R, uint32_t W,
                                                const uint32_t* __restrict__ row, const uint32_t* __restrict__ wgt,
-                                               const uint64_t* __restrict__ front, uint64_t* next, uint32_t* dist)
+                                               const uint64_t* __restrict__ front, uint64_t* next, uint32_t* dist,
+                                               uint32_t limit, uint32_t& lmin)
 {
   const uint32_t u = i / W, w = i % W;
-  const uint64_t f = front[i];
+  uint64_t f = front[i];
+  if (limit != kNoWindow)
+  {
+    const uint32_t r0 = w * 64 + lane;
+    const bool h0 = (f >> lane) & 1ull, h1 = (f >> (lane + 32)) & 1ull;
+    const uint32_t m0 = h0 ? __ldcg(&dist[(uint64_t) u * R + r0]) : 0u;
+    const uint32_t m1 = h1 ? __ldcg(&dist[(uint64_t) u * R + r0 + 32]) : 0u;
+    const bool far0 = h0 && m0 > limit, far1 = h1 && m1 > limit;
+    const uint64_t far = (uint64_t) __ballot_sync(0xffffffffu, far0) | ((uint64_t) __ballot_sync(0xffffffffu, far1) << 32);
+    if (far)
+    {
+      if (far0) lmin = min(lmin, m0);
+      if (far1) lmin = min(lmin, m1);
+      if (lane == 0) atomicOr((unsigned long long*) &next[i], (unsigned long long) far);
+      f &= ~far;
+      if (!f) return;
+    }
+  }
   const int k = __popcll(f);
-  if (k > 32) bs_relax_dense(k0, k1, lane, R, W, row, wgt, u, w, f, next, dist);
-  else bs_relax_sparse(k0, k1, lane, R, W, row, wgt, u, w, f, k, next, dist);
+  if (k > 32) bs_relax_dense(k0, k1, lane, R, W, row, wgt, u, w, f, next, dist, lmin);
+  else bs_relax_sparse(k0, k1, lane, R, W, row, wgt, u, w, f, k, next, dist, lmin);
 }
 
 static __global__ void __launch_bounds__(256, 4)
 k_bs_relax(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ reg_end, const uint32_t* __restrict__ row,
            const uint32_t* __restrict__ wgt, uint32_t R, uint32_t W, const uint64_t* __restrict__ front, PairList L,
-           uint64_t* next, uint32_t* dist)
+           uint64_t* next, uint32_t* dist, uint32_t limit = kNoWindow, unsigned int* pend_min = nullptr)
 {
   const int lane = threadIdx.x & 31;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -184,6 +221,7 @@ k_bs_relax(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ reg_en
   const uint32_t ns = (uint32_t) *L.nsmall;
   const unsigned long long pk = *L.packed;
   const uint32_t nbig = hub_count(pk), ntasks = hub_tasks(pk);
+  uint32_t lmin = 0xFFFFFFFFu;
   for (uint32_t a = warp; a < ntasks + ns; a += nwarps)
   {
     if (a < ntasks)
@@ -191,13 +229,18 @@ k_bs_relax(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ reg_en
       const uint32_t slot = hub_of_task(L.hub_t0, nbig, a);
       const uint32_t i = L.hub[slot], u = i / W;
       const uint32_t k0 = ptr[u] + (a - L.hub_t0[slot]) * kHubTask;
-      bs_relax_range(i, k0, min(k0 + kHubTask, reg_end[u]), lane, R, W, row, wgt, front, next, dist);
+      bs_relax_range(i, k0, min(k0 + kHubTask, reg_end[u]), lane, R, W, row, wgt, front, next, dist, limit, lmin);
     }
     else
     {
       const uint32_t i = L.small[a - ntasks], u = i / W;
-      bs_relax_range(i, ptr[u], reg_end[u], lane, R, W, row, wgt, front, next, dist);
+      bs_relax_range(i, ptr[u], reg_end[u], lane, R, W, row, wgt, front, next, dist, limit, lmin);
     }
+  }
+  if (pend_min)
+  {
+    for (int o = 16; o > 0; o >>= 1) lmin = min(lmin, __shfl_xor_sync(0xffffffffu, lmin, o));
+    if (lane == 0 && lmin != 0xFFFFFFFFu) atomicMin(pend_min, lmin);
   }
 }
 

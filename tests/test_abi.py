@@ -152,3 +152,4 @@ def test_new_entry_points_reject_bad_arguments(native):
     # the tiled PageRank and the push view refuse a null graph
     assert L.la3g_pr_f32_tiled(None, 5, 0.0, None, None, None) == 1
     assert L.la3g_graph_push_view(None, None, None) == 1
+    assert L.la3g_batch_sssp_window(None, 0) == 1

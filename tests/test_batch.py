@@ -77,6 +77,26 @@ def test_sssp_batch_equals_single(gpu, graphs):
         assert np.array_equal(dist[i], d1), (i, int(roots[i]))
 
 
+@pytest.mark.parametrize("delta", [1, 16, 128, 0xFFFFFFFF, 0])
+def test_sssp_batch_window_equals_single(gpu, graphs, delta):
+    """The batched SSSP's distance window (delta-stepping's buckets over all
+    roots of a chunk) only reorders relaxations: for every width, on a graph
+    with hubs (R-MAT) and one without (ER, where the automatic width is on),
+    each root's distances equal the single-root call's."""
+    L = gpu
+    n = graphs["n"]
+    ge = L.Graph.from_edges(L.EdgeList.er(n, 16 * n, seed=31, weighted=True, wseed=8), L.DIRECTED | L.WEIGHTED)
+    for g in (graphs["w"], ge):
+        L.batch_sssp_window(g, delta)
+        roots = _roots(n, 130, 12)
+        dist, st = L.sssp_batch(g, roots)
+        for i in list(range(0, 130, 11)) + [0, 1, 2, 3, 129]:
+            d1, _ = L.sssp(g, int(roots[i]))
+            assert np.array_equal(dist[i], d1), (delta, i, int(roots[i]))
+        L.batch_sssp_window(g, 0)
+    ge.free()
+
+
 def test_persistent_barrier_wait_runs_out_cleanly(gpu, graphs):
     """The persistent kernel's grid-barrier waits are bounded: with a limit
     of zero polls the first block that has to wait gives up, every block
